@@ -1,0 +1,235 @@
+/*
+ * namics_gb300 — GB300-native Scheutjens–Fleer SCF hot path behind a C ABI.
+ *
+ * The entry points below replace, one for one, the reference's hot path for
+ * an SCF solve (leermakers/Namics; all citations are file:line into its
+ * src/ directory):
+ *
+ *   Lattice  (lattice.h:123-155)  propagate / Side / set_bounds /
+ *                                 ComputeGN / AddPhiS / WeightedSum
+ *   Molecule (molecule.h:185-197) ComputePhi, propagate_forward/backward
+ *   System   (system.cpp:2087)    Classical_residual (+ ComputePhis,
+ *                                 PutU, PrepareForCalculations)
+ *   SFNewton (sfnewton.h:102)     iterate_DIIS, DIIS, Ax, computeresidual
+ *   System   (system.cpp:2809,3038,3246) GetFreeEnergy,
+ *                                 GetGrandPotential, CreateMu
+ *
+ * Plain C types only.  Arrays named *_dev are device pointers (cudaMalloc'd
+ * or any CUDA-visible allocation); all other arrays are host pointers.
+ * Every entry point returns NM_OK (0) or a negative status; the reference's
+ * integer exceptions map onto NM_ERR_GN (-1, system.cpp:2402),
+ * NM_ERR_NAN_DIIS (-2, sfnewton.cpp:808), NM_ERR_NAN_SVD (-3,
+ * tools.cpp:1225) and NM_ERR_NEG_SOLVENT (-4, system.cpp:2524).
+ * nm_last_error() returns a thread-local message for the last failure.
+ *
+ * Layout: identical to the reference (lattice.cpp:245-254).  Sites are
+ * padded by one halo layer per side; index = x*JX + y*JY + z with
+ * 1-D: M=MX+2, JX=1; 2-D: M=(MX+2)(MY+2), JX=MY+2, JY=1;
+ * 3-D: M=(MX+2)(MY+2)(MZ+2), JX=(MY+2)(MZ+2), JY=MZ+2.
+ * The iteration vector x (and the residual g) is [n_it blocks of M]
+ * (solve_scf.cpp:79-85), the same as the reference's `xx`.
+ */
+#ifndef NAMICS_GB300_H
+#define NAMICS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define NM_OK               0
+#define NM_ERR_GN          -1   /* G(N) <= 0 for a restricted molecule      */
+#define NM_ERR_NAN_DIIS    -2   /* NaN in the DIIS matrix                   */
+#define NM_ERR_NAN_SVD     -3   /* NaN in the small DIIS solve              */
+#define NM_ERR_NEG_SOLVENT -4   /* solvent bulk volume fraction < 0         */
+#define NM_ERR_INPUT      -10   /* input text not understood / unsupported  */
+#define NM_ERR_CUDA       -11   /* CUDA runtime error                       */
+#define NM_ERR_ARG        -12   /* bad argument                             */
+#define NM_ERR_NOMEM      -13   /* device allocation failed                 */
+#define NM_ERR_NOT_CONVERGED -14 /* iteration limit reached (solve only)   */
+
+/* ---- enumerations (values are part of the ABI) -------------------------- */
+enum nm_geometry  { NM_PLANAR = 0, NM_CYLINDRICAL = 1, NM_SPHERICAL = 2 };
+enum nm_lattype   { NM_SIMPLE_CUBIC = 0, NM_HEXAGONAL = 1 };
+enum nm_bc        { NM_BC_MIRROR = 0, NM_BC_PERIODIC = 1, NM_BC_SURFACE = 2 };
+enum nm_segfree   { NM_SEG_FREE = 0, NM_SEG_PINNED = 1, NM_SEG_FROZEN = 2 };
+enum nm_molfree   { NM_MOL_FREE = 0, NM_MOL_RESTRICTED = 1, NM_MOL_SOLVENT = 2,
+                    NM_MOL_NEUTRALIZER = 3 };
+enum nm_precision { NM_FP64 = 0, NM_FP32 = 1 };
+
+/* ---- compiled problem ("plan") -------------------------------------------
+ * Produced on the host from Namics input text by nm_plan_create().  It holds
+ * every per-site constant the hot path needs (masks, curvature weights) and
+ * each molecule as a tree of blocks.  Read-only for callers.               */
+
+/* One block: a run of `length` bonded segments of one segment type.  Blocks
+ * form a tree rooted at the molecule's last segment (linear chains), at the
+ * first-written segment of a branched composition (mol_branched, reversed
+ * numbering, molecule.cpp:1740-1766) or at the dendrimer core
+ * (mol_dendrimer.cpp:113-184).  Children attach to the block's first
+ * segment.  `mult` identical copies of the child subtree attach there
+ * (dendrimer arms; 1 otherwise); `degeneracy` is the number of equivalent
+ * copies of each segment of the block in one molecule (d_mon). */
+typedef struct nm_block {
+    int    seg;          /* segment type                                   */
+    int    molmon;       /* index into the molecule's monomer list          */
+    int    length;       /* segments in the run                             */
+    int    s0;           /* storage index of the run's first segment        */
+    int    parent;       /* parent block (-1 for the root block)            */
+    int    mult;         /* copies of this subtree at the parent's join      */
+    double degeneracy;   /* d_mon                                           */
+    int    n_child;      /* child blocks (each a distinct group)             */
+    int    child0;       /* offset of this block's children in child_index  */
+} nm_block;
+
+typedef struct nm_molecule {
+    int    freedom;          /* enum nm_molfree                              */
+    int    pinned;           /* contains a pinned segment (IsPinned)         */
+    double n, theta, phibulk;/* input values (restricted: n/theta; free: φb) */
+    double chainlength;      /* N (with degeneracies)                        */
+    int    n_molmon;         /* distinct segment types in the molecule       */
+    const int*    molmon_seg;      /* [n_molmon] segment type              */
+    const double* molmon_fraction; /* [n_molmon] fraction(seg)             */
+    int    n_blocks;
+    const nm_block* blocks;  /* [n_blocks], forward (post-)order: children
+                                come before their parent; root is last      */
+    const int* child_index;  /* children lists                               */
+    int    n_store;          /* forward propagators stored per site          */
+    double charge;           /* Σ valence·fraction (Mol::Charge)             */
+} nm_molecule;
+
+typedef struct nm_plan {
+    /* lattice (fjc = 1) */
+    int    gradients, MX, MY, MZ;
+    int    geometry, lattice_type, stencil_full;
+    int    bc[6];            /* x-low, y-low, z-low, x-high, y-high, z-high  */
+    int    JX, JY, M;
+    double lambda;           /* 1/6 simple cubic, 1/4 hexagonal             */
+    double offset_first_layer, bond_length, volume;
+    const double* L;         /* [M] site volume (1 for planar)               */
+    const double* lambda_1;  /* [M] curved-lattice weights, NULL if planar  */
+    const double* lambda0;
+    const double* lambda1;
+    const int*    ksam;      /* [M] 0 on frozen sites, 1 elsewhere          */
+    /* segments */
+    int    n_seg;
+    const char* const* seg_name;
+    const int*    seg_freedom;   /* enum nm_segfree                         */
+    const int*    seg_it;        /* iteration block of each segment, -1 frozen */
+    const double* seg_gmask;     /* [n_seg*M] G1 = exp(-u)·gmask           */
+    const double* seg_phi_frozen;/* [n_seg*M] frozen volume fraction       */
+    const double* chi;           /* [n_seg*n_seg]                           */
+    const double* seg_valence;   /* [n_seg]                                 */
+    const double* seg_epsilon;   /* [n_seg]                                 */
+    int    n_it;                 /* iteration species (ItMonList)          */
+    const int*    it_seg;        /* [n_it] representative segment          */
+    int    iv;                   /* length of x: n_it*M (+M if charged)    */
+    int    charged;
+    /* molecules */
+    int    n_mol;
+    const nm_molecule* mols;
+    int    solvent, neutralizer; /* molecule index or -1                   */
+    /* solver (newton : ... keys) */
+    int    diis_m, iterationlimit, max_norm;
+    double tolerance, deltamax;
+} nm_plan;
+
+/* Parse Namics input text (the `lat/mon/mol/sys/newton` key subset of the
+ * first `start` block; input.cpp:3-78) into a plan.  Replaces the object
+ * construction of namics.cpp:165-417 and the Check/Prepare steps of
+ * Lattice, Segment, Molecule and System.  On error returns NM_ERR_INPUT. */
+int  nm_plan_create(const char* input_text, nm_plan** out);
+void nm_plan_destroy(nm_plan* plan);
+const char* nm_last_error(void);
+const char* nm_version(void);
+
+/* ---- device context --------------------------------------------------- */
+typedef struct nm_ctx nm_ctx;
+
+typedef struct nm_ctx_options {
+    int precision;           /* enum nm_precision for propagators           */
+    int checkpoint_stride;   /* store every k-th forward propagator (0=all) */
+    int device;              /* CUDA device ordinal                          */
+    void* stream;            /* cudaStream_t, NULL = a private stream       */
+} nm_ctx_options;
+
+/* Allocates all device state for one problem (fields, G1, propagators,
+ * volume fractions, DIIS history).  Replaces the AllocateMemory chain
+ * (solve_scf.cpp:67-106, system.cpp:100-190, molecule.cpp:130-270). */
+int nm_ctx_create(const nm_plan* plan, const nm_ctx_options* opt, nm_ctx** out);
+int nm_ctx_destroy(nm_ctx* ctx);
+
+/* One residual evaluation g(x) on device buffers of length plan->iv.
+ * Replaces Solve_scf::residuals -> System::Classical_residual
+ * (solve_scf.cpp:752-908, system.cpp:2087-2189). */
+int nm_residual_dev(nm_ctx* ctx, const double* x_dev, double* g_dev);
+
+typedef struct nm_solve_result {
+    int    iterations;
+    double residual;         /* ‖g‖₂ (or max|g|) at exit                     */
+    int    status;           /* NM_OK, NM_ERR_NOT_CONVERGED or an error     */
+} nm_solve_result;
+
+/* DIIS solve from the field x (device, length iv; updated in place).
+ * Replaces SFNewton::iterate_DIIS (sfnewton.cpp:1037-1130). */
+int nm_solve_dev(nm_ctx* ctx, double* x_dev, nm_solve_result* res);
+
+/* Same solve with host buffers: copies x in, solves, copies x back and the
+ * per-segment volume fractions out (phi_host: [n_seg*M], may be NULL). */
+int nm_solve_host(nm_ctx* ctx, double* x_host, double* phi_host,
+                  nm_solve_result* res);
+
+/* Results of the last residual evaluation (device -> host copies).
+ * which: 0 segment φ [n_seg*M], 1 G1 [n_seg*M], 2 α [M], 3 φ_tot [M],
+ * 4 molecule φ_tot [n_mol*M], 5 φ_side [n_seg*M]. */
+int nm_get_field(nm_ctx* ctx, int which, double* out_host);
+
+/* Per-molecule scalars of the last residual: GN, n, θ, φ_bulk, norm. */
+int nm_get_molecule(nm_ctx* ctx, int mol, double* GN, double* n,
+                    double* theta, double* phibulk);
+
+/* Free energy, grand potential and chemical potentials (mu: [n_mol]) of
+ * the state of the last residual evaluation (system.cpp:2809-3244). */
+int nm_free_energy(nm_ctx* ctx, double* F, double* Omega, double* mu);
+
+/* Unit-testable pieces on device arrays of length M.
+ * nm_propagate: G_out = Side(set_bounds(G_in))·G1 (Lattice::propagate,
+ * LG1Planar.cpp:138-159, LGrad1.cpp:432-454, LG2Planar.cpp:1039-1127,
+ * LGrad2.cpp:1053-1090, LGrad3.cpp:673-744).  G_in's halo is updated in
+ * place by set_bounds, as in the reference.  G1 may be NULL (≡1).
+ * nm_side: X_side = Side(X) (Lattice::Side) without set_bounds. */
+int nm_propagate_dev(nm_ctx* ctx, double* G_in_dev, const double* G1_dev,
+                     double* G_out_dev);
+int nm_side_dev(nm_ctx* ctx, const double* X_dev, double* X_side_dev);
+
+/* Device launches issued by this context since creation (diagnostics). */
+long long nm_ctx_launch_count(nm_ctx* ctx);
+
+/* ---- batched 1-gradient solver ------------------------------------------
+ * Many independent 1-gradient problems solved to convergence in one
+ * persistent launch (one CTA per problem, DIIS on the device). */
+typedef struct nm_batch nm_batch;
+
+int nm_batch_create(const nm_plan* const* plans, int n_plans,
+                    const nm_ctx_options* opt, nm_batch** out);
+int nm_batch_destroy(nm_batch* b);
+/* x_dev: concatenated iteration vectors (offsets from nm_batch_offsets);
+ * updated in place.  iterations/residual/status: [n_plans] host arrays. */
+int nm_batch_solve_dev(nm_batch* b, double* x_dev, int* iterations,
+                       double* residual, int* status);
+int nm_batch_solve_host(nm_batch* b, double* x_host, int* iterations,
+                        double* residual, int* status);
+/* element offset of problem i's x in the concatenated vector; total in
+ * offsets[n_plans] */
+int nm_batch_offsets(nm_batch* b, long long* offsets);
+/* per-problem free energy / grand potential of the final state */
+int nm_batch_free_energy(nm_batch* b, double* F, double* Omega);
+long long nm_batch_launch_count(nm_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NAMICS_GB300_H */

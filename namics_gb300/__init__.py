@@ -1,0 +1,255 @@
+"""namics_gb300: GB300-native Scheutjens–Fleer SCF hot path.
+
+The compute lives in the CUDA/C++ library ``lib/libnamics_gb300.so`` behind
+the C ABI of ``include/namics_gb300.h``.  This module is a thin ctypes layer
+over it for Python callers (tests, benchmarks, scripts).  There is no CPU
+fallback: every compute call needs the CUDA library and a GPU, and fails
+loudly without them.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+from ._abi import NM_FP32, NM_FP64  # noqa: F401
+
+__all__ = ["Plan", "Context", "Batch", "NamicsError", "load_library", "NM_FP32", "NM_FP64"]
+
+
+class NamicsError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"namics_gb300 error {code}: {msg}")
+        self.code = code
+
+
+def load_library() -> C.CDLL:
+    return _abi.load()
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        lib = _abi.load()
+        raise NamicsError(rc, lib.nm_last_error().decode(errors="replace"))
+
+
+def _dptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_abi.dp)
+
+
+class Plan:
+    """A compiled problem: Namics input text -> lattice, segments, molecules."""
+
+    def __init__(self, text: str):
+        lib = _abi.load()
+        p = _abi.P_plan()
+        _check(lib.nm_plan_create(text.encode(), C.byref(p)))
+        self._p = p
+        self.text = text
+
+    def __del__(self):
+        try:
+            if getattr(self, "_p", None):
+                _abi.load().nm_plan_destroy(self._p)
+                self._p = None
+        except Exception:
+            pass
+
+    @property
+    def ptr(self):
+        return self._p
+
+    @property
+    def c(self) -> _abi.nm_plan:
+        return self._p.contents
+
+    # convenient views
+    @property
+    def M(self) -> int:
+        return self.c.M
+
+    @property
+    def iv(self) -> int:
+        return self.c.iv
+
+    @property
+    def n_seg(self) -> int:
+        return self.c.n_seg
+
+    @property
+    def n_mol(self) -> int:
+        return self.c.n_mol
+
+    @property
+    def seg_names(self) -> list[str]:
+        return [self.c.seg_name[i].decode() for i in range(self.n_seg)]
+
+    @property
+    def it_seg(self) -> list[int]:
+        return [self.c.it_seg[i] for i in range(self.c.n_it)]
+
+    @property
+    def shape(self) -> tuple[int, ...]:
+        c = self.c
+        if c.gradients == 1:
+            return (c.MX + 2,)
+        if c.gradients == 2:
+            return (c.MX + 2, c.MY + 2)
+        return (c.MX + 2, c.MY + 2, c.MZ + 2)
+
+    def interior_mask(self) -> np.ndarray:
+        m = np.zeros(self.shape, dtype=bool)
+        m[tuple(slice(1, -1) for _ in self.shape)] = True
+        return m.reshape(-1)
+
+    def chainlength(self, mol: int) -> float:
+        return self.c.mols[mol].chainlength
+
+    def segment_updates(self) -> float:
+        """Segment-site updates of one residual evaluation: 2·Σ_mol n_store·sites."""
+        c = self.c
+        sites = c.MX * max(c.MY, 1) * max(c.MZ, 1)
+        return 2.0 * sum(c.mols[m].n_store for m in range(c.n_mol)) * sites
+
+
+@dataclass
+class SolveResult:
+    iterations: int
+    residual: float
+    status: int
+
+
+class Context:
+    """Device state for one problem (nm_ctx)."""
+
+    def __init__(self, plan: Plan, precision: int = NM_FP64, device: int = 0, stream: int | None = None):
+        lib = _abi.load()
+        self.plan = plan
+        opt = _abi.nm_ctx_options(precision, 0, device, C.c_void_p(stream) if stream else None)
+        h = C.c_void_p()
+        _check(lib.nm_ctx_create(plan.ptr, C.byref(opt), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _abi.load().nm_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def residual_dev(self, x_ptr: int, g_ptr: int) -> None:
+        _check(_abi.load().nm_residual_dev(self._h, C.c_void_p(x_ptr), C.c_void_p(g_ptr)))
+
+    def solve_dev(self, x_ptr: int) -> SolveResult:
+        r = _abi.nm_solve_result()
+        rc = _abi.load().nm_solve_dev(self._h, C.c_void_p(x_ptr), C.byref(r))
+        if rc not in (0, _abi.NM_ERR_NOT_CONVERGED) and r.status == 0:
+            _check(rc)
+        return SolveResult(r.iterations, r.residual, r.status if r.status else rc)
+
+    def solve_host(self, x: np.ndarray, want_phi: bool = True) -> tuple[SolveResult, np.ndarray | None]:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        phi = np.empty(self.plan.n_seg * self.plan.M) if want_phi else None
+        r = _abi.nm_solve_result()
+        rc = _abi.load().nm_solve_host(self._h, _dptr(x), _dptr(phi) if want_phi else None, C.byref(r))
+        if rc not in (0, _abi.NM_ERR_NOT_CONVERGED):
+            _check(rc)
+        return SolveResult(r.iterations, r.residual, r.status), phi
+
+    def field(self, which: int) -> np.ndarray:
+        p = self.plan
+        n = {0: p.n_seg, 1: p.n_seg, 2: 1, 3: 1, 4: p.n_mol, 5: p.n_seg}[which] * p.M
+        out = np.empty(n)
+        _check(_abi.load().nm_get_field(self._h, which, _dptr(out)))
+        return out
+
+    def molecule(self, m: int) -> dict:
+        v = [C.c_double() for _ in range(4)]
+        _check(_abi.load().nm_get_molecule(self._h, m, *[C.byref(t) for t in v]))
+        return dict(GN=v[0].value, n=v[1].value, theta=v[2].value, phibulk=v[3].value)
+
+    def free_energy(self) -> tuple[float, float, np.ndarray]:
+        F, O = C.c_double(), C.c_double()
+        mu = np.empty(self.plan.n_mol)
+        _check(_abi.load().nm_free_energy(self._h, C.byref(F), C.byref(O), _dptr(mu)))
+        return F.value, O.value, mu
+
+    def propagate_dev(self, g_in_ptr: int, g1_ptr: int | None, g_out_ptr: int) -> None:
+        _check(_abi.load().nm_propagate_dev(self._h, C.c_void_p(g_in_ptr),
+                                            C.c_void_p(g1_ptr) if g1_ptr else None, C.c_void_p(g_out_ptr)))
+
+    def side_dev(self, x_ptr: int, out_ptr: int) -> None:
+        _check(_abi.load().nm_side_dev(self._h, C.c_void_p(x_ptr), C.c_void_p(out_ptr)))
+
+    def launch_count(self) -> int:
+        return int(_abi.load().nm_ctx_launch_count(self._h))
+
+
+class Batch:
+    """Many independent 1-gradient problems solved in one persistent launch."""
+
+    def __init__(self, plans: list[Plan], precision: int = NM_FP64, device: int = 0, stream: int | None = None):
+        lib = _abi.load()
+        self.plans = plans
+        arr = (_abi.P_plan * len(plans))(*[p.ptr for p in plans])
+        opt = _abi.nm_ctx_options(precision, 0, device, C.c_void_p(stream) if stream else None)
+        h = C.c_void_p()
+        _check(lib.nm_batch_create(arr, len(plans), C.byref(opt), C.byref(h)))
+        self._h = h
+        offs = (C.c_longlong * (len(plans) + 1))()
+        _check(lib.nm_batch_offsets(h, offs))
+        self.offsets = np.array(list(offs), dtype=np.int64)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _abi.load().nm_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def total(self) -> int:
+        return int(self.offsets[-1])
+
+    def solve_dev(self, x_ptr: int):
+        n = len(self.plans)
+        it = np.zeros(n, dtype=np.int32)
+        res = np.zeros(n)
+        st = np.zeros(n, dtype=np.int32)
+        _check(_abi.load().nm_batch_solve_dev(self._h, C.c_void_p(x_ptr), it.ctypes.data_as(_abi.ip),
+                                              _dptr(res), st.ctypes.data_as(_abi.ip)))
+        return it, res, st
+
+    def solve_host(self, x: np.ndarray):
+        n = len(self.plans)
+        it = np.zeros(n, dtype=np.int32)
+        res = np.zeros(n)
+        st = np.zeros(n, dtype=np.int32)
+        _check(_abi.load().nm_batch_solve_host(self._h, _dptr(x), it.ctypes.data_as(_abi.ip),
+                                               _dptr(res), st.ctypes.data_as(_abi.ip)))
+        return it, res, st
+
+    def free_energy(self):
+        n = len(self.plans)
+        F = np.zeros(n)
+        O = np.zeros(n)
+        _check(_abi.load().nm_batch_free_energy(self._h, _dptr(F), _dptr(O)))
+        return F, O
+
+    def launch_count(self) -> int:
+        return int(_abi.load().nm_batch_launch_count(self._h))

@@ -1,0 +1,932 @@
+// Device context: the SCF hot path for one problem of any gradient count.
+//
+// Per residual evaluation (System::Classical_residual, system.cpp:2087-2189):
+//   k_g1          G1 = exp(-u)·mask·KSAM        (segment.cpp:855-879)
+//   per molecule  forward sweep  k_prop         (molecule.cpp:2300-2362)
+//                 G(N)           k_wsum_*       (LGrad*::ComputeGN)
+//                 backward sweep k_prop_back    (molecule.cpp:2364-2446)
+//                 fused with composition rho += d·Gf·Gb (LGrad1.cpp:876-922)
+//   k_norms       normalisation of every molecule (system.cpp:2368-2560)
+//   k_phi         φ = rho/G1·norm, φ_tot       (system.cpp:2438-2610)
+//   k_residual    φ_side stencil + χ terms + α + incompressibility + KSAM
+// and per DIIS iteration (sfnewton.cpp:1078-1095, 837-880):
+//   k_diis_step   x -= δ·g, history slot, ‖g‖² partials
+//   k_gram        Gram row of the history (deterministic two-pass sums)
+//   k_diis_solve  small solve A c = 1, c /= Σc  (one thread, FP64)
+//   k_diis_mix    x = Σ c_i xR_i
+// All arithmetic is FP64; all reductions are two-pass with a fixed grid, so
+// repeated runs are bit-identical.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ctx_internal.h"
+
+using nmdev::Lat;
+
+namespace nm {
+
+#define CK(call)                                                                   \
+    do {                                                                           \
+        cudaError_t e_ = (call);                                                   \
+        if (e_ != cudaSuccess) {                                                   \
+            set_error(std::string("CUDA: ") + cudaGetErrorString(e_) + " at " +    \
+                      __FILE__ + ":" + std::to_string(__LINE__));                  \
+            return NM_ERR_CUDA;                                                    \
+        }                                                                          \
+    } while (0)
+
+static const int RED_THREADS = 256;
+
+// ---------------------------------------------------------------- kernels --
+
+__global__ void k_g1(Lat L, int ns, const double* __restrict__ x, const int* __restrict__ seg_it,
+                     const double* __restrict__ gmask, double* __restrict__ G1) {
+    int M = L.M;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < M; s += gridDim.x * blockDim.x) {
+        int src = nmdev::bc_source(L, s);
+        for (int i = 0; i < ns; i++) {
+            int it = seg_it[i];
+            double u = it >= 0 ? x[(size_t)it * M + src] : 0.0;
+            G1[(size_t)i * M + s] = exp(-u) * gmask[(size_t)i * M + s];
+        }
+    }
+}
+
+// out = stencil(in)·G1 at interior sites (G1 may be null: ≡ 1)
+__global__ void k_prop(Lat L, const double* __restrict__ in, const double* __restrict__ G1,
+                       double* __restrict__ out) {
+    int n = nmdev::interior_count(L);
+    nmdev::GLoad<double> ld{in};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int x, y, z;
+        nmdev::site_coords(L, i, x, y, z);
+        int s = x * L.JX + y * L.JY + z;
+        double v = nmdev::stencil_at(L, ld, x, y, z);
+        out[s] = G1 ? v * G1[s] : v;
+    }
+}
+
+// backward step fused with composition: out = stencil(in)·G1; rho += d·Gf·out
+__global__ void k_prop_back(Lat L, const double* __restrict__ in, const double* __restrict__ G1,
+                            double* __restrict__ out, const double* __restrict__ Gf,
+                            double* __restrict__ rho, double d) {
+    int n = nmdev::interior_count(L);
+    nmdev::GLoad<double> ld{in};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int x, y, z;
+        nmdev::site_coords(L, i, x, y, z);
+        int s = x * L.JX + y * L.JY + z;
+        double v = nmdev::stencil_at(L, ld, x, y, z) * G1[s];
+        out[s] = v;
+        if (d == 1.0) rho[s] += Gf[s] * v;
+        else rho[s] += d * Gf[s] * v;
+    }
+}
+
+// root of the backward sweep: out = G1; rho += d·Gf·G1
+__global__ void k_back_init(Lat L, const double* __restrict__ G1, double* __restrict__ out,
+                            const double* __restrict__ Gf, double* __restrict__ rho, double d) {
+    int n = nmdev::interior_count(L);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int x, y, z;
+        nmdev::site_coords(L, i, x, y, z);
+        int s = x * L.JX + y * L.JY + z;
+        double v = G1[s];
+        out[s] = v;
+        if (d == 1.0) rho[s] += Gf[s] * v;
+        else rho[s] += d * Gf[s] * v;
+    }
+}
+
+__global__ void k_copy_interior(Lat L, const double* __restrict__ in, double* __restrict__ out) {
+    int n = nmdev::interior_count(L);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int x, y, z;
+        nmdev::site_coords(L, i, x, y, z);
+        int s = x * L.JX + y * L.JY + z;
+        out[s] = in[s];
+    }
+}
+
+// out *= a^pow (interior)
+__global__ void k_mul_pow(Lat L, double* __restrict__ out, const double* __restrict__ a, int pw) {
+    int n = nmdev::interior_count(L);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int x, y, z;
+        nmdev::site_coords(L, i, x, y, z);
+        int s = x * L.JX + y * L.JY + z;
+        double v = out[s];
+        for (int k = 0; k < pw; k++) v *= a[s];
+        out[s] = v;
+    }
+}
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    // fixed-order block reduction (deterministic)
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0;
+    if (threadIdx.x == 0) {
+        int nw = (blockDim.x + 31) >> 5;
+        for (int i = 0; i < nw; i++) r += sh[i];
+    }
+    __syncthreads();
+    return r;
+}
+
+// partial sums of X (times L when given) over interior sites
+__global__ void k_wsum_partial(Lat L, const double* __restrict__ X, const double* __restrict__ W,
+                               double* __restrict__ partial) {
+    __shared__ double sh[32];
+    int n = nmdev::interior_count(L);
+    double acc = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int x, y, z;
+        nmdev::site_coords(L, i, x, y, z);
+        int s = x * L.JX + y * L.JY + z;
+        acc += W ? X[s] * W[s] : X[s];
+    }
+    double r = block_sum(acc, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = r;
+}
+
+__global__ void k_final_sum(const double* __restrict__ partial, int nb, double* __restrict__ out) {
+    __shared__ double sh[32];
+    double acc = 0;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) acc += partial[i];
+    double r = block_sum(acc, sh);
+    if (threadIdx.x == 0) *out = r;
+}
+
+// molecule scalars: [GN, norm, n, theta, phibulk] per molecule
+__global__ void k_norms(NormArgs a, double* __restrict__ sc, double* __restrict__ seg_phibulk,
+                        int* __restrict__ status) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double A = 0, B = 0;
+    int st = 0;
+    for (int m = 0; m < a.n_mol; m++) {
+        const MolScal& M = a.mol[m];
+        double* s = sc + 5 * m;
+        double GN = s[0], norm = 0;
+        s[2] = M.n_in; s[3] = M.theta_in;
+        if (M.freedom == NM_MOL_FREE) {
+            s[4] = M.phibulk_in;
+            norm = M.phibulk_in / M.N;
+            s[2] = norm * GN;
+            A += M.phibulk_in * M.charge; B += M.phibulk_in;
+        } else if (M.freedom == NM_MOL_RESTRICTED) {
+            if (GN > 0) {
+                norm = M.n_in / GN;
+                if (M.pinned) s[4] = 0;
+                else { s[4] = M.N * norm; A += s[4] * M.charge; B += s[4]; }
+            } else { st = NM_ERR_GN; norm = 0; }
+        } else s[4] = 0;
+        s[1] = norm;
+    }
+    if (a.solvent >= 0) {
+        double* s = sc + 5 * a.solvent;
+        s[4] = 1.0 - B;
+        if (s[4] < 0 && st == 0) st = NM_ERR_NEG_SOLVENT;
+        double norm = s[4] / a.mol[a.solvent].N;
+        s[2] = norm * s[0];
+        s[3] = s[2] * a.mol[a.solvent].N;
+        s[1] = norm;
+    }
+    for (int i = 0; i < a.ns; i++) seg_phibulk[i] = 0;
+    for (int k = 0; k < a.n_mm; k++) seg_phibulk[a.mm_seg[k]] += a.mm_frac[k] * sc[5 * a.mm_mol[k] + 4];
+    if (st) *status = st;
+}
+
+__global__ void k_phi(Lat L, PhiArgs a, const double* __restrict__ sc, const double* __restrict__ G1,
+                      const double* __restrict__ phi_frozen, const int* __restrict__ seg_frozen,
+                      double* __restrict__ phi, double* __restrict__ phitot,
+                      double* __restrict__ mol_phitot) {
+    int M = L.M;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < M; s += gridDim.x * blockDim.x) {
+        bool in = nmdev::is_interior(L, s);
+        double pt = 0;
+        for (int i = 0; i < a.ns; i++) {
+            double v = phi_frozen[(size_t)i * M + s];
+            phi[(size_t)i * M + s] = v;
+            if (seg_frozen[i]) pt += v;
+        }
+        for (int m = 0; m < a.n_mol; m++) mol_phitot[(size_t)m * M + s] = 0;
+        if (in) {
+            for (int k = 0; k < a.n_mm; k++) {
+                int sg = a.mm_seg[k], m = a.mm_mol[k];
+                double g1 = G1[(size_t)sg * M + s];
+                double v = g1 != 0 ? a.mm_rho[k][s] / g1 : 0.0;
+                double norm = sc[5 * m + 1];
+                if (norm > 0) v *= norm;
+                phi[(size_t)sg * M + s] += v;
+                pt += v;
+                mol_phitot[(size_t)m * M + s] += v;
+            }
+        }
+        phitot[s] = pt;
+    }
+}
+
+__global__ void k_residual(Lat L, ResArgs a, const double* __restrict__ x, const double* __restrict__ phi,
+                           const double* __restrict__ phitot, const double* __restrict__ seg_phibulk,
+                           const double* __restrict__ ksam, double* __restrict__ g,
+                           double* __restrict__ alpha, double* __restrict__ phi_side) {
+    int M = L.M;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < M; s += gridDim.x * blockDim.x) {
+        if (!nmdev::is_interior(L, s)) {
+            for (int i = 0; i < a.nit; i++) g[(size_t)i * M + s] = 0;
+            alpha[s] = 0;
+            for (int k = 0; k < a.ns; k++) phi_side[(size_t)k * M + s] = 0;
+            continue;
+        }
+        int cx, cy, cz;
+        if (L.g == 1) { cx = s; cy = 0; cz = 0; }
+        else if (L.g == 2) { cx = s / L.JX; cy = s % L.JX; cz = 0; }
+        else { cx = s / L.JX; int r = s % L.JX; cy = r / L.JY; cz = r % L.JY; }
+        double ps[NM_MAX_SEG];
+        for (int k = 0; k < a.ns; k++) {
+            nmdev::GLoad<double> ld{phi + (size_t)k * M};
+            ps[k] = nmdev::stencil_at(L, ld, cx, cy, cz);
+            phi_side[(size_t)k * M + s] = ps[k];
+        }
+        double pt = phitot[s];
+        double gi[NM_MAX_SEG];
+        double al = 0;
+        for (int i = 0; i < a.nit; i++) {
+            double v = x[(size_t)i * M + s];
+            int r = a.it_seg[i];
+            for (int k = 0; k < a.ns; k++) {
+                double chi = a.chi[r * a.ns + k];
+                if (chi != 0 && pt > 0) v = v - chi * (ps[k] / pt - seg_phibulk[k]);
+            }
+            gi[i] = v;
+            al += v;
+        }
+        al = al * (1.0 / a.nit);
+        alpha[s] = al;
+        double km = ksam[s];
+        for (int i = 0; i < a.nit; i++) {
+            double v = pt > 0 ? gi[i] - al + 1 / pt - 1.0 : 0.0;
+            g[(size_t)i * M + s] = v * km;
+        }
+    }
+}
+
+// x_new = x - δ·g ; xR[k] = x_new ; x_x0[k] = x_new - x ; partial Σ g² (or max|g|)
+__global__ void k_diis_step(int n, double dmax, double* __restrict__ x, const double* __restrict__ g,
+                            double* __restrict__ xR, double* __restrict__ xx0,
+                            double* __restrict__ partial, int max_norm) {
+    __shared__ double sh[32];
+    double acc = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double xo = x[i], gv = g[i];
+        double xn = xo + (-dmax) * gv;
+        x[i] = xn;
+        if (xR) xR[i] = xn;
+        if (xx0) xx0[i] = xn - xo;
+        if (max_norm) acc = fmax(acc, fabs(gv));
+        else acc += gv * gv;
+    }
+    if (max_norm) {
+        for (int o = 16; o > 0; o >>= 1) acc = fmax(acc, __shfl_down_sync(0xffffffffu, acc, o));
+        int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+        if (l == 0) sh[w] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double r = 0;
+            for (int i = 0; i < (int)(blockDim.x >> 5); i++) r = fmax(r, sh[i]);
+            partial[blockIdx.x] = r;
+        }
+    } else {
+        double r = block_sum(acc, sh);
+        if (threadIdx.x == 0) partial[blockIdx.x] = r;
+    }
+}
+
+__global__ void k_final_norm(const double* __restrict__ partial, int nb, double* __restrict__ out, int max_norm) {
+    __shared__ double sh[32];
+    if (max_norm) {
+        if (threadIdx.x == 0) {
+            double r = 0;
+            for (int i = 0; i < nb; i++) r = fmax(r, partial[i]);
+            *out = r;
+        }
+        return;
+    }
+    double acc = 0;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) acc += partial[i];
+    double r = block_sum(acc, sh);
+    if (threadIdx.x == 0) *out = sqrt(r);
+}
+
+// Gram row: partial[i*nb + b] = Σ_b x_x0[posi_i]·x_x0[k]
+__global__ void k_gram(int n, const double* __restrict__ xx0, int k, int kd, int m,
+                       double* __restrict__ partial) {
+    __shared__ double sh[32];
+    int i = blockIdx.y;
+    int posi = k - kd + 1 + i;
+    if (posi < 0) posi += m;
+    const double* a = xx0 + (size_t)posi * n;
+    const double* b = xx0 + (size_t)k * n;
+    double acc = 0;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) acc += a[j] * b[j];
+    double r = block_sum(acc, sh);
+    if (threadIdx.x == 0) partial[(size_t)i * gridDim.x + blockIdx.x] = r;
+}
+
+// one thread: finish the Gram row, slide the window, solve, normalise
+__global__ void k_diis_solve(const double* __restrict__ partial, int nb, int kd_in, int m,
+                             double* __restrict__ Aij, double* __restrict__ Ci, int* __restrict__ status) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int kd = kd_in;
+    if (kd > m) {
+        kd = m;
+        for (int i = 1; i < m; i++)
+            for (int j = 1; j < m; j++) Aij[m * (i - 1) + j - 1] = Aij[m * i + j];
+    }
+    for (int i = 0; i < kd; i++) {
+        double D = 0;
+        for (int b = 0; b < nb; b++) D += partial[(size_t)i * nb + b];
+        Aij[i + m * (kd - 1)] = Aij[kd - 1 + m * i] = D + 1e-9;
+    }
+    double A[NM_MAX_DIIS * NM_MAX_DIIS], c[NM_MAX_DIIS];
+    for (int i = 0; i < kd; i++)
+        for (int j = 0; j < kd; j++) {
+            double v = Aij[j + m * i];
+            if (v != v) { *status = NM_ERR_NAN_DIIS; return; }
+            A[i * kd + j] = v;
+        }
+    nm_small_solve(A, c, kd);
+    double normC = 0;
+    for (int i = 0; i < kd; i++) normC += c[i];
+    for (int i = 0; i < kd; i++) {
+        Ci[i] = c[i] / normC;
+        if (Ci[i] != Ci[i]) *status = NM_ERR_NAN_SVD;
+    }
+}
+
+__global__ void k_diis_mix(int n, double* __restrict__ x, const double* __restrict__ xR,
+                           const double* __restrict__ Ci, int k, int kd_in, int m) {
+    int kd = kd_in > m ? m : kd_in;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        double v = 0;
+        for (int i = 0; i < kd; i++) {
+            int posi = k - kd + 1 + i;
+            if (posi < 0) posi += m;
+            v += Ci[i] * xR[(size_t)posi * n + j];
+        }
+        x[j] = v;
+    }
+}
+
+// free-energy and grand-potential densities (system.cpp:2809-3244)
+struct FeArgs {
+    int ns, n_mol;
+    int seg_frozen[NM_MAX_SEG], seg_in_mol[NM_MAX_SEG];
+    double chi[NM_MAX_SEG * NM_MAX_SEG];
+    double cF[NM_MAX_MOL], cF2[NM_MAX_MOL], invN[NM_MAX_MOL];
+};
+
+__global__ void k_fe_density(Lat L, FeArgs a, const double* __restrict__ sc, const double* __restrict__ phi,
+                             const double* __restrict__ phi_side, const double* __restrict__ G1,
+                             const double* __restrict__ mol_phitot, const double* __restrict__ alpha,
+                             const double* __restrict__ seg_phibulk, const double* __restrict__ ksam,
+                             double* __restrict__ F, double* __restrict__ GP) {
+    int M = L.M;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < M; s += gridDim.x * blockDim.x) {
+        if (!nmdev::is_interior(L, s)) { F[s] = 0; GP[s] = 0; continue; }
+        double f = 0, gp = 0;
+        for (int m = 0; m < a.n_mol; m++) f += a.cF[m] * mol_phitot[(size_t)m * M + s];
+        for (int i = 0; i < a.ns; i++) {
+            if (!a.seg_in_mol[i]) continue;
+            double g1 = G1[(size_t)i * M + s];
+            double ml = g1 > 0 ? -log(g1) : 0.0;
+            f += -1.0 * (phi[(size_t)i * M + s] * ml);
+        }
+        for (int j = 0; j < a.ns; j++) {
+            if (a.seg_frozen[j]) continue;
+            double pj = phi[(size_t)j * M + s];
+            for (int k = 0; k < a.ns; k++) {
+                double chi = a.seg_frozen[k] ? a.chi[j * a.ns + k] : a.chi[j * a.ns + k] / 2;
+                if (chi == 0) continue;
+                f += chi * (pj * phi_side[(size_t)k * M + s]);
+            }
+        }
+        for (int m = 0; m < a.n_mol; m++) f += a.cF2[m] * mol_phitot[(size_t)m * M + s];
+        double km = ksam[s];
+        F[s] = f * km;
+        for (int m = 0; m < a.n_mol; m++) gp += (mol_phitot[(size_t)m * M + s] + (-sc[5 * m + 4])) * a.invN[m];
+        gp += alpha[s];
+        for (int j = 0; j < a.ns; j++) {
+            if (a.seg_frozen[j]) continue;
+            double pj = phi[(size_t)j * M + s], pbA = seg_phibulk[j];
+            for (int k = 0; k < a.ns; k++) {
+                if (a.seg_frozen[k]) continue;
+                double chi = a.chi[j * a.ns + k] / 2;
+                if (chi == 0) continue;
+                gp += chi * (pj * phi_side[(size_t)k * M + s] + (-pbA * seg_phibulk[k]));
+            }
+        }
+        GP[s] = (-gp) * km;
+    }
+}
+
+// ------------------------------------------------------------- host side --
+
+static int grid_for(int n, int threads = 256) {
+    int b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > 4 * 152 * 8) b = 4 * 152 * 8;
+    return b;
+}
+
+int Ctx::launch_prop(const double* in, const double* G1, double* out) {
+    int n = interior;
+    k_prop<<<grid_for(n), 256, 0, stream>>>(lat, in, G1, out);
+    launches++;
+    return NM_OK;
+}
+
+int Ctx::wsum(const double* X, double* out_dev) {
+    const double* W = (plan->gradients < 3 && plan->geometry != NM_PLANAR) ? d_L : nullptr;
+    k_wsum_partial<<<red_blocks, RED_THREADS, 0, stream>>>(lat, X, W, d_partial);
+    k_final_sum<<<1, RED_THREADS, 0, stream>>>(d_partial, red_blocks, out_dev);
+    launches += 2;
+    return NM_OK;
+}
+
+int Ctx::molecule_pass(int m) {
+    const nm_molecule& mol = plan->mols[m];
+    MolDev& D = mols[m];
+    size_t M = plan->M;
+    int n = interior;
+    int gb = grid_for(n);
+    CK(cudaMemsetAsync(D.rho, 0, sizeof(double) * M * mol.n_molmon, stream));
+    // forward
+    for (int b = 0; b < mol.n_blocks; b++) {
+        const nm_block& B = mol.blocks[b];
+        const double* G1 = d_G1 + (size_t)B.seg * M;
+        double* out = D.Gf + (size_t)B.s0 * M;
+        if (B.n_child == 0) {
+            k_copy_interior<<<gb, 256, 0, stream>>>(lat, G1, out);
+            launches++;
+        } else {
+            bool simple = (B.n_child == 1 && mol.blocks[mol.child_index[B.child0]].mult == 1);
+            if (!simple) {
+                for (int c = 0; c < B.n_child; c++) {
+                    int cb = mol.child_index[B.child0 + c];
+                    const nm_block& C = mol.blocks[cb];
+                    launch_prop(D.Gf + (size_t)(C.s0 + C.length - 1) * M, d_ksam, D.Pc + (size_t)cb * M);
+                }
+            }
+            int c0 = mol.child_index[B.child0];
+            const nm_block& C0 = mol.blocks[c0];
+            launch_prop(D.Gf + (size_t)(C0.s0 + C0.length - 1) * M, G1, out);
+            if (!simple) {
+                if (C0.mult > 1) { k_mul_pow<<<gb, 256, 0, stream>>>(lat, out, D.Pc + (size_t)c0 * M, C0.mult - 1); launches++; }
+                for (int c = 1; c < B.n_child; c++) {
+                    int cb = mol.child_index[B.child0 + c];
+                    k_mul_pow<<<gb, 256, 0, stream>>>(lat, out, D.Pc + (size_t)cb * M, mol.blocks[cb].mult);
+                    launches++;
+                }
+            }
+        }
+        for (int k = 1; k < B.length; k++)
+            launch_prop(D.Gf + (size_t)(B.s0 + k - 1) * M, G1, D.Gf + (size_t)(B.s0 + k) * M);
+    }
+    const nm_block& R = mol.blocks[mol.n_blocks - 1];
+    wsum(D.Gf + (size_t)(R.s0 + R.length - 1) * M, d_sc + 5 * m);
+    // backward (pre-order, explicit stack)
+    std::vector<int> stack;
+    stack.push_back(mol.n_blocks - 1);
+    while (!stack.empty()) {
+        int b = stack.back();
+        stack.pop_back();
+        const nm_block& B = mol.blocks[b];
+        const double* G1 = d_G1 + (size_t)B.seg * M;
+        double* rho = D.rho + (size_t)B.molmon * M;
+        double* cur = d_gb;
+        double* nxt = d_gb + M;
+        int s = B.s0 + B.length - 1;
+        if (B.parent < 0) {
+            k_back_init<<<gb, 256, 0, stream>>>(lat, G1, cur, D.Gf + (size_t)s * M, rho, B.degeneracy);
+        } else {
+            k_prop_back<<<gb, 256, 0, stream>>>(lat, D.Q + (size_t)b * M, G1, cur, D.Gf + (size_t)s * M, rho, B.degeneracy);
+        }
+        launches++;
+        for (s = s - 1; s >= B.s0; s--) {
+            k_prop_back<<<gb, 256, 0, stream>>>(lat, cur, G1, nxt, D.Gf + (size_t)s * M, rho, B.degeneracy);
+            launches++;
+            double* t = cur; cur = nxt; nxt = t;
+        }
+        if (B.n_child == 0) continue;
+        for (int c = 0; c < B.n_child; c++) {
+            int cb = mol.child_index[B.child0 + c];
+            double* q = D.Q + (size_t)cb * M;
+            k_copy_interior<<<gb, 256, 0, stream>>>(lat, cur, q);
+            launches++;
+            bool simple = (B.n_child == 1 && mol.blocks[cb].mult == 1);
+            if (!simple) {
+                if (mol.blocks[cb].mult > 1) { k_mul_pow<<<gb, 256, 0, stream>>>(lat, q, D.Pc + (size_t)cb * M, mol.blocks[cb].mult - 1); launches++; }
+                for (int o = 0; o < B.n_child; o++) {
+                    if (o == c) continue;
+                    int ob = mol.child_index[B.child0 + o];
+                    k_mul_pow<<<gb, 256, 0, stream>>>(lat, q, D.Pc + (size_t)ob * M, mol.blocks[ob].mult);
+                    launches++;
+                }
+            }
+        }
+        for (int c = B.n_child - 1; c >= 0; c--) stack.push_back(mol.child_index[B.child0 + c]);
+    }
+    return NM_OK;
+}
+
+int Ctx::residual(const double* x, double* g) {
+    int M = plan->M;
+    k_g1<<<grid_for(M), 256, 0, stream>>>(lat, plan->n_seg, x, d_seg_it, d_gmask, d_G1);
+    launches++;
+    for (int m = 0; m < plan->n_mol; m++) {
+        int rc = molecule_pass(m);
+        if (rc) return rc;
+    }
+    k_norms<<<1, 32, 0, stream>>>(norm_args, d_sc, d_seg_phibulk, d_status);
+    k_phi<<<grid_for(M), 256, 0, stream>>>(lat, phi_args, d_sc, d_G1, d_phi_frozen, d_seg_frozen, d_phi, d_phitot, d_mol_phitot);
+    k_residual<<<grid_for(M), 256, 0, stream>>>(lat, res_args, x, d_phi, d_phitot, d_seg_phibulk, d_ksam, g, d_alpha, d_phi_side);
+    launches += 3;
+    have_state = true;
+    return NM_OK;
+}
+
+int Ctx::check_status() {
+    int st = 0;
+    CK(cudaMemcpyAsync(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    if (st) {
+        CK(cudaMemsetAsync(d_status, 0, sizeof(int), stream));
+        set_error("device status " + std::to_string(st));
+    }
+    return st;
+}
+
+int Ctx::solve(double* x, nm_solve_result* res, int max_iter) {
+    int nvar = plan->iv, m = plan->diis_m;
+    double dmax = plan->deltamax, tol = plan->tolerance;
+    int nb = red_blocks;
+    int it = 0, k_diis = 0;
+    double resid = 0;
+    // initial residual and simple mixing step into slot 0
+    int rc = residual(x, d_g);
+    if (rc) return rc;
+    k_diis_step<<<nb, RED_THREADS, 0, stream>>>(nvar, dmax, x, d_g, d_xR, d_xx0, d_partial, plan->max_norm);
+    k_final_norm<<<1, RED_THREADS, 0, stream>>>(d_partial, nb, d_resid, plan->max_norm);
+    launches += 2;
+    CK(cudaMemcpyAsync(&resid, d_resid, sizeof(double), cudaMemcpyDeviceToHost, stream));
+    rc = check_status();
+    if (rc) { res->iterations = 0; res->residual = resid; res->status = rc; return rc; }
+    while (resid > tol && it < max_iter) {
+        it++;
+        rc = residual(x, d_g);
+        if (rc) return rc;
+        int k = it % m;
+        k_diis++;
+        k_diis_step<<<nb, RED_THREADS, 0, stream>>>(nvar, dmax, x, d_g, d_xR + (size_t)k * nvar,
+                                                    d_xx0 + (size_t)k * nvar, d_partial, plan->max_norm);
+        k_final_norm<<<1, RED_THREADS, 0, stream>>>(d_partial, nb, d_resid, plan->max_norm);
+        int kd = k_diis > m ? m : k_diis;
+        dim3 gg(nb, kd);
+        k_gram<<<gg, RED_THREADS, 0, stream>>>(nvar, d_xx0, k, kd, m, d_gram_partial);
+        k_diis_solve<<<1, 1, 0, stream>>>(d_gram_partial, nb, k_diis, m, d_Aij, d_Ci, d_status);
+        k_diis_mix<<<grid_for(nvar), 256, 0, stream>>>(nvar, x, d_xR, d_Ci, k, k_diis, m);
+        launches += 5;
+        CK(cudaMemcpyAsync(&resid, d_resid, sizeof(double), cudaMemcpyDeviceToHost, stream));
+        rc = check_status();
+        if (rc) break;
+    }
+    res->iterations = it;
+    res->residual = resid;
+    res->status = rc ? rc : (resid > tol ? NM_ERR_NOT_CONVERGED : NM_OK);
+    return rc;
+}
+
+int Ctx::free_energy(double* F, double* Omega, double* mu) {
+    if (!have_state) { set_error("no residual evaluated yet"); return NM_ERR_ARG; }
+    int M = plan->M, ns = plan->n_seg;
+    std::vector<double> sc(5 * plan->n_mol), spb(ns);
+    CK(cudaMemcpyAsync(sc.data(), d_sc, sizeof(double) * sc.size(), cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(spb.data(), d_seg_phibulk, sizeof(double) * ns, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    FeArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.ns = ns; a.n_mol = plan->n_mol;
+    for (int i = 0; i < ns; i++) {
+        a.seg_frozen[i] = plan->seg_freedom[i] == NM_SEG_FROZEN;
+        a.seg_in_mol[i] = plan->seg_it[i] >= 0;
+    }
+    for (int i = 0; i < ns * ns; i++) a.chi[i] = plan->chi[i];
+    for (int m = 0; m < plan->n_mol; m++) {
+        const nm_molecule& mol = plan->mols[m];
+        double N = mol.chainlength;
+        a.cF[m] = std::log(N * sc[5 * m + 2] / sc[5 * m + 0]) / N;
+        double constant = 0;
+        for (int j = 0; j < mol.n_molmon; j++)
+            for (int k = 0; k < mol.n_molmon; k++)
+                constant -= mol.molmon_fraction[j] * mol.molmon_fraction[k] *
+                            (plan->chi[mol.molmon_seg[j] * ns + mol.molmon_seg[k]] / 2);
+        a.cF2[m] = constant;
+        a.invN[m] = 1.0 / N;
+    }
+    k_fe_density<<<grid_for(M), 256, 0, stream>>>(lat, a, d_sc, d_phi, d_phi_side, d_G1, d_mol_phitot,
+                                                  d_alpha, d_seg_phibulk, d_ksam, d_tmpF, d_tmpGP);
+    launches++;
+    wsum(d_tmpF, d_resid + 1);
+    wsum(d_tmpGP, d_resid + 2);
+    double out[2];
+    CK(cudaMemcpyAsync(out, d_resid + 1, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    if (F) *F = out[0];
+    if (Omega) *Omega = out[1];
+    if (mu) {
+        for (int i = 0; i < plan->n_mol; i++) {
+            const nm_molecule& mol = plan->mols[i];
+            double NA = mol.chainlength;
+            double Mu = std::log(NA * sc[5 * i + 2] / sc[5 * i + 0]) + 1;
+            double constant = 0;
+            for (int k = 0; k < plan->n_mol; k++) constant += sc[5 * k + 4] / plan->mols[k].chainlength;
+            Mu = Mu - NA * constant;
+            for (int j = 0; j < ns; j++) {
+                double FA = 0;
+                for (int q = 0; q < mol.n_molmon; q++) if (mol.molmon_seg[q] == j) FA = mol.molmon_fraction[q];
+                for (int k = 0; k < ns; k++) {
+                    double FB = 0;
+                    for (int q = 0; q < mol.n_molmon; q++) if (mol.molmon_seg[q] == k) FB = mol.molmon_fraction[q];
+                    Mu = Mu - NA * (plan->chi[j * ns + k] / 2) * (spb[j] - FA) * (spb[k] - FB);
+                }
+            }
+            mu[i] = Mu;
+        }
+    }
+    return NM_OK;
+}
+
+template <typename T>
+static int dalloc(T** p, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * n);
+    if (e != cudaSuccess) { set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e)); return NM_ERR_NOMEM; }
+    e = cudaMemset(*p, 0, sizeof(T) * n);
+    if (e != cudaSuccess) { set_error(std::string("cudaMemset: ") + cudaGetErrorString(e)); return NM_ERR_CUDA; }
+    return NM_OK;
+}
+
+#define TRY(x) do { int r_ = (x); if (r_) return r_; } while (0)
+
+int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
+    plan = p;
+    if (p->charged) { set_error("charged systems (electrostatics) are not supported by the device path"); return NM_ERR_INPUT; }
+    if (p->n_seg > NM_MAX_SEG || p->n_mol > NM_MAX_MOL || p->diis_m > NM_MAX_DIIS) {
+        set_error("problem exceeds the device path's compiled limits (segments, molecules, DIIS m)");
+        return NM_ERR_INPUT;
+    }
+    int dev = opt ? opt->device : 0;
+    CK(cudaSetDevice(dev));
+    if (opt && opt->stream) { stream = (cudaStream_t)opt->stream; own_stream = false; }
+    else { CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking)); own_stream = true; }
+    int M = p->M, ns = p->n_seg;
+    lat = make_lat(p);
+    interior = p->gradients == 1 ? p->MX : (p->gradients == 2 ? p->MX * p->MY : p->MX * p->MY * p->MZ);
+    red_blocks = 2 * 152;
+    // constants
+    TRY(dalloc(&d_L, M));
+    CK(cudaMemcpy(d_L, p->L, sizeof(double) * M, cudaMemcpyHostToDevice));
+    if (p->lambda_1) {
+        TRY(dalloc(&d_lm1, M)); TRY(dalloc(&d_l0, M)); TRY(dalloc(&d_l1, M));
+        CK(cudaMemcpy(d_lm1, p->lambda_1, sizeof(double) * M, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d_l0, p->lambda0, sizeof(double) * M, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d_l1, p->lambda1, sizeof(double) * M, cudaMemcpyHostToDevice));
+        lat.lm1 = d_lm1; lat.l0 = d_l0; lat.l1 = d_l1;
+    }
+    std::vector<double> ks(M);
+    for (int s = 0; s < M; s++) ks[s] = p->ksam[s];
+    TRY(dalloc(&d_ksam, M));
+    CK(cudaMemcpy(d_ksam, ks.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
+    TRY(dalloc(&d_gmask, (size_t)ns * M));
+    CK(cudaMemcpy(d_gmask, p->seg_gmask, sizeof(double) * ns * M, cudaMemcpyHostToDevice));
+    TRY(dalloc(&d_phi_frozen, (size_t)ns * M));
+    CK(cudaMemcpy(d_phi_frozen, p->seg_phi_frozen, sizeof(double) * ns * M, cudaMemcpyHostToDevice));
+    TRY(dalloc(&d_seg_it, ns));
+    CK(cudaMemcpy(d_seg_it, p->seg_it, sizeof(int) * ns, cudaMemcpyHostToDevice));
+    std::vector<int> sf(ns);
+    for (int i = 0; i < ns; i++) sf[i] = p->seg_freedom[i] == NM_SEG_FROZEN;
+    TRY(dalloc(&d_seg_frozen, ns));
+    CK(cudaMemcpy(d_seg_frozen, sf.data(), sizeof(int) * ns, cudaMemcpyHostToDevice));
+    // state
+    TRY(dalloc(&d_G1, (size_t)ns * M));
+    TRY(dalloc(&d_phi, (size_t)ns * M));
+    TRY(dalloc(&d_phi_side, (size_t)ns * M));
+    TRY(dalloc(&d_phitot, M));
+    TRY(dalloc(&d_alpha, M));
+    TRY(dalloc(&d_mol_phitot, (size_t)p->n_mol * M));
+    TRY(dalloc(&d_gb, 2 * (size_t)M));
+    TRY(dalloc(&d_tmpF, M));
+    TRY(dalloc(&d_tmpGP, M));
+    TRY(dalloc(&d_sc, 5 * (size_t)p->n_mol));
+    TRY(dalloc(&d_seg_phibulk, ns));
+    TRY(dalloc(&d_status, 1));
+    TRY(dalloc(&d_partial, (size_t)red_blocks));
+    TRY(dalloc(&d_resid, 4));
+    mols.resize(p->n_mol);
+    for (int m = 0; m < p->n_mol; m++) {
+        const nm_molecule& mol = p->mols[m];
+        TRY(dalloc(&mols[m].Gf, (size_t)mol.n_store * M));
+        TRY(dalloc(&mols[m].rho, (size_t)mol.n_molmon * M));
+        TRY(dalloc(&mols[m].Pc, (size_t)mol.n_blocks * M));
+        TRY(dalloc(&mols[m].Q, (size_t)mol.n_blocks * M));
+    }
+    // DIIS
+    int mm = p->diis_m;
+    TRY(dalloc(&d_xR, (size_t)mm * p->iv));
+    TRY(dalloc(&d_xx0, (size_t)mm * p->iv));
+    TRY(dalloc(&d_g, (size_t)p->iv));
+    TRY(dalloc(&d_x, (size_t)p->iv));
+    TRY(dalloc(&d_Aij, (size_t)mm * mm));
+    TRY(dalloc(&d_Ci, (size_t)mm));
+    TRY(dalloc(&d_gram_partial, (size_t)mm * red_blocks));
+    // kernel argument blocks
+    std::memset(&norm_args, 0, sizeof(norm_args));
+    std::memset(&phi_args, 0, sizeof(phi_args));
+    std::memset(&res_args, 0, sizeof(res_args));
+    norm_args.n_mol = p->n_mol; norm_args.solvent = p->solvent; norm_args.ns = ns;
+    phi_args.ns = ns; phi_args.n_mol = p->n_mol;
+    int k = 0;
+    for (int m = 0; m < p->n_mol; m++) {
+        const nm_molecule& mol = p->mols[m];
+        MolScal& S = norm_args.mol[m];
+        S.freedom = mol.freedom; S.pinned = mol.pinned; S.n_in = mol.n; S.theta_in = mol.theta;
+        S.phibulk_in = mol.phibulk; S.N = mol.chainlength; S.charge = mol.charge;
+        for (int j = 0; j < mol.n_molmon; j++) {
+            if (k >= NM_MAX_MM) { set_error("too many (molecule, segment) pairs"); return NM_ERR_INPUT; }
+            norm_args.mm_mol[k] = m; norm_args.mm_seg[k] = mol.molmon_seg[j]; norm_args.mm_frac[k] = mol.molmon_fraction[j];
+            phi_args.mm_mol[k] = m; phi_args.mm_seg[k] = mol.molmon_seg[j];
+            phi_args.mm_rho[k] = mols[m].rho + (size_t)j * M;
+            k++;
+        }
+    }
+    norm_args.n_mm = k; phi_args.n_mm = k;
+    res_args.ns = ns; res_args.nit = p->n_it;
+    for (int i = 0; i < p->n_it; i++) res_args.it_seg[i] = p->it_seg[i];
+    for (int i = 0; i < ns * ns; i++) res_args.chi[i] = p->chi[i];
+    CK(cudaDeviceSynchronize());
+    return NM_OK;
+}
+
+Ctx::~Ctx() {
+    double* ptrs[] = {d_L, d_lm1, d_l0, d_l1, d_ksam, d_gmask, d_phi_frozen, d_G1, d_phi, d_phi_side,
+                      d_phitot, d_alpha, d_mol_phitot, d_gb, d_tmpF, d_tmpGP, d_sc, d_seg_phibulk,
+                      d_partial, d_resid, d_xR, d_xx0, d_g, d_x, d_Aij, d_Ci, d_gram_partial};
+    for (double* q : ptrs) if (q) cudaFree(q);
+    if (d_seg_it) cudaFree(d_seg_it);
+    if (d_seg_frozen) cudaFree(d_seg_frozen);
+    if (d_status) cudaFree(d_status);
+    for (auto& D : mols) { cudaFree(D.Gf); cudaFree(D.rho); cudaFree(D.Pc); cudaFree(D.Q); }
+    if (own_stream && stream) cudaStreamDestroy(stream);
+}
+
+Lat make_lat(const nm_plan* p) {
+    Lat L;
+    std::memset(&L, 0, sizeof(L));
+    L.g = p->gradients; L.MX = p->MX; L.MY = p->MY; L.MZ = p->MZ;
+    L.JX = p->JX; L.JY = p->JY; L.M = p->M;
+    L.geom = p->geometry; L.lat = p->lattice_type; L.lam = p->lambda;
+    int n[3] = {p->MX, p->MY, p->MZ};
+    for (int d = 0; d < 3; d++) {
+        int bl = p->bc[d], bh = p->bc[d + 3];
+        L.b1[d] = bl == NM_BC_MIRROR ? 1 : bl == NM_BC_PERIODIC ? n[d] : 0;
+        L.bm[d] = bh == NM_BC_MIRROR ? n[d] : bh == NM_BC_PERIODIC ? 1 : n[d] + 1;
+    }
+    return L;
+}
+
+}  // namespace nm
+
+// ---------------------------------------------------------------- C ABI ---
+using nm::Ctx;
+
+extern "C" {
+
+int nm_ctx_create(const nm_plan* plan, const nm_ctx_options* opt, nm_ctx** out) {
+    if (!plan || !out) { nm::set_error("nm_ctx_create: null argument"); return NM_ERR_ARG; }
+    *out = nullptr;
+    Ctx* c = new Ctx();
+    int rc = c->init(plan, opt);
+    if (rc) { delete c; return rc; }
+    *out = reinterpret_cast<nm_ctx*>(c);
+    return NM_OK;
+}
+
+int nm_ctx_destroy(nm_ctx* ctx) {
+    delete reinterpret_cast<Ctx*>(ctx);
+    return NM_OK;
+}
+
+int nm_residual_dev(nm_ctx* ctx, const double* x_dev, double* g_dev) {
+    if (!ctx || !x_dev || !g_dev) { nm::set_error("nm_residual_dev: null argument"); return NM_ERR_ARG; }
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    int rc = c->residual(x_dev, g_dev);
+    if (rc) return rc;
+    return c->check_status();
+}
+
+int nm_solve_dev(nm_ctx* ctx, double* x_dev, nm_solve_result* res) {
+    if (!ctx || !x_dev || !res) { nm::set_error("nm_solve_dev: null argument"); return NM_ERR_ARG; }
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    return c->solve(x_dev, res, c->plan->iterationlimit);
+}
+
+int nm_solve_host(nm_ctx* ctx, double* x_host, double* phi_host, nm_solve_result* res) {
+    if (!ctx || !x_host || !res) { nm::set_error("nm_solve_host: null argument"); return NM_ERR_ARG; }
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    size_t iv = c->plan->iv;
+    cudaError_t e = cudaMemcpyAsync(c->d_x, x_host, sizeof(double) * iv, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) { nm::set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
+    int rc = c->solve(c->d_x, res, c->plan->iterationlimit);
+    e = cudaMemcpyAsync(x_host, c->d_x, sizeof(double) * iv, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && phi_host)
+        e = cudaMemcpyAsync(phi_host, c->d_phi, sizeof(double) * c->plan->n_seg * c->plan->M,
+                            cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) { nm::set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
+    return rc;
+}
+
+int nm_get_field(nm_ctx* ctx, int which, double* out_host) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c || !out_host || !c->have_state) { nm::set_error("nm_get_field: no state"); return NM_ERR_ARG; }
+    size_t M = c->plan->M, ns = c->plan->n_seg;
+    const double* src = nullptr;
+    size_t n = 0;
+    switch (which) {
+        case 0: src = c->d_phi; n = ns * M; break;
+        case 1: src = c->d_G1; n = ns * M; break;
+        case 2: src = c->d_alpha; n = M; break;
+        case 3: src = c->d_phitot; n = M; break;
+        case 4: src = c->d_mol_phitot; n = c->plan->n_mol * M; break;
+        case 5: src = c->d_phi_side; n = ns * M; break;
+        default: nm::set_error("nm_get_field: unknown field"); return NM_ERR_ARG;
+    }
+    cudaError_t e = cudaMemcpyAsync(out_host, src, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) { nm::set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
+    return NM_OK;
+}
+
+int nm_get_molecule(nm_ctx* ctx, int mol, double* GN, double* n, double* theta, double* phibulk) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c || !c->have_state || mol < 0 || mol >= c->plan->n_mol) { nm::set_error("nm_get_molecule: bad argument"); return NM_ERR_ARG; }
+    double s[5];
+    cudaError_t e = cudaMemcpyAsync(s, c->d_sc + 5 * mol, sizeof(s), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) { nm::set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
+    if (GN) *GN = s[0];
+    if (n) *n = s[2];
+    if (theta) *theta = s[3];
+    if (phibulk) *phibulk = s[4];
+    return NM_OK;
+}
+
+int nm_free_energy(nm_ctx* ctx, double* F, double* Omega, double* mu) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c) { nm::set_error("nm_free_energy: null context"); return NM_ERR_ARG; }
+    return c->free_energy(F, Omega, mu);
+}
+
+int nm_propagate_dev(nm_ctx* ctx, double* G_in_dev, const double* G1_dev, double* G_out_dev) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c || !G_in_dev || !G_out_dev) { nm::set_error("nm_propagate_dev: null argument"); return NM_ERR_ARG; }
+    c->launch_prop(G_in_dev, G1_dev, G_out_dev);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) { nm::set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
+    return NM_OK;
+}
+
+int nm_side_dev(nm_ctx* ctx, const double* X_dev, double* X_side_dev) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c || !X_dev || !X_side_dev) { nm::set_error("nm_side_dev: null argument"); return NM_ERR_ARG; }
+    c->launch_prop(X_dev, nullptr, X_side_dev);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) { nm::set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
+    return NM_OK;
+}
+
+long long nm_ctx_launch_count(nm_ctx* ctx) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    return c ? c->launches : 0;
+}
+
+}  // extern "C"

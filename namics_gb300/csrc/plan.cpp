@@ -1,0 +1,859 @@
+// Host-side problem compiler: Namics input text -> nm_plan.
+//
+// Replaces the object construction and the Check/Prepare steps that the
+// reference runs before its SCF loop (namics.cpp:165-417; Lattice::CheckInput
+// lattice.cpp:267-601, AllocateMemory :79-234; Segment::ParseFreedoms
+// segment.cpp:156-792; Molecule::Decomposition molecule.cpp:1282-1779;
+// System::CheckChi_values, generate_mask, MakeItsLists system.cpp:190-500).
+// Only the key subset an SCF solve of the supported problem classes needs is
+// understood; anything else is reported, never silently ignored when it
+// would change the result.
+#include "plan_internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+namespace nm {
+
+thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+namespace {
+
+const double PIE = 3.14159265;  // namics.cpp:49 (the reference's truncated pi)
+
+std::string trim(const std::string& s) {
+    size_t a = s.find_first_not_of(" \t\r\n");
+    if (a == std::string::npos) return "";
+    size_t b = s.find_last_not_of(" \t\r\n");
+    return s.substr(a, b - a + 1);
+}
+
+std::vector<std::string> split(const std::string& s, char c) {
+    std::vector<std::string> out;
+    std::string cur;
+    for (char ch : s) {
+        if (ch == c) { out.push_back(cur); cur.clear(); }
+        else cur.push_back(ch);
+    }
+    out.push_back(cur);
+    return out;
+}
+
+struct Entry { std::string cls, name, key, value; };
+
+// Keyed view of one `start` block of the input (input.cpp:3-78).
+struct InputBlock {
+    std::vector<Entry> entries;
+    std::vector<std::string> order(const std::string& cls) const {
+        std::vector<std::string> names;
+        for (auto& e : entries)
+            if (e.cls == cls && std::find(names.begin(), names.end(), e.name) == names.end())
+                names.push_back(e.name);
+        return names;
+    }
+    bool has(const std::string& cls, const std::string& name, const std::string& key) const {
+        for (auto& e : entries) if (e.cls == cls && e.name == name && e.key == key) return true;
+        return false;
+    }
+    std::string get(const std::string& cls, const std::string& name, const std::string& key,
+                    const std::string& dflt = "") const {
+        std::string v = dflt;  // last occurrence wins
+        for (auto& e : entries) if (e.cls == cls && e.name == name && e.key == key) v = e.value;
+        return v;
+    }
+};
+
+bool parse_input(const std::string& text, InputBlock& blk) {
+    std::istringstream is(text);
+    std::string line;
+    while (std::getline(is, line)) {
+        size_t c = line.find("//");
+        if (c != std::string::npos) line = line.substr(0, c);
+        line = trim(line);
+        if (line.empty()) continue;
+        if (line == "start") break;  // first start block only
+        std::vector<std::string> p = split(line, ':');
+        if (p.size() < 4) {
+            set_error("input line not of the form 'class : name : key : value': " + line);
+            return false;
+        }
+        Entry e;
+        e.cls = trim(p[0]); e.name = trim(p[1]); e.key = trim(p[2]);
+        std::string v = p[3];
+        for (size_t i = 4; i < p.size(); i++) v += ":" + p[i];
+        e.value = trim(v);
+        blk.entries.push_back(e);
+    }
+    return true;
+}
+
+bool to_int(const std::string& s, int& v) {
+    char* end = nullptr;
+    long r = std::strtol(s.c_str(), &end, 10);
+    if (end == s.c_str() || *end != '\0') return false;
+    v = (int)r;
+    return true;
+}
+
+bool to_real(const std::string& s, double& v) {
+    char* end = nullptr;
+    double r = std::strtod(s.c_str(), &end);
+    if (end == s.c_str() || *end != '\0') return false;
+    v = r;
+    return true;
+}
+
+int bc_code(const std::string& s, bool& ok) {
+    if (s == "mirror") return NM_BC_MIRROR;
+    if (s == "periodic") return NM_BC_PERIODIC;
+    if (s == "surface") return NM_BC_SURFACE;
+    ok = false;
+    return 0;
+}
+
+// ---- composition grammar -------------------------------------------------
+// A written chain is a list of items: runs `(name)count`, repeated groups
+// `((...)...)count` and side chains `[...]` attached to the segment written
+// just before the bracket (molecule.cpp:1156-1275, mol_branched.cpp).
+
+struct SegNode {  // one segment of the written molecule
+    int seg;
+    int parent = -1;               // towards the root
+    std::vector<int> children;
+};
+
+struct CompParser {
+    const std::string& s;
+    size_t pos = 0;
+    const std::map<std::string, int>& segidx;
+    std::string err;
+    CompParser(const std::string& s_, const std::map<std::string, int>& m) : s(s_), segidx(m) {}
+
+    bool read_int(int& v) {
+        size_t st = pos;
+        while (pos < s.size() && isdigit((unsigned char)s[pos])) pos++;
+        if (st == pos) return false;
+        v = std::atoi(s.substr(st, pos - st).c_str());
+        return true;
+    }
+    // parse a chain until ']' or end; emits a flat token list where
+    // side chains are nested vectors.
+    struct Item { int seg = -1; int count = 0; std::vector<Item> side; bool is_side = false; };
+
+    bool parse_chain(std::vector<Item>& out, bool inside_bracket) {
+        while (pos < s.size()) {
+            char c = s[pos];
+            if (c == ' ') { pos++; continue; }
+            if (c == ']') {
+                if (!inside_bracket) { err = "unbalanced ']'"; return false; }
+                return true;
+            }
+            if (c == '[') {
+                pos++;
+                Item side; side.is_side = true;
+                if (!parse_chain(side.side, true)) return false;
+                if (pos >= s.size() || s[pos] != ']') { err = "missing ']'"; return false; }
+                pos++;
+                out.push_back(side);
+                continue;
+            }
+            if (c == '(') {
+                // find matching ')'
+                int depth = 0; size_t q = pos;
+                for (; q < s.size(); q++) {
+                    if (s[q] == '(') depth++;
+                    else if (s[q] == ')') { depth--; if (depth == 0) break; }
+                }
+                if (q >= s.size()) { err = "unbalanced '('"; return false; }
+                std::string inner = s.substr(pos + 1, q - pos - 1);
+                pos = q + 1;
+                int cnt;
+                if (!read_int(cnt) || cnt < 1) { err = "repeat count expected after ')'"; return false; }
+                if (inner.find('(') != std::string::npos || inner.find('[') != std::string::npos) {
+                    // repeated group: expand
+                    CompParser sub(inner, segidx);
+                    std::vector<Item> grp;
+                    if (!sub.parse_chain(grp, false)) { err = sub.err; return false; }
+                    for (int r = 0; r < cnt; r++) out.insert(out.end(), grp.begin(), grp.end());
+                } else {
+                    auto it = segidx.find(trim(inner));
+                    if (it == segidx.end()) { err = "segment '" + inner + "' in composition is not a mon"; return false; }
+                    Item run; run.seg = it->second; run.count = cnt;
+                    out.push_back(run);
+                }
+                continue;
+            }
+            err = std::string("unexpected character '") + c + "' in composition";
+            return false;
+        }
+        return true;
+    }
+};
+
+// Emit segment nodes for a parsed chain.  Returns false on grammar errors.
+bool emit_chain(const std::vector<CompParser::Item>& items, std::vector<SegNode>& nodes,
+                int attach, std::vector<int>& chain_order, std::string& err) {
+    int prev = attach;  // segment the next one bonds to
+    for (auto& it : items) {
+        if (it.is_side) {
+            if (prev < 0) { err = "side chain '[' before any segment"; return false; }
+            if (!emit_chain(it.side, nodes, prev, chain_order, err)) return false;
+            continue;  // the main chain continues from `prev`
+        }
+        for (int k = 0; k < it.count; k++) {
+            SegNode n; n.seg = it.seg;
+            nodes.push_back(n);
+            int id = (int)nodes.size() - 1;
+            chain_order.push_back(id);
+            if (prev >= 0) {
+                // bond prev -- id (direction fixed later)
+                nodes[id].parent = prev;
+            }
+            prev = id;
+        }
+    }
+    return true;
+}
+
+}  // namespace
+
+// Turn an undirected written tree (parent = previous written segment) into a
+// rooted tree at `root` and compress it into blocks.
+static bool build_blocks_from_tree(std::vector<SegNode>& nodes, int root, PlanHolder& H,
+                                   MolBuild& mb, std::string& err) {
+    int n = (int)nodes.size();
+    std::vector<std::vector<int>> adj(n);
+    for (int i = 0; i < n; i++)
+        if (nodes[i].parent >= 0) { adj[i].push_back(nodes[i].parent); adj[nodes[i].parent].push_back(i); }
+    // BFS from root to orient
+    std::vector<int> par(n, -2), order;
+    order.reserve(n);
+    par[root] = -1; order.push_back(root);
+    for (size_t q = 0; q < order.size(); q++) {
+        int u = order[q];
+        for (int v : adj[u]) if (par[v] == -2) { par[v] = u; order.push_back(v); }
+    }
+    if ((int)order.size() != n) { err = "composition is not connected"; return false; }
+    std::vector<std::vector<int>> ch(n);
+    // children in written order (stable): iterate nodes in index order
+    for (int i = 0; i < n; i++) if (par[i] >= 0) ch[par[i]].push_back(i);
+    // block starts: segment with !=1 children, or whose single child differs in type
+    std::vector<int> blk_of(n, -1);
+    // build blocks root-ward from each start
+    struct TmpBlock { int seg; std::vector<int> segs; int parent_seg; };
+    std::vector<TmpBlock> tb;
+    for (int i = 0; i < n; i++) {
+        bool start = (ch[i].size() != 1) || (nodes[ch[i][0]].seg != nodes[i].seg);
+        if (!start) continue;
+        TmpBlock b; b.seg = nodes[i].seg;
+        int cur = i;
+        b.segs.push_back(cur);
+        while (true) {
+            int p = par[cur];
+            if (p < 0) break;
+            if (ch[p].size() != 1 || nodes[p].seg != b.seg) break;
+            cur = p;
+            b.segs.push_back(cur);
+        }
+        b.parent_seg = par[cur];
+        for (int sgi : b.segs) blk_of[sgi] = (int)tb.size();
+        tb.push_back(b);
+    }
+    for (int i = 0; i < n; i++) if (blk_of[i] < 0) { err = "internal: block cover"; return false; }
+    int nb = (int)tb.size();
+    std::vector<int> bparent(nb, -1);
+    std::vector<std::vector<int>> bchildren(nb);
+    int broot = blk_of[root];
+    for (int b = 0; b < nb; b++) {
+        if (tb[b].parent_seg >= 0) {
+            int pb = blk_of[tb[b].parent_seg];
+            // children must attach at the parent block's first segment
+            if (tb[pb].segs.front() != tb[b].parent_seg) { err = "internal: join not at block start"; return false; }
+            bparent[b] = pb;
+        }
+    }
+    // children order: by the written index of the child block's top segment
+    for (int b = 0; b < nb; b++) if (bparent[b] >= 0) bchildren[bparent[b]].push_back(b);
+    // post-order numbering
+    std::vector<int> post;
+    std::vector<std::pair<int, int>> stack;
+    stack.push_back({broot, 0});
+    while (!stack.empty()) {
+        auto& top = stack.back();
+        if (top.second < (int)bchildren[top.first].size()) {
+            int c = bchildren[top.first][top.second++];
+            stack.push_back({c, 0});
+        } else {
+            post.push_back(top.first);
+            stack.pop_back();
+        }
+    }
+    std::vector<int> newid(nb);
+    for (int i = 0; i < nb; i++) newid[post[i]] = i;
+    int s = 0;
+    mb.blocks.resize(nb);
+    for (int i = 0; i < nb; i++) {
+        int b = post[i];
+        nm_block& B = mb.blocks[i];
+        B.seg = tb[b].seg;
+        B.length = (int)tb[b].segs.size();
+        B.s0 = s; s += B.length;
+        B.parent = bparent[b] >= 0 ? newid[bparent[b]] : -1;
+        B.mult = 1;
+        B.degeneracy = 1.0;
+        B.n_child = (int)bchildren[b].size();
+        B.child0 = (int)mb.child_index.size();
+        for (int c : bchildren[b]) mb.child_index.push_back(newid[c]);
+        B.molmon = -1;
+    }
+    mb.n_store = s;
+    (void)H;
+    return true;
+}
+
+// Symmetric dendrimer `@dend(A,(B)2,3; A,(B)2,3)`: generations separated by
+// ';', each `bp,(arm),n_arm` (molecule.cpp:1437-1560, mol_dendrimer.cpp).
+static bool build_dendrimer(const std::string& body, const std::map<std::string, int>& segidx,
+                            MolBuild& mb, std::string& err) {
+    std::vector<std::string> gens = split(body, ';');
+    struct Gen { int bp; std::vector<std::pair<int, int>> arm; int n_arm; };
+    std::vector<Gen> G;
+    for (auto& g : gens) {
+        std::vector<std::string> a = split(trim(g), ',');
+        if (a.size() != 3) { err = "only symmetric dendrimers '@dend(bp,(arm)n,f;...)' are supported"; return false; }
+        Gen gg;
+        auto it = segidx.find(trim(a[0]));
+        if (it == segidx.end()) { err = "dendrimer branch point '" + a[0] + "' is not a mon"; return false; }
+        gg.bp = it->second;
+        CompParser cp(trim(a[1]), segidx);
+        std::vector<CompParser::Item> items;
+        if (!cp.parse_chain(items, false)) { err = cp.err; return false; }
+        for (auto& itm : items) {
+            if (itm.is_side) { err = "side chains inside dendrimer arms are not supported"; return false; }
+            gg.arm.push_back({itm.seg, itm.count});
+        }
+        if (!to_int(trim(a[2]), gg.n_arm) || gg.n_arm < 1) { err = "dendrimer functionality must be a positive integer"; return false; }
+        G.push_back(gg);
+    }
+    // Tree (root = core bp of generation 0).  Per generation g: bp_g, then
+    // the arm runs written from bp outward; the next generation's bp is
+    // bonded to the arm's last run.  Blocks in post-order: outermost first.
+    // Build top-down list first, then number in post-order (reverse of the
+    // top-down chain since every level has a single child group).
+    struct TB { int seg, len, mult; double d; };
+    std::vector<TB> chain;  // root-first
+    double d = 1.0;
+    for (size_t g = 0; g < G.size(); g++) {
+        chain.push_back({G[g].bp, 1, 1, d});
+        d *= G[g].n_arm;
+        for (size_t r = 0; r < G[g].arm.size(); r++)
+            chain.push_back({G[g].arm[r].first, G[g].arm[r].second, r == 0 ? G[g].n_arm : 1, d});
+    }
+    // chain[0] is root; chain[i+1] is the child of chain[i].  Merge nothing
+    // (runs of equal type across a bp are kept separate: the bp is a join).
+    int nb = (int)chain.size();
+    mb.blocks.resize(nb);
+    int s = 0;
+    for (int i = 0; i < nb; i++) {
+        // post-order index i corresponds to chain[nb-1-i]
+        const TB& t = chain[nb - 1 - i];
+        nm_block& B = mb.blocks[i];
+        B.seg = t.seg; B.length = t.len; B.s0 = s; s += t.len;
+        B.parent = (i == nb - 1) ? -1 : i + 1;
+        B.mult = t.mult;
+        B.degeneracy = t.d;
+        B.n_child = (i == 0) ? 0 : 1;
+        B.child0 = (int)mb.child_index.size();
+        if (i > 0) mb.child_index.push_back(i - 1);
+        B.molmon = -1;
+    }
+    mb.n_store = s;
+    return true;
+}
+
+static bool parse_range_coord(const std::string& tok, int axis, int nl, bool frozen,
+                              const int bc_low, const int bc_high, int& v, std::string& err) {
+    std::string t = trim(tok);
+    if (t == "firstlayer") { v = 1; return true; }
+    if (t == "lastlayer") { v = nl; return true; }
+    if (t == "lowerbound") {
+        if (!frozen || bc_low != NM_BC_SURFACE) { err = "'lowerbound' in a range needs a frozen segment and a 'surface' boundary"; return false; }
+        v = 0; return true;
+    }
+    if (t == "upperbound") {
+        if (!frozen || bc_high != NM_BC_SURFACE) { err = "'upperbound' in a range needs a frozen segment and a 'surface' boundary"; return false; }
+        v = nl + 1; return true;
+    }
+    if (!to_int(t, v)) { err = "range coordinate '" + t + "' not understood"; return false; }
+    if (v < 0 || v > nl + 1) { err = "range coordinate out of bounds"; return false; }
+    (void)axis;
+    return true;
+}
+
+// pinned_range / frozen_range -> MASK (segment.cpp:248-500, LGrad*::CreateMASK)
+static bool make_range_mask(const PlanHolder& H, const std::string& range_in, bool frozen,
+                            std::vector<double>& mask, std::string& err) {
+    const nm_plan& P = H.plan;
+    int g = P.gradients;
+    int nl[3] = {P.MX, P.MY, P.MZ};
+    std::string range = trim(range_in);
+    // single keyword forms
+    auto kw = [&](const std::string& k) -> std::string {
+        std::string axes[3] = {"_x", "_y", "_z"};
+        for (int a = 0; a < 3; a++) {
+            if (k == "firstlayer" + axes[a] || k == "lastlayer" + axes[a] ||
+                k == "lowerbound" + axes[a] || k == "upperbound" + axes[a]) {
+                std::string base = k.substr(0, k.size() - 2);
+                std::vector<std::string> lo(g), hi(g);
+                for (int b = 0; b < g; b++) {
+                    if (b == a) { lo[b] = base; hi[b] = base; }
+                    else { lo[b] = "1"; hi[b] = std::to_string(nl[b]); }
+                }
+                std::string r;
+                for (int b = 0; b < g; b++) r += (b ? "," : "") + lo[b];
+                r += ";";
+                for (int b = 0; b < g; b++) r += (b ? "," : "") + hi[b];
+                return r;
+            }
+        }
+        return "";
+    };
+    if (range.find(';') == std::string::npos) {
+        std::string r = kw(range);
+        if (r.empty()) r = kw(range + "_x");
+        if (r.empty()) { err = "range '" + range + "' not understood"; return false; }
+        range = r;
+    }
+    std::vector<std::string> ends = split(range, ';');
+    if (ends.size() != 2) { err = "range must be 'lo;hi'"; return false; }
+    std::vector<std::string> lo = split(ends[0], ','), hi = split(ends[1], ',');
+    if ((int)lo.size() != g || (int)hi.size() != g) {
+        // reference expands a single keyword coordinate of the first axis
+        if ((int)lo.size() == 1 && (int)hi.size() == 1 && g > 1) {
+            std::string r = kw(trim(lo[0]) + "_x");
+            if (r.empty()) { err = "range needs one coordinate per gradient"; return false; }
+            ends = split(r, ';'); lo = split(ends[0], ','); hi = split(ends[1], ',');
+        } else { err = "range needs one coordinate per gradient"; return false; }
+    }
+    int a[3] = {0, 0, 0}, b[3] = {0, 0, 0};
+    for (int d = 0; d < g; d++) {
+        if (!parse_range_coord(lo[d], d, nl[d], frozen, P.bc[d], P.bc[d + 3], a[d], err)) return false;
+        if (!parse_range_coord(hi[d], d, nl[d], frozen, P.bc[d], P.bc[d + 3], b[d], err)) return false;
+        if (a[d] > b[d]) { err = "range lower corner above upper corner"; return false; }
+    }
+    mask.assign(P.M, 0.0);
+    for (int x = a[0]; x <= b[0]; x++)
+        for (int y = (g > 1 ? a[1] : 0); y <= (g > 1 ? b[1] : 0); y++)
+            for (int z = (g > 2 ? a[2] : 0); z <= (g > 2 ? b[2] : 0); z++)
+                mask[x * P.JX + y * P.JY + z] = 1.0;
+    return true;
+}
+
+static bool setup_lattice(const InputBlock& in, PlanHolder& H, std::string& err) {
+    nm_plan& P = H.plan;
+    auto lats = in.order("lat");
+    if (lats.size() != 1) { err = "exactly one 'lat' is required"; return false; }
+    std::string ln = lats[0];
+    auto get = [&](const char* k, const char* d = "") { return in.get("lat", ln, k, d); };
+    int g = 1;
+    if (!to_int(get("gradients", "1"), g) || g < 1 || g > 3) { err = "lat gradients must be 1..3"; return false; }
+    P.gradients = g;
+    std::string lt = get("lattice_type");
+    if (lt == "simple_cubic") { P.lattice_type = NM_SIMPLE_CUBIC; P.lambda = 1.0 / 6.0; }
+    else if (lt == "hexagonal") { P.lattice_type = NM_HEXAGONAL; P.lambda = 1.0 / 4.0; }
+    else { err = "lat lattice_type must be simple_cubic or hexagonal"; return false; }
+    std::string geo = get("geometry", "planar");
+    if (geo == "flat" || geo == "planar") P.geometry = NM_PLANAR;
+    else if (geo == "cylindrical") P.geometry = NM_CYLINDRICAL;
+    else if (geo == "spherical") P.geometry = NM_SPHERICAL;
+    else { err = "lat geometry not understood"; return false; }
+    if (in.has("lat", ln, "FJC_choices") || in.has("lat", ln, "b/l")) {
+        std::string v = in.has("lat", ln, "b/l") ? get("b/l") : get("FJC_choices");
+        if (v != "1" && v != "3") { err = "FJC_choices > 3 (fjc > 1) is not supported"; return false; }
+    }
+    if (in.has("lat", ln, "Markov") && get("Markov") != "1") { err = "Markov 2 chains are not supported"; return false; }
+    P.stencil_full = 1;
+    if (in.has("lat", ln, "stencil_full")) {
+        std::string v = get("stencil_full");
+        P.stencil_full = (v == "true" || v == "TRUE" || v == "1") ? 1 : 0;
+    }
+    if (!P.stencil_full) { err = "stencil_full : false is not supported"; return false; }
+    P.offset_first_layer = 0;
+    if (P.geometry != NM_PLANAR) {
+        double o = 0; to_real(get("offset_first_layer", "0"), o);
+        if (o < 0) o = 0;
+        P.offset_first_layer = o;
+    }
+    P.bond_length = 0;
+    if (in.has("lat", ln, "bondlength")) to_real(get("bondlength"), P.bond_length);
+    bool ok = true;
+    P.MX = P.MY = P.MZ = 0;
+    for (int i = 0; i < 6; i++) P.bc[i] = NM_BC_MIRROR;
+    if (g == 1) {
+        if (!to_int(get("n_layers"), P.MX) || P.MX < 1) { err = "lat n_layers required"; return false; }
+        if (in.has("lat", ln, "lowerbound")) P.bc[0] = bc_code(get("lowerbound"), ok);
+        if (in.has("lat", ln, "upperbound")) P.bc[3] = bc_code(get("upperbound"), ok);
+        P.JX = 1; P.JY = 0; P.M = P.MX + 2;
+    } else {
+        if (!to_int(get("n_layers_x"), P.MX) || P.MX < 1) { err = "lat n_layers_x required"; return false; }
+        if (!to_int(get("n_layers_y"), P.MY) || P.MY < 1) { err = "lat n_layers_y required"; return false; }
+        const char* lk[3] = {"lowerbound_x", "lowerbound_y", "lowerbound_z"};
+        const char* uk[3] = {"upperbound_x", "upperbound_y", "upperbound_z"};
+        for (int d = 0; d < g; d++) {
+            if (in.has("lat", ln, lk[d])) P.bc[d] = bc_code(get(lk[d]), ok);
+            if (in.has("lat", ln, uk[d])) P.bc[d + 3] = bc_code(get(uk[d]), ok);
+        }
+        if (g == 2) {
+            if (P.geometry == NM_SPHERICAL) { err = "spherical geometry needs 1 gradient"; return false; }
+            P.JX = P.MY + 2; P.JY = 1; P.M = (P.MX + 2) * (P.MY + 2);
+        } else {
+            if (!to_int(get("n_layers_z"), P.MZ) || P.MZ < 1) { err = "lat n_layers_z required"; return false; }
+            if (P.geometry != NM_PLANAR) { err = "3 gradients need planar geometry"; return false; }
+            for (int d = 0; d < 6; d++)
+                if (P.bc[d] == NM_BC_SURFACE) { err = "3-gradient lattices take mirror or periodic bounds"; return false; }
+            P.JX = (P.MY + 2) * (P.MZ + 2); P.JY = P.MZ + 2; P.M = (P.MX + 2) * (P.MY + 2) * (P.MZ + 2);
+        }
+    }
+    if (!ok) { err = "boundary condition not understood (mirror, periodic, surface)"; return false; }
+    for (int d = 0; d < 3; d++)
+        if ((P.bc[d] == NM_BC_PERIODIC) != (P.bc[d + 3] == NM_BC_PERIODIC)) {
+            err = "a periodic boundary must be set on both sides"; return false;
+        }
+    // curvature weights (LGrad1.cpp:16-70 for 1 gradient, LGrad2.cpp:13-50 for 2)
+    int M = P.M;
+    H.L.assign(M, 0.0);
+    if (P.geometry == NM_PLANAR) {
+        if (g == 1) for (int i = 1; i <= P.MX; i++) H.L[i] = 1.0;   // LG1Planar.cpp:11-12
+        else for (int i = 0; i < M; i++) H.L[i] = 1.0;              // LG2Planar.cpp:16-19 (3-D: unused)
+        P.lambda_1 = P.lambda0 = P.lambda1 = nullptr;
+    } else {
+        H.lm1.assign(M, 0.0); H.l0.assign(M, 0.0); H.lp1.assign(M, 0.0);
+        double lam = P.lambda;
+        int ny = (g == 2) ? P.MY : 1;
+        for (int x = 1; x <= P.MX; x++)
+            for (int yy = 1; yy <= ny; yy++) {
+                int i = (g == 2) ? x * P.JX + yy : x;
+                double r = P.offset_first_layer + 1.0 * x;
+                if (P.geometry == NM_CYLINDRICAL) {
+                    H.L[i] = PIE * (std::pow(r, 2) - std::pow(r - 1, 2));
+                    H.lp1[i] = 2.0 * PIE * r / H.L[i] * lam;
+                    H.lm1[i] = 2.0 * PIE * (r - 1) / H.L[i] * lam;
+                    H.l0[i] = 1.0 - 2.0 * lam;
+                } else {
+                    H.L[i] = 4.0 / 3.0 * PIE * (std::pow(r, 3) - std::pow(r - 1, 3));
+                    H.lp1[i] = 4.0 * PIE * std::pow(r, 2) / H.L[i] * lam;
+                    H.lm1[i] = 4.0 * PIE * std::pow(r - 1, 2) / H.L[i] * lam;
+                    H.l0[i] = 1.0 - H.lp1[i] - H.lm1[i];
+                }
+            }
+        P.lambda_1 = H.lm1.data(); P.lambda0 = H.l0.data(); P.lambda1 = H.lp1.data();
+    }
+    P.L = H.L.data();
+    // volume (LGrad1.cpp PutM, LGrad2.cpp PutM, LGrad3.cpp PutM)
+    if (g == 1) {
+        if (P.geometry == NM_PLANAR) P.volume = P.MX;
+        else if (P.geometry == NM_SPHERICAL)
+            P.volume = 4.0 / 3.0 * PIE * (std::pow(P.MX + P.offset_first_layer, 3) - std::pow(P.offset_first_layer, 3));
+        else P.volume = PIE * (std::pow(P.MX + P.offset_first_layer, 2) - std::pow(P.offset_first_layer, 2));
+    } else if (g == 2) {
+        if (P.geometry == NM_CYLINDRICAL)
+            P.volume = P.MY * PIE * (std::pow(P.MX + P.offset_first_layer, 2) - std::pow(P.offset_first_layer, 2));
+        else P.volume = (double)P.MX * P.MY;
+    } else P.volume = (double)P.MX * P.MY * P.MZ;
+    return true;
+}
+
+static nm_plan* build_plan(const InputBlock& in, std::string& err) {
+    PlanHolder* H = new PlanHolder();
+    nm_plan& P = H->plan;
+    std::memset(&P, 0, sizeof(P));
+    if (!setup_lattice(in, *H, err)) { delete H; return nullptr; }
+    int M = P.M;
+    // ---- segments ----
+    H->seg_names = in.order("mon");
+    int ns = (int)H->seg_names.size();
+    if (ns < 1) { err = "at least one 'mon' is required"; delete H; return nullptr; }
+    std::map<std::string, int> segidx;
+    for (int i = 0; i < ns; i++) segidx[H->seg_names[i]] = i;
+    P.n_seg = ns;
+    H->seg_freedom.assign(ns, NM_SEG_FREE);
+    H->seg_valence.assign(ns, 0.0);
+    H->seg_epsilon.assign(ns, 80.0);
+    H->seg_mask.assign((size_t)ns * M, 0.0);
+    for (int i = 0; i < ns; i++) {
+        const std::string& nm_ = H->seg_names[i];
+        std::string fr = in.get("mon", nm_, "freedom", "free");
+        if (fr == "free") H->seg_freedom[i] = NM_SEG_FREE;
+        else if (fr == "pinned") H->seg_freedom[i] = NM_SEG_PINNED;
+        else if (fr == "frozen") H->seg_freedom[i] = NM_SEG_FROZEN;
+        else { err = "mon " + nm_ + " freedom '" + fr + "' is not supported (free, pinned, frozen)"; delete H; return nullptr; }
+        if (H->seg_freedom[i] != NM_SEG_FREE) {
+            const char* key = H->seg_freedom[i] == NM_SEG_PINNED ? "pinned_range" : "frozen_range";
+            if (!in.has("mon", nm_, key)) { err = "mon " + nm_ + " needs '" + key + "'"; delete H; return nullptr; }
+            std::vector<double> mask;
+            if (!make_range_mask(*H, in.get("mon", nm_, key), H->seg_freedom[i] == NM_SEG_FROZEN, mask, err)) {
+                err = "mon " + nm_ + ": " + err; delete H; return nullptr;
+            }
+            std::copy(mask.begin(), mask.end(), H->seg_mask.begin() + (size_t)i * M);
+        }
+        if (in.has("mon", nm_, "valence")) to_real(in.get("mon", nm_, "valence"), H->seg_valence[i]);
+        if (in.has("mon", nm_, "epsilon")) to_real(in.get("mon", nm_, "epsilon"), H->seg_epsilon[i]);
+        if (in.has("mon", nm_, "fluctuation_potentials") || in.has("mon", nm_, "state1")) {
+            err = "mon " + nm_ + ": external potentials / internal states are not supported"; delete H; return nullptr;
+        }
+    }
+    // chi (system.cpp CheckChi_values)
+    H->chi.assign((size_t)ns * ns, 123.0);
+    for (int i = 0; i < ns; i++)
+        for (int k = 0; k < ns; k++) {
+            std::string key = "chi_" + H->seg_names[k];
+            if (in.has("mon", H->seg_names[i], key)) {
+                double v;
+                if (!to_real(in.get("mon", H->seg_names[i], key), v)) { err = "chi value not a number"; delete H; return nullptr; }
+                H->chi[i * ns + k] = v;
+            }
+        }
+    for (int i = 0; i < ns; i++) for (int k = 0; k < ns; k++)
+        if (H->chi[i * ns + k] == 123.0) H->chi[i * ns + k] = H->chi[k * ns + i];
+    for (int i = 0; i < ns; i++) for (int k = 0; k < ns; k++)
+        if (H->chi[i * ns + k] == 123.0) H->chi[i * ns + k] = 0.0;
+    for (int i = 0; i < ns; i++) {
+        if (H->chi[i * ns + i] != 0) { err = "chi of a segment with itself must be zero"; delete H; return nullptr; }
+        for (int k = 0; k < ns; k++)
+            if (H->chi[i * ns + k] != H->chi[k * ns + i]) { err = "chi matrix must be symmetric"; delete H; return nullptr; }
+    }
+    // KSAM (system.cpp generate_mask): 0 where any frozen segment sits
+    H->ksam.assign(M, 1);
+    for (int i = 0; i < ns; i++)
+        if (H->seg_freedom[i] == NM_SEG_FROZEN)
+            for (int s = 0; s < M; s++) if (H->seg_mask[(size_t)i * M + s] != 0) H->ksam[s] = 0;
+    H->seg_gmask.assign((size_t)ns * M, 0.0);
+    H->seg_phi_frozen.assign((size_t)ns * M, 0.0);
+    for (int i = 0; i < ns; i++)
+        for (int s = 0; s < M; s++) {
+            double km = H->ksam[s];
+            if (H->seg_freedom[i] == NM_SEG_PINNED) H->seg_gmask[(size_t)i * M + s] = H->seg_mask[(size_t)i * M + s] * km;
+            else if (H->seg_freedom[i] == NM_SEG_FREE) H->seg_gmask[(size_t)i * M + s] = km;
+            else H->seg_phi_frozen[(size_t)i * M + s] = H->seg_mask[(size_t)i * M + s];
+        }
+    // surface bounds must be frozen (the halo layer is then a G = 0 wall)
+    for (int d = 0; d < P.gradients; d++)
+        for (int side = 0; side < 2; side++) {
+            if (P.bc[d + 3 * side] != NM_BC_SURFACE) continue;
+            int nl[3] = {P.MX, P.MY, P.MZ};
+            int layer = side ? nl[d] + 1 : 0;
+            // every non-corner site of that halo layer must carry KSAM = 0
+            int g = P.gradients;
+            for (int x = 1; x <= P.MX; x++)
+                for (int y = (g > 1 ? 1 : 0); y <= (g > 1 ? P.MY : 0); y++)
+                    for (int z = (g > 2 ? 1 : 0); z <= (g > 2 ? P.MZ : 0); z++) {
+                        int c[3] = {x, y, z};
+                        c[d] = layer;
+                        int s = c[0] * P.JX + c[1] * P.JY + c[2];
+                        if (H->ksam[s] != 0) {
+                            err = "a 'surface' boundary needs a frozen segment on its halo layer "
+                                  "(frozen_range : lowerbound / upperbound)";
+                            delete H; return nullptr;
+                        }
+                    }
+        }
+    // ---- molecules ----
+    auto molnames = in.order("mol");
+    int nmol = (int)molnames.size();
+    if (nmol < 1) { err = "at least one 'mol' is required"; delete H; return nullptr; }
+    H->mb.resize(nmol);
+    P.solvent = -1; P.neutralizer = -1;
+    for (int m = 0; m < nmol; m++) {
+        MolBuild& mb = H->mb[m];
+        const std::string& mn = molnames[m];
+        std::string comp = in.get("mol", mn, "composition");
+        if (comp.empty()) { err = "mol " + mn + " needs a composition"; delete H; return nullptr; }
+        if (comp.find('#') != std::string::npos) { err = "aliases in compositions are not supported"; delete H; return nullptr; }
+        std::string fr = in.get("mol", mn, "freedom");
+        if (fr == "free") mb.mol.freedom = NM_MOL_FREE;
+        else if (fr == "restricted") mb.mol.freedom = NM_MOL_RESTRICTED;
+        else if (fr == "solvent") { mb.mol.freedom = NM_MOL_SOLVENT; P.solvent = m; }
+        else if (fr == "neutralizer") { mb.mol.freedom = NM_MOL_NEUTRALIZER; P.neutralizer = m; }
+        else { err = "mol " + mn + " freedom '" + fr + "' is not supported"; delete H; return nullptr; }
+        if (mb.mol.freedom == NM_MOL_FREE) {
+            if (!in.has("mol", mn, "phibulk")) { err = "free mol " + mn + " needs phibulk"; delete H; return nullptr; }
+            to_real(in.get("mol", mn, "phibulk"), mb.mol.phibulk);
+        }
+        // parse composition
+        std::vector<std::string> order_seen;
+        if (comp.rfind("@dend(", 0) == 0) {
+            if (comp.back() != ')') { err = "dendrimer composition must end with ')'"; delete H; return nullptr; }
+            if (!build_dendrimer(comp.substr(6, comp.size() - 7), segidx, mb, err)) { delete H; return nullptr; }
+            mb.is_dendrimer = true;
+        } else if (comp[0] == '@') {
+            err = "composition keyword not supported (only @dend)"; delete H; return nullptr;
+        } else {
+            CompParser cp(comp, segidx);
+            std::vector<CompParser::Item> items;
+            if (!cp.parse_chain(items, false) || cp.pos != comp.size()) {
+                err = "mol " + mn + " composition: " + (cp.err.empty() ? "trailing text" : cp.err); delete H; return nullptr;
+            }
+            bool branched = comp.find('[') != std::string::npos;
+            std::vector<SegNode> nodes;
+            std::vector<int> written;
+            if (!emit_chain(items, nodes, -1, written, err)) { delete H; return nullptr; }
+            if (nodes.empty()) { err = "empty composition"; delete H; return nullptr; }
+            // reference roots: linear chains at the last written segment
+            // (mol_linear.cpp:113-131), branched ones at the first
+            // (molecule.cpp:1740-1766 reverses the numbering)
+            int root = branched ? written.front() : written.back();
+            if (!build_blocks_from_tree(nodes, root, *H, mb, err)) { delete H; return nullptr; }
+        }
+        // molmon list in written order of first appearance
+        {
+            std::vector<int> segs_in_order;
+            if (mb.is_dendrimer) {
+                // written order: generation by generation, bp then arm runs
+                for (int i = (int)mb.blocks.size() - 1; i >= 0; i--) segs_in_order.push_back(mb.blocks[i].seg);
+            } else {
+                // recover written order from the composition text
+                CompParser cp(comp, segidx);
+                std::vector<CompParser::Item> items;
+                cp.parse_chain(items, false);
+                std::function<void(const std::vector<CompParser::Item>&)> walk =
+                    [&](const std::vector<CompParser::Item>& v) {
+                        for (auto& it : v) { if (it.is_side) walk(it.side); else segs_in_order.push_back(it.seg); }
+                    };
+                walk(items);
+                // branched compositions are numbered back to front
+                // (molecule.cpp:1740-1766), and MolMonList follows that
+                // numbering (Molecule::MakeMonList, molecule.cpp:1785-1800)
+                if (comp.find('[') != std::string::npos)
+                    std::reverse(segs_in_order.begin(), segs_in_order.end());
+            }
+            for (int sgi : segs_in_order)
+                if (std::find(mb.molmon.begin(), mb.molmon.end(), sgi) == mb.molmon.end()) mb.molmon.push_back(sgi);
+        }
+        double N = 0;
+        for (auto& B : mb.blocks) N += B.length * B.degeneracy;
+        mb.mol.chainlength = N;
+        mb.fraction.assign(mb.molmon.size(), 0.0);
+        for (auto& B : mb.blocks) {
+            int k = (int)(std::find(mb.molmon.begin(), mb.molmon.end(), B.seg) - mb.molmon.begin());
+            B.molmon = k;
+            mb.fraction[k] += B.length * B.degeneracy;
+            if (H->seg_freedom[B.seg] == NM_SEG_FROZEN) { err = "frozen segment used in a molecule"; delete H; return nullptr; }
+            if (H->seg_freedom[B.seg] == NM_SEG_PINNED) mb.mol.pinned = 1;
+        }
+        for (auto& f : mb.fraction) f /= N;
+        mb.mol.charge = 0;
+        for (size_t k = 0; k < mb.molmon.size(); k++) mb.mol.charge += mb.fraction[k] * H->seg_valence[mb.molmon[k]];
+        if (mb.mol.freedom == NM_MOL_RESTRICTED) {
+            bool hn = in.has("mol", mn, "n"), ht = in.has("mol", mn, "theta");
+            if (hn == ht) { err = "restricted mol " + mn + " needs exactly one of n / theta"; delete H; return nullptr; }
+            if (hn) { to_real(in.get("mol", mn, "n"), mb.mol.n); mb.mol.theta = mb.mol.n * N; }
+            else { to_real(in.get("mol", mn, "theta"), mb.mol.theta); mb.mol.n = mb.mol.theta / N; }
+        }
+        if (mb.mol.pinned && mb.mol.freedom != NM_MOL_RESTRICTED) {
+            err = "mol " + mn + " with a pinned segment must be restricted"; delete H; return nullptr;
+        }
+        mb.mol.n_molmon = (int)mb.molmon.size();
+        mb.mol.n_blocks = (int)mb.blocks.size();
+        mb.mol.n_store = mb.n_store;
+    }
+    // solvent rules (system.cpp CheckInput)
+    if (P.solvent < 0) {
+        if (!(nmol == 1 && H->mb[0].mol.pinned)) { err = "one molecule must have freedom : solvent"; delete H; return nullptr; }
+    }
+    // ---- iteration list (MakeItsLists / IsUnique, system.cpp:430-500, 1218+) ----
+    H->seg_it.assign(ns, -1);
+    std::vector<int> sysmon;
+    for (int m = 0; m < nmol; m++)
+        for (int sgi : H->mb[m].molmon) {
+            if (std::find(sysmon.begin(), sysmon.end(), sgi) != sysmon.end()) continue;
+            sysmon.push_back(sgi);
+            int copy_of = -1;
+            for (size_t j = 0; j < H->it_seg.size() && copy_of < 0; j++) {
+                int r = H->it_seg[j];
+                bool eq = true;
+                for (int k = 0; k < ns; k++) if (H->chi[sgi * ns + k] != H->chi[r * ns + k]) { eq = false; break; }
+                if (eq) copy_of = (int)j;
+            }
+            if (copy_of < 0) { H->seg_it[sgi] = (int)H->it_seg.size(); H->it_seg.push_back(sgi); }
+            else H->seg_it[sgi] = copy_of;
+        }
+    P.n_it = (int)H->it_seg.size();
+    P.charged = 0;
+    for (int i = 0; i < ns; i++) if (H->seg_valence[i] != 0) P.charged = 1;
+    P.iv = P.n_it * M + (P.charged ? M : 0);
+    // ---- newton ----
+    auto newt = in.order("newton");
+    P.diis_m = 10; P.iterationlimit = 1000; P.tolerance = 1e-7; P.deltamax = 0.1; P.max_norm = 0;
+    if (!newt.empty()) {
+        const std::string& nn = newt[0];
+        std::string meth = in.get("newton", nn, "method", "DIIS");
+        if (meth != "DIIS") H->method_note = "newton method '" + meth + "' replaced by DIIS";
+        double v; int iv;
+        if (in.has("newton", nn, "tolerance") && to_real(in.get("newton", nn, "tolerance"), v)) P.tolerance = v;
+        if (in.has("newton", nn, "deltamax") && to_real(in.get("newton", nn, "deltamax"), v)) P.deltamax = v;
+        if (in.has("newton", nn, "m") && to_int(in.get("newton", nn, "m"), iv)) P.diis_m = iv;
+        if (in.has("newton", nn, "iterationlimit") && to_int(in.get("newton", nn, "iterationlimit"), iv)) P.iterationlimit = iv;
+        if (in.get("newton", nn, "stop_criterion") == "max_of_element_of_|g|") P.max_norm = 1;
+        if (P.diis_m < 1 || P.diis_m > 100) P.diis_m = 10;
+        if (P.iterationlimit < 0 || P.iterationlimit > 1000000) P.iterationlimit = 1000;
+    }
+    // ---- publish pointers ----
+    for (auto& s : H->seg_names) H->seg_name_ptrs.push_back(s.c_str());
+    P.seg_name = H->seg_name_ptrs.data();
+    P.seg_freedom = H->seg_freedom.data();
+    P.seg_it = H->seg_it.data();
+    P.seg_gmask = H->seg_gmask.data();
+    P.seg_phi_frozen = H->seg_phi_frozen.data();
+    P.chi = H->chi.data();
+    P.seg_valence = H->seg_valence.data();
+    P.seg_epsilon = H->seg_epsilon.data();
+    P.ksam = H->ksam.data();
+    P.it_seg = H->it_seg.data();
+    H->mols.resize(nmol);
+    for (int m = 0; m < nmol; m++) {
+        MolBuild& mb = H->mb[m];
+        mb.mol.molmon_seg = mb.molmon.data();
+        mb.mol.molmon_fraction = mb.fraction.data();
+        mb.mol.blocks = mb.blocks.data();
+        mb.mol.child_index = mb.child_index.data();
+        H->mols[m] = mb.mol;
+    }
+    P.n_mol = nmol;
+    P.mols = H->mols.data();
+    return &H->plan;
+}
+
+}  // namespace nm
+
+extern "C" {
+
+int nm_plan_create(const char* input_text, nm_plan** out) {
+    if (!input_text || !out) { nm::set_error("nm_plan_create: null argument"); return NM_ERR_ARG; }
+    *out = nullptr;
+    nm::InputBlock blk;
+    if (!nm::parse_input(input_text, blk)) return NM_ERR_INPUT;
+    std::string err;
+    nm_plan* p = nm::build_plan(blk, err);
+    if (!p) { nm::set_error(err); return NM_ERR_INPUT; }
+    *out = p;
+    return NM_OK;
+}
+
+void nm_plan_destroy(nm_plan* plan) {
+    if (plan) delete reinterpret_cast<nm::PlanHolder*>(plan);
+}
+
+const char* nm_last_error(void) { return nm::g_last_error.c_str(); }
+
+const char* nm_version(void) { return "namics_gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,792 @@
+/*
+ * CPU oracle for the Namics SCF hot path — TEST INFRASTRUCTURE ONLY
+ * (see scf_oracle.h).  A restatement of the reference algorithm in plain C.
+ * Each function names the reference code it follows (file:line into
+ * leermakers/Namics src/).  Arrays use the reference's padded flat layout
+ * and its flat-array stencil semantics (neighbour sums taken over the whole
+ * array, halo layers refreshed by set_bounds before each use), so halo
+ * contents evolve exactly as in the reference.
+ */
+#include "scf_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+struct orc_state {
+    const nm_plan* P;
+    int M;
+    int BX1, BXM, BY1, BYM, BZ1, BZM;
+    double *u, *G1, *phi, *phi_side, *phitot, *alpha, *tmp, *unity;
+    double *mol_phitot;
+    double **Gf, **rho, **jGb, **Pc, **Qb;
+    double *gb;
+    double *GN, *norm, *mol_n, *mol_theta, *mol_phibulk, *seg_phibulk;
+    int have_state;
+};
+
+/* ---- L0 primitives (tools_host.h:185-470) ------------------------------ */
+static void Zero(double* P, int M) { memset(P, 0, sizeof(double) * (size_t)M); }
+static void Cp(double* P, const double* A, int M) { memcpy(P, A, sizeof(double) * (size_t)M); }
+static void Times(double* P, const double* A, const double* B, int M) { for (int i = 0; i < M; i++) P[i] = A[i] * B[i]; }
+static void AddTimes(double* P, const double* A, const double* B, int M) { for (int i = 0; i < M; i++) P[i] += A[i] * B[i]; }
+static void YplusisCtimesX(double* Y, const double* X, double C, int M) { for (int i = 0; i < M; i++) Y[i] += C * X[i]; }
+static void Add(double* P, const double* A, int M) { for (int i = 0; i < M; i++) P[i] += A[i]; }
+static void Norm(double* P, double C, int M) { for (int i = 0; i < M; i++) P[i] *= C; }
+static double Sum(const double* X, int M) { double s = 0; for (int i = 0; i < M; i++) s += X[i]; return s; }
+static double Dot(const double* X, const double* Y, int M) { double s = 0; for (int i = 0; i < M; i++) s += X[i] * Y[i]; return s; }
+static void Div(double* P, const double* A, int M) { for (int i = 0; i < M; i++) { if (A[i] != 0) P[i] /= A[i]; else P[i] = 0; } }
+
+/* ---- boundaries -------------------------------------------------------- */
+/* Halo source layers per boundary type (lattice.cpp:94-196, fjc = 1). */
+static void bc_sources(orc_state* st) {
+    const nm_plan* P = st->P;
+    int n[3] = {P->MX, P->MY, P->MZ};
+    int lo[3], hi[3];
+    for (int d = 0; d < 3; d++) {
+        int bl = P->bc[d], bh = P->bc[d + 3];
+        lo[d] = bl == NM_BC_MIRROR ? 1 : bl == NM_BC_PERIODIC ? n[d] : 0;
+        hi[d] = bh == NM_BC_MIRROR ? n[d] : bh == NM_BC_PERIODIC ? 1 : n[d] + 1;
+    }
+    st->BX1 = lo[0]; st->BXM = hi[0];
+    st->BY1 = lo[1]; st->BYM = hi[1];
+    st->BZ1 = lo[2]; st->BZM = hi[2];
+}
+
+/* LGrad1.cpp:806-818, LGrad2.cpp:1652-1680, LGrad3.cpp:1549-1616 */
+static void set_bounds(orc_state* st, double* X) {
+    const nm_plan* P = st->P;
+    int MX = P->MX, MY = P->MY, MZ = P->MZ, JX = P->JX, JY = P->JY;
+    int BX1 = st->BX1, BXM = st->BXM, BY1 = st->BY1, BYM = st->BYM, BZ1 = st->BZ1, BZM = st->BZM;
+    if (P->gradients == 1) {
+        X[0] = X[BX1];
+        X[MX + 1] = X[BXM];
+    } else if (P->gradients == 2) {
+        for (int x = 1; x < MX + 1; x++) { X[x * JX + 0] = X[x * JX + BY1]; X[x * JX + MY + 1] = X[x * JX + BYM]; }
+        for (int y = 1; y < MY + 1; y++) { X[0 + y] = X[BX1 * JX + y]; X[(MX + 1) * JX + y] = X[BXM * JX + y]; }
+        X[0] = X[BY1];
+        X[MY + 1] = X[BYM];
+        X[(MX + 1) * JX + 0] = X[(MX + 1) * JX + BY1];
+        X[(MX + 1) * JX + MY + 1] = X[(MX + 1) * JX + BYM];
+    } else {
+        int x, y, z;
+        for (x = 1; x < MX + 1; x++) for (y = 1; y < MY + 1; y++) {
+            X[x * JX + y * JY + 0] = X[x * JX + y * JY + BZ1];
+            X[x * JX + y * JY + MZ + 1] = X[x * JX + y * JY + BZM];
+        }
+        for (y = 1; y < MY + 1; y++) for (z = 1; z < MZ + 1; z++) {
+            X[0 + y * JY + z] = X[BX1 * JX + y * JY + z];
+            X[(MX + 1) * JX + y * JY + z] = X[BXM * JX + y * JY + z];
+        }
+        for (z = 1; z < MZ + 1; z++) for (x = 1; x < MX + 1; x++) {
+            X[x * JX + 0 + z] = X[x * JX + BY1 * JY + z];
+            X[x * JX + (MY + 1) * JY + z] = X[x * JX + BYM * JY + z];
+        }
+        x = 0;
+        for (y = 1; y < MY + 1; y++) { X[y * JY + 0] = X[y * JY + BZ1]; X[y * JY + MZ + 1] = X[y * JY + BZM]; }
+        for (z = 1; z < MZ + 1; z++) { X[0 + z] = X[BY1 * JY + z]; X[(MY + 1) * JY + z] = X[BYM * JY + z]; }
+        x = MX + 1;
+        for (y = 1; y < MY + 1; y++) { X[x * JX + y * JY + 0] = X[x * JX + y * JY + BZ1]; X[x * JX + y * JY + MZ + 1] = X[x * JX + y * JY + BZM]; }
+        for (z = 1; z < MZ + 1; z++) { X[x * JX + 0 + z] = X[x * JX + BY1 * JY + z]; X[x * JX + (MY + 1) * JY + z] = X[x * JX + BYM * JY + z]; }
+        y = 0;
+        for (x = 1; x < MX + 1; x++) { X[x * JX + 0] = X[x * JX + BZ1]; X[x * JX + MZ + 1] = X[x * JX + BZM]; }
+        y = MY + 1;
+        for (x = 1; x < MX + 1; x++) { X[x * JX + y * JY + 0] = X[x * JX + y * JY + BZ1]; X[x * JX + y * JY + MZ + 1] = X[x * JX + y * JY + BZM]; }
+        X[0] = X[BX1 * JX + BY1 * JY + BZ1];
+        X[(MX + 1) * JX] = X[BXM * JX + BY1 * JY + BZ1];
+        X[(MY + 1) * JY] = X[BX1 * JX + BYM * JY + BZ1];
+        X[MZ + 1] = X[BX1 * JX + BY1 * JY + BZM];
+        X[(MX + 1) * JX + (MY + 1) * JY] = X[BXM * JX + BYM * JY + BZ1];
+        X[(MX + 1) * JX + MZ + 1] = X[BXM * JX + BY1 * JY + BZM];
+        X[(MY + 1) * JY + MZ + 1] = X[BX1 * JX + BYM * JY + BZM];
+        X[(MX + 1) * JX + (MY + 1) * JY + MZ + 1] = X[BXM * JX + BYM * JY + BZM];
+    }
+}
+
+/* LGrad1.cpp:787-798, LGrad2.cpp remove_bounds, LGrad3.cpp:1521-1545 */
+static void remove_bounds(orc_state* st, double* X) {
+    const nm_plan* P = st->P;
+    int MX = P->MX, MY = P->MY, MZ = P->MZ, JX = P->JX, JY = P->JY;
+    if (P->gradients == 1) { X[0] = 0; X[MX + 1] = 0; return; }
+    if (P->gradients == 2) {
+        for (int x = 0; x < MX + 2; x++) { X[x * JX] = 0; X[x * JX + MY + 1] = 0; }
+        for (int y = 0; y < MY + 2; y++) { X[y] = 0; X[(MX + 1) * JX + y] = 0; }
+        return;
+    }
+    for (int y = 0; y < MY + 2; y++) for (int z = 0; z < MZ + 2; z++) { X[y * JY + z] = 0; X[(MX + 1) * JX + y * JY + z] = 0; }
+    for (int x = 0; x < MX + 2; x++) for (int z = 0; z < MZ + 2; z++) { X[x * JX + z] = 0; X[x * JX + (MY + 1) * JY + z] = 0; }
+    for (int x = 0; x < MX + 2; x++) for (int y = 0; y < MY + 2; y++) { X[x * JX + y * JY] = 0; X[x * JX + y * JY + MZ + 1] = 0; }
+}
+
+/* WeightedSum: LGrad1.cpp:213-221, LGrad2.cpp:147-157, LGrad3.cpp:40-46 */
+static double weighted_sum(orc_state* st, double* X) {
+    const nm_plan* P = st->P;
+    remove_bounds(st, X);
+    if (P->gradients == 3 || P->geometry == NM_PLANAR) return Sum(X, st->M);
+    return Dot(X, P->L, st->M);
+}
+
+/* ---- stencils ------------------------------------------------------------
+ * stencil(): the neighbour sum of Lattice::Side / Lattice::propagate, added
+ * into a zeroed gs (LG1Planar.cpp:28-55,138-159; LGrad1.cpp:251-281,432-454;
+ * LG2Planar.cpp:27-135,1039-1127; LGrad2.cpp:207-278,1053-1090;
+ * LGrad3.cpp:103-243,673-782).  side != 0 picks the Side() operation order. */
+static void stencil(orc_state* st, double* gs, const double* g, int side) {
+    const nm_plan* P = st->P;
+    int M = st->M, JX = P->JX, JY = P->JY;
+    double lam = P->lambda;
+    Zero(gs, M);
+    if (P->gradients == 1) {
+        if (P->geometry == NM_PLANAR) {
+            if (side) {
+                YplusisCtimesX(gs + 1, g, lam, M - 1);
+                YplusisCtimesX(gs, g + 1, lam, M - 1);
+                YplusisCtimesX(gs, g, 1.0 - 2.0 * lam, M);
+            } else {
+                YplusisCtimesX(gs + 1, g, lam, M - 1);
+                YplusisCtimesX(gs, g, 1.0 - 2.0 * lam, M);
+                YplusisCtimesX(gs, g + 1, lam, M - 1);
+            }
+        } else {
+            AddTimes(gs, g, P->lambda0, M);
+            AddTimes(gs + 1, g, P->lambda_1 + 1, M - 1);
+            AddTimes(gs, g + 1, P->lambda1, M - 1);
+        }
+        return;
+    }
+    if (P->gradients == 2) {
+        if (P->geometry == NM_PLANAR) {
+            if (P->lattice_type == NM_SIMPLE_CUBIC) {
+                double C1 = 16.0 / 36.0, C2 = 4.0 / 36.0, C3 = 1.0 / 36.0;
+                YplusisCtimesX(gs, g, C1, M);
+                YplusisCtimesX(gs + 1, g, C2, M - 1);
+                YplusisCtimesX(gs, g + 1, C2, M - 1);
+                YplusisCtimesX(gs + JX, g, C2, M - JX);
+                YplusisCtimesX(gs, g + JX, C2, M - JX);
+                YplusisCtimesX(gs + JX + 1, g, C3, M - JX - 1);
+                YplusisCtimesX(gs + JX, g + 1, C3, M - JX);
+                YplusisCtimesX(gs + 1, g + JX, C3, M - JX);
+                YplusisCtimesX(gs, g + JX + 1, C3, M - JX - 1);
+            } else {
+                double Two = 2.0, C = 1.0 / 16.0;
+                YplusisCtimesX(gs, g, Two, M);
+                Add(gs + JX, g, M - JX);
+                Add(gs, g + JX, M - JX);
+                Add(gs + JY, g, M - JY);
+                Add(gs, g + JY, M - JY);
+                Norm(gs, Two, M);
+                Add(gs + JX + JY, g, M - JX - JY);
+                Add(gs, g + JX + JY, M - JX - JY);
+                Add(gs + JX, g + JY, M - JX - JY);
+                Add(gs + JY, g + JX, M - JX - JY);
+                Norm(gs, C, M);
+            }
+        } else {
+            double C1, C2, C3;
+            if (P->lattice_type == NM_SIMPLE_CUBIC) { C1 = 4.0 / 6.0; C2 = 1.0 / 6.0; C3 = 4.0; }
+            else { C1 = 0.5; C2 = 0.25; C3 = 2.0; }
+            const double *l_1 = P->lambda_1, *l1 = P->lambda1;
+            YplusisCtimesX(gs, g, C1, M);
+            AddTimes(gs + JX, g, l_1 + JX, M - JX);
+            AddTimes(gs, g + JX, l1, M - JX);
+            YplusisCtimesX(gs + 1, g, C2, M - 1);
+            YplusisCtimesX(gs, g + 1, C2, M - 1);
+            Norm(gs, C3, M);
+            AddTimes(gs + JX + 1, g, l_1 + JX + 1, M - JX - 1);
+            AddTimes(gs + JX, g + 1, l_1 + JX, M - JX - 1);
+            AddTimes(gs + 1, g + JX, l1 + 1, M - JX - 1);
+            AddTimes(gs, g + JX + 1, l1, M - JX - 1);
+            Norm(gs, C2, M);
+        }
+        return;
+    }
+    /* 3 gradients, stencil_full */
+    if (P->lattice_type == NM_SIMPLE_CUBIC) {
+        Add(gs + JX, g, M - JX);
+        Add(gs, g + JX, M - JX);
+        Add(gs + JY, g, M - JY);
+        Add(gs, g + JY, M - JY);
+        Add(gs + 1, g, M - 1);
+        Add(gs, g + 1, M - 1);
+        Norm(gs, 1.0 / 6.0, M);
+    } else {
+        double Two = 2.0, C = 1.0 / 40.0;
+        YplusisCtimesX(gs, g, Two, M);
+        Add(gs + JX, g, M - JX);
+        Add(gs, g + JX, M - JX);
+        Add(gs + JY, g, M - JY);
+        Add(gs, g + JY, M - JY);
+        Add(gs + 1, g, M - 1);
+        Add(gs, g + 1, M - 1);
+        Norm(gs, Two, M);
+        Add(gs + JX + JY, g, M - JX - JY);
+        Add(gs, g + JX + JY, M - JX - JY);
+        Add(gs + JX, g + JY, M - JX - JY);
+        Add(gs + JY, g + JX, M - JX - JY);
+        Add(gs + JX + 1, g, M - JX - 1);
+        Add(gs + 1, g + JX, M - JX - 1);
+        Add(gs + JY + 1, g, M - JY - 1);
+        Add(gs + 1, g + JY, M - JY - 1);
+        Add(gs + JX, g + 1, M - JX - 1);
+        Add(gs, g + JX + 1, M - JX - 1);
+        Add(gs + JY, g + 1, M - JY - 1);
+        Add(gs, g + JY + 1, M - JY - 1);
+        Norm(gs, Two, M);
+        Add(gs + JX + JY + 1, g, M - JX - JY - 1);
+        Add(gs, g + JX + JY + 1, M - JX - JY - 1);
+        Add(gs + JX + JY, g + 1, M - JX - JY - 1);
+        Add(gs + 1, g + JX + JY, M - JX - JY - 1);
+        Add(gs + JX + 1, g + JY, M - JX - JY - 1);
+        Add(gs + JY, g + JX + 1, M - JX - JY - 1);
+        Add(gs + JY + 1, g + JX, M - JX - JY - 1);
+        Add(gs + JX, g + JY + 1, M - JX - JY - 1);
+        Norm(gs, C, M);
+    }
+}
+
+/* Lattice::propagate: Zero(gs); set_bounds(gs_1); stencil; Times(gs,G1). */
+static void propagate(orc_state* st, double* gs, double* gs_1, const double* G1) {
+    set_bounds(st, gs_1);
+    stencil(st, gs, gs_1, 0);
+    Times(gs, gs, G1, st->M);
+}
+
+void orc_propagate(orc_state* st, double* G_in, const double* G1, double* G_out) {
+    propagate(st, G_out, G_in, G1 ? G1 : st->unity);
+}
+
+void orc_side(orc_state* st, double* X, double* X_side) { stencil(st, X_side, X, 1); }
+
+/* ---- molecules ----------------------------------------------------------- */
+static int blk_last(const nm_block* B) { return B->s0 + B->length - 1; }
+
+/* Forward propagators of one molecule (Molecule::propagate_forward,
+ * molecule.cpp:2300-2362; joins as mol_branched.cpp:250-299 and
+ * mol_dendrimer.cpp:113-146).  A block's first segment joins its children:
+ * Gf = P(Gf[child_0])*G1 * prod_c [P(Gf[c])*UNITY]^(mult-...) . */
+static void mol_forward(orc_state* st, int m) {
+    const nm_plan* P = st->P;
+    const nm_molecule* mol = &P->mols[m];
+    int M = st->M;
+    double* Gf = st->Gf[m];
+    for (int b = 0; b < mol->n_blocks; b++) {
+        const nm_block* B = &mol->blocks[b];
+        const double* G1 = st->G1 + (size_t)B->seg * M;
+        int s = B->s0;
+        if (B->n_child == 0) {
+            Cp(Gf + (size_t)s * M, G1, M);  /* Initiate (LGrad1.cpp:943-949) */
+        } else {
+            /* every child's end propagator, once with UNITY, cached for the
+             * backward pass */
+            for (int c = 0; c < B->n_child; c++) {
+                int cb = mol->child_index[B->child0 + c];
+                propagate(st, st->Pc[m] + (size_t)cb * M, Gf + (size_t)blk_last(&mol->blocks[cb]) * M, st->unity);
+            }
+            int c0 = mol->child_index[B->child0];
+            const nm_block* C0 = &mol->blocks[c0];
+            double* out = Gf + (size_t)s * M;
+            propagate(st, out, Gf + (size_t)blk_last(C0) * M, G1);
+            for (int k = 1; k < C0->mult; k++) Times(out, out, st->Pc[m] + (size_t)c0 * M, M);
+            for (int c = 1; c < B->n_child; c++) {
+                int cb = mol->child_index[B->child0 + c];
+                for (int k = 0; k < mol->blocks[cb].mult; k++) Times(out, out, st->Pc[m] + (size_t)cb * M, M);
+            }
+        }
+        for (int k = 1; k < B->length; k++) {
+            s++;
+            propagate(st, Gf + (size_t)s * M, Gf + (size_t)(s - 1) * M, G1);
+        }
+    }
+    /* GN = ComputeGN(G_root) (LGrad1.cpp:863-874): WeightedSum, which clears
+     * the halo of the stored end propagator as a side effect. */
+    const nm_block* R = &mol->blocks[mol->n_blocks - 1];
+    st->GN[m] = weighted_sum(st, Gf + (size_t)blk_last(R) * M);
+}
+
+/* AddPhiS (LGrad1.cpp:876-922): rho += d*Gf*Gb */
+static void add_phi(double* rho, const double* Gf, const double* Gb, double d, int M) {
+    if (d == 1.0) AddTimes(rho, Gf, Gb, M);
+    else for (int i = 0; i < M; i++) rho[i] += d * Gf[i] * Gb[i];
+}
+
+/* Backward sweep of block b starting from Q (NULL for the root block):
+ * Molecule::propagate_backward (molecule.cpp:2364-2446), with the branch
+ * logic of mol_branched.cpp:170-248 and mol_dendrimer.cpp:148-184. */
+static void mol_backward_block(orc_state* st, int m, int b, double* Q) {
+    const nm_plan* P = st->P;
+    const nm_molecule* mol = &P->mols[m];
+    const nm_block* B = &mol->blocks[b];
+    int M = st->M;
+    const double* G1 = st->G1 + (size_t)B->seg * M;
+    double* rho = st->rho[m] + (size_t)B->molmon * M;
+    double* Gf = st->Gf[m];
+    double *cur = st->gb, *nxt = st->gb + M;
+    int s = blk_last(B);
+    if (!Q) Cp(cur, G1, M);
+    else propagate(st, cur, Q, G1);
+    add_phi(rho, Gf + (size_t)s * M, cur, B->degeneracy, M);
+    for (s = s - 1; s >= B->s0; s--) {
+        propagate(st, nxt, cur, G1);
+        double* t = cur; cur = nxt; nxt = t;
+        add_phi(rho, Gf + (size_t)s * M, cur, B->degeneracy, M);
+    }
+    if (B->n_child == 0) return;
+    double* jg = st->jGb[m] + (size_t)b * M;
+    Cp(jg, cur, M);
+    for (int c = 0; c < B->n_child; c++) {
+        int cb = mol->child_index[B->child0 + c];
+        double* q = st->Qb[m] + (size_t)cb * M;
+        Cp(q, jg, M);
+        for (int k = 1; k < mol->blocks[cb].mult; k++) Times(q, q, st->Pc[m] + (size_t)cb * M, M);
+        for (int o = 0; o < B->n_child; o++) {
+            if (o == c) continue;
+            int ob = mol->child_index[B->child0 + o];
+            for (int k = 0; k < mol->blocks[ob].mult; k++) Times(q, q, st->Pc[m] + (size_t)ob * M, M);
+        }
+        mol_backward_block(st, m, cb, q);
+    }
+}
+
+/* ---- residual ------------------------------------------------------------ */
+static int compute_phis(orc_state* st, const double* x) {
+    const nm_plan* P = st->P;
+    int M = st->M, ns = P->n_seg;
+    /* PutU (system.cpp:1987-2085) + Segment::PrepareForCalculations
+     * (segment.cpp:835-879): u = x[it(seg)], set_bounds(u), G1 = exp(-u),
+     * times MASK (pinned) and KSAM. */
+    for (int i = 0; i < ns; i++) {
+        double* u = st->u + (size_t)i * M;
+        double* G1 = st->G1 + (size_t)i * M;
+        if (P->seg_it[i] >= 0) Cp(u, x + (size_t)P->seg_it[i] * M, M);
+        else Zero(u, M);
+        set_bounds(st, u);
+        for (int s = 0; s < M; s++) G1[s] = exp(-u[s]);
+        if (P->seg_freedom[i] != NM_SEG_FROZEN) Times(G1, G1, P->seg_gmask + (size_t)i * M, M);
+        /* Segment phi: frozen -> MASK, else 0 */
+        Cp(st->phi + (size_t)i * M, P->seg_phi_frozen + (size_t)i * M, M);
+        st->seg_phibulk[i] = 0;
+    }
+    /* System::ComputePhis (system.cpp:2324-2640) */
+    Zero(st->phitot, M);
+    for (int i = 0; i < ns; i++)
+        if (P->seg_freedom[i] == NM_SEG_FROZEN) Add(st->phitot, st->phi + (size_t)i * M, M);
+    for (int m = 0; m < P->n_mol; m++) {
+        const nm_molecule* mol = &P->mols[m];
+        Zero(st->rho[m], mol->n_molmon * M);
+        Zero(st->mol_phitot + (size_t)m * M, M);
+        if (mol->n_store == 1 && mol->n_blocks == 1) {
+            /* monomer: Molecule::ComputePhi (molecule.cpp:2669-2683) */
+            const double* G1 = st->G1 + (size_t)mol->blocks[0].seg * M;
+            double* phi = st->rho[m];
+            Cp(phi, G1, M);
+            st->GN[m] = weighted_sum(st, phi);
+            Times(phi, phi, G1, M);
+        } else {
+            mol_forward(st, m);
+            mol_backward_block(st, m, mol->n_blocks - 1, NULL);
+        }
+    }
+    double A = 0, B = 0;
+    for (int m = 0; m < P->n_mol; m++) {
+        const nm_molecule* mol = &P->mols[m];
+        double N = mol->chainlength;
+        double norm = 0;
+        st->mol_n[m] = mol->n; st->mol_theta[m] = mol->theta;
+        if (mol->freedom == NM_MOL_FREE) {
+            st->mol_phibulk[m] = mol->phibulk;
+            norm = mol->phibulk / N;
+            st->mol_n[m] = norm * st->GN[m];
+            A += mol->phibulk * mol->charge; B += mol->phibulk;
+        } else if (mol->freedom == NM_MOL_RESTRICTED) {
+            if (st->GN[m] > 0) {
+                norm = mol->n / st->GN[m];
+                if (mol->pinned) st->mol_phibulk[m] = 0;
+                else {
+                    st->mol_phibulk[m] = N * norm;
+                    A += st->mol_phibulk[m] * mol->charge; B += st->mol_phibulk[m];
+                }
+            } else return NM_ERR_GN;
+        } else st->mol_phibulk[m] = 0;
+        st->norm[m] = norm;
+        for (int k = 0; k < mol->n_molmon; k++) {
+            double* phi = st->rho[m] + (size_t)k * M;
+            Div(phi, st->G1 + (size_t)mol->molmon_seg[k] * M, M);
+            if (norm > 0) Norm(phi, norm, M);
+        }
+    }
+    if (P->solvent >= 0) {
+        int sv = P->solvent;
+        const nm_molecule* mol = &P->mols[sv];
+        st->mol_phibulk[sv] = 1.0 - B;
+        if (st->mol_phibulk[sv] < 0) return NM_ERR_NEG_SOLVENT;
+        double norm = st->mol_phibulk[sv] / mol->chainlength;
+        st->mol_n[sv] = norm * st->GN[sv];
+        st->mol_theta[sv] = st->mol_n[sv] * mol->chainlength;
+        st->norm[sv] = norm;
+        for (int k = 0; k < mol->n_molmon; k++)
+            if (norm > 0) Norm(st->rho[sv] + (size_t)k * M, norm, M);
+    }
+    for (int m = 0; m < P->n_mol; m++) {
+        const nm_molecule* mol = &P->mols[m];
+        for (int k = 0; k < mol->n_molmon; k++) {
+            int sg = mol->molmon_seg[k];
+            double* pm = st->rho[m] + (size_t)k * M;
+            Add(st->phi + (size_t)sg * M, pm, M);
+            Add(st->phitot, pm, M);
+            Add(st->mol_phitot + (size_t)m * M, pm, M);
+            st->seg_phibulk[sg] += mol->molmon_fraction[k] * st->mol_phibulk[m];
+        }
+    }
+    for (int i = 0; i < ns; i++) set_bounds(st, st->phi + (size_t)i * M);
+    /* Segment::SetPhiSide (segment.cpp:1331-1353) */
+    for (int i = 0; i < ns; i++) stencil(st, st->phi_side + (size_t)i * M, st->phi + (size_t)i * M, 1);
+    return NM_OK;
+}
+
+int orc_residual(orc_state* st, const double* x, double* g) {
+    const nm_plan* P = st->P;
+    int M = st->M, ns = P->n_seg, nit = P->n_it;
+    if (P->charged) return NM_ERR_INPUT;
+    /* System::Classical_residual (system.cpp:2087-2189) */
+    Cp(g, x, P->iv);
+    int rc = compute_phis(st, x);
+    st->have_state = (rc == NM_OK);
+    if (rc) return rc;
+    Zero(st->alpha, M);
+    for (int i = 0; i < nit; i++) {
+        double* gi = g + (size_t)i * M;
+        int r = P->it_seg[i];
+        for (int k = 0; k < ns; k++) {
+            double chi = P->chi[r * ns + k];
+            if (chi == 0) continue;
+            const double* ps = st->phi_side + (size_t)k * M;
+            double pb = st->seg_phibulk[k];
+            for (int s = 0; s < M; s++)  /* PutAlpha, tools_host.h:428-431 */
+                if (st->phitot[s] > 0) gi[s] = gi[s] - chi * (ps[s] / st->phitot[s] - pb);
+        }
+    }
+    for (int i = 0; i < nit; i++) Add(st->alpha, g + (size_t)i * M, M);
+    Norm(st->alpha, 1.0 / nit, M);
+    for (int i = 0; i < nit; i++) {
+        double* gi = g + (size_t)i * M;
+        for (int s = 0; s < M; s++) {  /* AddG, tools_host.h:446-451 */
+            if (st->phitot[s] > 0) gi[s] = gi[s] - st->alpha[s] + 1 / st->phitot[s] - 1.0;
+            else gi[s] = 0;
+        }
+        remove_bounds(st, gi);
+        for (int s = 0; s < M; s++) gi[s] *= P->ksam[s];
+    }
+    return NM_OK;
+}
+
+/* ---- DIIS (sfnewton.cpp:793-926, 1037-1130) ------------------------------ */
+/* Solve A c = 1 for symmetric A by a cyclic Jacobi eigen-decomposition,
+ * c = Q diag(1/λ) Qᵀ 1 — the unregularised pseudo-inverse that the
+ * reference's SVD solve (Ax, sfnewton.cpp:793-835) evaluates. */
+static int small_solve(const double* A, double* c, int n) {
+    double a[100 * 100], q[100 * 100];
+    for (int i = 0; i < n * n; i++) { if (A[i] != A[i]) return NM_ERR_NAN_DIIS; a[i] = A[i]; }
+    if (n == 1) { c[0] = 1; return NM_OK; }
+    for (int i = 0; i < n; i++) for (int j = 0; j < n; j++) q[i * n + j] = (i == j);
+    for (int sweep = 0; sweep < 60; sweep++) {
+        double off = 0, diag = 0;
+        for (int i = 0; i < n; i++) for (int j = 0; j < n; j++) {
+            if (i != j) off += a[i * n + j] * a[i * n + j]; else diag += a[i * n + j] * a[i * n + j];
+        }
+        if (off <= 1e-30 * diag || off == 0) break;
+        for (int p = 0; p < n - 1; p++)
+            for (int r = p + 1; r < n; r++) {
+                double apr = a[p * n + r];
+                if (apr == 0) continue;
+                double app = a[p * n + p], arr = a[r * n + r];
+                double theta = (arr - app) / (2 * apr);
+                double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1));
+                double cs = 1 / sqrt(t * t + 1), sn = t * cs;
+                for (int k = 0; k < n; k++) {
+                    double akp = a[k * n + p], akr = a[k * n + r];
+                    a[k * n + p] = cs * akp - sn * akr;
+                    a[k * n + r] = sn * akp + cs * akr;
+                }
+                for (int k = 0; k < n; k++) {
+                    double apk = a[p * n + k], ark = a[r * n + k];
+                    a[p * n + k] = cs * apk - sn * ark;
+                    a[r * n + k] = sn * apk + cs * ark;
+                }
+                for (int k = 0; k < n; k++) {
+                    double qkp = q[k * n + p], qkr = q[k * n + r];
+                    q[k * n + p] = cs * qkp - sn * qkr;
+                    q[k * n + r] = sn * qkp + cs * qkr;
+                }
+            }
+    }
+    for (int i = 0; i < n; i++) c[i] = 0;
+    for (int j = 0; j < n; j++) {
+        double proj = 0;
+        for (int k = 0; k < n; k++) proj += q[k * n + j];
+        double w = proj / a[j * n + j];
+        for (int i = 0; i < n; i++) c[i] += q[i * n + j] * w;
+    }
+    for (int i = 0; i < n; i++) if (c[i] != c[i]) return NM_ERR_NAN_SVD;
+    return NM_OK;
+}
+
+static double resid_norm(const double* g, int n, int max_norm) {
+    if (max_norm) {
+        double mx = 0;
+        for (int i = 0; i < n; i++) if (fabs(g[i]) > mx) mx = fabs(g[i]);
+        return mx;
+    }
+    return sqrt(Dot(g, g, n));
+}
+
+int orc_solve_n(orc_state* st, double* x, int max_iter, int* iterations, double* residual) {
+    const nm_plan* P = st->P;
+    int nvar = P->iv, m = P->diis_m;
+    double dmax = P->deltamax, tol = P->tolerance;
+    double* xR = calloc((size_t)m * nvar, sizeof(double));
+    double* x_x0 = calloc((size_t)m * nvar, sizeof(double));
+    double* x0 = calloc((size_t)nvar, sizeof(double));
+    double* g = calloc((size_t)nvar, sizeof(double));
+    double* Aij = calloc((size_t)m * m, sizeof(double));
+    double* Apij = calloc((size_t)m * m, sizeof(double));
+    double* Ci = calloc((size_t)m, sizeof(double));
+    int it = 0, k_diis = 0, rc = NM_OK;
+    double res = 0;
+    Cp(x0, x, nvar);
+    rc = orc_residual(st, x, g);
+    if (rc) goto done;
+    YplusisCtimesX(x, g, -dmax, nvar);
+    for (int i = 0; i < nvar; i++) x_x0[i] = x[i] - x0[i];
+    Cp(xR, x, nvar);
+    res = resid_norm(g, nvar, P->max_norm);
+    while (res > tol && it < max_iter) {
+        it++;
+        Cp(x0, x, nvar);
+        rc = orc_residual(st, x, g);
+        if (rc) goto done;
+        int k = it % m;
+        k_diis++;
+        YplusisCtimesX(x, g, -dmax, nvar);
+        Cp(xR + (size_t)k * nvar, x, nvar);
+        for (int i = 0; i < nvar; i++) x_x0[(size_t)k * nvar + i] = x[i] - x0[i];
+        /* SFNewton::DIIS (sfnewton.cpp:837-880) */
+        int kd = k_diis;
+        if (kd > m) {
+            kd = m;
+            for (int i = 1; i < m; i++) for (int j = 1; j < m; j++) Aij[m * (i - 1) + j - 1] = Aij[m * i + j];
+        }
+        for (int i = 0; i < kd; i++) {
+            int posi = k - kd + 1 + i;
+            if (posi < 0) posi += m;
+            double D = Dot(x_x0 + (size_t)posi * nvar, x_x0 + (size_t)k * nvar, nvar);
+            Aij[i + m * (kd - 1)] = Aij[kd - 1 + m * i] = D + 1e-9;
+            for (int j = 0; j < kd; j++) Apij[j + kd * i] = Aij[j + m * i];
+        }
+        rc = small_solve(Apij, Ci, kd);
+        if (rc) goto done;
+        double normC = 0;
+        for (int i = 0; i < kd; i++) normC += Ci[i];
+        for (int i = 0; i < kd; i++) Ci[i] = Ci[i] / normC;
+        Zero(x, nvar);
+        int posi = k - kd + 1;
+        if (posi < 0) posi += m;
+        YplusisCtimesX(x, xR + (size_t)posi * nvar, Ci[0], nvar);  /* Xr_times_ci */
+        for (int i = 1; i < kd; i++) {
+            posi = k - kd + 1 + i;
+            if (posi < 0) posi += m;
+            YplusisCtimesX(x, xR + (size_t)posi * nvar, Ci[i], nvar);
+        }
+        res = resid_norm(g, nvar, P->max_norm);
+    }
+done:
+    if (iterations) *iterations = it;
+    if (residual) *residual = res;
+    free(xR); free(x_x0); free(x0); free(g); free(Aij); free(Apij); free(Ci);
+    return rc;
+}
+
+int orc_solve(orc_state* st, double* x, int* iterations, double* residual) {
+    return orc_solve_n(st, x, st->P->iterationlimit, iterations, residual);
+}
+
+/* ---- outputs -------------------------------------------------------------- */
+int orc_get_field(orc_state* st, int which, double* out) {
+    const nm_plan* P = st->P;
+    int M = st->M;
+    if (!st->have_state) return NM_ERR_ARG;
+    switch (which) {
+        case 0: Cp(out, st->phi, P->n_seg * M); return NM_OK;
+        case 1: Cp(out, st->G1, P->n_seg * M); return NM_OK;
+        case 2: Cp(out, st->alpha, M); return NM_OK;
+        case 3: Cp(out, st->phitot, M); return NM_OK;
+        case 4: Cp(out, st->mol_phitot, P->n_mol * M); return NM_OK;
+        case 5: Cp(out, st->phi_side, P->n_seg * M); return NM_OK;
+    }
+    return NM_ERR_ARG;
+}
+
+int orc_get_molecule(orc_state* st, int m, double* GN, double* n, double* theta, double* phibulk) {
+    if (!st->have_state || m < 0 || m >= st->P->n_mol) return NM_ERR_ARG;
+    if (GN) *GN = st->GN[m];
+    if (n) *n = st->mol_n[m];
+    if (theta) *theta = st->mol_theta[m];
+    if (phibulk) *phibulk = st->mol_phibulk[m];
+    return NM_OK;
+}
+
+/* GetFreeEnergy (system.cpp:2809-3029), GetGrandPotential (:3038-3244),
+ * CreateMu (:3246-3400) for uncharged, state-free systems. */
+int orc_free_energy(orc_state* st, double* Fout, double* Omega, double* mu) {
+    const nm_plan* P = st->P;
+    int M = st->M, ns = P->n_seg;
+    if (!st->have_state) return NM_ERR_ARG;
+    double* F = calloc((size_t)M, sizeof(double));
+    double* T = st->tmp;
+    for (int m = 0; m < P->n_mol; m++) remove_bounds(st, st->mol_phitot + (size_t)m * M);
+    for (int i = 0; i < ns; i++) remove_bounds(st, st->phi_side + (size_t)i * M);
+    for (int m = 0; m < P->n_mol; m++) {
+        const nm_molecule* mol = &P->mols[m];
+        double N = mol->chainlength;
+        double constant = log(N * st->mol_n[m] / st->GN[m]) / N;
+        Cp(T, st->mol_phitot + (size_t)m * M, M);
+        Norm(T, constant, M);
+        Add(F, T, M);
+    }
+    /* SysMonList: segments that occur in molecules */
+    for (int i = 0; i < ns; i++) {
+        if (P->seg_it[i] < 0) continue;
+        const double* G1 = st->G1 + (size_t)i * M;
+        const double* phi = st->phi + (size_t)i * M;
+        for (int s = 0; s < M; s++) {
+            double ml = G1[s] > 0 ? -log(G1[s]) : 0;
+            F[s] += -1.0 * (phi[s] * ml);
+        }
+    }
+    for (int j = 0; j < ns; j++) {
+        const double* phi = st->phi + (size_t)j * M;
+        for (int k = 0; k < ns; k++) {
+            double chi = (P->seg_freedom[k] == NM_SEG_FROZEN) ? P->chi[j * ns + k] : P->chi[j * ns + k] / 2;
+            if (P->seg_freedom[j] == NM_SEG_FROZEN || chi == 0) continue;
+            const double* ps = st->phi_side + (size_t)k * M;
+            for (int s = 0; s < M; s++) F[s] += chi * (phi[s] * ps[s]);
+        }
+    }
+    for (int m = 0; m < P->n_mol; m++) {
+        const nm_molecule* mol = &P->mols[m];
+        double constant = 0;
+        for (int j = 0; j < mol->n_molmon; j++)
+            for (int k = 0; k < mol->n_molmon; k++) {
+                double fA = mol->molmon_fraction[j], fB = mol->molmon_fraction[k];
+                double chi = P->chi[mol->molmon_seg[j] * ns + mol->molmon_seg[k]] / 2;
+                constant -= fA * fB * chi;
+            }
+        Cp(T, st->mol_phitot + (size_t)m * M, M);
+        Norm(T, constant, M);
+        Add(F, T, M);
+    }
+    for (int s = 0; s < M; s++) F[s] *= P->ksam[s];
+    double Fv = weighted_sum(st, F);
+    /* grand potential */
+    double* GP = F;
+    Zero(GP, M);
+    for (int m = 0; m < P->n_mol; m++) {
+        double N = P->mols[m].chainlength;
+        const double* pt = st->mol_phitot + (size_t)m * M;
+        for (int s = 0; s < M; s++) T[s] = (pt[s] + (-st->mol_phibulk[m])) * (1.0 / N);
+        Add(GP, T, M);
+    }
+    Add(GP, st->alpha, M);
+    for (int j = 0; j < ns; j++) {
+        if (P->seg_freedom[j] == NM_SEG_FROZEN) continue;
+        const double* phi = st->phi + (size_t)j * M;
+        double pbA = st->seg_phibulk[j];
+        for (int k = 0; k < ns; k++) {
+            if (P->seg_freedom[k] == NM_SEG_FROZEN) continue;
+            double chi = P->chi[j * ns + k] / 2;
+            if (chi == 0) continue;
+            const double* ps = st->phi_side + (size_t)k * M;
+            double pbB = st->seg_phibulk[k];
+            for (int s = 0; s < M; s++) GP[s] += chi * (phi[s] * ps[s] + (-pbA * pbB));
+        }
+    }
+    Norm(GP, -1.0, M);
+    for (int s = 0; s < M; s++) GP[s] *= P->ksam[s];
+    double Ov = weighted_sum(st, GP);
+    free(F);
+    if (Fout) *Fout = Fv;
+    if (Omega) *Omega = Ov;
+    if (mu) {
+        for (int i = 0; i < P->n_mol; i++) {
+            const nm_molecule* mol = &P->mols[i];
+            double NA = mol->chainlength;
+            double Mu = log(NA * st->mol_n[i] / st->GN[i]) + 1;
+            double constant = 0;
+            for (int k = 0; k < P->n_mol; k++) constant += st->mol_phibulk[k] / P->mols[k].chainlength;
+            Mu = Mu - NA * constant;
+            for (int j = 0; j < ns; j++) {
+                double pbA = st->seg_phibulk[j], FA = 0;
+                for (int q = 0; q < mol->n_molmon; q++) if (mol->molmon_seg[q] == j) FA = mol->molmon_fraction[q];
+                for (int k = 0; k < ns; k++) {
+                    double pbB = st->seg_phibulk[k], FB = 0;
+                    for (int q = 0; q < mol->n_molmon; q++) if (mol->molmon_seg[q] == k) FB = mol->molmon_fraction[q];
+                    double chi = P->chi[j * ns + k] / 2;
+                    Mu = Mu - NA * chi * (pbA - FA) * (pbB - FB);
+                }
+            }
+            mu[i] = Mu;
+        }
+    }
+    return NM_OK;
+}
+
+/* ---- lifetime --------------------------------------------------------------- */
+orc_state* orc_create(const nm_plan* P) {
+    orc_state* st = calloc(1, sizeof(orc_state));
+    int M = P->M, ns = P->n_seg, nm = P->n_mol;
+    st->P = P; st->M = M;
+    bc_sources(st);
+    st->u = calloc((size_t)ns * M, sizeof(double));
+    st->G1 = calloc((size_t)ns * M, sizeof(double));
+    st->phi = calloc((size_t)ns * M, sizeof(double));
+    st->phi_side = calloc((size_t)ns * M, sizeof(double));
+    st->phitot = calloc((size_t)M, sizeof(double));
+    st->alpha = calloc((size_t)M, sizeof(double));
+    st->tmp = calloc((size_t)M, sizeof(double));
+    st->unity = calloc((size_t)M, sizeof(double));
+    for (int s = 0; s < M; s++) st->unity[s] = P->ksam[s];  /* UNITY = KSAM, molecule.cpp:304 */
+    st->gb = calloc((size_t)2 * M, sizeof(double));
+    st->mol_phitot = calloc((size_t)nm * M, sizeof(double));
+    st->Gf = calloc((size_t)nm, sizeof(double*));
+    st->rho = calloc((size_t)nm, sizeof(double*));
+    st->jGb = calloc((size_t)nm, sizeof(double*));
+    st->Pc = calloc((size_t)nm, sizeof(double*));
+    st->Qb = calloc((size_t)nm, sizeof(double*));
+    for (int m = 0; m < nm; m++) {
+        const nm_molecule* mol = &P->mols[m];
+        st->Gf[m] = calloc((size_t)mol->n_store * M, sizeof(double));
+        st->rho[m] = calloc((size_t)mol->n_molmon * M, sizeof(double));
+        st->jGb[m] = calloc((size_t)mol->n_blocks * M, sizeof(double));
+        st->Pc[m] = calloc((size_t)mol->n_blocks * M, sizeof(double));
+        st->Qb[m] = calloc((size_t)mol->n_blocks * M, sizeof(double));
+    }
+    st->GN = calloc((size_t)nm, sizeof(double));
+    st->norm = calloc((size_t)nm, sizeof(double));
+    st->mol_n = calloc((size_t)nm, sizeof(double));
+    st->mol_theta = calloc((size_t)nm, sizeof(double));
+    st->mol_phibulk = calloc((size_t)nm, sizeof(double));
+    st->seg_phibulk = calloc((size_t)ns, sizeof(double));
+    return st;
+}
+
+void orc_destroy(orc_state* st) {
+    if (!st) return;
+    for (int m = 0; m < st->P->n_mol; m++) {
+        free(st->Gf[m]); free(st->rho[m]); free(st->jGb[m]); free(st->Pc[m]); free(st->Qb[m]);
+    }
+    free(st->Gf); free(st->rho); free(st->jGb); free(st->Pc); free(st->Qb);
+    free(st->u); free(st->G1); free(st->phi); free(st->phi_side); free(st->phitot);
+    free(st->alpha); free(st->tmp); free(st->unity); free(st->gb); free(st->mol_phitot);
+    free(st->GN); free(st->norm); free(st->mol_n); free(st->mol_theta); free(st->mol_phibulk);
+    free(st->seg_phibulk);
+    free(st);
+}

@@ -1,0 +1,32 @@
+import json
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "oracle"))
+GOLDEN = ROOT / "tests" / "golden"
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (run with -m gpu)")
+
+
+def golden_names():
+    return sorted(p.stem for p in GOLDEN.glob("*.json"))
+
+
+def load_golden(name):
+    return json.loads((GOLDEN / f"{name}.json").read_text())
+
+
+@pytest.fixture(scope="session", autouse=True)
+def built_libraries():
+    """Build the product library and the oracle once per session (both are
+    needed on CPU too: the plan compiler and the oracle run without a GPU)."""
+    from namics_gb300 import build
+    build.build_product()
+    build.build_oracle()
+    return True

@@ -1,0 +1,273 @@
+"""Generate the golden fixtures in tests/golden/*.json from the reference.
+
+Each case is a Namics input file plus a seeded initial field.  The field is
+written as a reference guess file (the format Lattice::ReadGuess reads,
+lattice.cpp:926-968, at %.17e) and the unmodified reference program
+(oracle/_ref/namics, built by oracle/Makefile.ref from the reference sources)
+is run on it.  Its .pro profiles (%.20g) and .kal scalars (%.16e) are parsed
+and stored, together with the input text and the field, so the tests can
+replay the same problem through the oracle and the GPU path without the
+reference present.
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+GOLDEN = Path(__file__).resolve().parent
+REF_BIN = ROOT / "oracle" / "_ref" / "namics"
+
+from namics_gb300 import Plan  # noqa: E402  (plan compiler only: no GPU needed)
+
+
+def lat1d(n, lower="surface", upper="mirror", geom="planar", lattype="simple_cubic", offset=None):
+    s = [f"lat : flat : n_layers : {n}", f"lat : flat : lattice_type : {lattype}",
+         f"lat : flat : geometry : {geom}", "lat : flat : gradients : 1",
+         f"lat : flat : lowerbound : {lower}", f"lat : flat : upperbound : {upper}"]
+    if offset is not None:
+        s.append(f"lat : flat : offset_first_layer : {offset}")
+    return s
+
+
+def lat2d(nx, ny, bcs, geom="planar", lattype="simple_cubic", offset=None):
+    s = ["lat : flat : gradients : 2", f"lat : flat : n_layers_x : {nx}", f"lat : flat : n_layers_y : {ny}",
+         f"lat : flat : geometry : {geom}", f"lat : flat : lattice_type : {lattype}"]
+    for k, v in zip(["lowerbound_x", "upperbound_x", "lowerbound_y", "upperbound_y"], bcs):
+        s.append(f"lat : flat : {k} : {v}")
+    if offset is not None:
+        s.append(f"lat : flat : offset_first_layer : {offset}")
+    return s
+
+
+def lat3d(n, bc="periodic", lattype="simple_cubic"):
+    s = ["lat : flat : gradients : 3", f"lat : flat : n_layers_x : {n[0]}", f"lat : flat : n_layers_y : {n[1]}",
+         f"lat : flat : n_layers_z : {n[2]}", "lat : flat : geometry : planar", f"lat : flat : lattice_type : {lattype}"]
+    for ax in "xyz":
+        s += [f"lat : flat : lowerbound_{ax} : {bc}", f"lat : flat : upperbound_{ax} : {bc}"]
+    return s
+
+
+def brush_lines(comp, n=None, theta=None, chi=0.5, chi_s=None, wall=True, pinned_range="firstlayer"):
+    s = []
+    if wall:
+        s += ["mon : S : freedom : frozen", "mon : S : frozen_range : lowerbound"]
+    s += ["mon : X : freedom : pinned", f"mon : X : pinned_range : {pinned_range}",
+          "mon : A : freedom : free", "mon : W : freedom : free",
+          f"mon : A : chi_W : {chi}", f"mon : X : chi_W : {chi}"]
+    if chi_s is not None and wall:
+        s += [f"mon : A : chi_S : {chi_s}", f"mon : X : chi_S : {chi_s}"]
+    s += [f"mol : pol : composition : {comp}", "mol : pol : freedom : restricted"]
+    s += [f"mol : pol : n : {n}"] if n is not None else [f"mol : pol : theta : {theta}"]
+    s += ["mol : water : composition : (W)1", "mol : water : freedom : solvent"]
+    return s
+
+
+def newton(tol=1e-7, dmax=0.1, itlim=1000, m=10):
+    return ["newton : isaac : method : DIIS", f"newton : isaac : tolerance : {tol}",
+            f"newton : isaac : deltamax : {dmax}", f"newton : isaac : iterationlimit : {itlim}",
+            f"newton : isaac : m : {m}", "newton : isaac : e_info : false"]
+
+
+def cases() -> list[dict]:
+    C = []
+    # config 1: 1-gradient planar simple-cubic brush, 100 layers, A_100 (X1A99) at σ=0.05
+    base = lat1d(100) + brush_lines("(X)1(A)99", n=0.05, chi=0.5)
+    C.append(dict(name="brush1d_cfg1", lines=base, field=(-0.01, 0.01), seed=1, modes=["it0", "conv"]))
+    # 3-arm star brush (configuration-4 star variant)
+    C.append(dict(name="star1d", lines=lat1d(80) + brush_lines("(X)1(A)19[(A)20](A)20", n=0.04, chi=0.4),
+                  field=(-0.01, 0.01), seed=2, modes=["it0", "conv"]))
+    # hexagonal planar brush with an adsorbing wall
+    C.append(dict(name="brush1d_hex", lines=lat1d(60, lattype="hexagonal") +
+                  brush_lines("(X)1(A)39", n=0.03, chi=0.8, chi_s=-0.5),
+                  field=(-0.05, 0.05), seed=3, modes=["it0", "conv"]))
+    # spherical brush
+    C.append(dict(name="brush1d_sph", lines=lat1d(50, geom="spherical", offset=5) +
+                  brush_lines("(X)1(A)29", theta=600, chi=0.3),
+                  field=(-0.02, 0.02), seed=4, modes=["it0", "conv"]))
+    # cylindrical homopolymer adsorption, hexagonal, free chains
+    lines = lat1d(40, geom="cylindrical", lattype="hexagonal", offset=3) + [
+        "mon : S : freedom : frozen", "mon : S : frozen_range : lowerbound",
+        "mon : A : freedom : free", "mon : W : freedom : free", "mon : A : chi_S : -1.2",
+        "mon : A : chi_W : 0.2",
+        "mol : pol : composition : (A)30", "mol : pol : freedom : free", "mol : pol : phibulk : 0.01",
+        "mol : water : composition : (W)1", "mol : water : freedom : solvent"]
+    C.append(dict(name="ads1d_cyl_hex", lines=lines, field=(-0.05, 0.05), seed=5, modes=["it0", "conv"]))
+    # symmetric dendrimer near an adsorbing wall
+    lines = lat1d(40) + ["mon : S : freedom : frozen", "mon : S : frozen_range : lowerbound",
+                         "mon : A : freedom : free", "mon : B : freedom : free", "mon : W : freedom : free",
+                         "mon : A : chi_S : -0.8", "mon : B : chi_W : 0.6",
+                         "mol : pol : composition : @dend(A,(B)3,3; A,(A)2(B)2,2)",
+                         "mol : pol : freedom : restricted", "mol : pol : theta : 4",
+                         "mol : water : composition : (W)1", "mol : water : freedom : solvent"]
+    C.append(dict(name="dend1d", lines=lines, field=(-0.05, 0.05), seed=6, modes=["it0", "conv"]))
+    # 2-gradient planar adsorption (configuration-5 2-D class, reduced size)
+    lines = lat2d(24, 16, ["surface", "mirror", "mirror", "mirror"]) + [
+        "mon : S : freedom : frozen", "mon : S : frozen_range : lowerbound",
+        "mon : A : freedom : free", "mon : W : freedom : free", "mon : A : chi_S : -1",
+        "mol : pol : composition : (A)40", "mol : pol : freedom : free", "mol : pol : phibulk : 1e-3",
+        "mol : water : composition : (W)1", "mol : water : freedom : solvent"]
+    C.append(dict(name="ads2d", lines=lines, field=(-0.05, 0.05), seed=7, modes=["it0", "conv"]))
+    # 2-gradient hexagonal planar, periodic y
+    lines = lat2d(16, 12, ["surface", "mirror", "periodic", "periodic"], lattype="hexagonal") + [
+        "mon : S : freedom : frozen", "mon : S : frozen_range : lowerbound",
+        "mon : A : freedom : free", "mon : W : freedom : free", "mon : A : chi_S : -1.5",
+        "mon : A : chi_W : 0.4",
+        "mol : pol : composition : (A)20", "mol : pol : freedom : free", "mol : pol : phibulk : 0.01",
+        "mol : water : composition : (W)1", "mol : water : freedom : solvent"]
+    C.append(dict(name="ads2d_hex", lines=lines, field=(-0.05, 0.05), seed=8, modes=["it0", "conv"]))
+    # 2-gradient cylindrical brush (configuration-3 geometry, uncharged, reduced)
+    lines = lat2d(20, 10, ["surface", "mirror", "mirror", "mirror"], geom="cylindrical", offset=10) + \
+        brush_lines("(X)1(A)39", n=12.0, chi=0.5, pinned_range="firstlayer")
+    C.append(dict(name="brush2d_cyl", lines=lines, field=(-0.02, 0.02), seed=9, modes=["it0", "conv"]))
+    # 3-gradient periodic diblock melt (configuration-2 class, reduced size)
+    lines = lat3d((10, 10, 10)) + ["mon : A : freedom : free", "mon : B : freedom : free", "mon : A : chi_B : 0.3",
+                                   "mol : AB : composition : (A)10(B)10", "mol : AB : freedom : solvent"]
+    C.append(dict(name="melt3d", lines=lines, field=(-0.1, 0.1), seed=10, antisym=True,
+                  modes=["it0", "it5"], newton=dict(dmax=0.01)))
+    # 3-gradient hexagonal, mirror bounds, homopolymer in solvent
+    lines = lat3d((8, 7, 6), bc="mirror", lattype="hexagonal") + [
+        "mon : A : freedom : free", "mon : W : freedom : free", "mon : A : chi_W : 0.8",
+        "mol : pol : composition : (A)12", "mol : pol : freedom : free", "mol : pol : phibulk : 0.1",
+        "mol : water : composition : (W)1", "mol : water : freedom : solvent"]
+    C.append(dict(name="sol3d_hex", lines=lines, field=(-0.1, 0.1), seed=11, modes=["it0", "it5"]))
+    # configuration-4 sample: random 1-gradient brushes (seeded), 10% stars
+    rng = np.random.default_rng(2024)
+    for i in range(6):
+        nl = int(rng.integers(50, 401))
+        N = int(rng.integers(20, 501))
+        sig = float(rng.uniform(0.01, 0.1))
+        chi = float(rng.uniform(0, 1))
+        star = (i == 5)
+        if star:
+            a = max(N // 3, 2)
+            comp = f"(X)1(A){a - 1}[(A){a}](A){a}"
+        else:
+            comp = f"(X)1(A){N - 1}"
+        nl = min(nl, 200)  # keep the reference run short
+        C.append(dict(name=f"cfg4_{i}", lines=lat1d(nl) + brush_lines(comp, n=round(sig, 6), chi=round(chi, 6)),
+                      field=(-0.01, 0.01), seed=100 + i, modes=["conv"]))
+    return C
+
+
+def outputs_block(plan: Plan) -> list[str]:
+    s = ["output : pro : append : false"]
+    for name in plan.seg_names:
+        s.append(f"pro : mon : {name} : phi")
+    for name in plan.seg_names:
+        s.append(f"pro : mon : {name} : G1")
+    s.append("pro : sys : noname : alpha")
+    s.append("output : kal : append : false")
+    s += ["kal : sys : noname : free_energy", "kal : sys : noname : grand_potential",
+          "kal : newton : isaac : residual", "kal : newton : isaac : iterations"]
+    for m in range(plan.n_mol):
+        mn = MOLNAMES[m]
+        s += [f"kal : mol : {mn} : GN", f"kal : mol : {mn} : n", f"kal : mol : {mn} : theta",
+              f"kal : mol : {mn} : phibulk", f"kal : mol : {mn} : Mu"]
+    return s
+
+
+MOLNAMES: list[str] = []
+
+
+def make_field(plan: Plan, lo: float, hi: float, seed: int, antisym: bool) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(lo, hi, size=plan.iv)
+    if antisym and plan.c.n_it == 2:
+        M = plan.M
+        x[M:2 * M] = -x[:M]
+    return x
+
+
+def write_guess(path: Path, plan: Plan, x: np.ndarray) -> None:
+    c = plan.c
+    names = [plan.seg_names[i] for i in plan.it_seg]
+    my = c.MY if c.gradients > 1 else 0
+    mz = c.MZ if c.gradients > 2 else 0
+    with open(path, "w") as f:
+        f.write("DIIS\n")
+        f.write(f" {c.MX}\t{my}\t{mz}\t1\n")
+        f.write("false\n")
+        f.write(f"{len(names)}\n")
+        for n in names:
+            f.write(n + "\n")
+        f.write("0\n")
+        for v in x:
+            f.write(f"{v:.17e}\n")
+
+
+def parse_pro(path: Path, ndim: int) -> dict:
+    lines = path.read_text().strip().splitlines()
+    head = [t for t in lines[0].split("\t") if t.strip()]
+    data = np.array([[float(t) for t in ln.split("\t") if t.strip()] for ln in lines[1:]])
+    return {"header": head, "data": data}
+
+
+def parse_kal(path: Path) -> dict:
+    lines = path.read_text().strip().splitlines()
+    head = lines[0].split("\t")
+    vals = [float(t) for t in lines[-1].split("\t")]
+    return dict(zip(head, vals))
+
+
+def run_case(case: dict, mode: str, workdir: Path) -> dict:
+    global MOLNAMES
+    body = list(case["lines"])
+    nw = dict(case.get("newton", {}))
+    base_text = "\n".join(body + newton(**nw)) + "\n"
+    plan = Plan(base_text)
+    MOLNAMES = [ln.split(":")[1].strip() for ln in body if ln.startswith("mol")]
+    MOLNAMES = list(dict.fromkeys(MOLNAMES))
+    x = make_field(plan, *case["field"], case["seed"], case.get("antisym", False))
+    itlim = {"it0": 0, "it5": 5, "conv": 1000}[mode]
+    nw["itlim"] = itlim
+    text = "\n".join(body + newton(**nw)) + "\n"
+    tag = f"{case['name']}_{mode}"
+    guess = workdir / f"{tag}.guess"
+    write_guess(guess, plan, x)
+    full = text + "sys : noname : initial_guess : file\n" + f"sys : noname : guess_inputfile : {guess.name}\n"
+    full += "\n".join(outputs_block(plan)) + "\nstart\n"
+    (workdir / f"{tag}.in").write_text(full)
+    r = subprocess.run([str(REF_BIN), f"{tag}.in"], cwd=workdir, capture_output=True, text=True, timeout=600)
+    out = {"returncode": r.returncode, "stdout_tail": r.stdout[-2000:]}
+    pro = workdir / "output" / f"{tag}.pro"
+    kal = workdir / "output" / f"{tag}.kal"
+    if r.returncode != 0 or not kal.exists():
+        raise RuntimeError(f"reference failed on {tag}: {r.stdout[-1500:]} {r.stderr[-500:]}")
+    prod = parse_pro(pro, plan.c.gradients)
+    kald = parse_kal(kal)
+    return dict(input=text, x=x.tolist(), mode=mode, iterationlimit=itlim,
+                pro_header=prod["header"], pro=prod["data"].tolist(), kal=kald,
+                molnames=MOLNAMES)
+
+
+def main():
+    if not REF_BIN.exists():
+        sys.exit(f"{REF_BIN} missing: build it with  make -f oracle/Makefile.ref")
+    only = set(sys.argv[1:])
+    with tempfile.TemporaryDirectory() as td:
+        wd = Path(td)
+        (wd / "output").mkdir()
+        for case in cases():
+            if only and case["name"] not in only:
+                continue
+            res = {"name": case["name"], "runs": {}}
+            for mode in case["modes"]:
+                res["runs"][mode] = run_case(case, mode, wd)
+                k = res["runs"][mode]["kal"]
+                print(f"{case['name']:>16s} {mode:5s} F={k.get('sys_noname_free_energy')!r:<24} "
+                      f"res={k.get('newton_isaac_residual')!r:<12} it={k.get('newton_isaac_iterations')}", flush=True)
+            (GOLDEN / f"{case['name']}.json").write_text(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,66 @@
+"""The CPU oracle against outputs of the reference program itself.
+
+The fixtures in tests/golden were produced by tests/golden/make_golden.py,
+which runs the unmodified reference (built from its sources by
+oracle/Makefile.ref) on the same input text and seeded field.  This pins the
+oracle; the GPU tests then compare the CUDA path with the oracle.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from helpers import interior, pro_column, rel_err
+
+from namics_gb300 import Plan
+from orc import Oracle
+
+CASES = golden_names()
+
+
+def _run(run):
+    plan = Plan(run["input"])
+    orc = Oracle(plan)
+    x = np.array(run["x"])
+    if run["mode"] == "it0":
+        rc, _ = orc.residual(x)
+        its = 0
+    else:
+        rc, _, its, _ = orc.solve(x, max_iter=run["iterationlimit"])
+    assert rc == 0
+    return plan, orc, its
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_matches_reference(name):
+    g = load_golden(name)
+    for mode, run in g["runs"].items():
+        plan, orc, its = _run(run)
+        k = run["kal"]
+        # Single residual evaluations replay the reference's arithmetic
+        # (bit-identical in practice).  Solves agree to 1e-8 while the DIIS
+        # path is the same (same iteration count); where the small DIIS solve
+        # (Jacobi here, SVD in the reference) rounds an ill-conditioned
+        # history differently the paths split, and both end within the
+        # convergence ball ‖g‖ < 1e-7 of the same solution.
+        same_path = mode == "it0" or its == int(k["newton_isaac_iterations"])
+        tol = 1e-12 if mode == "it0" else (1e-8 if same_path else 1e-5)
+        if mode.startswith("it") and mode != "it0":
+            tol = 1e-7  # fixed iteration count on an unstable start
+        phi = orc.field(0).reshape(plan.n_seg, plan.M)
+        g1 = orc.field(1).reshape(plan.n_seg, plan.M)
+        for i, seg in enumerate(plan.seg_names):
+            assert rel_err(interior(plan, phi[i]), pro_column(run, f"mon_{seg}_phi")) < tol, (mode, seg)
+            if plan.c.seg_freedom[i] != 2:
+                assert rel_err(interior(plan, g1[i]), pro_column(run, f"mon_{seg}_G1")) < tol, (mode, seg)
+        alpha = orc.field(2)
+        assert rel_err(interior(plan, alpha), pro_column(run, "sys_noname_alpha")) < max(tol, 1e-12)
+        F, O, mu = orc.free_energy()
+        assert abs(F - k["sys_noname_free_energy"]) <= tol * max(1.0, abs(k["sys_noname_free_energy"]))
+        assert abs(O - k["sys_noname_grand_potential"]) <= tol * max(1.0, abs(k["sys_noname_grand_potential"]))
+        for m, mn in enumerate(run["molnames"]):
+            mol = orc.molecule(m)
+            assert abs(mol["GN"] - k[f"mol_{mn}_GN"]) <= tol * abs(k[f"mol_{mn}_GN"])
+            assert abs(mu[m] - k[f"mol_{mn}_Mu"]) <= tol * max(1.0, abs(k[f"mol_{mn}_Mu"]))
+        if mode == "conv":
+            assert abs(its - int(k["newton_isaac_iterations"])) <= max(2, its)  # both converged
+            assert run["kal"]["newton_isaac_residual"] < 1e-7
