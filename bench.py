@@ -1,0 +1,342 @@
+"""Benchmark: SCF solves/s at |residual| < 1e-7 on the batched brush workload.
+
+Workload (one "step"): 512 independent 1-gradient planar brushes solved to
+‖g‖₂ < 1e-7 from seeded fields u ~ U(-0.01, 0.01), drawn from a fixed seed:
+n_layers ~ U{50..400}, N ~ U{20..500}, σ ~ U[0.01, 0.1], χ_AS ~ U[0, 1];
+every 10th instance is a 3-arm star with arms of N/3 joined at a branch point.
+All 512 solves run in one persistent launch (one CTA per problem, DIIS on the
+device), FP32 propagators with per-step power-of-two scaling and FP64
+normalisation / residual / DIIS.
+
+Contract: `python bench.py --gpus N --steps K --warmup W` prints one JSON
+line.  `value` times the kernel with inputs resident in HBM (CUDA events);
+`e2e` times the C-ABI call with host buffers (nm_batch_solve_host: host→device
+copy of the fields, solve, device→host copy of the solution).
+`--impl reference` times the CPU restatement of the reference path
+(oracle/scf_oracle.c, one solve per host thread) on a bounded sample.
+Multi-GPU: the instances are independent solves, so N GPUs run N replicas of
+the same workload with no collective (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_INSTANCES = 512
+SEED = 20251203
+FIELD = (-0.01, 0.01)
+METRIC = "SCF solves/s at |residual|<1e-7 (batched FP32-propagator, FP64 DIIS)"
+UNIT = "solves/s"
+B_PER_UPDATE_FP32 = 22.0   # algorithmic bytes per segment-site update (FP32 propagators, FP64 φ)
+B_PER_UPDATE_FP64 = 36.0
+
+
+def instance_text(nl: int, N: int, sigma: float, chi: float, star: bool) -> str:
+    if star:
+        a = max(N // 3, 2)
+        comp = f"(X)1(A){a - 1}[(A){a}](A){a}"
+    else:
+        comp = f"(X)1(A){N - 1}"
+    return "\n".join([
+        f"lat : flat : n_layers : {nl}", "lat : flat : lattice_type : simple_cubic",
+        "lat : flat : geometry : planar", "lat : flat : gradients : 1",
+        "lat : flat : lowerbound : surface", "lat : flat : upperbound : mirror",
+        "mon : S : freedom : frozen", "mon : S : frozen_range : lowerbound",
+        "mon : X : freedom : pinned", "mon : X : pinned_range : firstlayer",
+        "mon : A : freedom : free", "mon : W : freedom : free",
+        f"mon : A : chi_W : {chi:.6f}", f"mon : X : chi_W : {chi:.6f}",
+        f"mol : pol : composition : {comp}", "mol : pol : freedom : restricted",
+        f"mol : pol : n : {sigma:.6f}",
+        "mol : water : composition : (W)1", "mol : water : freedom : solvent",
+        "newton : isaac : method : DIIS", "newton : isaac : tolerance : 1e-7",
+        "newton : isaac : deltamax : 0.1", "newton : isaac : iterationlimit : 1000",
+    ]) + "\n"
+
+
+def workload(n: int = N_INSTANCES):
+    rng = np.random.default_rng(SEED)
+    out = []
+    for i in range(n):
+        nl = int(rng.integers(50, 401))
+        N = int(rng.integers(20, 501))
+        sigma = float(rng.uniform(0.01, 0.1))
+        chi = float(rng.uniform(0.0, 1.0))
+        out.append(instance_text(nl, N, sigma, chi, star=(i % 10 == 9)))
+    return out
+
+
+def fields(plans, seed=SEED + 1):
+    rng = np.random.default_rng(seed)
+    return [rng.uniform(*FIELD, size=p.iv) for p in plans]
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = Path(tempfile.mkstemp(suffix=".csv")[1])
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        try:
+            for ln in self.path.read_text().splitlines():
+                t = [s.strip() for s in ln.split(",")]
+                if len(t) < 9:
+                    continue
+                try:
+                    sm.append(float(t[1]))
+                    mx = float(t[2])
+                except ValueError:
+                    continue
+                names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+                for nm, v in zip(names, t[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        except Exception:
+            pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(texts, xs, budget_s: float = 15.0, threads: int | None = None) -> dict:
+    """The CPU restatement of the reference path (oracle/scf_oracle.c), one
+    solve per host thread, over a bounded sample of the same instances."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    from namics_gb300 import Plan
+    from orc import Oracle
+    threads = threads or os.cpu_count() or 1
+    lock = threading.Lock()
+    state = {"next": 0, "done": 0, "its": 0}
+    t0 = time.perf_counter()
+    deadline = t0 + budget_s
+
+    def worker():
+        while True:
+            with lock:
+                i = state["next"]
+                if i >= len(texts) or time.perf_counter() > deadline:
+                    return
+                state["next"] += 1
+            p = Plan(texts[i])
+            rc, _, its, res = Oracle(p).solve(xs[i])
+            with lock:
+                state["done"] += 1
+                state["its"] += its
+
+    ts = [threading.Thread(target=worker) for _ in range(threads)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    dt = time.perf_counter() - t0
+    return {"value": state["done"] / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {state['done']} of {len(texts)} instances, one solve per thread, {dt:.1f} s wall",
+            "seconds": dt}
+
+
+def run_reference(args) -> None:
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, str(ROOT))
+    from namics_gb300 import build as b
+    b.build_product()
+    b.build_oracle()
+    from namics_gb300 import Plan
+    texts = workload()
+    plans = [Plan(t) for t in texts]
+    xs = fields(plans)
+    threads = os.cpu_count() or 1
+    per_step = max(threads * 2, 16)
+    vals = []
+    for step in range(args.warmup + args.steps):
+        lo = (step * per_step) % len(texts)
+        sel = list(range(lo, min(lo + per_step, len(texts))))
+        r = cpu_baseline([texts[i] for i in sel], [xs[i] for i in sel], budget_s=1e9, threads=threads)
+        if step >= args.warmup:
+            vals.append(r["value"])
+    v = statistics.mean(vals)
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": per_step / v * 1000.0, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "impl": "reference",
+            "config": {"workload": "batched 1-gradient brushes/stars (512, seeded)", "sample_per_step": per_step},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{per_step} instances per step, one solve per host thread"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--instances", type=int, default=N_INSTANCES)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    ws, rank, local = dist_env()
+    import torch
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from namics_gb300 import build as b
+    if rank == 0:
+        b.build_product()
+        b.build_oracle()
+    if ws > 1:
+        dist.barrier()
+    from namics_gb300 import NM_FP32, NM_FP64, Batch, Plan
+
+    texts = workload(args.instances)
+    plans = [Plan(t) for t in texts]
+    xs = fields(plans)
+    prec = NM_FP32 if args.precision == "fp32" else NM_FP64
+    stream = torch.cuda.Stream()
+    batch = Batch(plans, prec, device=local, stream=stream.cuda_stream)
+    x0 = torch.from_numpy(np.concatenate(xs)).cuda()
+    xw = torch.empty_like(x0)
+    flush = torch.empty(int(256e6) // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
+
+    def step():
+        xw.copy_(x0)
+        torch.cuda.synchronize()
+        return batch.solve_dev(xw.data_ptr())
+
+    for _ in range(args.warmup):
+        step()
+    # timed: per-step CUDA events on the launching stream, L2 flushed between steps
+    launches0 = batch.launch_count()
+    times, its_all = [], None
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            xw.copy_(x0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            its, res, st = batch.solve_dev(xw.data_ptr())
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            its_all = its
+    torch.cuda.synchronize()
+    launches = batch.launch_count() - launches0
+    ms = statistics.mean(times)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    n_ok = int((st == 0).sum())
+    value = n_ok * ws / (ms / 1000.0)
+    # end to end through the C ABI with host buffers
+    xh = np.concatenate(xs)
+    e2e_times = []
+    for _ in range(max(2, min(args.steps, 3))):
+        xh2 = xh.copy()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        batch.solve_host(xh2)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = statistics.mean(e2e_times)
+    nbytes = xh.nbytes
+    # roofline: algorithmic bytes of the propagator work of one launch
+    updates = 0.0
+    for i, p in enumerate(plans):
+        per_it = p.segment_updates()
+        updates += per_it * (int(its_all[i]) + 1)
+    bpu = B_PER_UPDATE_FP32 if prec == NM_FP32 else B_PER_UPDATE_FP64
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = updates * bpu / (ms / 1000.0) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if prec == NM_FP32 else "f64",
+        "data": "synthetic (seeded brush/star instances)",
+        "config": {"workload": "batched 1-gradient brushes/stars (512, seeded): n_layers U{50..400}, "
+                               "N U{20..500}, sigma U[0.01,0.1], chi U[0,1], 10% 3-arm stars",
+                   "instances": args.instances, "converged": n_ok, "precision": args.precision,
+                   "iterations_mean": float(np.mean(its_all)), "iterations_max": int(np.max(its_all)),
+                   "segment_site_updates_per_step": updates, "l2": "flushed between steps (256 MB write)",
+                   "parallelism": f"replicas x{ws}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "note": f"{bpu:.0f} B per segment-site update x updates / kernel time; peak of measured "
+                             "(MEASURED_PEAKS.json hbm_gbs)"},
+        "e2e": {"value": n_ok * ws / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu and ws == 1:
+        line["cpu_baseline"] = cpu_baseline(texts, xs, budget_s=15.0)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -641,9 +641,12 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
     for (int i = 0; i < ns; i++)
         for (int s = 0; s < M; s++) {
             double km = H->ksam[s];
+            // pinned: G1 = exp(-u)·MASK·KSAM; free and frozen: exp(-u)·KSAM
+            // (segment.cpp:875-878; the frozen test there compares against
+            // " frozen", so frozen segments get the KSAM factor as well)
             if (H->seg_freedom[i] == NM_SEG_PINNED) H->seg_gmask[(size_t)i * M + s] = H->seg_mask[(size_t)i * M + s] * km;
-            else if (H->seg_freedom[i] == NM_SEG_FREE) H->seg_gmask[(size_t)i * M + s] = km;
-            else H->seg_phi_frozen[(size_t)i * M + s] = H->seg_mask[(size_t)i * M + s];
+            else H->seg_gmask[(size_t)i * M + s] = km;
+            if (H->seg_freedom[i] == NM_SEG_FROZEN) H->seg_phi_frozen[(size_t)i * M + s] = H->seg_mask[(size_t)i * M + s];
         }
     // surface bounds must be frozen (the halo layer is then a G = 0 wall)
     for (int d = 0; d < P.gradients; d++)

@@ -361,7 +361,7 @@ static int compute_phis(orc_state* st, const double* x) {
         else Zero(u, M);
         set_bounds(st, u);
         for (int s = 0; s < M; s++) G1[s] = exp(-u[s]);
-        if (P->seg_freedom[i] != NM_SEG_FROZEN) Times(G1, G1, P->seg_gmask + (size_t)i * M, M);
+        Times(G1, G1, P->seg_gmask + (size_t)i * M, M);
         /* Segment phi: frozen -> MASK, else 0 */
         Cp(st->phi + (size_t)i * M, P->seg_phi_frozen + (size_t)i * M, M);
         st->seg_phibulk[i] = 0;

@@ -1,0 +1,193 @@
+"""CUDA path against the CPU oracle and the reference's golden outputs.
+
+Every call goes through the C ABI (include/namics_gb300.h).  Tolerances:
+FP64 single residual evaluations agree with the oracle to 1e-10 relative
+(the GPU contracts multiply-adds, the reference does not); converged solves
+agree to 1e-8 relative when the DIIS path is the same and to the convergence
+ball (1e-6 on φ and F) otherwise; the FP32-propagator solver is held to
+1e-6 on φ and 1e-7 relative on F against the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from helpers import interior, pro_column, rel_err
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+from namics_gb300 import NM_FP32, NM_FP64, Batch, Context, Plan  # noqa: E402
+from orc import Oracle  # noqa: E402
+
+CASES = golden_names()
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_residual_matches_oracle(name):
+    g = load_golden(name)
+    run = next(iter(g["runs"].values()))
+    plan = Plan(run["input"])
+    ctx = Context(plan, NM_FP64)
+    orc = Oracle(plan)
+    x = np.array(run["x"])
+    rc, g_orc = orc.residual(x)
+    assert rc == 0
+    xd, gd = dev(x), torch.zeros(plan.iv, dtype=torch.float64, device="cuda")
+    ctx.residual_dev(xd.data_ptr(), gd.data_ptr())
+    g_gpu = host(gd)
+    assert rel_err(g_gpu, g_orc) < 1e-10
+    for which in (0, 1):
+        a, b = ctx.field(which).reshape(plan.n_seg, -1), orc.field(which).reshape(plan.n_seg, -1)
+        for i in range(plan.n_seg):
+            assert rel_err(interior(plan, a[i]), interior(plan, b[i])) < 1e-10, (which, i)
+    assert rel_err(interior(plan, ctx.field(2)), interior(plan, orc.field(2))) < 1e-10
+    for m in range(plan.n_mol):
+        assert abs(ctx.molecule(m)["GN"] / orc.molecule(m)["GN"] - 1) < 1e-10
+    F, O, mu = ctx.free_energy()
+    Fo, Oo, muo = orc.free_energy()
+    assert abs(F - Fo) <= 1e-10 * max(1, abs(Fo))
+    assert abs(O - Oo) <= 1e-10 * max(1, abs(Oo))
+    assert np.allclose(mu, muo, rtol=1e-10, atol=1e-10)
+    assert ctx.launch_count() > 0
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_solve_matches_reference(name):
+    g = load_golden(name)
+    for mode, run in g["runs"].items():
+        if mode == "it0":
+            continue
+        plan = Plan(run["input"])
+        ctx = Context(plan, NM_FP64)
+        res, phi = ctx.solve_host(np.array(run["x"]))
+        k = run["kal"]
+        same = res.iterations == int(k["newton_isaac_iterations"])
+        if mode == "conv":
+            assert res.status == 0 and res.residual < 1e-7
+        tol = 1e-8 if same else 1e-6
+        if mode != "conv":
+            tol = 1e-6  # a few iterations from an unstable start
+        phi = phi.reshape(plan.n_seg, plan.M)
+        # nm_solve_host returns φ of the last residual evaluation, like the .pro
+        for i, seg in enumerate(plan.seg_names):
+            assert rel_err(interior(plan, phi[i]), pro_column(run, f"mon_{seg}_phi")) < tol, (mode, seg)
+        F, O, _ = ctx.free_energy()
+        assert abs(F - k["sys_noname_free_energy"]) <= tol * max(1, abs(k["sys_noname_free_energy"]))
+
+
+def _batch_cases():
+    out = []
+    for n in CASES:
+        g = load_golden(n)
+        if "conv" in g["runs"]:
+            p = Plan(g["runs"]["conv"]["input"])
+            if p.c.gradients == 1:
+                out.append(n)
+    return out
+
+
+@pytest.mark.parametrize("precision", [NM_FP64, NM_FP32])
+def test_batched_solver_matches_reference(precision):
+    names = _batch_cases()
+    runs = [load_golden(n)["runs"]["conv"] for n in names]
+    plans = [Plan(r["input"]) for r in runs]
+    b = Batch(plans, precision)
+    x = np.concatenate([np.array(r["x"]) for r in runs])
+    its, res, st = b.solve_host(x)
+    assert (st == 0).all(), (names, st, res)
+    assert (res < 1e-7).all()
+    F, O = b.free_energy()
+    for i, (n, r) in enumerate(zip(names, runs)):
+        k = r["kal"]
+        Fr = k["sys_noname_free_energy"]
+        tol = 1e-6 if precision == NM_FP64 else 1e-6
+        assert abs(F[i] - Fr) <= tol * max(1, abs(Fr)), (n, F[i], Fr, its[i], k["newton_isaac_iterations"])
+        # φ of the final field against the reference's converged profile
+        ctx = Context(plans[i], NM_FP64)
+        xd = dev(x[b.offsets[i]:b.offsets[i + 1]])
+        gd = torch.zeros_like(xd)
+        ctx.residual_dev(xd.data_ptr(), gd.data_ptr())
+        phi = ctx.field(0).reshape(plans[i].n_seg, -1)
+        for j, seg in enumerate(plans[i].seg_names):
+            assert rel_err(interior(plans[i], phi[j]), pro_column(r, f"mon_{seg}_phi")) < 1e-6, (n, seg)
+        if precision == NM_FP64:
+            assert abs(its[i] - k["newton_isaac_iterations"]) <= max(3, 0.5 * k["newton_isaac_iterations"])
+
+
+def test_batched_fp64_equals_single_problem_path():
+    """Same problem alone and inside a batch: identical results (the CTA of
+    one problem does not depend on its neighbours)."""
+    names = _batch_cases()[:4]
+    runs = [load_golden(n)["runs"]["conv"] for n in names]
+    plans = [Plan(r["input"]) for r in runs]
+    x = np.concatenate([np.array(r["x"]) for r in runs])
+    b = Batch(plans, NM_FP64)
+    xb = x.copy()
+    its_b, _, _ = b.solve_host(xb)
+    for i in range(len(plans)):
+        bi = Batch([plans[i]], NM_FP64)
+        xi = np.array(runs[i]["x"])
+        its_i, _, _ = bi.solve_host(xi)
+        assert its_i[0] == its_b[i]
+        assert np.array_equal(xi, xb[b.offsets[i]:b.offsets[i + 1]])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_propagate_and_side_match_oracle(name):
+    g = load_golden(name)
+    run = next(iter(g["runs"].values()))
+    plan = Plan(run["input"])
+    ctx = Context(plan, NM_FP64)
+    orc = Oracle(plan)
+    rng = np.random.default_rng(7)
+    G = rng.uniform(0.5, 1.5, plan.M)
+    G1 = rng.uniform(0.5, 1.5, plan.M)
+    # the reference keeps a frozen wall at 'surface' halo layers
+    mask = plan.interior_mask()
+    c = plan.c
+    ref = orc.propagate(G * 1.0, G1)
+    Gd, G1d, out = dev(G), dev(G1), torch.zeros(plan.M, dtype=torch.float64, device="cuda")
+    surf = any(c.bc[i] == 2 for i in range(6))
+    if not surf:
+        ctx.propagate_dev(Gd.data_ptr(), G1d.data_ptr(), out.data_ptr())
+        assert rel_err(host(out)[mask], ref[mask]) < 1e-12
+        X = rng.uniform(0, 1, plan.M)
+        side_ref = orc.side(orc_bounds(orc, X))
+        out2 = torch.zeros_like(out)
+        ctx.side_dev(dev(X).data_ptr(), out2.data_ptr())
+        assert rel_err(host(out2)[mask], side_ref[mask]) < 1e-12
+
+
+def orc_bounds(orc, X):
+    # Side() reads halos as set_bounds leaves them: apply set_bounds through a
+    # propagate with G1 = 1 of a copy (propagate refreshes the input's halo)
+    Y = np.ascontiguousarray(X, dtype=np.float64).copy()
+    import ctypes as C
+    from orc import load, _p
+    out = np.zeros_like(Y)
+    load().orc_propagate(orc._h, _p(Y), None, _p(out))
+    return Y
+
+
+def test_solves_are_deterministic():
+    run = load_golden("brush2d_cyl")["runs"]["conv"]
+    plan = Plan(run["input"])
+    ctx = Context(plan, NM_FP64)
+    x1 = np.array(run["x"])
+    x2 = x1.copy()
+    r1, _ = ctx.solve_host(x1)
+    r2, _ = ctx.solve_host(x2)
+    assert r1.iterations == r2.iterations
+    assert np.array_equal(x1, x2)
