@@ -67,13 +67,19 @@ def instance_text(nl: int, N: int, sigma: float, chi: float, star: bool) -> str:
 
 
 def workload(n: int = N_INSTANCES):
+    """Seeded instances.  Draws whose grafted amount θ = σN exceeds 40% of
+    the lattice (a brush that would fill the box; the reference itself
+    refuses θ > volume, molecule.cpp CheckInput) are redrawn."""
     rng = np.random.default_rng(SEED)
     out = []
     for i in range(n):
-        nl = int(rng.integers(50, 401))
-        N = int(rng.integers(20, 501))
-        sigma = float(rng.uniform(0.01, 0.1))
-        chi = float(rng.uniform(0.0, 1.0))
+        while True:
+            nl = int(rng.integers(50, 401))
+            N = int(rng.integers(20, 501))
+            sigma = float(rng.uniform(0.01, 0.1))
+            chi = float(rng.uniform(0.0, 1.0))
+            if sigma * N <= 0.4 * nl:
+                break
         out.append(instance_text(nl, N, sigma, chi, star=(i % 10 == 9)))
     return out
 

@@ -225,6 +225,9 @@ int nm_batch_solve_host(nm_batch* b, double* x_host, int* iterations,
 /* element offset of problem i's x in the concatenated vector; total in
  * offsets[n_plans] */
 int nm_batch_offsets(nm_batch* b, long long* offsets);
+/* per-problem iteration counts of the FP32-propagator phase of the last
+ * solve (0 for FP64 batches) */
+int nm_batch_stats(nm_batch* b, int* fp32_iterations);
 /* per-problem free energy / grand potential of the final state */
 int nm_batch_free_energy(nm_batch* b, double* F, double* Omega);
 long long nm_batch_launch_count(nm_batch* b);

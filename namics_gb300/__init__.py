@@ -244,6 +244,11 @@ class Batch:
                                                _dptr(res), st.ctypes.data_as(_abi.ip)))
         return it, res, st
 
+    def fp32_iterations(self) -> np.ndarray:
+        out = np.zeros(len(self.plans), dtype=np.int32)
+        _check(_abi.load().nm_batch_stats(self._h, out.ctypes.data_as(_abi.ip)))
+        return out
+
     def free_energy(self):
         n = len(self.plans)
         F = np.zeros(n)

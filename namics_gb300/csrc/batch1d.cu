@@ -27,9 +27,10 @@
 
 namespace nm {
 
-#define B1_THREADS 256
+#define B1_THREADS 128
+#define B1_KS 4         // sites per thread in the register path: MX <= 512
 #define B1_MAXB 64      // blocks per molecule
-#define B1_MAXM 16      // DIIS history in the batched path
+#define B1_MAXM 12      // DIIS history in the batched path
 
 struct B1Mol {
     int freedom, pinned, n_blocks, n_store, n_molmon, mm0;  // mm0: first (mol, molmon) pair index
@@ -54,6 +55,7 @@ struct B1Prob {
     double mm_frac[NM_MAX_MM];
     B1Mol mol[NM_MAX_MOL];
     double* x;           // [iv] in/out
+    double* g;           // [iv] residual scratch
     double* xR;          // [m*iv]
     double* xx0;         // [m*iv]
     // results
@@ -64,6 +66,33 @@ struct B1Prob {
 };
 
 // ---------------------------------------------------------------- helpers
+// Hot lattice constants, kept in registers (the descriptor itself lives in
+// global memory and would be re-read after every global store otherwise).
+struct Lat1 { int MX, M, b1, bm, geom; };
+template <typename T> struct Coef { T lam, lmid; const T* lm1; const T* l0; const T* l1; };
+
+// 1-gradient neighbour sum at interior site x (LG1Planar.cpp:138-159,
+// LGrad1.cpp:432-454).  WALL: a 'surface' halo is a frozen wall where every
+// propagator is 0, so it is not read; otherwise the stored halo value is used
+// (φ of a frozen wall segment, for Side()).
+template <typename T, bool WALL>
+__device__ __forceinline__ T sten1(const Lat1& L, const Coef<T>& C, const T* __restrict__ g, int x) {
+    int xm = x - 1 == 0 ? L.b1 : x - 1;
+    int xp = x + 1 == L.MX + 1 ? L.bm : x + 1;
+    T gm = (WALL && xm == 0) ? (T)0 : g[xm];
+    T gp = (WALL && xp == L.MX + 1) ? (T)0 : g[xp];
+    if (L.geom == 0) return C.lam * gm + C.lmid * g[x] + C.lam * gp;
+    return g[x] * C.l0[x] + gm * C.lm1[x] + gp * C.l1[x];
+}
+
+// Branch-free step stencil on a shared-memory propagator whose halo slots hold
+// the values set_bounds would copy there (0 at a frozen 'surface' wall).
+template <typename T, bool CURV>
+__device__ __forceinline__ T stb(const T* __restrict__ g, int x, T lam, T lmid, T cm, T c0, T cp) {
+    if (CURV) return g[x] * c0 + g[x - 1] * cm + g[x + 1] * cp;
+    return lam * g[x - 1] + lmid * g[x] + lam * g[x + 1];
+}
+
 __device__ __forceinline__ double b1_block_sum(double v, double* red) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -76,126 +105,210 @@ __device__ __forceinline__ double b1_block_sum(double v, double* red) {
     return r;
 }
 
-__device__ __forceinline__ double b1_block_max(double v, double* red) {
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
-    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+__device__ __forceinline__ float b1_block_maxf(float v, double* red) {
+    unsigned wm = __reduce_max_sync(0xffffffffu, __float_as_uint(fmaxf(v, 0.f)));
+    float* rf = (float*)red;
     __syncthreads();
-    if (l == 0) red[w] = v;
+    if ((threadIdx.x & 31) == 0) rf[threadIdx.x >> 5] = __uint_as_float(wm);
     __syncthreads();
-    double r = 0;
-    for (int i = 0; i < (int)(blockDim.x >> 5); i++) r = fmax(r, red[i]);
+    float r = 0.f;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) r = fmaxf(r, rf[i]);
     __syncthreads();
     return r;
 }
 
-// one 1-gradient stencil value at interior site x of array g (halo mapped)
-template <typename T>
-__device__ __forceinline__ T b1_stencil(const B1Prob& P, const T* g, int x) {
-    int xm = x - 1 == 0 ? P.b1 : x - 1;
-    int xp = x + 1 == P.MX + 1 ? P.bm : x + 1;
-    if (P.geom == 0) {
-        T lam = (T)P.lam;
-        return lam * g[xm] + ((T)1.0 - (T)2.0 * lam) * g[x] + lam * g[xp];
-    }
-    return g[x] * (T)P.l0[x] + g[xm] * (T)P.lm1[x] + g[xp] * (T)P.l1[x];
+// exact 2^e without FP64 or library calls: 0 below the normal range (such
+// contributions are < 1e-38 of the largest), +inf above it
+__device__ __forceinline__ float pow2f(int e) {
+    if (e < -126) return 0.f;
+    if (e > 127) return __int_as_float(0x7f800000);
+    return __int_as_float((e + 127) << 23);
+}
+__device__ __forceinline__ int expo(float v) {  // frexp exponent of v > 0
+    int e = ((__float_as_int(v) >> 23) & 0xff) - 126;
+    return v > 0.f ? e : 0;
 }
 
-__device__ __forceinline__ double b1_stencil_d(const B1Prob& P, const double* g, int x) {
-    return b1_stencil<double>(P, g, x);
-}
-
-// Scale bookkeeping for FP32 propagators: after a step, every thread knows
-// the block-wide max of the new vector (double-buffered warp slots) and the
-// next step multiplies by 2^-e.
+// Double-buffered warp slots: one barrier per step gives every thread the
+// block max of the vector just written.
 struct Scaler {
     float* slots;  // [2][32]
     int par;
-};
-
-template <typename T, bool SCALED>
-struct Prop {
-    // out(x) = stencil(in)(x)·w(x)·2^-e_in for interior x; returns block max
-    // exponent of out when SCALED (0 otherwise).  Ends with __syncthreads.
-    __device__ static int step(const B1Prob& P, const T* in, const T* w, T* out, int e_in,
-                               T* gstore, Scaler& sc) {
-        float lmax = 0.f;
-        T f = (T)1.0;
-        if (SCALED) f = (T)ldexpf(1.0f, -e_in);
-        for (int x = threadIdx.x + 1; x <= P.MX; x += blockDim.x) {
-            T v = b1_stencil<T>(P, in, x) * w[x];
-            if (SCALED) { v = v * f; lmax = fmaxf(lmax, fabsf((float)v)); }
-            out[x] = v;
-            if (gstore) gstore[x] = v;
-        }
-        int e = 0;
-        if (SCALED) {
-            for (int o = 16; o > 0; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-            if ((threadIdx.x & 31) == 0) sc.slots[sc.par * 32 + (threadIdx.x >> 5)] = lmax;
-        }
+    __device__ __forceinline__ int block_exp(float lmax) {
+        unsigned wm = __reduce_max_sync(0xffffffffu, __float_as_uint(lmax));
+        if ((threadIdx.x & 31) == 0) slots[par * 32 + (threadIdx.x >> 5)] = __uint_as_float(wm);
         __syncthreads();
-        if (SCALED) {
-            float gm = 0.f;
-            for (int i = 0; i < (int)(blockDim.x >> 5); i++) gm = fmaxf(gm, sc.slots[sc.par * 32 + i]);
-            sc.par ^= 1;
-            if (gm > 0.f) frexpf(gm, &e);
-        }
-        return e;
+        float gm = 0.f;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) gm = fmaxf(gm, slots[par * 32 + i]);
+        par ^= 1;
+        return expo(gm);
     }
 };
 
+// Solve A c = 1 (A: kd×kd in shared memory, row-major with stride kd+1 and
+// the right-hand side in column kd) by Gaussian elimination with partial
+// pivoting, FP64, one warp.  Same system as SFNewton::Ax (sfnewton.cpp:793).
+__device__ void warp_solve(double* A, double* c, int kd) {
+    const int lane = threadIdx.x & 31;
+    const int ld = kd + 1;
+    for (int k = 0; k < kd; k++) {
+        // pivot: max |A[i][k]| for i >= k
+        double best = -1;
+        int bi = k;
+        for (int i = k + lane; i < kd; i += 32) {
+            double v = fabs(A[i * ld + k]);
+            if (v > best) { best = v; bi = i; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            double ob = __shfl_down_sync(0xffffffffu, best, o);
+            int oi = __shfl_down_sync(0xffffffffu, bi, o);
+            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+        }
+        bi = __shfl_sync(0xffffffffu, bi, 0);
+        if (bi != k)
+            for (int j = k + lane; j <= kd; j += 32) {
+                double t = A[k * ld + j]; A[k * ld + j] = A[bi * ld + j]; A[bi * ld + j] = t;
+            }
+        __syncwarp();
+        double piv = A[k * ld + k];
+        int rows = kd - k - 1, cols = kd - k;  // columns k+1..kd
+        for (int e = lane; e < rows * cols; e += 32) {
+            int i = k + 1 + e / cols, j = k + 1 + e % cols;
+            A[i * ld + j] -= (A[i * ld + k] / piv) * A[k * ld + j];
+        }
+        __syncwarp();
+    }
+    if (lane == 0)
+        for (int i = kd - 1; i >= 0; i--) {
+            double v = A[i * ld + kd];
+            for (int j = i + 1; j < kd; j++) v -= A[i * ld + j] * c[j];
+            c[i] = v / A[i * ld + i];
+        }
+    __syncwarp();
+}
+
 // ---------------------------------------------------------------- kernel
-// Shared-memory working set of one problem.
 struct B1S {
-    double *G1, *phi, *phitot, *alpha, *x, *g, *rho, *red, *Aij, *Ci, *sc, *spb, *gram;
-    void *cur, *nxt, *G1t;
-    double *phif;
-    int *phie;
+    void* G1;       // [ns*M] T   (FP32 phase: G1·2^-eg)
+    void* phi;      // [ns*M] R
+    void* rho;      // [n_mm*M] R
+    void* phitot;   // [M] R
+    void *cur, *nxt;  // [M] T
+    float *cm1, *c0, *cp1;  // curved-lattice weights as float
+    double *red, *Aij, *Ci, *As, *sc, *spb, *gram;
+    double* phif;
+    int* phie;
+    int* eg;
     int* status;
 };
 
 // One residual evaluation g(x) (System::Classical_residual) with propagators
-// of type T.  Ends with __syncthreads; S.g holds the residual.
-template <typename T, bool SCALED>
-__device__ void b1_residual(B1Prob& P, B1S& S, Scaler& scl) {
-    const int M = P.M, MX = P.MX, ns = P.ns, nit = P.nit;
+// of type T and the composition / residual arithmetic in type R.  FP64 phase:
+// T = R = double, the reference's arithmetic.  FP32 phase: T = R = float with
+// power-of-two scale bookkeeping; G(N), normalisation and DIIS stay FP64.
+#define B1_RS 4  // FP32: block max and rescale every B1_RS steps
+
+template <typename T, bool SC, bool CURV>
+__device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Scaler& scl,
+                            const double* __restrict__ x, double* __restrict__ g) {
+    typedef T R;
+    const int M = L.M, MX = L.MX, ns = P.ns, nit = P.nit, n_mm = P.n_mm;
     const int tid = threadIdx.x, nth = blockDim.x;
-    double *G1 = S.G1, *phi = S.phi, *phitot = S.phitot, *alpha = S.alpha, *x = S.x, *g = S.g,
-           *rho = S.rho, *red = S.red, *sc = S.sc, *spb = S.spb;
+    T* G1 = (T*)S.G1;
+    R* phi = (R*)S.phi;
+    R* rho = (R*)S.rho;
+    R* phitot = (R*)S.phitot;
     T* cur = (T*)S.cur;
     T* nxt = (T*)S.nxt;
-    T* G1t = (T*)S.G1t;
-    // G1 (PutU + PrepareForCalculations)
-    for (int s = tid; s < M; s += nth) {
-        int src = s == 0 ? P.b1 : (s == MX + 1 ? P.bm : s);
-        for (int i = 0; i < ns; i++) {
-            int itx = P.seg_it[i];
-            double u = itx >= 0 ? x[itx * M + src] : 0.0;
-            double v = exp(-u) * P.gmask[i * M + s];
-            G1[i * M + s] = v;
-            G1t[i * M + s] = (T)v;
+    double *red = S.red, *sc = S.sc, *spb = S.spb;
+    int nk = 0;
+    for (int k = 0; k < B1_KS; k++) if (tid + 1 + k * nth <= MX) nk = k + 1;
+    // per owned site: curved-lattice weights and the halo slots it feeds
+    T cmr[B1_KS], c0r[B1_KS], cpr[B1_KS];
+    bool lor[B1_KS], hir[B1_KS];
+#pragma unroll
+    for (int q = 0; q < B1_KS; q++) {
+        int xk = tid + 1 + q * nth;
+        bool ok = q < nk;
+        cmr[q] = (CURV && ok) ? C.lm1[xk] : (T)0;
+        c0r[q] = (CURV && ok) ? C.l0[xk] : (T)0;
+        cpr[q] = (CURV && ok) ? C.l1[xk] : (T)0;
+        lor[q] = ok && xk == L.b1;          // b1 in 1..MX unless 'surface'
+        hir[q] = ok && xk == L.bm;          // bm in 1..MX unless 'surface'
+    }
+    const T lam = C.lam, lmid = C.lmid;
+    if (tid == 0) { cur[0] = cur[MX + 1] = nxt[0] = nxt[MX + 1] = (T)0; }
+    // G1 = exp(-u)·mask (PutU + Segment::PrepareForCalculations)
+    for (int i = 0; i < ns; i++) {
+        int itx = P.seg_it[i];
+        const double* gm = P.gmask + i * M;
+        if (SC) {
+            // G1·2^-eg = 2^(-u·log2e - eg) with eg = ceil(max(-u·log2e)):
+            // exact power-of-two scaling that cannot overflow for any u
+            float vmax = -3.0e38f;
+            for (int s = tid; s < M; s += nth) {
+                int src = s == 0 ? L.b1 : (s == MX + 1 ? L.bm : s);
+                float v = itx >= 0 ? -(float)x[itx * M + src] * 1.4426950408889634f : 0.f;
+                if (gm[s] != 0.0) vmax = fmaxf(vmax, v);
+            }
+            // block max of a possibly negative value: shift to the ordered-int domain
+            int key = __float_as_int(vmax);
+            key = key >= 0 ? key : (key ^ 0x7fffffff);
+            int wk = __reduce_max_sync(0xffffffffu, key);
+            int* rk = (int*)red;
+            __syncthreads();
+            if ((tid & 31) == 0) rk[tid >> 5] = wk;
+            __syncthreads();
+            int bk = rk[0];
+            for (int w2 = 1; w2 < nth / 32; w2++) bk = max(bk, rk[w2]);
+            __syncthreads();
+            bk = bk >= 0 ? bk : (bk ^ 0x7fffffff);
+            float vm = __int_as_float(bk);
+            int e = vm > -1.0e30f ? (int)ceilf(vm) : 0;
+            if (tid == 0) S.eg[i] = e;
+            for (int s = tid; s < M; s += nth) {
+                int src = s == 0 ? L.b1 : (s == MX + 1 ? L.bm : s);
+                float v = itx >= 0 ? -(float)x[itx * M + src] * 1.4426950408889634f : 0.f;
+                G1[i * M + s] = (T)(exp2f(v - (float)e) * (float)gm[s]);
+            }
+        } else {
+            for (int s = tid; s < M; s += nth) {
+                int src = s == 0 ? L.b1 : (s == MX + 1 ? L.bm : s);
+                double u = itx >= 0 ? x[itx * M + src] : 0.0;
+                G1[i * M + s] = (T)(exp(-u) * gm[s]);
+            }
         }
     }
-    for (int i = tid; i < P.n_mm * M; i += nth) rho[i] = 0;
-    for (int i = tid; i < 2 * M; i += nth) cur[i] = (T)0;  // halos of cur/nxt are 0
+    for (int i = tid; i < n_mm * M; i += nth) rho[i] = (R)0;
     __syncthreads();
     for (int m = 0; m < P.nmol; m++) {
         const B1Mol& D = P.mol[m];
-        T* Gf = (T*)D.Gf;
-        T* Pc = (T*)D.Pc;
-        T* Qb = (T*)D.Q;
-        // forward sweep (post-order blocks)
+        T* __restrict__ Gf = (T*)D.Gf;
+        T* __restrict__ Pc = (T*)D.Pc;
+        T* __restrict__ Qb = (T*)D.Q;
+        int* __restrict__ ef = D.ef;
+        // ---- forward sweep (post-order blocks) ----
         for (int b = 0; b < D.n_blocks; b++) {
             const nm_block B = D.blocks[b];
-            const T* w = G1t + B.seg * M;
-            int s = B.s0;
-            int ecur = 0;
+            const T* w = G1 + B.seg * M;
+            const int egs = SC ? S.eg[B.seg] : 0;
+            T wr[B1_KS];
+#pragma unroll
+            for (int q = 0; q < B1_KS; q++) wr[q] = q < nk ? w[tid + 1 + q * nth] : (T)0;
+            int s = B.s0, ecur = 0;
+            float lmax = 0.f;
             if (B.n_child == 0) {
-                for (int xx = tid + 1; xx <= MX; xx += nth) {
-                    T v = w[xx];
-                    cur[xx] = v;
-                    Gf[(size_t)s * M + xx] = v;
-                }
-                if (SCALED && tid == 0) D.ef[s] = 0;
+#pragma unroll
+                for (int q = 0; q < B1_KS; q++)
+                    if (q < nk) {
+                        int xk = tid + 1 + q * nth;
+                        cur[xk] = wr[q];
+                        if (lor[q]) cur[0] = wr[q];
+                        if (hir[q]) cur[MX + 1] = wr[q];
+                        Gf[(size_t)s * M + xk] = wr[q];
+                        if (SC) lmax = fmaxf(lmax, (float)wr[q]);
+                    }
+                ecur = egs;
             } else {
                 // join: Gf = P(Gf[c0])·G1 · Π_c [P(Gf[c])·KSAM]^mult
                 int nc = B.n_child;
@@ -205,75 +318,84 @@ __device__ void b1_residual(B1Prob& P, B1S& S, Scaler& scl) {
                 if (!simple) {
                     for (int c = 0; c < nc; c++) {
                         int cb = D.child_index[B.child0 + c];
-                        const nm_block C = D.blocks[cb];
-                        int sl = C.s0 + C.length - 1;
-                        const T* src = Gf + (size_t)sl * M;
-                        T* dst = Pc + (size_t)cb * M;
+                        const nm_block Cb = D.blocks[cb];
+                        int sl = Cb.s0 + Cb.length - 1;
                         for (int xx = tid + 1; xx <= MX; xx += nth)
-                            dst[xx] = b1_stencil<T>(P, src, xx) * (T)P.ksam[xx];
-                        if (SCALED && tid == 0) D.epc[cb] = D.ef[sl];
+                            Pc[(size_t)cb * M + xx] = sten1<T, true>(L, C, Gf + (size_t)sl * M, xx) * (T)P.ksam[xx];
+                        if (SC && tid == 0) D.epc[cb] = ef[sl];
                     }
                     __syncthreads();
                 }
                 int sl0 = C0.s0 + C0.length - 1;
-                const T* src = Gf + (size_t)sl0 * M;
-                int ejoin = SCALED ? D.ef[sl0] : 0;
+                int ejoin = SC ? ef[sl0] + egs : 0;
                 for (int xx = tid + 1; xx <= MX; xx += nth) {
-                    T v = b1_stencil<T>(P, src, xx) * w[xx];
+                    T v = sten1<T, true>(L, C, Gf + (size_t)sl0 * M, xx) * w[xx];
                     if (!simple) {
                         for (int k = 1; k < C0.mult; k++) v = v * Pc[(size_t)c0 * M + xx];
                         for (int c = 1; c < nc; c++) {
                             int cb = D.child_index[B.child0 + c];
-                            int mu = D.blocks[cb].mult;
-                            for (int k = 0; k < mu; k++) v = v * Pc[(size_t)cb * M + xx];
+                            for (int k = 0; k < D.blocks[cb].mult; k++) v = v * Pc[(size_t)cb * M + xx];
                         }
                     }
                     cur[xx] = v;
                 }
-                if (SCALED && !simple) {
+                if (SC && !simple) {
                     ejoin += (C0.mult - 1) * D.epc[c0];
                     for (int c = 1; c < nc; c++) {
                         int cb = D.child_index[B.child0 + c];
                         ejoin += D.blocks[cb].mult * D.epc[cb];
                     }
                 }
-                if (SCALED) {
-                    float lmax = 0.f;
-                    for (int xx = tid + 1; xx <= MX; xx += nth) lmax = fmaxf(lmax, fabsf((float)cur[xx]));
-                    double gm = b1_block_max((double)lmax, red);  // syncs
-                    int e = 0;
-                    if (gm > 0) frexp(gm, &e);
-                    T f = (T)ldexp(1.0, -e);
-                    for (int xx = tid + 1; xx <= MX; xx += nth) cur[xx] = cur[xx] * f;
+                if (SC) {
+                    float lm = 0.f;
+                    for (int xx = tid + 1; xx <= MX; xx += nth) lm = fmaxf(lm, (float)cur[xx]);
+                    int e = expo(b1_block_maxf(lm, red));
+                    float f = pow2f(-e);
+                    for (int xx = tid + 1; xx <= MX; xx += nth) cur[xx] = (T)((float)cur[xx] * f);
                     ejoin += e;
                 }
-                for (int xx = tid + 1; xx <= MX; xx += nth) Gf[(size_t)s * M + xx] = cur[xx];
-                if (SCALED && tid == 0) D.ef[s] = ejoin;
+                __syncthreads();
+                for (int xx = tid + 1; xx <= MX; xx += nth) {
+                    Gf[(size_t)s * M + xx] = cur[xx];
+                    if (xx == L.b1) cur[0] = cur[xx];
+                    if (xx == L.bm) cur[MX + 1] = cur[xx];
+                    if (SC) lmax = fmaxf(lmax, (float)cur[xx]);
+                }
                 ecur = ejoin;
             }
-            // exponent of cur's max, for the first step's scale
-            int enext = 0;
-            if (SCALED) {
-                float lmax = 0.f;
-                for (int xx = tid + 1; xx <= MX; xx += nth) lmax = fmaxf(lmax, fabsf((float)cur[xx]));
-                double gm = b1_block_max((double)lmax, red);
-                if (gm > 0) frexp(gm, &enext);
-            } else {
-                __syncthreads();
-            }
+            if (SC && tid == 0) ef[s] = ecur;
+            int enext = SC ? scl.block_exp(lmax) : 0;
+            if (!SC) __syncthreads();
+            // steps: Gf[s] = P(Gf[s-1])·G1·2^-enext (rescale every B1_RS steps)
             for (int k = 1; k < B.length; k++) {
                 s++;
-                int e2 = Prop<T, SCALED>::step(P, cur, w, nxt, enext, Gf + (size_t)s * M, scl);
-                if (SCALED) { ecur += enext; if (tid == 0) D.ef[s] = ecur; }
+                T f = SC ? (T)pow2f(-enext) : (T)1;
+                T* __restrict__ gs = Gf + (size_t)s * M;
+                const bool red_step = SC && (k % B1_RS) == 0;
+                float lm = 0.f;
+#pragma unroll
+                for (int q = 0; q < B1_KS; q++)
+                    if (q < nk) {
+                        int xk = tid + 1 + q * nth;
+                        T v = stb<T, CURV>(cur, xk, lam, lmid, cmr[q], c0r[q], cpr[q]) * wr[q];
+                        if (SC) { v = v * f; lm = fmaxf(lm, (float)v); }
+                        nxt[xk] = v;
+                        if (lor[q]) nxt[0] = v;
+                        if (hir[q]) nxt[MX + 1] = v;
+                        gs[xk] = v;
+                    }
+                int e2 = 0;
+                if (red_step) e2 = scl.block_exp(lm); else __syncthreads();
+                if (SC) { ecur += enext + egs; if (tid == 0) ef[s] = ecur; }
                 T* t = cur; cur = nxt; nxt = t;
                 enext = e2;
             }
             __syncthreads();
         }
-        // G(N) = Σ Gf[root]·L (ComputeGN; planar: plain sum)
-        const nm_block R = D.blocks[D.n_blocks - 1];
-        int sroot = R.s0 + R.length - 1;
-        int eroot = SCALED ? D.ef[sroot] : 0;
+        // ---- G(N) = Σ Gf[root]·L (ComputeGN), FP64 ----
+        const nm_block Rb = D.blocks[D.n_blocks - 1];
+        int sroot = Rb.s0 + Rb.length - 1;
+        int eroot = SC ? ef[sroot] : 0;
         {
             double acc = 0;
             for (int xx = tid + 1; xx <= MX; xx += nth) {
@@ -283,47 +405,116 @@ __device__ void b1_residual(B1Prob& P, B1S& S, Scaler& scl) {
             double GN = b1_block_sum(acc, red);
             if (tid == 0) { sc[5 * m + 0] = GN; sc[5 * m + 3] = (double)eroot; }
         }
-        // backward sweep (pre-order, explicit stack)
+        // ---- backward sweep fused with composition (pre-order) ----
         int stack[B1_MAXB];
         int sp = 0;
         stack[sp++] = D.n_blocks - 1;
         while (sp > 0) {
             int b = stack[--sp];
             const nm_block B = D.blocks[b];
-            const T* w = G1t + B.seg * M;
-            double* rr = rho + (D.mm0 + B.molmon) * M;
-            double d = B.degeneracy;
+            const T* w = G1 + B.seg * M;
+            const int egs = SC ? S.eg[B.seg] : 0;
+            R* rr = rho + (D.mm0 + B.molmon) * M;
+            const T d = (T)B.degeneracy;
+            T wr[B1_KS], acc[B1_KS], cmp[B1_KS], gfn[B1_KS];
+#pragma unroll
+            for (int q = 0; q < B1_KS; q++) {
+                wr[q] = q < nk ? w[tid + 1 + q * nth] : (T)0;
+                acc[q] = (T)0; cmp[q] = (T)0;
+            }
             int s = B.s0 + B.length - 1;
-            int eb = 0, enext = 0;
+            int eb, enext;
+            float lm = 0.f;
             if (B.parent < 0) {
-                for (int xx = tid + 1; xx <= MX; xx += nth) cur[xx] = w[xx];
-                if (SCALED) {
-                    float lmax = 0.f;
-                    for (int xx = tid + 1; xx <= MX; xx += nth) lmax = fmaxf(lmax, fabsf((float)cur[xx]));
-                    double gm = b1_block_max((double)lmax, red);
-                    if (gm > 0) frexp(gm, &enext);
-                } else __syncthreads();
+#pragma unroll
+                for (int q = 0; q < B1_KS; q++)
+                    if (q < nk) {
+                        cur[tid + 1 + q * nth] = wr[q];
+                        if (lor[q]) cur[0] = wr[q];
+                        if (hir[q]) cur[MX + 1] = wr[q];
+                        if (SC) lm = fmaxf(lm, (float)wr[q]);
+                    }
+                eb = egs;
             } else {
-                const T* q = Qb + (size_t)b * M;
-                eb = SCALED ? D.eq[b] : 0;
-                enext = Prop<T, SCALED>::step(P, q, w, cur, 0, nullptr, scl);
+                const T* q0 = Qb + (size_t)b * M;
+#pragma unroll
+                for (int q = 0; q < B1_KS; q++)
+                    if (q < nk) {
+                        int xk = tid + 1 + q * nth;
+                        T v = sten1<T, true>(L, C, q0, xk) * wr[q];
+                        cur[xk] = v;
+                        if (lor[q]) cur[0] = v;
+                        if (hir[q]) cur[MX + 1] = v;
+                        if (SC) lm = fmaxf(lm, (float)v);
+                    }
+                eb = (SC ? D.eq[b] : 0) + egs;
             }
-            for (int xx = tid + 1; xx <= MX; xx += nth) {
-                double f = (double)Gf[(size_t)s * M + xx] * (double)cur[xx];
-                if (SCALED) f = ldexp(f, D.ef[s] + eb - eroot);
-                rr[xx] += d == 1.0 ? f : d * f;
+            enext = SC ? scl.block_exp(lm) : 0;
+            if (!SC) __syncthreads();
+            {   // top segment of the block
+                const T* gsrc = Gf + (size_t)s * M;
+                T sf = SC ? (T)pow2f(ef[s] + eb - eroot) * d : d;
+#pragma unroll
+                for (int q = 0; q < B1_KS; q++)
+                    if (q < nk) acc[q] = gsrc[tid + 1 + q * nth] * cur[tid + 1 + q * nth] * sf;
             }
+            // prefetch the stored forward propagator of the next segment
+            int efn = 0;
+            if (s - 1 >= B.s0) {
+                const T* gsrc = Gf + (size_t)(s - 1) * M;
+#pragma unroll
+                for (int q = 0; q < B1_KS; q++) gfn[q] = q < nk ? gsrc[tid + 1 + q * nth] : (T)0;
+                if (SC) efn = ef[s - 1];
+            }
+            int nacc = 0, kstep = 0;
             for (s = s - 1; s >= B.s0; s--) {
-                int e2 = Prop<T, SCALED>::step(P, cur, w, nxt, enext, nullptr, scl);
-                if (SCALED) eb += enext;
+                T gf[B1_KS];
+#pragma unroll
+                for (int q = 0; q < B1_KS; q++) gf[q] = gfn[q];
+                int efs = efn;
+                if (s - 1 >= B.s0) {
+                    const T* gsrc = Gf + (size_t)(s - 1) * M;
+#pragma unroll
+                    for (int q = 0; q < B1_KS; q++) if (q < nk) gfn[q] = gsrc[tid + 1 + q * nth];
+                    if (SC) efn = ef[s - 1];
+                }
+                T f = SC ? (T)pow2f(-enext) : (T)1;
+                const bool red_step = SC && (++kstep % B1_RS) == 0;
+                float lmx = 0.f;
+#pragma unroll
+                for (int q = 0; q < B1_KS; q++)
+                    if (q < nk) {
+                        int xk = tid + 1 + q * nth;
+                        T v = stb<T, CURV>(cur, xk, lam, lmid, cmr[q], c0r[q], cpr[q]) * wr[q];
+                        if (SC) { v = v * f; lmx = fmaxf(lmx, (float)v); }
+                        nxt[xk] = v;
+                        if (lor[q]) nxt[0] = v;
+                        if (hir[q]) nxt[MX + 1] = v;
+                        gf[q] *= v;
+                    }
+                int e2 = 0;
+                if (red_step) e2 = scl.block_exp(lmx); else __syncthreads();
+                if (SC) eb += enext + egs;
                 T* t = cur; cur = nxt; nxt = t;
                 enext = e2;
-                for (int xx = tid + 1; xx <= MX; xx += nth) {
-                    double f = (double)Gf[(size_t)s * M + xx] * (double)cur[xx];
-                    if (SCALED) f = ldexp(f, D.ef[s] + eb - eroot);
-                    rr[xx] += d == 1.0 ? f : d * f;
+                T sf = SC ? (T)pow2f(efs + eb - eroot) * d : d;
+#pragma unroll
+                for (int q = 0; q < B1_KS; q++) {  // compensated sum (Kahan)
+                    T y = gf[q] * sf - cmp[q];
+                    T t2 = acc[q] + y;
+                    cmp[q] = (t2 - acc[q]) - y;
+                    acc[q] = t2;
+                }
+                if (SC && ++nacc == 32) {  // FP32: flush into rho
+#pragma unroll
+                    for (int q = 0; q < B1_KS; q++)
+                        if (q < nk) { rr[tid + 1 + q * nth] += acc[q] - cmp[q]; acc[q] = (T)0; cmp[q] = (T)0; }
+                    nacc = 0;
                 }
             }
+#pragma unroll
+            for (int q = 0; q < B1_KS; q++)
+                if (q < nk) rr[tid + 1 + q * nth] += acc[q] - cmp[q];
             __syncthreads();
             if (B.n_child == 0) continue;
             // backward starts of the children: Q = Gb(join)·Π other P(Gf)
@@ -344,7 +535,7 @@ __device__ void b1_residual(B1Prob& P, B1S& S, Scaler& scl) {
                     }
                     q[xx] = v;
                 }
-                if (SCALED && !simple) {
+                if (SC && !simple) {
                     eq += (D.blocks[cb].mult - 1) * D.epc[cb];
                     for (int o = 0; o < B.n_child; o++) {
                         if (o == c) continue;
@@ -352,25 +543,25 @@ __device__ void b1_residual(B1Prob& P, B1S& S, Scaler& scl) {
                         eq += D.blocks[ob].mult * D.epc[ob];
                     }
                 }
-                if (SCALED && tid == 0) D.eq[cb] = eq;
+                if (SC && tid == 0) D.eq[cb] = eq;
             }
             __syncthreads();
             for (int c = B.n_child - 1; c >= 0; c--) stack[sp++] = D.child_index[B.child0 + c];
         }
         __syncthreads();
     }
-    // normalisation (system.cpp:2368-2560), one thread.  In scaled mode rho
-    // and G(N) carry the root exponent e: rho_true = rho·2^e and
-    // GN_true = GNm·2^e.  Restricted chains use n/GNm (the exponents cancel);
-    // free chains and the solvent apply φb/N and 2^e.
+    // ---- normalisation (system.cpp:2368-2560), one thread, FP64 ----
+    // FP32 phase: rho and G(N) carry the root exponent e (rho_true = rho·2^e,
+    // GN_true = GNm·2^e) and G1 is stored as G1·2^-eg.  Restricted chains use
+    // n/GNm (the e cancel); free chains and the solvent apply φb/N·2^e.
     if (tid == 0) {
         double Bsum = 0;
         for (int m = 0; m < P.nmol; m++) {
             const B1Mol& D = P.mol[m];
             double* s5 = sc + 5 * m;
             double GNm = s5[0];
-            int e = SCALED ? (int)s5[3] : 0;
-            double GN = SCALED ? ldexp(GNm, e) : GNm;
+            int e = SC ? (int)s5[3] : 0;
+            double GN = SC ? ldexp(GNm, e) : GNm;
             double norm = 0, fac = 0;
             int pe = 0;
             s5[0] = GN;
@@ -384,7 +575,7 @@ __device__ void b1_residual(B1Prob& P, B1S& S, Scaler& scl) {
             } else if (D.freedom == NM_MOL_RESTRICTED) {
                 if (GNm > 0) {
                     norm = D.n_in / GN;
-                    fac = SCALED ? D.n_in / GNm : norm;
+                    fac = SC ? D.n_in / GNm : norm;
                     if (D.pinned) s5[4] = 0;
                     else { s5[4] = D.N * norm; Bsum += s5[4]; }
                 } else if (*S.status == 0) *S.status = NM_ERR_GN;
@@ -405,101 +596,118 @@ __device__ void b1_residual(B1Prob& P, B1S& S, Scaler& scl) {
             S.phif[sv] = norm > 0 ? norm : 1.0;
         }
         for (int i = 0; i < ns; i++) spb[i] = 0;
-        for (int k = 0; k < P.n_mm; k++) spb[P.mm_seg[k]] += P.mm_frac[k] * sc[5 * P.mm_mol[k] + 4];
+        for (int k = 0; k < n_mm; k++) spb[P.mm_seg[k]] += P.mm_frac[k] * sc[5 * P.mm_mol[k] + 4];
     }
     __syncthreads();
-    // φ, φ_tot
+    // ---- φ = rho/G1·norm, φ_tot ----
+    R mmf[NM_MAX_MM];
+    for (int k = 0; k < n_mm; k++) {
+        int m = P.mm_mol[k], sg = P.mm_seg[k];
+        // FP32 phase: 2^phie / 2^eg folded into one factor
+        double f = S.phif[m];
+        if (SC) f = ldexp(f, S.phie[m] - S.eg[sg]);
+        mmf[k] = (R)f;
+    }
     for (int s = tid; s < M; s += nth) {
         bool in = s >= 1 && s <= MX;
-        double pt = 0;
+        R pt = 0;
         for (int i = 0; i < ns; i++) {
-            double v = P.phi_frozen[i * M + s];
+            R v = (R)P.phi_frozen[i * M + s];
             phi[i * M + s] = v;
             if (P.seg_frozen[i]) pt += v;
         }
-        if (in) {
-            for (int k = 0; k < P.n_mm; k++) {
-                int sg = P.mm_seg[k], m = P.mm_mol[k];
-                double g1 = G1[sg * M + s];
-                double v = g1 != 0 ? rho[k * M + s] / g1 : 0.0;
-                v *= S.phif[m];
-                if (SCALED && S.phie[m]) v = ldexp(v, S.phie[m]);
+        if (in)
+            for (int k = 0; k < n_mm; k++) {
+                int sg = P.mm_seg[k];
+                R g1 = (R)G1[sg * M + s];
+                R v = g1 != (R)0 ? rho[k * M + s] / g1 : (R)0;
+                v *= mmf[k];
                 phi[sg * M + s] += v;
                 pt += v;
             }
-        }
         phitot[s] = pt;
     }
     __syncthreads();
-    // residual (Classical_residual)
+    // ---- residual (Classical_residual) ----
+    R chir[NM_MAX_SEG * NM_MAX_SEG];
+    for (int i = 0; i < nit; i++)
+        for (int k = 0; k < ns; k++) chir[i * ns + k] = (R)P.chi[P.it_seg[i] * ns + k];
+    R spbr[NM_MAX_SEG];
+    for (int k = 0; k < ns; k++) spbr[k] = (R)spb[k];
+    Coef<R> CR = C;
+    R rinv = (R)(1.0 / nit);
     for (int s = tid; s < M; s += nth) {
         if (s < 1 || s > MX) {
             for (int i = 0; i < nit; i++) g[i * M + s] = 0;
-            alpha[s] = 0;
             continue;
         }
-        double ps[NM_MAX_SEG];
-        for (int k = 0; k < ns; k++) ps[k] = b1_stencil_d(P, phi + k * M, s);
-        double pt = phitot[s];
-        double gi[NM_MAX_SEG];
-        double al = 0;
+        R ps[NM_MAX_SEG];
+        for (int k = 0; k < ns; k++) ps[k] = sten1<R, false>(L, CR, phi + k * M, s);
+        R pt = phitot[s];
+        R gi[NM_MAX_SEG];
+        R al = 0;
         for (int i = 0; i < nit; i++) {
-            double v = x[i * M + s];
-            int r = P.it_seg[i];
+            R v = (R)x[i * M + s];
             for (int k = 0; k < ns; k++) {
-                double chi = P.chi[r * ns + k];
-                if (chi != 0 && pt > 0) v = v - chi * (ps[k] / pt - spb[k]);
+                R chi = chir[i * ns + k];
+                if (chi != (R)0 && pt > (R)0) v = v - chi * (ps[k] / pt - spbr[k]);
             }
             gi[i] = v;
             al += v;
         }
-        al = al * (1.0 / nit);
-        alpha[s] = al;
-        double km = P.ksam[s];
+        al = al * rinv;
+        R km = (R)P.ksam[s];
         for (int i = 0; i < nit; i++) {
-            double v = pt > 0 ? gi[i] - al + 1 / pt - 1.0 : 0.0;
-            g[i * M + s] = v * km;
+            R v = pt > (R)0 ? gi[i] - al + (R)1 / pt - (R)1 : (R)0;
+            g[i * M + s] = (double)(v * km);
         }
     }
     __syncthreads();
 }
 
-// fp32_first: FP32 propagators until ‖g‖ < P.sw_tol or a stall, then FP64
-// propagators (DIIS history restarted) for the final iterations, so the
-// stopping test ‖g‖ < tol is always made on an FP64 residual.
-__global__ void __launch_bounds__(B1_THREADS) k_batch1d(B1Prob* __restrict__ probs, int fp32_first) {
+// fp32_first: FP32 propagators until ‖g‖ < P.sw_tol (or a stall close to
+// convergence), then FP64 (DIIS history restarted), so the stopping test
+// ‖g‖ < tol is always made on an FP64 residual.
+__global__ void __launch_bounds__(B1_THREADS, 4) k_batch1d(B1Prob* __restrict__ probs, int fp32_first) {
     B1Prob& P = probs[blockIdx.x];
     extern __shared__ double sm[];
-    const int M = P.M, ns = P.ns, iv = P.iv;
+    const int M = P.M, ns = P.ns, iv = P.iv, n_mm = P.n_mm, m = P.m;
     const int tid = threadIdx.x, nth = blockDim.x;
+    const Lat1 L{P.MX, P.M, P.b1, P.bm, P.geom};
     B1S S;
-    S.G1 = sm;
-    S.phi = S.G1 + ns * M;
-    S.phitot = S.phi + ns * M;
-    S.alpha = S.phitot + M;
-    S.x = S.alpha + M;
-    S.g = S.x + iv;
-    S.rho = S.g + iv;
-    S.red = S.rho + P.n_mm * M;
-    S.Aij = S.red + 64;
-    S.Ci = S.Aij + B1_MAXM * B1_MAXM;
-    S.sc = S.Ci + B1_MAXM;
-    S.spb = S.sc + 5 * NM_MAX_MOL;
-    S.gram = S.spb + NM_MAX_SEG;
-    double* tail = S.gram + 8 * B1_MAXM;
-    S.cur = tail;                 // sized for double
-    S.nxt = tail + M;
-    S.G1t = tail + 2 * M;
+    double* q = sm;
+    S.G1 = q; q += ns * M;
+    S.phi = q; q += ns * M;
+    S.rho = q; q += n_mm * M;
+    S.phitot = q; q += M;
+    S.cur = q; q += M;
+    S.nxt = q; q += M;
+    S.cm1 = (float*)q; S.c0 = S.cm1 + M; S.cp1 = S.c0 + M; q += (3 * M + 1) / 2;
+    S.red = q; q += 64;
+    S.Aij = q; q += B1_MAXM * B1_MAXM;
+    S.Ci = q; q += B1_MAXM;
+    S.As = q; q += B1_MAXM * (B1_MAXM + 1);
+    S.sc = q; q += 5 * NM_MAX_MOL;
+    S.spb = q; q += NM_MAX_SEG;
+    S.gram = q; q += B1_MAXM;
     __shared__ float slots[64];
     __shared__ int sh_status;
     __shared__ double phif[NM_MAX_MOL];
     __shared__ int phie[NM_MAX_MOL];
-    S.phif = phif; S.phie = phie; S.status = &sh_status;
+    __shared__ int egs[NM_MAX_SEG];
+    S.phif = phif; S.phie = phie; S.status = &sh_status; S.eg = egs;
     Scaler scl{slots, 0};
-    double *x = S.x, *g = S.g, *red = S.red, *Aij = S.Aij, *Ci = S.Ci, *gram = S.gram;
-
-    for (int i = tid; i < iv; i += nth) x[i] = P.x[i];
+    double* __restrict__ x = P.x;
+    double* __restrict__ g = P.g;
+    double *red = S.red, *Aij = S.Aij, *Ci = S.Ci;
+    Coef<double> C64{P.lam, 1.0 - 2.0 * P.lam, P.lm1, P.l0, P.l1};
+    Coef<float> C32{(float)P.lam, 1.0f - 2.0f * (float)P.lam, S.cm1, S.c0, S.cp1};
+    if (P.geom != 0)
+        for (int s = tid; s < M; s += nth) {
+            S.cm1[s] = (float)P.lm1[s]; S.c0[s] = (float)P.l0[s]; S.cp1[s] = (float)P.l1[s];
+        }
     for (int i = tid; i < B1_MAXM * B1_MAXM; i += nth) Aij[i] = 0;
+    for (int i = tid; i < 2 * M; i += nth) ((double*)S.cur)[i] = 0;  // wall halos
     if (tid == 0) sh_status = 0;
     __syncthreads();
 
@@ -508,13 +716,19 @@ __global__ void __launch_bounds__(B1_THREADS) k_batch1d(B1Prob* __restrict__ pro
     double resid = 0, best = 1e300;
     int since_best = 0;
     for (;;) {
-        if (use32) { b1_residual<float, true>(P, S, scl); fp32_its++; }
-        else b1_residual<double, false>(P, S, scl);
+        if (use32) {
+            if (L.geom == 0) b1_residual<float, true, false>(P, L, C32, S, scl, x, g);
+            else b1_residual<float, true, true>(P, L, C32, S, scl, x, g);
+            fp32_its++;
+        } else {
+            if (L.geom == 0) b1_residual<double, false, false>(P, L, C64, S, scl, x, g);
+            else b1_residual<double, false, true>(P, L, C64, S, scl, x, g);
+        }
         if (sh_status) break;
-        // ---------------- DIIS (iterate_DIIS / DIIS / Ax) ----------------
-        int k = it % P.m;
-        double* xRk = P.xR + (size_t)k * iv;
-        double* xxk = P.xx0 + (size_t)k * iv;
+        // ---------------- DIIS (iterate_DIIS / DIIS / Ax), FP64 ----------------
+        int k = it % m;
+        double* __restrict__ xRk = P.xR + (size_t)k * iv;
+        double* __restrict__ xxk = P.xx0 + (size_t)k * iv;
         double gsq = 0;
         for (int i = tid; i < iv; i += nth) {
             double xo = x[i], gv = g[i];
@@ -524,53 +738,59 @@ __global__ void __launch_bounds__(B1_THREADS) k_batch1d(B1Prob* __restrict__ pro
             xxk[i] = xn - xo;
             gsq = P.max_norm ? fmax(gsq, fabs(gv)) : gsq + gv * gv;
         }
-        resid = P.max_norm ? b1_block_max(gsq, red) : sqrt(b1_block_sum(gsq, red));
+        if (P.max_norm) {
+            for (int o = 16; o > 0; o >>= 1) gsq = fmax(gsq, __shfl_down_sync(0xffffffffu, gsq, o));
+            __syncthreads();
+            if ((tid & 31) == 0) red[tid >> 5] = gsq;
+            __syncthreads();
+            resid = 0;
+            for (int i = 0; i < nth / 32; i++) resid = fmax(resid, red[i]);
+            __syncthreads();
+        } else resid = sqrt(b1_block_sum(gsq, red));
         if (it > 0) k_diis++;  // iteration 0 is the plain mixing step
         if (k_diis > 0) {
-            int kd = k_diis > P.m ? P.m : k_diis;
-            double acc[B1_MAXM];
-            for (int i = 0; i < kd; i++) acc[i] = 0;
-            for (int j = tid; j < iv; j += nth) {
-                double bk = xxk[j];
-                for (int i = 0; i < kd; i++) {
-                    int posi = k - kd + 1 + i;
-                    if (posi < 0) posi += P.m;
-                    acc[i] += P.xx0[(size_t)posi * iv + j] * bk;
-                }
-            }
+            int kd = k_diis > m ? m : k_diis;
+            // Gram row: warp w takes histories i = w, w+4, ...
             int w = tid >> 5, l = tid & 31;
-            for (int i = 0; i < kd; i++) {
-                double v = acc[i];
-                for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-                if (l == 0) gram[w * B1_MAXM + i] = v;
+            for (int i = w; i < kd; i += nth / 32) {
+                int posi = k - kd + 1 + i;
+                if (posi < 0) posi += m;
+                const double* a = P.xx0 + (size_t)posi * iv;
+                double acc = 0;
+                for (int j = l; j < iv; j += 32) acc += a[j] * xxk[j];
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+                if (l == 0) S.gram[i] = acc;
             }
             __syncthreads();
-            if (tid == 0) {
-                int m = P.m;
-                if (k_diis > m)
-                    for (int i = 1; i < m; i++)
-                        for (int j = 1; j < m; j++) Aij[m * (i - 1) + j - 1] = Aij[m * i + j];
-                for (int i = 0; i < kd; i++) {
-                    double D = 0;
-                    for (int ww = 0; ww < nth / 32; ww++) D += gram[ww * B1_MAXM + i];
-                    Aij[i + m * (kd - 1)] = Aij[kd - 1 + m * i] = D + 1e-9;
+            if (w == 0) {
+                if (l == 0) {
+                    if (k_diis > m)
+                        for (int i = 1; i < m; i++)
+                            for (int j = 1; j < m; j++) Aij[m * (i - 1) + j - 1] = Aij[m * i + j];
+                    for (int i = 0; i < kd; i++) Aij[i + m * (kd - 1)] = Aij[kd - 1 + m * i] = S.gram[i] + 1e-9;
                 }
-                double A[B1_MAXM * B1_MAXM], c[B1_MAXM];
+                __syncwarp();
                 bool nan = false;
-                for (int i = 0; i < kd; i++)
-                    for (int j = 0; j < kd; j++) {
-                        double v = Aij[j + m * i];
-                        if (v != v) nan = true;
-                        A[i * kd + j] = v;
-                    }
-                if (nan) sh_status = NM_ERR_NAN_DIIS;
+                for (int e = l; e < kd * kd; e += 32) {
+                    int i = e / kd, j = e % kd;
+                    double v = Aij[j + m * i];
+                    if (v != v) nan = true;
+                    S.As[i * (kd + 1) + j] = v;
+                }
+                for (int i = l; i < kd; i += 32) S.As[i * (kd + 1) + kd] = 1.0;
+                nan = __any_sync(0xffffffffu, nan);
+                __syncwarp();
+                if (nan) { if (l == 0) sh_status = NM_ERR_NAN_DIIS; }
                 else {
-                    nm_small_solve(A, c, kd);
-                    double nC = 0;
-                    for (int i = 0; i < kd; i++) nC += c[i];
-                    for (int i = 0; i < kd; i++) {
-                        Ci[i] = c[i] / nC;
-                        if (Ci[i] != Ci[i]) sh_status = NM_ERR_NAN_SVD;
+                    if (kd == 1) { if (l == 0) Ci[0] = 1.0; }
+                    else warp_solve(S.As, Ci, kd);
+                    if (l == 0) {
+                        double nC = 0;
+                        for (int i = 0; i < kd; i++) nC += Ci[i];
+                        for (int i = 0; i < kd; i++) {
+                            Ci[i] = Ci[i] / nC;
+                            if (Ci[i] != Ci[i]) sh_status = NM_ERR_NAN_SVD;
+                        }
                     }
                 }
             }
@@ -580,7 +800,7 @@ __global__ void __launch_bounds__(B1_THREADS) k_batch1d(B1Prob* __restrict__ pro
                 double v = 0;
                 for (int i = 0; i < kd; i++) {
                     int posi = k - kd + 1 + i;
-                    if (posi < 0) posi += P.m;
+                    if (posi < 0) posi += m;
                     v += Ci[i] * P.xR[(size_t)posi * iv + j];
                 }
                 x[j] = v;
@@ -588,12 +808,12 @@ __global__ void __launch_bounds__(B1_THREADS) k_batch1d(B1Prob* __restrict__ pro
             __syncthreads();
         }
         if (use32) {
-            // leave the FP32 phase on reaching the switch tolerance or stalling
+            // leave the FP32 phase at the switch tolerance, or on a stall close
+            // to convergence; instances far from convergence stay in FP32
             if (resid < 0.9 * best) { best = resid; since_best = 0; } else since_best++;
-            if (!(resid > P.sw_tol) || since_best > 25) {
+            if (!(resid > P.sw_tol) || (since_best > 25 && resid < 1e-2)) {
                 use32 = false;
                 k_diis = 0;  // restart the DIIS history on the FP64 residual
-                best = 1e300;
                 if (it >= P.itlim) break;
                 it++;
                 continue;
@@ -604,7 +824,6 @@ __global__ void __launch_bounds__(B1_THREADS) k_batch1d(B1Prob* __restrict__ pro
         if (it >= P.itlim) break;
         it++;
     }
-    for (int i = tid; i < iv; i += nth) P.x[i] = x[i];
     if (tid == 0) {
         P.iterations = it;
         P.fp32_iterations = fp32_its;
@@ -622,6 +841,7 @@ struct Batch {
     B1Prob* d_probs = nullptr;
     std::vector<void*> allocs;
     double* d_x = nullptr;
+    double* d_g = nullptr;
     std::vector<long long> offsets;
     int precision = NM_FP64;
     size_t smem = 0;
@@ -670,9 +890,10 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
         const nm_plan* P = plans[p];
         B.plans.push_back(P);
         if (P->gradients != 1) { set_error("batched solver takes 1-gradient problems only"); return NM_ERR_INPUT; }
+        if (P->MX > B1_KS * B1_THREADS) { set_error("batched solver takes at most 512 layers"); return NM_ERR_INPUT; }
         if (P->charged) { set_error("charged systems are not supported by the batched solver"); return NM_ERR_INPUT; }
         if (P->n_seg > NM_MAX_SEG || P->n_mol > NM_MAX_MOL || P->diis_m > B1_MAXM) {
-            set_error("problem exceeds the batched solver's limits (segments, molecules, DIIS m <= 16)");
+            set_error("problem exceeds the batched solver's limits (segments, molecules, DIIS m <= 12)");
             return NM_ERR_INPUT;
         }
         B1Prob& H = B.hp[p];
@@ -737,14 +958,15 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
         B.offsets[p] = off;
         off += P->iv;
         H.sw_tol = 2e-6;
-        size_t smem = sizeof(double) * ((size_t)(2 * P->n_seg + 2) * M + 2 * (size_t)P->iv + (size_t)kk * M + 64 +
-                                        B1_MAXM * B1_MAXM + B1_MAXM + 5 * NM_MAX_MOL + NM_MAX_SEG + 8 * B1_MAXM +
-                                        (size_t)2 * M + (size_t)P->n_seg * M) + 64;
+        size_t smem = sizeof(double) * ((size_t)(2 * P->n_seg + kk + 3) * M + (3 * (size_t)M + 1) / 2 + 64 +
+                                        B1_MAXM * B1_MAXM + B1_MAXM + B1_MAXM * (B1_MAXM + 1) +
+                                        5 * NM_MAX_MOL + NM_MAX_SEG + B1_MAXM);
         maxsmem = std::max(maxsmem, smem);
     }
     B.offsets[n] = off;
     TRYB(B.alloc(&B.d_x, (size_t)off));
-    for (int p = 0; p < n; p++) B.hp[p].x = B.d_x + B.offsets[p];
+    TRYB(B.alloc(&B.d_g, (size_t)off));
+    for (int p = 0; p < n; p++) { B.hp[p].x = B.d_x + B.offsets[p]; B.hp[p].g = B.d_g + B.offsets[p]; }
     TRYB(B.alloc(&B.d_probs, (size_t)n));
     B.smem = maxsmem;
     if (maxsmem > 220 * 1024) { set_error("problem too large for the batched solver's shared memory"); return NM_ERR_INPUT; }
@@ -828,6 +1050,13 @@ int nm_batch_offsets(nm_batch* b, long long* offsets) {
     Batch* B = reinterpret_cast<Batch*>(b);
     if (!B || !offsets) { nm::set_error("nm_batch_offsets: bad argument"); return NM_ERR_ARG; }
     for (size_t i = 0; i < B->offsets.size(); i++) offsets[i] = B->offsets[i];
+    return NM_OK;
+}
+
+int nm_batch_stats(nm_batch* b, int* fp32_iterations) {
+    Batch* B = reinterpret_cast<Batch*>(b);
+    if (!B || !fp32_iterations) { nm::set_error("nm_batch_stats: bad argument"); return NM_ERR_ARG; }
+    for (size_t p = 0; p < B->hp.size(); p++) fp32_iterations[p] = B->hp[p].fp32_iterations;
     return NM_OK;
 }
 
