@@ -225,6 +225,9 @@ int nm_batch_solve_host(nm_batch* b, double* x_host, int* iterations,
 /* element offset of problem i's x in the concatenated vector; total in
  * offsets[n_plans] */
 int nm_batch_offsets(nm_batch* b, long long* offsets);
+/* One residual evaluation g(x) per problem (no DIIS), FP64 or FP32
+ * propagators; x_dev and g_dev are concatenated like nm_batch_solve_dev. */
+int nm_batch_residual_dev(nm_batch* b, const double* x_dev, double* g_dev, int precision);
 /* per-problem iteration counts of the FP32-propagator phase of the last
  * solve (0 for FP64 batches) */
 int nm_batch_stats(nm_batch* b, int* fp32_iterations);

@@ -244,6 +244,9 @@ class Batch:
                                                _dptr(res), st.ctypes.data_as(_abi.ip)))
         return it, res, st
 
+    def residual_dev(self, x_ptr: int, g_ptr: int, precision: int) -> None:
+        _check(_abi.load().nm_batch_residual_dev(self._h, C.c_void_p(x_ptr), C.c_void_p(g_ptr), precision))
+
     def fp32_iterations(self) -> np.ndarray:
         out = np.zeros(len(self.plans), dtype=np.int32)
         _check(_abi.load().nm_batch_stats(self._h, out.ctypes.data_as(_abi.ip)))

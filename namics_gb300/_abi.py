@@ -87,6 +87,7 @@ SIGNATURES = [
     ("nm_batch_solve_dev", C.c_int, [C.c_void_p, C.c_void_p, ip, dp, ip]),
     ("nm_batch_solve_host", C.c_int, [C.c_void_p, dp, ip, dp, ip]),
     ("nm_batch_offsets", C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
+    ("nm_batch_residual_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     ("nm_batch_stats", C.c_int, [C.c_void_p, ip]),
     ("nm_batch_free_energy", C.c_int, [C.c_void_p, dp, dp]),
     ("nm_batch_launch_count", C.c_longlong, [C.c_void_p]),

@@ -59,7 +59,7 @@ struct B1Prob {
     double* xR;          // [m*iv]
     double* xx0;         // [m*iv]
     // results
-    int iterations, fp32_iterations, status;
+    int iterations, fp32_iterations, status, handoff, wS, eval_only;
     double residual, F, Omega, sw_tol;
     double sc[5 * NM_MAX_MOL];  // GN, norm, n, theta, phibulk per molecule
     double seg_phibulk[NM_MAX_SEG];
@@ -117,11 +117,12 @@ __device__ __forceinline__ float b1_block_maxf(float v, double* red) {
     return r;
 }
 
-// exact 2^e without FP64 or library calls: 0 below the normal range (such
-// contributions are < 1e-38 of the largest), +inf above it
+// exact 2^e without FP64 or library calls, subnormal powers included; 0
+// below 2^-149, +inf above 2^127
 __device__ __forceinline__ float pow2f(int e) {
-    if (e < -126) return 0.f;
+    if (e < -149) return 0.f;
     if (e > 127) return __int_as_float(0x7f800000);
+    if (e < -126) return __int_as_float(1 << (e + 149));
     return __int_as_float((e + 127) << 23);
 }
 __device__ __forceinline__ int expo(float v) {  // frexp exponent of v > 0
@@ -185,6 +186,28 @@ __device__ void warp_solve(double* A, double* c, int kd) {
             c[i] = v / A[i * ld + i];
         }
     __syncwarp();
+}
+
+}  // namespace nm
+#include "batch1d_warp.cuh"
+namespace nm {
+
+#define BW_DOUBLES (B1_MAXM * B1_MAXM + B1_MAXM + B1_MAXM * (B1_MAXM + 1) + 5 * NM_MAX_MOL + NM_MAX_SEG + \
+                    NM_MAX_MOL + B1_MAXM + NM_MAX_MOL + NM_MAX_SEG)
+
+// FP32 phase, one warp per problem (batch1d_warp.cuh)
+__global__ void __launch_bounds__(32) k_batch1d_w(B1Prob* __restrict__ probs) {
+    B1Prob& P = probs[blockIdx.x];
+    extern __shared__ double sm[];
+    double* smd = sm;
+    float* smf = (float*)(sm + BW_DOUBLES);
+    const bool curv = P.geom != 0;
+    switch (P.wS) {
+        case 4: if (curv) bw_phase<4, true>(P, smd, smf); else bw_phase<4, false>(P, smd, smf); break;
+        case 8: if (curv) bw_phase<8, true>(P, smd, smf); else bw_phase<8, false>(P, smd, smf); break;
+        case 12: if (curv) bw_phase<12, true>(P, smd, smf); else bw_phase<12, false>(P, smd, smf); break;
+        default: if (curv) bw_phase<16, true>(P, smd, smf); else bw_phase<16, false>(P, smd, smf); break;
+    }
 }
 
 // ---------------------------------------------------------------- kernel
@@ -668,8 +691,11 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Sc
 // fp32_first: FP32 propagators until ‖g‖ < P.sw_tol (or a stall close to
 // convergence), then FP64 (DIIS history restarted), so the stopping test
 // ‖g‖ < tol is always made on an FP64 residual.
-__global__ void __launch_bounds__(B1_THREADS, 4) k_batch1d(B1Prob* __restrict__ probs, int fp32_first) {
+// mode 0: FP64 from the start; 1: FP32 propagators first (this kernel);
+// 2: FP64 continuation of a problem handed over by k_batch1d_w.
+__global__ void __launch_bounds__(B1_THREADS, 4) k_batch1d(B1Prob* __restrict__ probs, int mode) {
     B1Prob& P = probs[blockIdx.x];
+    if (mode == 2 && !P.handoff) return;
     extern __shared__ double sm[];
     const int M = P.M, ns = P.ns, iv = P.iv, n_mm = P.n_mm, m = P.m;
     const int tid = threadIdx.x, nth = blockDim.x;
@@ -711,8 +737,9 @@ __global__ void __launch_bounds__(B1_THREADS, 4) k_batch1d(B1Prob* __restrict__ 
     if (tid == 0) sh_status = 0;
     __syncthreads();
 
-    bool use32 = fp32_first != 0;
+    bool use32 = mode == 1;
     int it = 0, k_diis = 0, fp32_its = 0;
+    if (mode == 2) { it = P.iterations + 1; fp32_its = P.fp32_iterations; }
     double resid = 0, best = 1e300;
     int since_best = 0;
     for (;;) {
@@ -724,7 +751,7 @@ __global__ void __launch_bounds__(B1_THREADS, 4) k_batch1d(B1Prob* __restrict__ 
             if (L.geom == 0) b1_residual<double, false, false>(P, L, C64, S, scl, x, g);
             else b1_residual<double, false, true>(P, L, C64, S, scl, x, g);
         }
-        if (sh_status) break;
+        if (sh_status || P.eval_only) break;
         // ---------------- DIIS (iterate_DIIS / DIIS / Ax), FP64 ----------------
         int k = it % m;
         double* __restrict__ xRk = P.xR + (size_t)k * iv;
@@ -844,7 +871,7 @@ struct Batch {
     double* d_g = nullptr;
     std::vector<long long> offsets;
     int precision = NM_FP64;
-    size_t smem = 0;
+    size_t smem = 0, smem_w = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     long long launches = 0;
@@ -881,7 +908,7 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
     if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
     if (opt && opt->stream) B.stream = (cudaStream_t)opt->stream;
     else { cudaStreamCreateWithFlags(&B.stream, cudaStreamNonBlocking); B.own_stream = true; }
-    size_t tsz = sizeof(double);  // storage sized for the FP64 phase
+    size_t maxsmem_w = 0;
     long long off = 0;
     size_t maxsmem = 0;
     B.hp.resize(n);
@@ -899,6 +926,12 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
         B1Prob& H = B.hp[p];
         std::memset(&H, 0, sizeof(H));
         int M = P->M;
+        {
+            int S = (P->MX + 31) / 32;
+            H.wS = S <= 4 ? 4 : (S <= 8 ? 8 : (S <= 12 ? 12 : 16));
+        }
+        // one stored vector: M doubles (FP64 phase) or 32·wS floats (warp FP32 phase)
+        size_t tsz = std::max((size_t)8 * M, (size_t)4 * 32 * H.wS);
         H.MX = P->MX; H.M = M; H.geom = P->geometry; H.ns = P->n_seg; H.nit = P->n_it;
         H.nmol = P->n_mol; H.solvent = P->solvent; H.m = P->diis_m; H.itlim = P->iterationlimit;
         H.max_norm = P->max_norm; H.iv = P->iv; H.lam = P->lambda; H.tol = P->tolerance; H.dmax = P->deltamax;
@@ -939,11 +972,14 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
             TRYB(B.upload(&dci, ci.data(), ci.size()));
             D.blocks = db; D.child_index = dci;
             char *gf, *pc, *q;
-            TRYB(B.alloc(&gf, tsz * (size_t)mol.n_store * M)); D.Gf = gf;
-            TRYB(B.alloc(&pc, tsz * (size_t)mol.n_blocks * M)); D.Pc = pc;
-            TRYB(B.alloc(&q, tsz * (size_t)mol.n_blocks * M)); D.Q = q;
+            TRYB(B.alloc(&gf, tsz * (size_t)mol.n_store)); D.Gf = gf;
+            TRYB(B.alloc(&pc, tsz * (size_t)mol.n_blocks)); D.Pc = pc;
+            TRYB(B.alloc(&q, tsz * (size_t)mol.n_blocks)); D.Q = q;
             int *ef, *epc, *eq;
-            TRYB(B.alloc(&ef, mol.n_store)); TRYB(B.alloc(&epc, mol.n_blocks)); TRYB(B.alloc(&eq, mol.n_blocks));
+            // power-of-two exponents: one per lane (32) per stored vector
+            TRYB(B.alloc(&ef, 32 * (size_t)mol.n_store));
+            TRYB(B.alloc(&epc, 32 * (size_t)mol.n_blocks));
+            TRYB(B.alloc(&eq, 32 * (size_t)mol.n_blocks));
             D.ef = ef; D.epc = epc; D.eq = eq;
             for (int j = 0; j < mol.n_molmon; j++) {
                 if (kk >= NM_MAX_MM) { set_error("too many (molecule, segment) pairs"); return NM_ERR_INPUT; }
@@ -962,6 +998,8 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
                                         B1_MAXM * B1_MAXM + B1_MAXM + B1_MAXM * (B1_MAXM + 1) +
                                         5 * NM_MAX_MOL + NM_MAX_SEG + B1_MAXM);
         maxsmem = std::max(maxsmem, smem);
+        size_t smem_w = sizeof(double) * BW_DOUBLES + sizeof(float) * (size_t)(2 * P->n_seg + kk + 3) * 32 * H.wS;
+        maxsmem_w = std::max(maxsmem_w, smem_w);
     }
     B.offsets[n] = off;
     TRYB(B.alloc(&B.d_x, (size_t)off));
@@ -970,8 +1008,10 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
     TRYB(B.alloc(&B.d_probs, (size_t)n));
     B.smem = maxsmem;
     if (maxsmem > 220 * 1024) { set_error("problem too large for the batched solver's shared memory"); return NM_ERR_INPUT; }
+    B.smem_w = maxsmem_w;
     cudaError_t e1 = cudaFuncSetAttribute(k_batch1d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxsmem);
-    if (e1 != cudaSuccess) { set_error("cudaFuncSetAttribute failed"); return NM_ERR_CUDA; }
+    cudaError_t e2 = cudaFuncSetAttribute(k_batch1d_w, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxsmem_w);
+    if (e1 != cudaSuccess || e2 != cudaSuccess) { set_error("cudaFuncSetAttribute failed"); return NM_ERR_CUDA; }
     return NM_OK;
 }
 
@@ -979,8 +1019,16 @@ static int batch_run(Batch& B) {
     int n = (int)B.hp.size();
     cudaError_t e = cudaMemcpyAsync(B.d_probs, B.hp.data(), sizeof(B1Prob) * n, cudaMemcpyHostToDevice, B.stream);
     if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
-    k_batch1d<<<n, B1_THREADS, B.smem, B.stream>>>(B.d_probs, B.precision == NM_FP32 ? 1 : 0);
-    B.launches++;
+    if (B.precision == NM_FP32) {
+        // FP32 phase one warp per problem, then the FP64 finish of every
+        // problem the warp phase handed over
+        k_batch1d_w<<<n, 32, B.smem_w, B.stream>>>(B.d_probs);
+        k_batch1d<<<n, B1_THREADS, B.smem, B.stream>>>(B.d_probs, 2);
+        B.launches += 2;
+    } else {
+        k_batch1d<<<n, B1_THREADS, B.smem, B.stream>>>(B.d_probs, 0);
+        B.launches++;
+    }
     e = cudaGetLastError();
     if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
     e = cudaMemcpyAsync(B.hp.data(), B.d_probs, sizeof(B1Prob) * n, cudaMemcpyDeviceToHost, B.stream);
@@ -1050,6 +1098,26 @@ int nm_batch_offsets(nm_batch* b, long long* offsets) {
     Batch* B = reinterpret_cast<Batch*>(b);
     if (!B || !offsets) { nm::set_error("nm_batch_offsets: bad argument"); return NM_ERR_ARG; }
     for (size_t i = 0; i < B->offsets.size(); i++) offsets[i] = B->offsets[i];
+    return NM_OK;
+}
+
+int nm_batch_residual_dev(nm_batch* b, const double* x_dev, double* g_dev, int precision) {
+    Batch* B = reinterpret_cast<Batch*>(b);
+    if (!B || !x_dev || !g_dev) { nm::set_error("nm_batch_residual_dev: bad argument"); return NM_ERR_ARG; }
+    size_t n = (size_t)B->offsets.back();
+    cudaError_t e = cudaMemcpyAsync(B->d_x, x_dev, sizeof(double) * n, cudaMemcpyDeviceToDevice, B->stream);
+    if (e != cudaSuccess) { nm::set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
+    int np = (int)B->hp.size();
+    for (int p = 0; p < np; p++) B->hp[p].eval_only = 1;
+    e = cudaMemcpyAsync(B->d_probs, B->hp.data(), sizeof(nm::B1Prob) * np, cudaMemcpyHostToDevice, B->stream);
+    if (e != cudaSuccess) { nm::set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
+    if (precision == NM_FP32) nm::k_batch1d_w<<<np, 32, B->smem_w, B->stream>>>(B->d_probs);
+    else nm::k_batch1d<<<np, B1_THREADS, B->smem, B->stream>>>(B->d_probs, 0);
+    B->launches++;
+    e = cudaMemcpyAsync(g_dev, B->d_g, sizeof(double) * n, cudaMemcpyDeviceToDevice, B->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(B->stream);
+    for (int p = 0; p < np; p++) B->hp[p].eval_only = 0;
+    if (e != cudaSuccess) { nm::set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
     return NM_OK;
 }
 

@@ -235,3 +235,63 @@ def test_solves_are_deterministic():
     r2, _ = ctx.solve_host(x2)
     assert r1.iterations == r2.iterations
     assert np.array_equal(x1, x2)
+
+
+def test_batched_residual_fp32_close_to_oracle():
+    """One FP32-propagator residual per problem against the FP64 oracle, at
+    the seeded start field and at the converged field (the FP32 phase hands
+    over at ‖g‖ < 2e-6, so its residual must be accurate well below that)."""
+    names = _batch_cases()
+    runs = [load_golden(n)["runs"]["conv"] for n in names]
+    plans = [Plan(r["input"]) for r in runs]
+    b = Batch(plans, NM_FP32)
+    x0 = np.concatenate([np.array(r["x"]) for r in runs])
+    xc = x0.copy()
+    Batch(plans, NM_FP64).solve_host(xc)
+    for x in (x0, xc):
+        xd = dev(x)
+        g32 = torch.zeros_like(xd)
+        g64 = torch.zeros_like(xd)
+        b.residual_dev(xd.data_ptr(), g32.data_ptr(), NM_FP32)
+        b.residual_dev(xd.data_ptr(), g64.data_ptr(), NM_FP64)
+        a32, a64 = host(g32), host(g64)
+        for i, p in enumerate(plans):
+            lo, hi = b.offsets[i], b.offsets[i + 1]
+            _, go = Oracle(p).residual(x[lo:hi])
+            assert np.max(np.abs(a64[lo:hi] - go)) < 1e-10, names[i]
+            assert np.linalg.norm(a32[lo:hi] - go) < _fp32_floor(p) * max(1.0, np.linalg.norm(go)), \
+                (names[i], np.linalg.norm(a32[lo:hi] - go), np.linalg.norm(go))
+
+
+def _fp32_floor(plan) -> float:
+    """Accuracy of an FP32-propagator residual.  G1 held in FP32 is the exact
+    G1 of a field perturbed by ~6e-8 per site, and a chain of N segments
+    answers such a perturbation with a change of φ up to ~N·6e-8."""
+    n = max(plan.chainlength(m) for m in range(plan.n_mol))
+    return 1e-7 * n + 1e-6
+
+
+def test_batched_residual_fp32_stretched_stars():
+    """Grafted stars of the 1-D batch workload at their converged fields: the
+    arms meet at the branch point with barely overlapping profiles, so the
+    join product and the composition must not underflow in FP32."""
+    import bench
+    texts = bench.workload(512)
+    pick = [319, 469, 479]
+    plans = [Plan(texts[i]) for i in pick]
+    xs = bench.fields([Plan(t) for t in texts])
+    x = np.concatenate([xs[i] for i in pick])
+    its, res, st = Batch(plans, NM_FP64).solve_host(x)
+    assert (st == 0).all(), st
+    b = Batch(plans, NM_FP32)
+    xd = dev(x)
+    g32 = torch.zeros_like(xd)
+    g64 = torch.zeros_like(xd)
+    b.residual_dev(xd.data_ptr(), g32.data_ptr(), NM_FP32)
+    b.residual_dev(xd.data_ptr(), g64.data_ptr(), NM_FP64)
+    a32, a64 = host(g32), host(g64)
+    for i, p in enumerate(plans):
+        lo, hi = b.offsets[i], b.offsets[i + 1]
+        _, go = Oracle(p).residual(x[lo:hi])
+        assert np.max(np.abs(a64[lo:hi] - go)) < 1e-10, pick[i]
+        assert np.linalg.norm(a32[lo:hi] - go) < _fp32_floor(p), (pick[i], np.linalg.norm(a32[lo:hi] - go))
