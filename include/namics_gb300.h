@@ -235,6 +235,26 @@ int nm_batch_stats(nm_batch* b, int* fp32_iterations);
 int nm_batch_free_energy(nm_batch* b, double* F, double* Omega);
 long long nm_batch_launch_count(nm_batch* b);
 
+/* ---- allocation-free single-problem solve --------------------------------
+ * No counterpart in the reference.  For callers that must not allocate
+ * device memory when they solve (a fixed memory budget carved up front, a
+ * sequence about to be captured, a re-solve on a latency-critical path):
+ * solves one 1-gradient problem with the batched solver's kernels, its
+ * whole device scratch (descriptor, lattice arrays, stored propagators,
+ * DIIS history, residual) carved from one static device array of
+ * NM_NOALLOC_SCRATCH_BYTES compiled into the library.  A problem that needs
+ * more is rejected with NM_ERR_INPUT and a message naming the limit.
+ * The array's address is looked up on the first call for each device, with
+ * that device current; make that first call before any stream capture.
+ * All calls share the array: calls that overlap in time race on it.
+ * x_dev: the plan's iteration vector (length iv), updated in place.
+ * stream: cudaStream_t or NULL for the default stream; the call returns
+ * after the stream has finished the solve.  Returns res->status (NM_OK,
+ * NM_ERR_NOT_CONVERGED or an error). */
+#define NM_NOALLOC_SCRATCH_BYTES (8u << 20)
+int nm_solve1d_noalloc(const nm_plan* plan, double* x_dev, int precision,
+                       void* stream, nm_solve_result* res);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1151,3 +1151,208 @@ long long nm_batch_launch_count(nm_batch* b) {
 }
 
 }  // extern "C"
+
+// ======================================================================
+// Allocation-free single-problem solve.
+//
+// Some callers cannot allocate device memory at the point where they solve:
+// a host that owns a fixed memory budget sliced before work begins, a
+// sequence about to be captured into a CUDA graph, or a signal-time
+// re-solve that must not touch the allocator.  nm_solve1d_noalloc runs the
+// same two kernels as nm_batch_solve_dev (FP32 warp phase + FP64 finish, or
+// FP64 only) on one 1-gradient problem, with every piece of device scratch
+// carved from one file-scope array compiled into the library.  The array's
+// address is looked up once per device (cudaGetSymbolAddress, with that
+// device current) on the first call for that device; make that first call
+// before any stream capture.  The scratch is shared, so calls that overlap
+// in time (two host threads, or two streams in flight) race on it.
+// ======================================================================
+namespace nm {
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NM_NOALLOC_SCRATCH_BYTES];
+
+#define NM_NOALLOC_MAX_DEVICES 64
+static unsigned char* g_noalloc_base[NM_NOALLOC_MAX_DEVICES];
+
+// bump allocator over the static scratch (256-byte aligned pieces)
+struct StaticArena {
+    unsigned char* base;
+    size_t used = 0;
+    bool overflow = false;
+    template <typename X>
+    X* take(size_t n) {
+        if (n == 0) n = 1;
+        size_t off = (used + 255) & ~(size_t)255;
+        size_t bytes = sizeof(X) * n;
+        if (off + bytes > (size_t)NM_NOALLOC_SCRATCH_BYTES) { overflow = true; return nullptr; }
+        used = off + bytes;
+        return reinterpret_cast<X*>(base + off);
+    }
+};
+
+struct NoallocCopy { void* dst; const void* src; size_t bytes; };
+
+// One problem's descriptor laid out in the arena, with the contents
+// batch_init gives it.  Host sources of the copies to make are listed in
+// `copies`; `ks` stages KSAM as doubles and must outlive those copies.
+static int noalloc_layout(const nm_plan* P, StaticArena& A, double* x_dev, B1Prob& H, size_t& smem,
+                          size_t& smem_w, std::vector<double>& ks, std::vector<NoallocCopy>& copies) {
+    if (P->gradients != 1) { set_error("nm_solve1d_noalloc: 1-gradient problems only"); return NM_ERR_INPUT; }
+    if (P->MX > B1_KS * B1_THREADS) { set_error("nm_solve1d_noalloc: at most 512 layers"); return NM_ERR_INPUT; }
+    if (P->charged) { set_error("nm_solve1d_noalloc: charged systems are not supported"); return NM_ERR_INPUT; }
+    if (P->n_seg > NM_MAX_SEG || P->n_mol > NM_MAX_MOL || P->diis_m > B1_MAXM) {
+        set_error("nm_solve1d_noalloc: problem exceeds the limits (segments, molecules, DIIS m <= 12)");
+        return NM_ERR_INPUT;
+    }
+    std::memset(&H, 0, sizeof(H));
+    const int M = P->M;
+    {
+        int S = (P->MX + 31) / 32;
+        H.wS = S <= 4 ? 4 : (S <= 8 ? 8 : (S <= 12 ? 12 : 16));
+    }
+    const size_t tsz = std::max((size_t)8 * M, (size_t)4 * 32 * H.wS);
+    H.MX = P->MX; H.M = M; H.geom = P->geometry; H.ns = P->n_seg; H.nit = P->n_it;
+    H.nmol = P->n_mol; H.solvent = P->solvent; H.m = P->diis_m; H.itlim = P->iterationlimit;
+    H.max_norm = P->max_norm; H.iv = P->iv; H.lam = P->lambda; H.tol = P->tolerance; H.dmax = P->deltamax;
+    H.b1 = P->bc[0] == NM_BC_MIRROR ? 1 : P->bc[0] == NM_BC_PERIODIC ? P->MX : 0;
+    H.bm = P->bc[3] == NM_BC_MIRROR ? P->MX : P->bc[3] == NM_BC_PERIODIC ? 1 : P->MX + 1;
+    auto put = [&](void* dst, const void* src, size_t bytes) { copies.push_back({dst, src, bytes}); };
+    if (P->geometry != NM_PLANAR) {
+        double* a = A.take<double>(M);
+        double* b = A.take<double>(M);
+        double* c = A.take<double>(M);
+        double* dL = A.take<double>(M);
+        if (A.overflow) goto full;
+        put(a, P->lambda_1, sizeof(double) * M);
+        put(b, P->lambda0, sizeof(double) * M);
+        put(c, P->lambda1, sizeof(double) * M);
+        put(dL, P->L, sizeof(double) * M);
+        H.lm1 = a; H.l0 = b; H.l1 = c; H.L = dL;
+    }
+    {
+        ks.assign(M, 0.0);
+        for (int s = 0; s < M; s++) ks[s] = P->ksam[s];
+        double* dk = A.take<double>(M);
+        double* dg = A.take<double>((size_t)P->n_seg * M);
+        double* dpf = A.take<double>((size_t)P->n_seg * M);
+        if (A.overflow) goto full;
+        put(dk, ks.data(), sizeof(double) * M);
+        put(dg, P->seg_gmask, sizeof(double) * P->n_seg * M);
+        put(dpf, P->seg_phi_frozen, sizeof(double) * P->n_seg * M);
+        H.ksam = dk; H.gmask = dg; H.phi_frozen = dpf;
+    }
+    for (int i = 0; i < P->n_seg; i++) {
+        H.seg_it[i] = P->seg_it[i];
+        H.seg_frozen[i] = P->seg_freedom[i] == NM_SEG_FROZEN;
+        H.seg_inmol[i] = P->seg_it[i] >= 0;
+    }
+    for (int i = 0; i < P->n_it; i++) H.it_seg[i] = P->it_seg[i];
+    for (int i = 0; i < P->n_seg * P->n_seg; i++) H.chi[i] = P->chi[i];
+    {
+        int kk = 0;
+        for (int m = 0; m < P->n_mol; m++) {
+            const nm_molecule& mol = P->mols[m];
+            if (mol.n_blocks > B1_MAXB) { set_error("nm_solve1d_noalloc: molecule has too many blocks"); return NM_ERR_INPUT; }
+            B1Mol& D = H.mol[m];
+            D.freedom = mol.freedom; D.pinned = mol.pinned; D.n_blocks = mol.n_blocks; D.n_store = mol.n_store;
+            D.n_molmon = mol.n_molmon; D.mm0 = kk;
+            D.n_in = mol.n; D.theta_in = mol.theta; D.phibulk_in = mol.phibulk; D.N = mol.chainlength;
+            const int nci = mol.n_blocks > 1 ? mol.n_blocks - 1 : 1;
+            nm_block* db = A.take<nm_block>(mol.n_blocks);
+            int* dci = A.take<int>(nci);
+            D.Gf = A.take<char>(tsz * (size_t)mol.n_store);
+            D.Pc = A.take<char>(tsz * (size_t)mol.n_blocks);
+            D.Q = A.take<char>(tsz * (size_t)mol.n_blocks);
+            D.ef = A.take<int>(32 * (size_t)mol.n_store);
+            D.epc = A.take<int>(32 * (size_t)mol.n_blocks);
+            D.eq = A.take<int>(32 * (size_t)mol.n_blocks);
+            if (A.overflow) goto full;
+            put(db, mol.blocks, sizeof(nm_block) * mol.n_blocks);
+            if (mol.n_blocks > 1) put(dci, mol.child_index, sizeof(int) * nci);
+            D.blocks = db; D.child_index = dci;
+            for (int j = 0; j < mol.n_molmon; j++) {
+                if (kk >= NM_MAX_MM) { set_error("nm_solve1d_noalloc: too many (molecule, segment) pairs"); return NM_ERR_INPUT; }
+                H.mm_mol[kk] = m; H.mm_seg[kk] = mol.molmon_seg[j]; H.mm_frac[kk] = mol.molmon_fraction[j];
+                kk++;
+            }
+        }
+        H.n_mm = kk;
+        H.xR = A.take<double>((size_t)P->diis_m * P->iv);
+        H.xx0 = A.take<double>((size_t)P->diis_m * P->iv);
+        H.g = A.take<double>((size_t)P->iv);
+        if (A.overflow) goto full;
+        H.x = x_dev;
+        H.sw_tol = 2e-6;
+        smem = sizeof(double) * ((size_t)(2 * P->n_seg + kk + 3) * M + (3 * (size_t)M + 1) / 2 + 64 +
+                                 B1_MAXM * B1_MAXM + B1_MAXM + B1_MAXM * (B1_MAXM + 1) + 5 * NM_MAX_MOL +
+                                 NM_MAX_SEG + B1_MAXM);
+        smem_w = sizeof(double) * BW_DOUBLES + sizeof(float) * (size_t)(2 * P->n_seg + kk + 3) * 32 * H.wS;
+        if (smem > 220 * 1024) { set_error("nm_solve1d_noalloc: problem too large for shared memory"); return NM_ERR_INPUT; }
+    }
+    return NM_OK;
+full:
+    set_error("nm_solve1d_noalloc: problem needs more than the " + std::to_string((size_t)NM_NOALLOC_SCRATCH_BYTES) +
+              " bytes of static device scratch");
+    return NM_ERR_INPUT;
+}
+
+// raise (never lower) a kernel's dynamic shared-memory limit
+template <typename K>
+static cudaError_t noalloc_smem(K kernel, size_t bytes) {
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess) return e;
+    if ((size_t)fa.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+}  // namespace nm
+
+extern "C" int nm_solve1d_noalloc(const nm_plan* plan, double* x_dev, int precision, void* stream,
+                                  nm_solve_result* res) {
+    using namespace nm;
+    if (!plan || !x_dev || !res) { set_error("nm_solve1d_noalloc: bad argument"); return NM_ERR_ARG; }
+    if (precision != NM_FP32 && precision != NM_FP64) { set_error("nm_solve1d_noalloc: bad precision"); return NM_ERR_ARG; }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
+    if (dev < 0 || dev >= NM_NOALLOC_MAX_DEVICES) { set_error("nm_solve1d_noalloc: device ordinal out of range"); return NM_ERR_ARG; }
+    if (!g_noalloc_base[dev]) {  // set-up, once per device, with that device current
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) { set_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e)); return NM_ERR_CUDA; }
+        g_noalloc_base[dev] = (unsigned char*)p;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    StaticArena A{g_noalloc_base[dev]};
+    B1Prob* d_prob = A.take<B1Prob>(1);
+    B1Prob H;
+    size_t smem = 0, smem_w = 0;
+    std::vector<double> ks;
+    std::vector<NoallocCopy> copies;
+    int rc = noalloc_layout(plan, A, x_dev, H, smem, smem_w, ks, copies);
+    if (rc) return rc;
+    e = noalloc_smem(k_batch1d, smem);
+    if (e == cudaSuccess) e = noalloc_smem(k_batch1d_w, smem_w);
+    if (e != cudaSuccess) { set_error(std::string("nm_solve1d_noalloc: ") + cudaGetErrorString(e)); return NM_ERR_CUDA; }
+    // what the batch path's zero-filled allocations start from
+    e = cudaMemsetAsync(A.base, 0, A.used, st);
+    for (size_t i = 0; e == cudaSuccess && i < copies.size(); i++)
+        e = cudaMemcpyAsync(copies[i].dst, copies[i].src, copies[i].bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_prob, &H, sizeof(B1Prob), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
+    if (precision == NM_FP32) {
+        k_batch1d_w<<<1, 32, smem_w, st>>>(d_prob);
+        k_batch1d<<<1, B1_THREADS, smem, st>>>(d_prob, 2);
+    } else {
+        k_batch1d<<<1, B1_THREADS, smem, st>>>(d_prob, 0);
+    }
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&H, d_prob, sizeof(B1Prob), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
+    res->iterations = H.iterations;
+    res->residual = H.residual;
+    res->status = H.status;
+    return H.status == NM_OK ? NM_OK : H.status;
+}
