@@ -37,12 +37,14 @@ struct B1Mol {
     double n_in, theta_in, phibulk_in, N;
     const nm_block* blocks;
     const int* child_index;
-    void* Gf;            // T[n_store*M]
-    int* ef;             // exponent of each stored forward propagator (scaled mode)
-    void* Pc;            // T[n_blocks*M]
-    int* epc;            // exponents of Pc
-    void* Q;             // T[n_blocks*M]
-    int* eq;
+    // stored vectors: FP64 [M] (FP64 phase) or FP32 mantissas [128·SP]
+    // with one exponent per thread (FP32 phase); same buffers for both
+    void* Gf;            // [n_store] vectors
+    int* ef;             // [n_store][128] exponents of Gf (FP32 phase)
+    void* Pc;            // [n_blocks] vectors: P(Gf of the block's end)·KSAM
+    int* epc;            // [n_blocks][128]
+    void* Q;             // [n_blocks] vectors: backward start of each block
+    int* eq;             // [n_blocks][128]
 };
 
 struct B1Prob {
@@ -59,7 +61,7 @@ struct B1Prob {
     double* xR;          // [m*iv]
     double* xx0;         // [m*iv]
     // results
-    int iterations, fp32_iterations, status, handoff, wS, eval_only;
+    int iterations, fp32_iterations, status, eval_only;
     double residual, F, Omega, sw_tol;
     double sc[5 * NM_MAX_MOL];  // GN, norm, n, theta, phibulk per molecule
     double seg_phibulk[NM_MAX_SEG];
@@ -105,18 +107,6 @@ __device__ __forceinline__ double b1_block_sum(double v, double* red) {
     return r;
 }
 
-__device__ __forceinline__ float b1_block_maxf(float v, double* red) {
-    unsigned wm = __reduce_max_sync(0xffffffffu, __float_as_uint(fmaxf(v, 0.f)));
-    float* rf = (float*)red;
-    __syncthreads();
-    if ((threadIdx.x & 31) == 0) rf[threadIdx.x >> 5] = __uint_as_float(wm);
-    __syncthreads();
-    float r = 0.f;
-    for (int i = 0; i < (int)(blockDim.x >> 5); i++) r = fmaxf(r, rf[i]);
-    __syncthreads();
-    return r;
-}
-
 // exact 2^e without FP64 or library calls, subnormal powers included; 0
 // below 2^-149, +inf above 2^127
 __device__ __forceinline__ float pow2f(int e) {
@@ -129,22 +119,6 @@ __device__ __forceinline__ int expo(float v) {  // frexp exponent of v > 0
     int e = ((__float_as_int(v) >> 23) & 0xff) - 126;
     return v > 0.f ? e : 0;
 }
-
-// Double-buffered warp slots: one barrier per step gives every thread the
-// block max of the vector just written.
-struct Scaler {
-    float* slots;  // [2][32]
-    int par;
-    __device__ __forceinline__ int block_exp(float lmax) {
-        unsigned wm = __reduce_max_sync(0xffffffffu, __float_as_uint(lmax));
-        if ((threadIdx.x & 31) == 0) slots[par * 32 + (threadIdx.x >> 5)] = __uint_as_float(wm);
-        __syncthreads();
-        float gm = 0.f;
-        for (int i = 0; i < (int)(blockDim.x >> 5); i++) gm = fmaxf(gm, slots[par * 32 + i]);
-        par ^= 1;
-        return expo(gm);
-    }
-};
 
 // Solve A c = 1 (A: kd×kd in shared memory, row-major with stride kd+1 and
 // the right-hand side in column kd) by Gaussian elimination with partial
@@ -189,35 +163,15 @@ __device__ void warp_solve(double* A, double* c, int kd) {
 }
 
 }  // namespace nm
-#include "batch1d_warp.cuh"
 namespace nm {
-
-#define BW_DOUBLES (B1_MAXM * B1_MAXM + B1_MAXM + B1_MAXM * (B1_MAXM + 1) + 5 * NM_MAX_MOL + NM_MAX_SEG + \
-                    NM_MAX_MOL + B1_MAXM + NM_MAX_MOL + NM_MAX_SEG)
-
-// FP32 phase, one warp per problem (batch1d_warp.cuh)
-__global__ void __launch_bounds__(32) k_batch1d_w(B1Prob* __restrict__ probs) {
-    B1Prob& P = probs[blockIdx.x];
-    extern __shared__ double sm[];
-    double* smd = sm;
-    float* smf = (float*)(sm + BW_DOUBLES);
-    const bool curv = P.geom != 0;
-    switch (P.wS) {
-        case 4: if (curv) bw_phase<4, true>(P, smd, smf); else bw_phase<4, false>(P, smd, smf); break;
-        case 8: if (curv) bw_phase<8, true>(P, smd, smf); else bw_phase<8, false>(P, smd, smf); break;
-        case 12: if (curv) bw_phase<12, true>(P, smd, smf); else bw_phase<12, false>(P, smd, smf); break;
-        default: if (curv) bw_phase<16, true>(P, smd, smf); else bw_phase<16, false>(P, smd, smf); break;
-    }
-}
-
 // ---------------------------------------------------------------- kernel
 struct B1S {
-    void* G1;       // [ns*M] T   (FP32 phase: G1·2^-eg)
-    void* phi;      // [ns*M] R
-    void* rho;      // [n_mm*M] R
-    void* phitot;   // [M] R
-    void *cur, *nxt;  // [M] T
-    float *cm1, *c0, *cp1;  // curved-lattice weights as float
+    double* G1;       // [ns*M] FP64 phase
+    double* phi;      // [ns*M]
+    double* rho;      // [n_mm*M]
+    double* phitot;   // [M]
+    double *cur, *nxt;  // [M] FP64 phase
+    void* uni;        // start of the region G1/cur/nxt share with the FP32 phase's arrays
     double *red, *Aij, *Ci, *As, *sc, *spb, *gram;
     double* phif;
     int* phie;
@@ -225,25 +179,20 @@ struct B1S {
     int* status;
 };
 
-// One residual evaluation g(x) (System::Classical_residual) with propagators
-// of type T and the composition / residual arithmetic in type R.  FP64 phase:
-// T = R = double, the reference's arithmetic.  FP32 phase: T = R = float with
-// power-of-two scale bookkeeping; G(N), normalisation and DIIS stay FP64.
-#define B1_RS 4  // FP32: block max and rescale every B1_RS steps
-
-template <typename T, bool SC, bool CURV>
-__device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Scaler& scl,
-                            const double* __restrict__ x, double* __restrict__ g) {
-    typedef T R;
-    const int M = L.M, MX = L.MX, ns = P.ns, nit = P.nit, n_mm = P.n_mm;
+// One residual evaluation g(x) (System::Classical_residual) in FP64, the
+// reference's arithmetic: G1, forward sweep, backward sweep fused with the
+// composition into rho, then b1_finish.
+template <bool CURV>
+__device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<double> C, B1S& S, const double* __restrict__ x,
+                            double* __restrict__ g) {
+    typedef double T;
+    const int M = L.M, MX = L.MX, ns = P.ns, n_mm = P.n_mm;
     const int tid = threadIdx.x, nth = blockDim.x;
-    T* G1 = (T*)S.G1;
-    R* phi = (R*)S.phi;
-    R* rho = (R*)S.rho;
-    R* phitot = (R*)S.phitot;
-    T* cur = (T*)S.cur;
-    T* nxt = (T*)S.nxt;
-    double *red = S.red, *sc = S.sc, *spb = S.spb;
+    T* G1 = S.G1;
+    T* rho = S.rho;
+    T* cur = S.cur;
+    T* nxt = S.nxt;
+    double *red = S.red, *sc = S.sc;
     int nk = 0;
     for (int k = 0; k < B1_KS; k++) if (tid + 1 + k * nth <= MX) nk = k + 1;
     // per owned site: curved-lattice weights and the halo slots it feeds
@@ -265,61 +214,27 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Sc
     for (int i = 0; i < ns; i++) {
         int itx = P.seg_it[i];
         const double* gm = P.gmask + i * M;
-        if (SC) {
-            // G1·2^-eg = 2^(-u·log2e - eg) with eg = ceil(max(-u·log2e)):
-            // exact power-of-two scaling that cannot overflow for any u
-            float vmax = -3.0e38f;
-            for (int s = tid; s < M; s += nth) {
-                int src = s == 0 ? L.b1 : (s == MX + 1 ? L.bm : s);
-                float v = itx >= 0 ? -(float)x[itx * M + src] * 1.4426950408889634f : 0.f;
-                if (gm[s] != 0.0) vmax = fmaxf(vmax, v);
-            }
-            // block max of a possibly negative value: shift to the ordered-int domain
-            int key = __float_as_int(vmax);
-            key = key >= 0 ? key : (key ^ 0x7fffffff);
-            int wk = __reduce_max_sync(0xffffffffu, key);
-            int* rk = (int*)red;
-            __syncthreads();
-            if ((tid & 31) == 0) rk[tid >> 5] = wk;
-            __syncthreads();
-            int bk = rk[0];
-            for (int w2 = 1; w2 < nth / 32; w2++) bk = max(bk, rk[w2]);
-            __syncthreads();
-            bk = bk >= 0 ? bk : (bk ^ 0x7fffffff);
-            float vm = __int_as_float(bk);
-            int e = vm > -1.0e30f ? (int)ceilf(vm) : 0;
-            if (tid == 0) S.eg[i] = e;
-            for (int s = tid; s < M; s += nth) {
-                int src = s == 0 ? L.b1 : (s == MX + 1 ? L.bm : s);
-                float v = itx >= 0 ? -(float)x[itx * M + src] * 1.4426950408889634f : 0.f;
-                G1[i * M + s] = (T)(exp2f(v - (float)e) * (float)gm[s]);
-            }
-        } else {
-            for (int s = tid; s < M; s += nth) {
-                int src = s == 0 ? L.b1 : (s == MX + 1 ? L.bm : s);
-                double u = itx >= 0 ? x[itx * M + src] : 0.0;
-                G1[i * M + s] = (T)(exp(-u) * gm[s]);
-            }
+        for (int s = tid; s < M; s += nth) {
+            int src = s == 0 ? L.b1 : (s == MX + 1 ? L.bm : s);
+            double u = itx >= 0 ? x[itx * M + src] : 0.0;
+            G1[i * M + s] = exp(-u) * gm[s];
         }
     }
-    for (int i = tid; i < n_mm * M; i += nth) rho[i] = (R)0;
+    for (int i = tid; i < n_mm * M; i += nth) rho[i] = (T)0;
     __syncthreads();
     for (int m = 0; m < P.nmol; m++) {
         const B1Mol& D = P.mol[m];
         T* __restrict__ Gf = (T*)D.Gf;
         T* __restrict__ Pc = (T*)D.Pc;
         T* __restrict__ Qb = (T*)D.Q;
-        int* __restrict__ ef = D.ef;
         // ---- forward sweep (post-order blocks) ----
         for (int b = 0; b < D.n_blocks; b++) {
             const nm_block B = D.blocks[b];
             const T* w = G1 + B.seg * M;
-            const int egs = SC ? S.eg[B.seg] : 0;
             T wr[B1_KS];
 #pragma unroll
             for (int q = 0; q < B1_KS; q++) wr[q] = q < nk ? w[tid + 1 + q * nth] : (T)0;
-            int s = B.s0, ecur = 0;
-            float lmax = 0.f;
+            int s = B.s0;
             if (B.n_child == 0) {
 #pragma unroll
                 for (int q = 0; q < B1_KS; q++)
@@ -329,9 +244,7 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Sc
                         if (lor[q]) cur[0] = wr[q];
                         if (hir[q]) cur[MX + 1] = wr[q];
                         Gf[(size_t)s * M + xk] = wr[q];
-                        if (SC) lmax = fmaxf(lmax, (float)wr[q]);
                     }
-                ecur = egs;
             } else {
                 // join: Gf = P(Gf[c0])·G1 · Π_c [P(Gf[c])·KSAM]^mult
                 int nc = B.n_child;
@@ -345,12 +258,10 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Sc
                         int sl = Cb.s0 + Cb.length - 1;
                         for (int xx = tid + 1; xx <= MX; xx += nth)
                             Pc[(size_t)cb * M + xx] = sten1<T, true>(L, C, Gf + (size_t)sl * M, xx) * (T)P.ksam[xx];
-                        if (SC && tid == 0) D.epc[cb] = ef[sl];
                     }
                     __syncthreads();
                 }
                 int sl0 = C0.s0 + C0.length - 1;
-                int ejoin = SC ? ef[sl0] + egs : 0;
                 for (int xx = tid + 1; xx <= MX; xx += nth) {
                     T v = sten1<T, true>(L, C, Gf + (size_t)sl0 * M, xx) * w[xx];
                     if (!simple) {
@@ -362,71 +273,44 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Sc
                     }
                     cur[xx] = v;
                 }
-                if (SC && !simple) {
-                    ejoin += (C0.mult - 1) * D.epc[c0];
-                    for (int c = 1; c < nc; c++) {
-                        int cb = D.child_index[B.child0 + c];
-                        ejoin += D.blocks[cb].mult * D.epc[cb];
-                    }
-                }
-                if (SC) {
-                    float lm = 0.f;
-                    for (int xx = tid + 1; xx <= MX; xx += nth) lm = fmaxf(lm, (float)cur[xx]);
-                    int e = expo(b1_block_maxf(lm, red));
-                    float f = pow2f(-e);
-                    for (int xx = tid + 1; xx <= MX; xx += nth) cur[xx] = (T)((float)cur[xx] * f);
-                    ejoin += e;
-                }
                 __syncthreads();
                 for (int xx = tid + 1; xx <= MX; xx += nth) {
                     Gf[(size_t)s * M + xx] = cur[xx];
                     if (xx == L.b1) cur[0] = cur[xx];
                     if (xx == L.bm) cur[MX + 1] = cur[xx];
-                    if (SC) lmax = fmaxf(lmax, (float)cur[xx]);
                 }
-                ecur = ejoin;
             }
-            if (SC && tid == 0) ef[s] = ecur;
-            int enext = SC ? scl.block_exp(lmax) : 0;
-            if (!SC) __syncthreads();
-            // steps: Gf[s] = P(Gf[s-1])·G1·2^-enext (rescale every B1_RS steps)
+            __syncthreads();
+            // steps: Gf[s] = P(Gf[s-1])·G1
             for (int k = 1; k < B.length; k++) {
                 s++;
-                T f = SC ? (T)pow2f(-enext) : (T)1;
                 T* __restrict__ gs = Gf + (size_t)s * M;
-                const bool red_step = SC && (k % B1_RS) == 0;
-                float lm = 0.f;
 #pragma unroll
                 for (int q = 0; q < B1_KS; q++)
                     if (q < nk) {
                         int xk = tid + 1 + q * nth;
                         T v = stb<T, CURV>(cur, xk, lam, lmid, cmr[q], c0r[q], cpr[q]) * wr[q];
-                        if (SC) { v = v * f; lm = fmaxf(lm, (float)v); }
                         nxt[xk] = v;
                         if (lor[q]) nxt[0] = v;
                         if (hir[q]) nxt[MX + 1] = v;
                         gs[xk] = v;
                     }
-                int e2 = 0;
-                if (red_step) e2 = scl.block_exp(lm); else __syncthreads();
-                if (SC) { ecur += enext + egs; if (tid == 0) ef[s] = ecur; }
+                __syncthreads();
                 T* t = cur; cur = nxt; nxt = t;
-                enext = e2;
             }
             __syncthreads();
         }
-        // ---- G(N) = Σ Gf[root]·L (ComputeGN), FP64 ----
+        // ---- G(N) = Σ Gf[root]·L (ComputeGN) ----
         const nm_block Rb = D.blocks[D.n_blocks - 1];
         int sroot = Rb.s0 + Rb.length - 1;
-        int eroot = SC ? ef[sroot] : 0;
         {
             double acc = 0;
             for (int xx = tid + 1; xx <= MX; xx += nth) {
-                double v = (double)Gf[(size_t)sroot * M + xx];
+                double v = Gf[(size_t)sroot * M + xx];
                 acc += P.L ? v * P.L[xx] : v;
             }
             double GN = b1_block_sum(acc, red);
-            if (tid == 0) { sc[5 * m + 0] = GN; sc[5 * m + 3] = (double)eroot; }
+            if (tid == 0) { sc[5 * m + 0] = GN; sc[5 * m + 3] = 0.0; }
         }
         // ---- backward sweep fused with composition (pre-order) ----
         int stack[B1_MAXB];
@@ -436,8 +320,7 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Sc
             int b = stack[--sp];
             const nm_block B = D.blocks[b];
             const T* w = G1 + B.seg * M;
-            const int egs = SC ? S.eg[B.seg] : 0;
-            R* rr = rho + (D.mm0 + B.molmon) * M;
+            T* rr = rho + (D.mm0 + B.molmon) * M;
             const T d = (T)B.degeneracy;
             T wr[B1_KS], acc[B1_KS], cmp[B1_KS], gfn[B1_KS];
 #pragma unroll
@@ -446,8 +329,6 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Sc
                 acc[q] = (T)0; cmp[q] = (T)0;
             }
             int s = B.s0 + B.length - 1;
-            int eb, enext;
-            float lm = 0.f;
             if (B.parent < 0) {
 #pragma unroll
                 for (int q = 0; q < B1_KS; q++)
@@ -455,9 +336,7 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Sc
                         cur[tid + 1 + q * nth] = wr[q];
                         if (lor[q]) cur[0] = wr[q];
                         if (hir[q]) cur[MX + 1] = wr[q];
-                        if (SC) lm = fmaxf(lm, (float)wr[q]);
                     }
-                eb = egs;
             } else {
                 const T* q0 = Qb + (size_t)b * M;
 #pragma unroll
@@ -468,71 +347,48 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Sc
                         cur[xk] = v;
                         if (lor[q]) cur[0] = v;
                         if (hir[q]) cur[MX + 1] = v;
-                        if (SC) lm = fmaxf(lm, (float)v);
                     }
-                eb = (SC ? D.eq[b] : 0) + egs;
             }
-            enext = SC ? scl.block_exp(lm) : 0;
-            if (!SC) __syncthreads();
+            __syncthreads();
             {   // top segment of the block
                 const T* gsrc = Gf + (size_t)s * M;
-                T sf = SC ? (T)pow2f(ef[s] + eb - eroot) * d : d;
 #pragma unroll
                 for (int q = 0; q < B1_KS; q++)
-                    if (q < nk) acc[q] = gsrc[tid + 1 + q * nth] * cur[tid + 1 + q * nth] * sf;
+                    if (q < nk) acc[q] = gsrc[tid + 1 + q * nth] * cur[tid + 1 + q * nth] * d;
             }
             // prefetch the stored forward propagator of the next segment
-            int efn = 0;
             if (s - 1 >= B.s0) {
                 const T* gsrc = Gf + (size_t)(s - 1) * M;
 #pragma unroll
                 for (int q = 0; q < B1_KS; q++) gfn[q] = q < nk ? gsrc[tid + 1 + q * nth] : (T)0;
-                if (SC) efn = ef[s - 1];
             }
-            int nacc = 0, kstep = 0;
             for (s = s - 1; s >= B.s0; s--) {
                 T gf[B1_KS];
 #pragma unroll
                 for (int q = 0; q < B1_KS; q++) gf[q] = gfn[q];
-                int efs = efn;
                 if (s - 1 >= B.s0) {
                     const T* gsrc = Gf + (size_t)(s - 1) * M;
 #pragma unroll
                     for (int q = 0; q < B1_KS; q++) if (q < nk) gfn[q] = gsrc[tid + 1 + q * nth];
-                    if (SC) efn = ef[s - 1];
                 }
-                T f = SC ? (T)pow2f(-enext) : (T)1;
-                const bool red_step = SC && (++kstep % B1_RS) == 0;
-                float lmx = 0.f;
 #pragma unroll
                 for (int q = 0; q < B1_KS; q++)
                     if (q < nk) {
                         int xk = tid + 1 + q * nth;
                         T v = stb<T, CURV>(cur, xk, lam, lmid, cmr[q], c0r[q], cpr[q]) * wr[q];
-                        if (SC) { v = v * f; lmx = fmaxf(lmx, (float)v); }
                         nxt[xk] = v;
                         if (lor[q]) nxt[0] = v;
                         if (hir[q]) nxt[MX + 1] = v;
                         gf[q] *= v;
                     }
-                int e2 = 0;
-                if (red_step) e2 = scl.block_exp(lmx); else __syncthreads();
-                if (SC) eb += enext + egs;
+                __syncthreads();
                 T* t = cur; cur = nxt; nxt = t;
-                enext = e2;
-                T sf = SC ? (T)pow2f(efs + eb - eroot) * d : d;
 #pragma unroll
                 for (int q = 0; q < B1_KS; q++) {  // compensated sum (Kahan)
-                    T y = gf[q] * sf - cmp[q];
+                    T y = gf[q] * d - cmp[q];
                     T t2 = acc[q] + y;
                     cmp[q] = (t2 - acc[q]) - y;
                     acc[q] = t2;
-                }
-                if (SC && ++nacc == 32) {  // FP32: flush into rho
-#pragma unroll
-                    for (int q = 0; q < B1_KS; q++)
-                        if (q < nk) { rr[tid + 1 + q * nth] += acc[q] - cmp[q]; acc[q] = (T)0; cmp[q] = (T)0; }
-                    nacc = 0;
                 }
             }
 #pragma unroll
@@ -545,7 +401,6 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Sc
                 int cb = D.child_index[B.child0 + c];
                 bool simple = (B.n_child == 1 && D.blocks[cb].mult == 1);
                 T* q = Qb + (size_t)cb * M;
-                int eq = eb;
                 for (int xx = tid + 1; xx <= MX; xx += nth) {
                     T v = cur[xx];
                     if (!simple) {
@@ -558,33 +413,42 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Sc
                     }
                     q[xx] = v;
                 }
-                if (SC && !simple) {
-                    eq += (D.blocks[cb].mult - 1) * D.epc[cb];
-                    for (int o = 0; o < B.n_child; o++) {
-                        if (o == c) continue;
-                        int ob = D.child_index[B.child0 + o];
-                        eq += D.blocks[ob].mult * D.epc[ob];
-                    }
-                }
-                if (SC && tid == 0) D.eq[cb] = eq;
             }
             __syncthreads();
             for (int c = B.n_child - 1; c >= 0; c--) stack[sp++] = D.child_index[B.child0 + c];
         }
         __syncthreads();
     }
-    // ---- normalisation (system.cpp:2368-2560), one thread, FP64 ----
-    // FP32 phase: rho and G(N) carry the root exponent e (rho_true = rho·2^e,
-    // GN_true = GNm·2^e) and G1 is stored as G1·2^-eg.  Restricted chains use
-    // n/GNm (the e cancel); free chains and the solvent apply φb/N·2^e.
+}
+
+// Normalisation, φ, φ_tot and the residual (system.cpp:2324-2560 and
+// System::Classical_residual, system.cpp:2087-2189), FP64, from rho in the
+// natural site layout [n_mm][M] and G(N) in sc[5m].
+//  SCALED = false: rho = Σ Gf·Gb (divided by G1 here), sc[5m] = G(N).
+//  SCALED = true (FP32 phase): rho already divided by G1 and, like G(N),
+//  stored relative to 2^e with e = sc[5m+3]: rho_true = rho·2^e,
+//  G(N)_true = sc[5m]·2^e.  Restricted chains use n/GNm (the 2^e cancel);
+//  free chains and the solvent carry φb/N·2^e.
+template <bool SCALED>
+__device__ __noinline__ void b1_finish(B1Prob& P, const Lat1 L, const Coef<double> C, B1S& S, const double* __restrict__ x,
+                          double* __restrict__ g) {
+    typedef double R;
+    const int M = L.M, MX = L.MX, ns = P.ns, nit = P.nit, n_mm = P.n_mm;
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const double* G1 = S.G1;
+    R* phi = S.phi;
+    R* rho = S.rho;
+    R* phitot = S.phitot;
+    double *sc = S.sc, *spb = S.spb;
+    // ---- normalisation (system.cpp:2368-2560), one thread ----
     if (tid == 0) {
         double Bsum = 0;
         for (int m = 0; m < P.nmol; m++) {
             const B1Mol& D = P.mol[m];
             double* s5 = sc + 5 * m;
             double GNm = s5[0];
-            int e = SC ? (int)s5[3] : 0;
-            double GN = SC ? ldexp(GNm, e) : GNm;
+            int e = SCALED ? (int)s5[3] : 0;
+            double GN = SCALED ? ldexp(GNm, e) : GNm;
             double norm = 0, fac = 0;
             int pe = 0;
             s5[0] = GN;
@@ -598,7 +462,7 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Sc
             } else if (D.freedom == NM_MOL_RESTRICTED) {
                 if (GNm > 0) {
                     norm = D.n_in / GN;
-                    fac = SC ? D.n_in / GNm : norm;
+                    fac = SCALED ? D.n_in / GNm : norm;
                     if (D.pinned) s5[4] = 0;
                     else { s5[4] = D.N * norm; Bsum += s5[4]; }
                 } else if (*S.status == 0) *S.status = NM_ERR_GN;
@@ -625,11 +489,8 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Sc
     // ---- φ = rho/G1·norm, φ_tot ----
     R mmf[NM_MAX_MM];
     for (int k = 0; k < n_mm; k++) {
-        int m = P.mm_mol[k], sg = P.mm_seg[k];
-        // FP32 phase: 2^phie / 2^eg folded into one factor
-        double f = S.phif[m];
-        if (SC) f = ldexp(f, S.phie[m] - S.eg[sg]);
-        mmf[k] = (R)f;
+        int m = P.mm_mol[k];
+        mmf[k] = SCALED ? ldexp(S.phif[m], S.phie[m]) : S.phif[m];
     }
     for (int s = tid; s < M; s += nth) {
         bool in = s >= 1 && s <= MX;
@@ -642,8 +503,12 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Sc
         if (in)
             for (int k = 0; k < n_mm; k++) {
                 int sg = P.mm_seg[k];
-                R g1 = (R)G1[sg * M + s];
-                R v = g1 != (R)0 ? rho[k * M + s] / g1 : (R)0;
+                R v;
+                if (SCALED) v = rho[k * M + s];
+                else {
+                    R g1 = G1[sg * M + s];
+                    v = g1 != (R)0 ? rho[k * M + s] / g1 : (R)0;
+                }
                 v *= mmf[k];
                 phi[sg * M + s] += v;
                 pt += v;
@@ -657,7 +522,6 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Sc
         for (int k = 0; k < ns; k++) chir[i * ns + k] = (R)P.chi[P.it_seg[i] * ns + k];
     R spbr[NM_MAX_SEG];
     for (int k = 0; k < ns; k++) spbr[k] = (R)spb[k];
-    Coef<R> CR = C;
     R rinv = (R)(1.0 / nit);
     for (int s = tid; s < M; s += nth) {
         if (s < 1 || s > MX) {
@@ -665,7 +529,7 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Sc
             continue;
         }
         R ps[NM_MAX_SEG];
-        for (int k = 0; k < ns; k++) ps[k] = sten1<R, false>(L, CR, phi + k * M, s);
+        for (int k = 0; k < ns; k++) ps[k] = sten1<R, false>(L, C, phi + k * M, s);
         R pt = phitot[s];
         R gi[NM_MAX_SEG];
         R al = 0;
@@ -688,27 +552,74 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<T> C, B1S& S, Sc
     __syncthreads();
 }
 
-// fp32_first: FP32 propagators until ‖g‖ < P.sw_tol (or a stall close to
-// convergence), then FP64 (DIIS history restarted), so the stopping test
-// ‖g‖ < tol is always made on an FP64 residual.
-// mode 0: FP64 from the start; 1: FP32 propagators first (this kernel);
-// 2: FP64 continuation of a problem handed over by k_batch1d_w.
+}  // namespace nm
+#include "batch1d_bfp.cuh"
+namespace nm {
+
+// Shared memory of k_batch1d, in doubles (host and device agree on it):
+// tail arrays phi [ns·M], rho [n_mm·M], phitot [M]; then one region shared by
+// the FP64 phase (G1 [ns·M], cur [M], nxt [M]) and the FP32 phase (G1s, rhos
+// [ns+n_mm][Wl] and three weight rows of Wl floats, Wl = 128·SP); then
+// reduction and DIIS scratch.
+__host__ __device__ inline int b1_sp(int MX) {  // sites per thread: 1, 2 or 4
+    const int sp = (MX + BC_NT - 1) / BC_NT;
+    return sp <= 2 ? sp : 4;
+}
+__host__ __device__ inline size_t b1_uni_doubles(int ns, int n_mm, int M, int MX) {
+    size_t f64 = (size_t)(ns + 2) * M;
+    size_t f32 = ((size_t)(ns + n_mm + 3) * BC_NT * b1_sp(MX) + 1) / 2;
+    return f64 > f32 ? f64 : f32;
+}
+__host__ __device__ inline size_t b1_smem_doubles(int ns, int n_mm, int M, int MX) {
+    return (size_t)(ns + n_mm + 1) * M + b1_uni_doubles(ns, n_mm, M, MX) + 64 +
+           B1_MAXM * B1_MAXM + B1_MAXM + B1_MAXM * (B1_MAXM + 1) + 5 * NM_MAX_MOL + NM_MAX_SEG + B1_MAXM;
+}
+
+// FP32 residual: sites per thread, curved lattice, periodic bounds
+__device__ __noinline__ void bc_dispatch(B1Prob& P, const Lat1 L, const Coef<double> C64, B1S& S, BcX& X,
+                                         const double* __restrict__ x, double* __restrict__ g, int sp) {
+    const bool cv = L.geom != 0, per = (L.b1 == L.MX && L.bm == 1 && L.MX > 1);
+#define BC_CALL(SPV)                                                             \
+    if (cv) {                                                                    \
+        if (per) bc_residual<SPV, true, true>(P, L, C64, S, X, x, g);            \
+        else bc_residual<SPV, true, false>(P, L, C64, S, X, x, g);               \
+    } else {                                                                     \
+        if (per) bc_residual<SPV, false, true>(P, L, C64, S, X, x, g);           \
+        else bc_residual<SPV, false, false>(P, L, C64, S, X, x, g);              \
+    }
+    switch (sp) {
+        case 1: BC_CALL(1) break;
+        case 2: BC_CALL(2) break;
+        default: BC_CALL(4) break;
+    }
+#undef BC_CALL
+}
+
+// One CTA per problem: residual + DIIS until ‖g‖ < tol or the iteration limit
+// (Solve_scf / SFNewton::iterate_DIIS, sfnewton.cpp:1037-1130).
+// mode 0: FP64 throughout, the reference's arithmetic.
+// mode 1: FP32 block-floating-point propagators (batch1d_bfp.cuh) until
+//   ‖g‖ < P.sw_tol, or a stall close to convergence, then FP64 in the same
+//   CTA with the DIIS history restarted, so the stopping test ‖g‖ < tol is
+//   always made on an FP64 residual.  A failure of the FP32 evaluation
+//   (G(N) <= 0, a non-finite residual) is a failure of the reduced precision,
+//   not a verdict on the problem: the FP64 phase takes over at the same x.
 __global__ void __launch_bounds__(B1_THREADS, 4) k_batch1d(B1Prob* __restrict__ probs, int mode) {
     B1Prob& P = probs[blockIdx.x];
-    if (mode == 2 && !P.handoff) return;
     extern __shared__ double sm[];
     const int M = P.M, ns = P.ns, iv = P.iv, n_mm = P.n_mm, m = P.m;
     const int tid = threadIdx.x, nth = blockDim.x;
     const Lat1 L{P.MX, P.M, P.b1, P.bm, P.geom};
     B1S S;
     double* q = sm;
-    S.G1 = q; q += ns * M;
     S.phi = q; q += ns * M;
     S.rho = q; q += n_mm * M;
     S.phitot = q; q += M;
-    S.cur = q; q += M;
-    S.nxt = q; q += M;
-    S.cm1 = (float*)q; S.c0 = S.cm1 + M; S.cp1 = S.c0 + M; q += (3 * M + 1) / 2;
+    S.uni = q;
+    S.G1 = q;
+    S.cur = q + ns * M;
+    S.nxt = q + (ns + 1) * M;
+    q += b1_uni_doubles(ns, n_mm, M, P.MX);
     S.red = q; q += 64;
     S.Aij = q; q += B1_MAXM * B1_MAXM;
     S.Ci = q; q += B1_MAXM;
@@ -716,53 +627,51 @@ __global__ void __launch_bounds__(B1_THREADS, 4) k_batch1d(B1Prob* __restrict__ 
     S.sc = q; q += 5 * NM_MAX_MOL;
     S.spb = q; q += NM_MAX_SEG;
     S.gram = q; q += B1_MAXM;
-    __shared__ float slots[64];
     __shared__ int sh_status;
     __shared__ double phif[NM_MAX_MOL];
     __shared__ int phie[NM_MAX_MOL];
     __shared__ int egs[NM_MAX_SEG];
+    __shared__ BcX bcx;
     S.phif = phif; S.phie = phie; S.status = &sh_status; S.eg = egs;
-    Scaler scl{slots, 0};
     double* __restrict__ x = P.x;
     double* __restrict__ g = P.g;
     double *red = S.red, *Aij = S.Aij, *Ci = S.Ci;
-    Coef<double> C64{P.lam, 1.0 - 2.0 * P.lam, P.lm1, P.l0, P.l1};
-    Coef<float> C32{(float)P.lam, 1.0f - 2.0f * (float)P.lam, S.cm1, S.c0, S.cp1};
-    if (P.geom != 0)
-        for (int s = tid; s < M; s += nth) {
-            S.cm1[s] = (float)P.lm1[s]; S.c0[s] = (float)P.l0[s]; S.cp1[s] = (float)P.l1[s];
-        }
+    const Coef<double> C64{P.lam, 1.0 - 2.0 * P.lam, P.lm1, P.l0, P.l1};
     for (int i = tid; i < B1_MAXM * B1_MAXM; i += nth) Aij[i] = 0;
-    for (int i = tid; i < 2 * M; i += nth) ((double*)S.cur)[i] = 0;  // wall halos
     if (tid == 0) sh_status = 0;
     __syncthreads();
 
     bool use32 = mode == 1;
+    const int sp32 = b1_sp(P.MX);
     int it = 0, k_diis = 0, fp32_its = 0;
-    if (mode == 2) { it = P.iterations + 1; fp32_its = P.fp32_iterations; }
     double resid = 0, best = 1e300;
     int since_best = 0;
     for (;;) {
         if (use32) {
-            if (L.geom == 0) b1_residual<float, true, false>(P, L, C32, S, scl, x, g);
-            else b1_residual<float, true, true>(P, L, C32, S, scl, x, g);
+            bc_dispatch(P, L, C64, S, bcx, x, g, sp32);
             fp32_its++;
+            if (sh_status && !P.eval_only) {  // reduced precision failed: FP64 from here
+                __syncthreads();
+                if (tid == 0) sh_status = 0;
+                use32 = false;
+                k_diis = 0;
+                __syncthreads();
+                continue;
+            }
         } else {
-            if (L.geom == 0) b1_residual<double, false, false>(P, L, C64, S, scl, x, g);
-            else b1_residual<double, false, true>(P, L, C64, S, scl, x, g);
+            if (L.geom == 0) b1_residual<false>(P, L, C64, S, x, g);
+            else b1_residual<true>(P, L, C64, S, x, g);
+            b1_finish<false>(P, L, C64, S, x, g);
         }
         if (sh_status || P.eval_only) break;
         // ---------------- DIIS (iterate_DIIS / DIIS / Ax), FP64 ----------------
         int k = it % m;
         double* __restrict__ xRk = P.xR + (size_t)k * iv;
         double* __restrict__ xxk = P.xx0 + (size_t)k * iv;
+        // ‖g‖ first: a non-finite FP32 residual must leave x as it was
         double gsq = 0;
         for (int i = tid; i < iv; i += nth) {
-            double xo = x[i], gv = g[i];
-            double xn = xo + (-P.dmax) * gv;
-            x[i] = xn;
-            xRk[i] = xn;
-            xxk[i] = xn - xo;
+            double gv = g[i];
             gsq = P.max_norm ? fmax(gsq, fabs(gv)) : gsq + gv * gv;
         }
         if (P.max_norm) {
@@ -774,6 +683,19 @@ __global__ void __launch_bounds__(B1_THREADS, 4) k_batch1d(B1Prob* __restrict__ 
             for (int i = 0; i < nth / 32; i++) resid = fmax(resid, red[i]);
             __syncthreads();
         } else resid = sqrt(b1_block_sum(gsq, red));
+        if (use32 && !isfinite(resid)) {
+            use32 = false;
+            k_diis = 0;
+            continue;
+        }
+        for (int i = tid; i < iv; i += nth) {
+            double xo = x[i];
+            double xn = xo + (-P.dmax) * g[i];
+            x[i] = xn;
+            xRk[i] = xn;
+            xxk[i] = xn - xo;
+        }
+        __syncthreads();
         if (it > 0) k_diis++;  // iteration 0 is the plain mixing step
         if (k_diis > 0) {
             int kd = k_diis > m ? m : k_diis;
@@ -871,7 +793,7 @@ struct Batch {
     double* d_g = nullptr;
     std::vector<long long> offsets;
     int precision = NM_FP64;
-    size_t smem = 0, smem_w = 0;
+    size_t smem = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     long long launches = 0;
@@ -908,7 +830,6 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
     if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
     if (opt && opt->stream) B.stream = (cudaStream_t)opt->stream;
     else { cudaStreamCreateWithFlags(&B.stream, cudaStreamNonBlocking); B.own_stream = true; }
-    size_t maxsmem_w = 0;
     long long off = 0;
     size_t maxsmem = 0;
     B.hp.resize(n);
@@ -926,12 +847,8 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
         B1Prob& H = B.hp[p];
         std::memset(&H, 0, sizeof(H));
         int M = P->M;
-        {
-            int S = (P->MX + 31) / 32;
-            H.wS = S <= 4 ? 4 : (S <= 8 ? 8 : (S <= 12 ? 12 : 16));
-        }
-        // one stored vector: M doubles (FP64 phase) or 32·wS floats (warp FP32 phase)
-        size_t tsz = std::max((size_t)8 * M, (size_t)4 * 32 * H.wS);
+        // one stored vector: M doubles (FP64 phase) or 128·SP floats (FP32 phase)
+        size_t tsz = std::max((size_t)8 * M, (size_t)4 * BC_NT * b1_sp(P->MX));
         H.MX = P->MX; H.M = M; H.geom = P->geometry; H.ns = P->n_seg; H.nit = P->n_it;
         H.nmol = P->n_mol; H.solvent = P->solvent; H.m = P->diis_m; H.itlim = P->iterationlimit;
         H.max_norm = P->max_norm; H.iv = P->iv; H.lam = P->lambda; H.tol = P->tolerance; H.dmax = P->deltamax;
@@ -976,10 +893,10 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
             TRYB(B.alloc(&pc, tsz * (size_t)mol.n_blocks)); D.Pc = pc;
             TRYB(B.alloc(&q, tsz * (size_t)mol.n_blocks)); D.Q = q;
             int *ef, *epc, *eq;
-            // power-of-two exponents: one per lane (32) per stored vector
-            TRYB(B.alloc(&ef, 32 * (size_t)mol.n_store));
-            TRYB(B.alloc(&epc, 32 * (size_t)mol.n_blocks));
-            TRYB(B.alloc(&eq, 32 * (size_t)mol.n_blocks));
+            // power-of-two exponents: one per thread (128) per stored vector
+            TRYB(B.alloc(&ef, BC_NT * (size_t)mol.n_store));
+            TRYB(B.alloc(&epc, BC_NT * (size_t)mol.n_blocks));
+            TRYB(B.alloc(&eq, BC_NT * (size_t)mol.n_blocks));
             D.ef = ef; D.epc = epc; D.eq = eq;
             for (int j = 0; j < mol.n_molmon; j++) {
                 if (kk >= NM_MAX_MM) { set_error("too many (molecule, segment) pairs"); return NM_ERR_INPUT; }
@@ -994,12 +911,8 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
         B.offsets[p] = off;
         off += P->iv;
         H.sw_tol = 2e-6;
-        size_t smem = sizeof(double) * ((size_t)(2 * P->n_seg + kk + 3) * M + (3 * (size_t)M + 1) / 2 + 64 +
-                                        B1_MAXM * B1_MAXM + B1_MAXM + B1_MAXM * (B1_MAXM + 1) +
-                                        5 * NM_MAX_MOL + NM_MAX_SEG + B1_MAXM);
+        size_t smem = sizeof(double) * b1_smem_doubles(P->n_seg, kk, M, P->MX);
         maxsmem = std::max(maxsmem, smem);
-        size_t smem_w = sizeof(double) * BW_DOUBLES + sizeof(float) * (size_t)(2 * P->n_seg + kk + 3) * 32 * H.wS;
-        maxsmem_w = std::max(maxsmem_w, smem_w);
     }
     B.offsets[n] = off;
     TRYB(B.alloc(&B.d_x, (size_t)off));
@@ -1008,10 +921,8 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
     TRYB(B.alloc(&B.d_probs, (size_t)n));
     B.smem = maxsmem;
     if (maxsmem > 220 * 1024) { set_error("problem too large for the batched solver's shared memory"); return NM_ERR_INPUT; }
-    B.smem_w = maxsmem_w;
     cudaError_t e1 = cudaFuncSetAttribute(k_batch1d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxsmem);
-    cudaError_t e2 = cudaFuncSetAttribute(k_batch1d_w, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxsmem_w);
-    if (e1 != cudaSuccess || e2 != cudaSuccess) { set_error("cudaFuncSetAttribute failed"); return NM_ERR_CUDA; }
+    if (e1 != cudaSuccess) { set_error("cudaFuncSetAttribute failed"); return NM_ERR_CUDA; }
     return NM_OK;
 }
 
@@ -1019,16 +930,9 @@ static int batch_run(Batch& B) {
     int n = (int)B.hp.size();
     cudaError_t e = cudaMemcpyAsync(B.d_probs, B.hp.data(), sizeof(B1Prob) * n, cudaMemcpyHostToDevice, B.stream);
     if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
-    if (B.precision == NM_FP32) {
-        // FP32 phase one warp per problem, then the FP64 finish of every
-        // problem the warp phase handed over
-        k_batch1d_w<<<n, 32, B.smem_w, B.stream>>>(B.d_probs);
-        k_batch1d<<<n, B1_THREADS, B.smem, B.stream>>>(B.d_probs, 2);
-        B.launches += 2;
-    } else {
-        k_batch1d<<<n, B1_THREADS, B.smem, B.stream>>>(B.d_probs, 0);
-        B.launches++;
-    }
+    // one CTA per problem; FP32 problems switch to FP64 inside their CTA
+    k_batch1d<<<n, B1_THREADS, B.smem, B.stream>>>(B.d_probs, B.precision == NM_FP32 ? 1 : 0);
+    B.launches++;
     e = cudaGetLastError();
     if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
     e = cudaMemcpyAsync(B.hp.data(), B.d_probs, sizeof(B1Prob) * n, cudaMemcpyDeviceToHost, B.stream);
@@ -1111,8 +1015,7 @@ int nm_batch_residual_dev(nm_batch* b, const double* x_dev, double* g_dev, int p
     for (int p = 0; p < np; p++) B->hp[p].eval_only = 1;
     e = cudaMemcpyAsync(B->d_probs, B->hp.data(), sizeof(nm::B1Prob) * np, cudaMemcpyHostToDevice, B->stream);
     if (e != cudaSuccess) { nm::set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
-    if (precision == NM_FP32) nm::k_batch1d_w<<<np, 32, B->smem_w, B->stream>>>(B->d_probs);
-    else nm::k_batch1d<<<np, B1_THREADS, B->smem, B->stream>>>(B->d_probs, 0);
+    nm::k_batch1d<<<np, B1_THREADS, B->smem, B->stream>>>(B->d_probs, precision == NM_FP32 ? 1 : 0);
     B->launches++;
     e = cudaMemcpyAsync(g_dev, B->d_g, sizeof(double) * n, cudaMemcpyDeviceToDevice, B->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(B->stream);
@@ -1159,8 +1062,7 @@ long long nm_batch_launch_count(nm_batch* b) {
 // a host that owns a fixed memory budget sliced before work begins, a
 // sequence about to be captured into a CUDA graph, or a signal-time
 // re-solve that must not touch the allocator.  nm_solve1d_noalloc runs the
-// same two kernels as nm_batch_solve_dev (FP32 warp phase + FP64 finish, or
-// FP64 only) on one 1-gradient problem, with every piece of device scratch
+// same kernel as nm_batch_solve_dev on one 1-gradient problem, with every piece of device scratch
 // carved from one file-scope array compiled into the library.  The array's
 // address is looked up once per device (cudaGetSymbolAddress, with that
 // device current) on the first call for that device; make that first call
@@ -1196,7 +1098,7 @@ struct NoallocCopy { void* dst; const void* src; size_t bytes; };
 // batch_init gives it.  Host sources of the copies to make are listed in
 // `copies`; `ks` stages KSAM as doubles and must outlive those copies.
 static int noalloc_layout(const nm_plan* P, StaticArena& A, double* x_dev, B1Prob& H, size_t& smem,
-                          size_t& smem_w, std::vector<double>& ks, std::vector<NoallocCopy>& copies) {
+                          std::vector<double>& ks, std::vector<NoallocCopy>& copies) {
     if (P->gradients != 1) { set_error("nm_solve1d_noalloc: 1-gradient problems only"); return NM_ERR_INPUT; }
     if (P->MX > B1_KS * B1_THREADS) { set_error("nm_solve1d_noalloc: at most 512 layers"); return NM_ERR_INPUT; }
     if (P->charged) { set_error("nm_solve1d_noalloc: charged systems are not supported"); return NM_ERR_INPUT; }
@@ -1206,11 +1108,7 @@ static int noalloc_layout(const nm_plan* P, StaticArena& A, double* x_dev, B1Pro
     }
     std::memset(&H, 0, sizeof(H));
     const int M = P->M;
-    {
-        int S = (P->MX + 31) / 32;
-        H.wS = S <= 4 ? 4 : (S <= 8 ? 8 : (S <= 12 ? 12 : 16));
-    }
-    const size_t tsz = std::max((size_t)8 * M, (size_t)4 * 32 * H.wS);
+    const size_t tsz = std::max((size_t)8 * M, (size_t)4 * BC_NT * b1_sp(P->MX));
     H.MX = P->MX; H.M = M; H.geom = P->geometry; H.ns = P->n_seg; H.nit = P->n_it;
     H.nmol = P->n_mol; H.solvent = P->solvent; H.m = P->diis_m; H.itlim = P->iterationlimit;
     H.max_norm = P->max_norm; H.iv = P->iv; H.lam = P->lambda; H.tol = P->tolerance; H.dmax = P->deltamax;
@@ -1263,9 +1161,9 @@ static int noalloc_layout(const nm_plan* P, StaticArena& A, double* x_dev, B1Pro
             D.Gf = A.take<char>(tsz * (size_t)mol.n_store);
             D.Pc = A.take<char>(tsz * (size_t)mol.n_blocks);
             D.Q = A.take<char>(tsz * (size_t)mol.n_blocks);
-            D.ef = A.take<int>(32 * (size_t)mol.n_store);
-            D.epc = A.take<int>(32 * (size_t)mol.n_blocks);
-            D.eq = A.take<int>(32 * (size_t)mol.n_blocks);
+            D.ef = A.take<int>(BC_NT * (size_t)mol.n_store);
+            D.epc = A.take<int>(BC_NT * (size_t)mol.n_blocks);
+            D.eq = A.take<int>(BC_NT * (size_t)mol.n_blocks);
             if (A.overflow) goto full;
             put(db, mol.blocks, sizeof(nm_block) * mol.n_blocks);
             if (mol.n_blocks > 1) put(dci, mol.child_index, sizeof(int) * nci);
@@ -1283,10 +1181,7 @@ static int noalloc_layout(const nm_plan* P, StaticArena& A, double* x_dev, B1Pro
         if (A.overflow) goto full;
         H.x = x_dev;
         H.sw_tol = 2e-6;
-        smem = sizeof(double) * ((size_t)(2 * P->n_seg + kk + 3) * M + (3 * (size_t)M + 1) / 2 + 64 +
-                                 B1_MAXM * B1_MAXM + B1_MAXM + B1_MAXM * (B1_MAXM + 1) + 5 * NM_MAX_MOL +
-                                 NM_MAX_SEG + B1_MAXM);
-        smem_w = sizeof(double) * BW_DOUBLES + sizeof(float) * (size_t)(2 * P->n_seg + kk + 3) * 32 * H.wS;
+        smem = sizeof(double) * b1_smem_doubles(P->n_seg, kk, M, P->MX);
         if (smem > 220 * 1024) { set_error("nm_solve1d_noalloc: problem too large for shared memory"); return NM_ERR_INPUT; }
     }
     return NM_OK;
@@ -1327,13 +1222,12 @@ extern "C" int nm_solve1d_noalloc(const nm_plan* plan, double* x_dev, int precis
     StaticArena A{g_noalloc_base[dev]};
     B1Prob* d_prob = A.take<B1Prob>(1);
     B1Prob H;
-    size_t smem = 0, smem_w = 0;
+    size_t smem = 0;
     std::vector<double> ks;
     std::vector<NoallocCopy> copies;
-    int rc = noalloc_layout(plan, A, x_dev, H, smem, smem_w, ks, copies);
+    int rc = noalloc_layout(plan, A, x_dev, H, smem, ks, copies);
     if (rc) return rc;
     e = noalloc_smem(k_batch1d, smem);
-    if (e == cudaSuccess) e = noalloc_smem(k_batch1d_w, smem_w);
     if (e != cudaSuccess) { set_error(std::string("nm_solve1d_noalloc: ") + cudaGetErrorString(e)); return NM_ERR_CUDA; }
     // what the batch path's zero-filled allocations start from
     e = cudaMemsetAsync(A.base, 0, A.used, st);
@@ -1341,12 +1235,7 @@ extern "C" int nm_solve1d_noalloc(const nm_plan* plan, double* x_dev, int precis
         e = cudaMemcpyAsync(copies[i].dst, copies[i].src, copies[i].bytes, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_prob, &H, sizeof(B1Prob), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
-    if (precision == NM_FP32) {
-        k_batch1d_w<<<1, 32, smem_w, st>>>(d_prob);
-        k_batch1d<<<1, B1_THREADS, smem, st>>>(d_prob, 2);
-    } else {
-        k_batch1d<<<1, B1_THREADS, smem, st>>>(d_prob, 0);
-    }
+    k_batch1d<<<1, B1_THREADS, smem, st>>>(d_prob, precision == NM_FP32 ? 1 : 0);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(&H, d_prob, sizeof(B1Prob), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
