@@ -4,9 +4,12 @@ Workload (one "step"): 512 independent 1-gradient planar brushes solved to
 ‖g‖₂ < 1e-7 from seeded fields u ~ U(-0.01, 0.01), drawn from a fixed seed:
 n_layers ~ U{50..400}, N ~ U{20..500}, σ ~ U[0.01, 0.1], χ_AS ~ U[0, 1];
 every 10th instance is a 3-arm star with arms of N/3 joined at a branch point.
-All 512 solves run in one persistent launch (one CTA per problem, DIIS on the
-device), FP32 propagators with per-step power-of-two scaling and FP64
-normalisation / residual / DIIS.
+All 512 solves run in one launch (one 128-thread CTA per problem, DIIS on
+the device): FP32 block-floating-point propagators, FP64 normalisation,
+residual and DIIS, and an FP64-propagator finish inside the same CTA.  The
+plain FP64 path (the same kernel with FP64 propagators throughout) is timed
+in the same run and reported beside it (`fp64_gpu`), and so are the p50/p99
+of the per-problem time to convergence inside the launch (device timer).
 
 Contract: `python bench.py --gpus N --steps K --warmup W` prints one JSON
 line.  `value` times the kernel with inputs resident in HBM (CUDA events);
@@ -38,7 +41,7 @@ sys.path.insert(0, str(ROOT))
 N_INSTANCES = 512
 SEED = 20251203
 FIELD = (-0.01, 0.01)
-METRIC = "SCF solves/s at |residual|<1e-7 (batched FP32-propagator, FP64 DIIS)"
+METRIC = "SCF solves/s at |residual|<1e-7 (served FP32 vs plain FP64 GPU); p50/p99 latency"
 UNIT = "solves/s"
 B_PER_UPDATE_FP32 = 22.0   # algorithmic bytes per segment-site update (FP32 propagators, FP64 φ)
 B_PER_UPDATE_FP64 = 36.0
@@ -228,6 +231,7 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU comparison")
     ap.add_argument("--instances", type=int, default=N_INSTANCES)
     args = ap.parse_args()
     if args.impl == "reference":
@@ -286,6 +290,33 @@ def main():
     torch.cuda.synchronize()
     launches = batch.launch_count() - launches0
     ms = statistics.mean(times)
+    lat = batch.times() * 1e3  # ms per problem, last timed step
+    ok = st == 0
+    latency = {"p50_ms": float(np.percentile(lat[ok], 50)) if ok.any() else None,
+               "p99_ms": float(np.percentile(lat[ok], 99)) if ok.any() else None,
+               "unit": "ms", "what": "per-problem time to convergence inside the launch (converged problems)"}
+    # the plain FP64 GPU path on the same instances (same kernel, FP64 propagators throughout)
+    fp64 = None
+    if prec == NM_FP32 and not args.no_fp64:
+        b64 = Batch(plans, NM_FP64, device=local, stream=stream.cuda_stream)
+        t64 = []
+        for k in range(3):
+            flush.zero_()
+            xw.copy_(x0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _, _, st64 = b64.solve_dev(xw.data_ptr())
+            e1.record(stream)
+            e1.synchronize()
+            if k > 0:
+                t64.append(e0.elapsed_time(e1))
+        ms64 = statistics.mean(t64)
+        n64 = int((st64 == 0).sum())
+        fp64 = {"value": n64 / (ms64 / 1000.0), "unit": UNIT, "ms_per_step": ms64, "converged": n64,
+                "steps": len(t64), "warmup": 1}
+        b64.close()
     if ws > 1:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -335,6 +366,8 @@ def main():
                 "d2h_bytes_per_step": nbytes},
         "gpu_launches": launches,
         "clocks": clk.summary(),
+        "latency": latency,
+        "fp64_gpu": fp64,
     }
     if rank == 0 and not args.no_cpu and ws == 1:
         line["cpu_baseline"] = cpu_baseline(texts, xs, budget_s=15.0)

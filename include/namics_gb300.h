@@ -231,6 +231,10 @@ int nm_batch_residual_dev(nm_batch* b, const double* x_dev, double* g_dev, int p
 /* per-problem iteration counts of the FP32-propagator phase of the last
  * solve (0 for FP64 batches) */
 int nm_batch_stats(nm_batch* b, int* fp32_iterations);
+/* per-problem time to convergence in the last solve: seconds from the
+ * start of the batch's first CTA to the end of the problem's CTA (device
+ * global timer), [n_plans] host array */
+int nm_batch_times(nm_batch* b, double* seconds);
 /* per-problem free energy / grand potential of the final state */
 int nm_batch_free_energy(nm_batch* b, double* F, double* Omega);
 long long nm_batch_launch_count(nm_batch* b);

@@ -252,6 +252,13 @@ class Batch:
         _check(_abi.load().nm_batch_stats(self._h, out.ctypes.data_as(_abi.ip)))
         return out
 
+    def times(self) -> np.ndarray:
+        """Per-problem time to convergence of the last solve (seconds from the
+        start of the batch's first CTA)."""
+        out = np.zeros(len(self.plans))
+        _check(_abi.load().nm_batch_times(self._h, _dptr(out)))
+        return out
+
     def free_energy(self):
         n = len(self.plans)
         F = np.zeros(n)

@@ -89,6 +89,7 @@ SIGNATURES = [
     ("nm_batch_offsets", C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
     ("nm_batch_residual_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     ("nm_batch_stats", C.c_int, [C.c_void_p, ip]),
+    ("nm_batch_times", C.c_int, [C.c_void_p, dp]),
     ("nm_batch_free_energy", C.c_int, [C.c_void_p, dp, dp]),
     ("nm_batch_launch_count", C.c_longlong, [C.c_void_p]),
     ("nm_solve1d_noalloc", C.c_int, [P_plan, C.c_void_p, C.c_int, C.c_void_p, C.POINTER(nm_solve_result)]),

@@ -62,7 +62,8 @@ struct B1Prob {
     double* xx0;         // [m*iv]
     // results
     int iterations, fp32_iterations, status, eval_only;
-    double residual, F, Omega, sw_tol;
+    double residual, F, Omega, sw_tol, sw_floor;
+    unsigned long long t_begin, t_end;  // %globaltimer (ns) at the CTA's start and end
     double sc[5 * NM_MAX_MOL];  // GN, norm, n, theta, phibulk per molecule
     double seg_phibulk[NM_MAX_SEG];
 };
@@ -604,8 +605,15 @@ __device__ __noinline__ void bc_dispatch(B1Prob& P, const Lat1 L, const Coef<dou
 //   always made on an FP64 residual.  A failure of the FP32 evaluation
 //   (G(N) <= 0, a non-finite residual) is a failure of the reduced precision,
 //   not a verdict on the problem: the FP64 phase takes over at the same x.
+__device__ __forceinline__ unsigned long long b1_clock() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 __global__ void __launch_bounds__(B1_THREADS, 4) k_batch1d(B1Prob* __restrict__ probs, int mode) {
     B1Prob& P = probs[blockIdx.x];
+    if (threadIdx.x == 0) P.t_begin = b1_clock();
     extern __shared__ double sm[];
     const int M = P.M, ns = P.ns, iv = P.iv, n_mm = P.n_mm, m = P.m;
     const int tid = threadIdx.x, nth = blockDim.x;
@@ -757,10 +765,14 @@ __global__ void __launch_bounds__(B1_THREADS, 4) k_batch1d(B1Prob* __restrict__ 
             __syncthreads();
         }
         if (use32) {
-            // leave the FP32 phase at the switch tolerance, or on a stall close
-            // to convergence; instances far from convergence stay in FP32
+            // Leave the FP32 phase at the switch tolerance; or on a stall near
+            // the FP32 accuracy floor sw_floor (~1e-7 per chain segment: a
+            // residual there is noise and DIIS stops making progress); or on
+            // a long stall close to convergence.  Instances far from
+            // convergence stay in FP32.
             if (resid < 0.9 * best) { best = resid; since_best = 0; } else since_best++;
-            if (!(resid > P.sw_tol) || (since_best > 25 && resid < 1e-2)) {
+            if (!(resid > P.sw_tol) || (since_best > 10 && resid < 10.0 * P.sw_floor) ||
+                (since_best > 25 && resid < 1e-2)) {
                 use32 = false;
                 k_diis = 0;  // restart the DIIS history on the FP64 residual
                 if (it >= P.itlim) break;
@@ -774,6 +786,7 @@ __global__ void __launch_bounds__(B1_THREADS, 4) k_batch1d(B1Prob* __restrict__ 
         it++;
     }
     if (tid == 0) {
+        P.t_end = b1_clock();
         P.iterations = it;
         P.fp32_iterations = fp32_its;
         P.residual = resid;
@@ -784,6 +797,15 @@ __global__ void __launch_bounds__(B1_THREADS, 4) k_batch1d(B1Prob* __restrict__ 
 }
 
 // ------------------------------------------------------------------ host
+// Accuracy floor of an FP32-propagator residual: G1 held in FP32 is the exact
+// G1 of a field perturbed by ~6e-8 per site, which a chain of N segments
+// answers with a change of φ (and of the residual) up to ~N·6e-8.
+static double b1_fp32_floor(const nm_plan* P) {
+    double n = 1;
+    for (int m = 0; m < P->n_mol; m++) n = std::max(n, P->mols[m].chainlength);
+    return 1e-7 * n + 1e-6;
+}
+
 struct Batch {
     std::vector<const nm_plan*> plans;
     std::vector<B1Prob> hp;
@@ -911,6 +933,7 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
         B.offsets[p] = off;
         off += P->iv;
         H.sw_tol = 2e-6;
+        H.sw_floor = b1_fp32_floor(P);
         size_t smem = sizeof(double) * b1_smem_doubles(P->n_seg, kk, M, P->MX);
         maxsmem = std::max(maxsmem, smem);
     }
@@ -1028,6 +1051,15 @@ int nm_batch_stats(nm_batch* b, int* fp32_iterations) {
     Batch* B = reinterpret_cast<Batch*>(b);
     if (!B || !fp32_iterations) { nm::set_error("nm_batch_stats: bad argument"); return NM_ERR_ARG; }
     for (size_t p = 0; p < B->hp.size(); p++) fp32_iterations[p] = B->hp[p].fp32_iterations;
+    return NM_OK;
+}
+
+int nm_batch_times(nm_batch* b, double* seconds) {
+    Batch* B = reinterpret_cast<Batch*>(b);
+    if (!B || !seconds) { nm::set_error("nm_batch_times: bad argument"); return NM_ERR_ARG; }
+    unsigned long long t0 = ~0ull;
+    for (auto& h : B->hp) t0 = std::min(t0, h.t_begin);
+    for (size_t p = 0; p < B->hp.size(); p++) seconds[p] = (double)(B->hp[p].t_end - t0) * 1e-9;
     return NM_OK;
 }
 
@@ -1181,6 +1213,7 @@ static int noalloc_layout(const nm_plan* P, StaticArena& A, double* x_dev, B1Pro
         if (A.overflow) goto full;
         H.x = x_dev;
         H.sw_tol = 2e-6;
+        H.sw_floor = b1_fp32_floor(P);
         smem = sizeof(double) * b1_smem_doubles(P->n_seg, kk, M, P->MX);
         if (smem > 220 * 1024) { set_error("nm_solve1d_noalloc: problem too large for shared memory"); return NM_ERR_INPUT; }
     }
