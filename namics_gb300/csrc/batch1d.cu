@@ -127,6 +127,14 @@ __device__ __forceinline__ int expo(float v) {  // frexp exponent of v > 0
 __device__ void warp_solve(double* A, double* c, int kd) {
     const int lane = threadIdx.x & 31;
     const int ld = kd + 1;
+    // pivots that rounding made (almost) zero are floored at 1e-30·max|A|
+    // (near convergence A ≈ 1e-9·(all ones) is numerically singular; the
+    // reference's SVD pseudo-inverse still returns finite coefficients)
+    double amax = 0;
+    for (int e = lane; e < kd * ld; e += 32)
+        if (e % ld < kd) amax = fmax(amax, fabs(A[e]));
+    for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    const double tiny = 1e-30 * amax;
     for (int k = 0; k < kd; k++) {
         // pivot: max |A[i][k]| for i >= k
         double best = -1;
@@ -147,6 +155,10 @@ __device__ void warp_solve(double* A, double* c, int kd) {
             }
         __syncwarp();
         double piv = A[k * ld + k];
+        if (!(fabs(piv) > tiny)) piv = piv < 0 ? -tiny : tiny;
+        __syncwarp();
+        if (lane == 0) A[k * ld + k] = piv;
+        __syncwarp();
         int rows = kd - k - 1, cols = kd - k;  // columns k+1..kd
         for (int e = lane; e < rows * cols; e += 32) {
             int i = k + 1 + e / cols, j = k + 1 + e % cols;

@@ -18,6 +18,7 @@
 // repeated runs are bit-identical.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -45,14 +46,16 @@ static const int RED_THREADS = 256;
 // ---------------------------------------------------------------- kernels --
 
 __global__ void k_g1(Lat L, int ns, const double* __restrict__ x, const int* __restrict__ seg_it,
-                     const double* __restrict__ gmask, double* __restrict__ G1) {
+                     const double* __restrict__ gmask, double* __restrict__ G1, float* __restrict__ G1f) {
     int M = L.M;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < M; s += gridDim.x * blockDim.x) {
         int src = nmdev::bc_source(L, s);
         for (int i = 0; i < ns; i++) {
             int it = seg_it[i];
             double u = it >= 0 ? x[(size_t)it * M + src] : 0.0;
-            G1[(size_t)i * M + s] = exp(-u) * gmask[(size_t)i * M + s];
+            double v = exp(-u) * gmask[(size_t)i * M + s];
+            G1[(size_t)i * M + s] = v;
+            if (G1f) G1f[(size_t)i * M + s] = (float)v;  // FP32 propagators (3-D path)
         }
     }
 }
@@ -280,17 +283,22 @@ __global__ void k_residual(Lat L, ResArgs a, const double* __restrict__ x, const
 }
 
 // x_new = x - δ·g ; xR[k] = x_new ; x_x0[k] = x_new - x ; partial Σ g² (or max|g|)
+// x ← x − δ·g into history slot k, and the partial norms of g.  update = 0:
+// the norms only, x untouched (checks an FP32 residual before x moves).
 __global__ void k_diis_step(int n, double dmax, double* __restrict__ x, const double* __restrict__ g,
                             double* __restrict__ xR, double* __restrict__ xx0,
-                            double* __restrict__ partial, int max_norm) {
+                            double* __restrict__ partial, int max_norm, int update = 1) {
     __shared__ double sh[32];
     double acc = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        double xo = x[i], gv = g[i];
-        double xn = xo + (-dmax) * gv;
-        x[i] = xn;
-        if (xR) xR[i] = xn;
-        if (xx0) xx0[i] = xn - xo;
+        double gv = g[i];
+        if (update) {
+            double xo = x[i];
+            double xn = xo + (-dmax) * gv;
+            x[i] = xn;
+            if (xR) xR[i] = xn;
+            if (xx0) xx0[i] = xn - xo;
+        }
         if (max_norm) acc = fmax(acc, fabs(gv));
         else acc += gv * gv;
     }
@@ -363,7 +371,7 @@ __global__ void k_diis_solve(const double* __restrict__ partial, int nb, int kd_
             if (v != v) { *status = NM_ERR_NAN_DIIS; return; }
             A[i * kd + j] = v;
         }
-    nm_small_solve(A, c, kd);
+    nm_pinv_solve(A, c, kd);
     double normC = 0;
     for (int i = 0; i < kd; i++) normC += c[i];
     for (int i = 0; i < kd; i++) {
@@ -548,18 +556,50 @@ int Ctx::molecule_pass(int m) {
     return NM_OK;
 }
 
-int Ctx::residual(const double* x, double* g) {
+// All launches of one residual evaluation, on `stream` (captured into a graph
+// by residual() on the 3-D path).
+int Ctx::residual_launches(const double* x, double* g) {
     int M = plan->M;
-    k_g1<<<grid_for(M), 256, 0, stream>>>(lat, plan->n_seg, x, d_seg_it, d_gmask, d_G1);
+    k_g1<<<grid_for(M), 256, 0, stream>>>(lat, plan->n_seg, x, d_seg_it, d_gmask, d_G1, phase32 ? d_G1f : nullptr);
     launches++;
     for (int m = 0; m < plan->n_mol; m++) {
-        int rc = molecule_pass(m);
+        int rc = use3d ? ctx3d_molecule_pass(*this, m, phase32) : molecule_pass(m);
         if (rc) return rc;
     }
     k_norms<<<1, 32, 0, stream>>>(norm_args, d_sc, d_seg_phibulk, d_status);
     k_phi<<<grid_for(M), 256, 0, stream>>>(lat, phi_args, d_sc, d_G1, d_phi_frozen, d_seg_frozen, d_phi, d_phitot, d_mol_phitot);
     k_residual<<<grid_for(M), 256, 0, stream>>>(lat, res_args, x, d_phi, d_phitot, d_seg_phibulk, d_ksam, g, d_alpha, d_phi_side);
     launches += 3;
+    return NM_OK;
+}
+
+// One residual evaluation.  The 3-D path issues about two launches per chain
+// segment with nothing returning to the host, so its launches are captured
+// into a CUDA graph once per (x, g, precision) and replayed after that.
+int Ctx::residual(const double* x, double* g) {
+    if (!use3d) {
+        int rc = residual_launches(x, g);
+        if (!rc) have_state = true;
+        return rc;
+    }
+    if (!graph || graph_x != x || graph_g != g || graph_32 != phase32) {
+        if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; }
+        long long l0 = launches;
+        CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        int rc = residual_launches(x, g);
+        cudaGraph_t gr = nullptr;
+        cudaError_t e = cudaStreamEndCapture(stream, &gr);
+        if (rc) { if (gr) cudaGraphDestroy(gr); return rc; }
+        CK(e);
+        e = cudaGraphInstantiate(&graph, gr, 0);
+        cudaGraphDestroy(gr);
+        CK(e);
+        graph_x = x; graph_g = g; graph_32 = phase32;
+        graph_launches = launches - l0;
+        launches = l0;
+    }
+    CK(cudaGraphLaunch(graph, stream));
+    launches += graph_launches;
     have_state = true;
     return NM_OK;
 }
@@ -581,8 +621,30 @@ int Ctx::solve(double* x, nm_solve_result* res, int max_iter) {
     int nb = red_blocks;
     int it = 0, k_diis = 0;
     double resid = 0;
+    phase32 = fp32;
+    double best = 1e300;
+    int since_best = 0;
+    // One residual evaluation.  In the FP32 phase its norm and status are
+    // checked before x moves: a failure of the reduced precision (G(N) <= 0,
+    // a non-finite residual) hands over to FP64 at the same x.
+    auto eval = [&]() -> int {
+        int r = residual(x, d_g);
+        if (r || !phase32) return r;
+        k_diis_step<<<nb, RED_THREADS, 0, stream>>>(nvar, 0.0, x, d_g, nullptr, nullptr, d_partial, plan->max_norm, 0);
+        k_final_norm<<<1, RED_THREADS, 0, stream>>>(d_partial, nb, d_resid, plan->max_norm);
+        launches += 2;
+        double r32 = 0;
+        CK(cudaMemcpyAsync(&r32, d_resid, sizeof(double), cudaMemcpyDeviceToHost, stream));
+        int st = check_status();
+        if (st || !std::isfinite(r32)) {
+            phase32 = false;
+            k_diis = 0;
+            r = residual(x, d_g);
+        }
+        return r;
+    };
     // initial residual and simple mixing step into slot 0
-    int rc = residual(x, d_g);
+    int rc = eval();
     if (rc) return rc;
     k_diis_step<<<nb, RED_THREADS, 0, stream>>>(nvar, dmax, x, d_g, d_xR, d_xx0, d_partial, plan->max_norm);
     k_final_norm<<<1, RED_THREADS, 0, stream>>>(d_partial, nb, d_resid, plan->max_norm);
@@ -592,7 +654,7 @@ int Ctx::solve(double* x, nm_solve_result* res, int max_iter) {
     if (rc) { res->iterations = 0; res->residual = resid; res->status = rc; return rc; }
     while (resid > tol && it < max_iter) {
         it++;
-        rc = residual(x, d_g);
+        rc = eval();
         if (rc) return rc;
         int k = it % m;
         k_diis++;
@@ -607,8 +669,24 @@ int Ctx::solve(double* x, nm_solve_result* res, int max_iter) {
         launches += 5;
         CK(cudaMemcpyAsync(&resid, d_resid, sizeof(double), cudaMemcpyDeviceToHost, stream));
         rc = check_status();
+        if (phase32) {
+            // FP32 propagators until a stall near their accuracy floor (or an
+            // FP32 failure); then FP64 residuals, DIIS history restarted, so
+            // the stopping test is made on an FP64 residual
+            if (resid < 0.9 * best) { best = resid; since_best = 0; } else since_best++;
+            bool fail = rc != 0 || !std::isfinite(resid);
+            if (fail || resid <= tol || resid < sw_floor || (since_best > 10 && resid < 10.0 * sw_floor) ||
+                (since_best > 25 && resid < 1e-2 * std::sqrt((double)nvar))) {
+                phase32 = false;
+                rc = 0;
+                k_diis = 0;
+                resid = 1e300;  // re-evaluated in FP64 by the next iteration
+                continue;
+            }
+        }
         if (rc) break;
     }
+    phase32 = fp32;
     res->iterations = it;
     res->residual = resid;
     res->status = rc ? rc : (resid > tol ? NM_ERR_NOT_CONVERGED : NM_OK);
@@ -700,6 +778,22 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
     else { CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking)); own_stream = true; }
     int M = p->M, ns = p->n_seg;
     lat = make_lat(p);
+    {
+        std::string why;
+        use3d = ctx3d_eligible(p, &why);
+        fp32 = opt && opt->precision == NM_FP32;
+        if (fp32 && !use3d) {
+            set_error("FP32 propagators in a device context: " + why +
+                      " (1-gradient problems take the batched solver, nm_batch_*)");
+            return NM_ERR_INPUT;
+        }
+        if (use3d) l3 = make_l3(p);
+        phase32 = fp32;  // residual calls outside a solve use the context's precision
+        // FP32 accuracy floor of ‖g‖₂: ~1e-7 per chain segment per entry
+        double n = 1;
+        for (int m = 0; m < p->n_mol; m++) n = std::max(n, p->mols[m].chainlength);
+        sw_floor = (1e-7 * n + 1e-6) * std::sqrt((double)p->iv);
+    }
     interior = p->gradients == 1 ? p->MX : (p->gradients == 2 ? p->MX * p->MY : p->MX * p->MY * p->MZ);
     red_blocks = 2 * 152;
     // constants
@@ -742,6 +836,21 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
     TRY(dalloc(&d_partial, (size_t)red_blocks));
     TRY(dalloc(&d_resid, 4));
     mols.resize(p->n_mol);
+    int max_store = 1;
+    for (int m = 0; m < p->n_mol; m++) max_store = std::max(max_store, p->mols[m].n_store);
+    if (use3d) {
+        TRY(dalloc(&d_maxbits, 2 * 32 * (size_t)max_store));  // 32 slots per stored vector
+        TRY(dalloc(&d_E, 2 * (size_t)max_store));
+    }
+    if (fp32) {
+        TRY(dalloc(&d_G1f, (size_t)ns * M));
+        TRY(dalloc(&d_gb32, 2 * (size_t)M));
+        for (int m = 0; m < p->n_mol; m++) {
+            const nm_molecule& mol = p->mols[m];
+            TRY(dalloc(&mols[m].Gf32, (size_t)mol.n_store * M));
+            TRY(dalloc(&mols[m].rho32, 2 * (size_t)mol.n_molmon * M));
+        }
+    }
     for (int m = 0; m < p->n_mol; m++) {
         const nm_molecule& mol = p->mols[m];
         TRY(dalloc(&mols[m].Gf, (size_t)mol.n_store * M));
@@ -794,7 +903,16 @@ Ctx::~Ctx() {
     if (d_seg_it) cudaFree(d_seg_it);
     if (d_seg_frozen) cudaFree(d_seg_frozen);
     if (d_status) cudaFree(d_status);
-    for (auto& D : mols) { cudaFree(D.Gf); cudaFree(D.rho); cudaFree(D.Pc); cudaFree(D.Q); }
+    for (auto& D : mols) {
+        cudaFree(D.Gf); cudaFree(D.rho); cudaFree(D.Pc); cudaFree(D.Q);
+        if (D.Gf32) cudaFree(D.Gf32);
+        if (D.rho32) cudaFree(D.rho32);
+    }
+    if (d_G1f) cudaFree(d_G1f);
+    if (d_gb32) cudaFree(d_gb32);
+    if (d_maxbits) cudaFree(d_maxbits);
+    if (d_E) cudaFree(d_E);
+    if (graph) cudaGraphExecDestroy(graph);
     if (own_stream && stream) cudaStreamDestroy(stream);
 }
 

@@ -1,0 +1,288 @@
+// 3-D simple-cubic propagator steps for the generic context (config-2 class
+// problems: 3-gradient planar lattices, linear chains), FP64 or FP32.
+//
+// One step is G_out(x,y,z) = G1·(Σ of the six neighbours)/6
+// (LGrad3::propagate, LGrad3.cpp:673-744, simple-cubic stencil), with the
+// halo coordinates mapped to the layers set_bounds copies (mirror, periodic)
+// or to the wall slot that holds 0 ('surface').  The grid is (z-chunk,
+// y-chunk, x): a block runs 128 consecutive z of C3_RY consecutive y rows,
+// so no site index is ever divided, every warp load is 32 consecutive z,
+// and the y±1 rows of a block's later rows come from L1.
+//
+// FP32 (block floating point per vector): every stored vector carries one
+// power-of-two exponent E, G_true = G·2^E.  Each step kernel publishes the
+// maximum of its output with atomicMax into 32 slots (block id mod 32, so
+// same-address atomics do not serialise); the next step reduces the 32
+// slots with one warp read, rescales by 2^-expo(max) and records
+// E_out = E_in + e.  Nothing returns to the host between steps, so the whole
+// residual is captured in a CUDA graph.  A melt's propagators span a few
+// binary orders across the box, well inside FP32; the stretched 1-D brushes
+// that need per-thread exponents go to the batched solver instead.
+//
+// Backward steps fuse the composition, ρ += d·Gf·Gb, accumulated in FP32
+// with Kahan compensation (rho_hi, rho_lo) relative to 2^E(root) and
+// converted once per residual to the FP64 ρ the normalisation reads.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ctx_internal.h"
+
+namespace nm {
+
+#define C3_SLOTS 32  // maximum slots per stored vector
+#define C3_RY 8      // rows along y per block
+
+// exact 2^e for e <= 127 (0 below 2^-149), selects only
+__device__ __forceinline__ float c3_p2f(int e) {
+    const int bits = e >= -126 ? (e + 127) << 23 : (e >= -149 ? 1 << max(e + 149, 0) : 0);
+    return __int_as_float(bits);
+}
+__device__ __forceinline__ int c3_expo(float v) {  // frexp exponent of v > 0, 0 for v <= 0
+    const int e = ((__float_as_int(v) >> 23) & 0xff) - 126;
+    return v > 0.f ? e : 0;
+}
+
+__device__ __forceinline__ int c3_map(int c, int n, int b1, int bm) {
+    return c == 0 ? b1 : (c == n + 1 ? bm : c);
+}
+
+// Step modes: 0 forward step, 1 forward start (copy G1), 2 backward start
+// (copy G1 + composition), 3 backward step (+ composition).
+template <typename T, int MODE>
+__global__ void __launch_bounds__(128) k3_prop(L3 L, const T* __restrict__ in, const T* __restrict__ G1,
+                                               T* __restrict__ out, unsigned* __restrict__ maxbits,
+                                               int* __restrict__ E, int sin, int sout,
+                                               const T* __restrict__ Gf, int sgf, int sroot,
+                                               T* __restrict__ rhi, T* __restrict__ rlo, T d) {
+    constexpr bool FP32 = sizeof(T) == 4;
+    const int z = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int x = blockIdx.z + 1;
+    int e = 0;
+    T f = (T)(1.0 / 6.0);
+    if (FP32 && (MODE == 0 || MODE == 3)) {
+        unsigned mb = maxbits[sin * C3_SLOTS + (threadIdx.x & 31)];
+        for (int o = 16; o > 0; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+        e = c3_expo(__uint_as_float(mb));
+        f = (T)c3_p2f(-e) * (T)(1.0 / 6.0);
+    }
+    const int Eout = FP32 ? ((MODE == 1 || MODE == 2) ? 0 : E[sin] + e) : 0;
+    float vmax = 0.f;
+    for (int yy = 0; yy < C3_RY; yy++) {
+        const int y = blockIdx.y * C3_RY + yy + 1;
+        if (y > L.MY) break;
+        T v = 0;
+        if (z <= L.MZ) {
+            const int s = x * L.JX + y * L.JY + z;
+            if (MODE == 1 || MODE == 2) {
+                v = G1[s];
+            } else {
+                const int xm = c3_map(x - 1, L.MX, L.b1x, L.bmx), xp = c3_map(x + 1, L.MX, L.b1x, L.bmx);
+                const int ym = c3_map(y - 1, L.MY, L.b1y, L.bmy), yp = c3_map(y + 1, L.MY, L.b1y, L.bmy);
+                const int zm = c3_map(z - 1, L.MZ, L.b1z, L.bmz), zp = c3_map(z + 1, L.MZ, L.b1z, L.bmz);
+                const int yz = y * L.JY + z, xz = x * L.JX + z, xy = x * L.JX + y * L.JY;
+                // summation order of LGrad3::propagate's simple-cubic branch: x pair, y pair, z pair
+                T s6 = ((in[xm * L.JX + yz] + in[xp * L.JX + yz]) + (in[xz + ym * L.JY] + in[xz + yp * L.JY])) +
+                       (in[xy + zm] + in[xy + zp]);
+                v = FP32 ? s6 * f * G1[s] : s6 * (T)(1.0 / 6.0) * G1[s];
+            }
+            out[s] = v;
+            if (MODE >= 2) {
+                if (FP32) {
+                    // ρ relative to 2^E(root): Gf·Gb·d·2^(Ef + Eout - Eroot), the
+                    // scale applied half to each factor
+                    const int Es = E[sgf] + Eout - E[sroot], h = Es >> 1;
+                    const float sa = c3_p2f(min(h, 127)), sb = c3_p2f(min(Es - h, 127));
+                    const float yv = ((float)Gf[s] * sa) * ((float)v * sb * (float)d) - (float)rlo[s];
+                    const float t2 = (float)rhi[s] + yv;
+                    rlo[s] = (T)((t2 - (float)rhi[s]) - yv);
+                    rhi[s] = (T)t2;
+                } else {
+                    rhi[s] += d == (T)1 ? Gf[s] * v : d * Gf[s] * v;
+                }
+            }
+        }
+        vmax = fmaxf(vmax, (float)v);
+    }
+    if (FP32) {
+        // block maximum of the output -> one of its 32 slots
+        float m = vmax;
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        __shared__ float wm[4];
+        if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int i = 1; i < (int)(blockDim.x >> 5); i++) m = fmaxf(m, wm[i]);
+            const int b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+            if (m > 0.f) atomicMax(&maxbits[sout * C3_SLOTS + (b & (C3_SLOTS - 1))], __float_as_uint(m));
+            if (b == 0) E[sout] = Eout;
+        }
+    }
+}
+
+// Σ_interior of an FP32 vector (FP64 partial sums), G(N) = Σ·2^E(root), and
+// the true-scale FP64 ρ
+__global__ void k3_wsum32(L3 L, const float* __restrict__ X, double* __restrict__ partial) {
+    __shared__ double sh[8];
+    double acc = 0;
+    const int n = L.MX * L.MY * L.MZ;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int z = i % L.MZ + 1, r = i / L.MZ, y = r % L.MY + 1, x = r / L.MY + 1;
+        acc += (double)X[x * L.JX + y * L.JY + z];
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) r += sh[i];
+        partial[blockIdx.x] = r;
+    }
+}
+__global__ void k3_gn32(const double* __restrict__ partial, int nb, const int* __restrict__ E, int sroot,
+                        double* __restrict__ out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double r = 0;
+        for (int i = 0; i < nb; i++) r += partial[i];  // fixed order
+        *out = ldexp(r, E[sroot]);
+    }
+}
+__global__ void k3_rho64(L3 L, const float* __restrict__ rhi, const float* __restrict__ rlo, const int* __restrict__ E,
+                         int sroot, double* __restrict__ rho) {
+    const double f = ldexp(1.0, E[sroot]);
+    const int n = L.MX * L.MY * L.MZ;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int z = i % L.MZ + 1, r = i / L.MZ, y = r % L.MY + 1, x = r / L.MY + 1;
+        const int s = x * L.JX + y * L.JY + z;
+        rho[s] += ((double)rhi[s] + (double)rlo[s]) * f;
+    }
+}
+
+// ------------------------------------------------------------------ host
+
+L3 make_l3(const nm_plan* p) {
+    auto src = [](int bc, int lo, int n) {  // lattice.cpp:94-196 halo source per axis side
+        if (bc == NM_BC_MIRROR) return lo ? 1 : n;
+        if (bc == NM_BC_PERIODIC) return lo ? n : 1;
+        return lo ? 0 : n + 1;
+    };
+    L3 L;
+    L.MX = p->MX; L.MY = p->MY; L.MZ = p->MZ; L.JX = p->JX; L.JY = p->JY;
+    L.b1x = src(p->bc[0], 1, p->MX); L.bmx = src(p->bc[3], 0, p->MX);
+    L.b1y = src(p->bc[1], 1, p->MY); L.bmy = src(p->bc[4], 0, p->MY);
+    L.b1z = src(p->bc[2], 1, p->MZ); L.bmz = src(p->bc[5], 0, p->MZ);
+    return L;
+}
+
+bool ctx3d_eligible(const nm_plan* p, std::string* why) {
+    auto no = [&](const char* w) { if (why) *why = w; return false; };
+    if (p->gradients != 3) return no("3-gradient lattices only");
+    if (p->lattice_type != NM_SIMPLE_CUBIC) return no("simple-cubic lattices only");
+    if (p->geometry != NM_PLANAR) return no("planar geometry only");
+    for (int m = 0; m < p->n_mol; m++) {
+        const nm_molecule& mol = p->mols[m];
+        for (int b = 0; b < mol.n_blocks; b++) {
+            const nm_block& B = mol.blocks[b];
+            if (B.n_child > 1 || (B.n_child == 1 && mol.blocks[mol.child_index[B.child0]].mult != 1))
+                return no("linear chains only");
+        }
+    }
+    return true;
+}
+
+template <typename T, int MODE>
+static void k3(Ctx& C, const T* in, const T* G1, T* out, int sin, int sout, const T* Gf, int sgf, int sroot, T* rhi,
+               T* rlo, double d) {
+    const nm_plan* p = C.plan;
+    dim3 grid((p->MZ + 127) / 128, (p->MY + C3_RY - 1) / C3_RY, p->MX);
+    k3_prop<T, MODE><<<grid, 128, 0, C.stream>>>(C.l3, in, G1, out, C.d_maxbits, C.d_E, sin, sout, Gf, sgf, sroot, rhi,
+                                                 rlo, (T)d);
+    C.launches++;
+}
+
+// One molecule: forward sweep storing every Gf(s), G(N), backward sweep fused
+// with the composition.  Slots: forward s -> s, backward s -> n_store + s.
+template <typename T>
+static int pass3d(Ctx& C, int m) {
+    const nm_plan* p = C.plan;
+    const nm_molecule& mol = p->mols[m];
+    MolDev& D = C.mols[m];
+    const size_t M = p->M;
+    const int ns = mol.n_store;
+    const bool f32 = sizeof(T) == 4;
+    T* Gf = f32 ? (T*)D.Gf32 : (T*)D.Gf;
+    const T* G1 = f32 ? (const T*)C.d_G1f : (const T*)C.d_G1;
+    T* gb = f32 ? (T*)C.d_gb32 : (T*)C.d_gb;
+    T* rhi = f32 ? (T*)D.rho32 : (T*)D.rho;
+    T* rlo = f32 ? (T*)D.rho32 + (size_t)mol.n_molmon * M : nullptr;
+    if (f32) {
+        cudaMemsetAsync(C.d_maxbits, 0, sizeof(unsigned) * 2 * ns * C3_SLOTS, C.stream);
+        cudaMemsetAsync(D.rho32, 0, sizeof(float) * 2 * M * mol.n_molmon, C.stream);
+    } else {
+        cudaMemsetAsync(D.rho, 0, sizeof(double) * M * mol.n_molmon, C.stream);
+    }
+    for (int b = 0; b < mol.n_blocks; b++) {
+        const nm_block& B = mol.blocks[b];
+        const T* g1 = G1 + (size_t)B.seg * M;
+        if (B.n_child == 0) {
+            k3<T, 1>(C, nullptr, g1, Gf + (size_t)B.s0 * M, 0, B.s0, nullptr, 0, 0, nullptr, nullptr, 1.0);
+        } else {
+            const nm_block& C0 = mol.blocks[mol.child_index[B.child0]];
+            const int sl = C0.s0 + C0.length - 1;
+            k3<T, 0>(C, Gf + (size_t)sl * M, g1, Gf + (size_t)B.s0 * M, sl, B.s0, nullptr, 0, 0, nullptr, nullptr, 1.0);
+        }
+        for (int k = 1; k < B.length; k++) {
+            const int s = B.s0 + k;
+            k3<T, 0>(C, Gf + (size_t)(s - 1) * M, g1, Gf + (size_t)s * M, s - 1, s, nullptr, 0, 0, nullptr, nullptr, 1.0);
+        }
+    }
+    const nm_block& R = mol.blocks[mol.n_blocks - 1];
+    const int sroot = R.s0 + R.length - 1;
+    if (f32) {
+        int nb = C.red_blocks;
+        k3_wsum32<<<nb, 256, 0, C.stream>>>(C.l3, (const float*)Gf + (size_t)sroot * M, C.d_partial);
+        k3_gn32<<<1, 32, 0, C.stream>>>(C.d_partial, nb, C.d_E, sroot, C.d_sc + 5 * m);
+        C.launches += 2;
+    } else {
+        C.wsum((const double*)Gf + (size_t)sroot * M, C.d_sc + 5 * m);
+    }
+    // backward: a linear chain walks its blocks from the root down, the
+    // first segment of each block continuing the previous block's sweep
+    int sprev = -1;
+    for (int b = mol.n_blocks - 1; b >= 0; b--) {
+        const nm_block& B = mol.blocks[b];
+        const T* g1 = G1 + (size_t)B.seg * M;
+        T* rh = rhi + (size_t)B.molmon * M;
+        T* rl = rlo ? rlo + (size_t)B.molmon * M : nullptr;
+        const int top = B.s0 + B.length - 1;
+        for (int s = top; s >= B.s0; s--) {
+            T* o = gb + (size_t)(s & 1) * M;
+            const int so = ns + s;
+            if (sprev < 0)
+                k3<T, 2>(C, nullptr, g1, o, 0, so, Gf + (size_t)s * M, s, sroot, rh, rl, B.degeneracy);
+            else
+                k3<T, 3>(C, gb + (size_t)(sprev & 1) * M, g1, o, ns + sprev, so, Gf + (size_t)s * M, s, sroot, rh, rl,
+                         B.degeneracy);
+            sprev = s;
+        }
+    }
+    if (f32) {
+        cudaMemsetAsync(D.rho, 0, sizeof(double) * M * mol.n_molmon, C.stream);
+        for (int k = 0; k < mol.n_molmon; k++) {
+            k3_rho64<<<4 * 152, 256, 0, C.stream>>>(C.l3, (const float*)rhi + (size_t)k * M,
+                                                    (const float*)rlo + (size_t)k * M, C.d_E, sroot,
+                                                    D.rho + (size_t)k * M);
+            C.launches++;
+        }
+    }
+    return NM_OK;
+}
+
+int ctx3d_molecule_pass(Ctx& C, int m, bool fp32) {
+    return fp32 ? pass3d<float>(C, m) : pass3d<double>(C, m);
+}
+
+}  // namespace nm

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <string>
 #include <vector>
 
 #include "../../include/namics_gb300.h"
@@ -15,38 +16,59 @@
 
 namespace nm {
 
-// Solve A c = 1 (A: n×n row-major, n ≤ NM_MAX_DIIS) by Gaussian elimination
-// with partial pivoting in FP64.  The reference solves the same system with an
-// unregularised SVD pseudo-inverse (SFNewton::Ax, sfnewton.cpp:793-835); for a
-// non-singular A both give the exact solution up to rounding.
-__host__ __device__ inline void nm_small_solve(const double* Ain, double* c, int n) {
-    double A[NM_MAX_DIIS * NM_MAX_DIIS];
-    double b[NM_MAX_DIIS];
-    for (int i = 0; i < n * n; i++) A[i] = Ain[i];
-    for (int i = 0; i < n; i++) b[i] = 1.0;
-    if (n == 1) { c[0] = 1.0; return; }  // Ax: N == 1 -> X[0] = 1
-    for (int k = 0; k < n; k++) {
-        int p = k;
-        double best = A[k * n + k] < 0 ? -A[k * n + k] : A[k * n + k];
-        for (int i = k + 1; i < n; i++) {
-            double v = A[i * n + k] < 0 ? -A[i * n + k] : A[i * n + k];
-            if (v > best) { best = v; p = i; }
-        }
-        if (p != k) {
-            for (int j = 0; j < n; j++) { double t = A[k * n + j]; A[k * n + j] = A[p * n + j]; A[p * n + j] = t; }
-            double t = b[k]; b[k] = b[p]; b[p] = t;
-        }
-        double piv = A[k * n + k];
-        for (int i = k + 1; i < n; i++) {
-            double f = A[i * n + k] / piv;
-            for (int j = k; j < n; j++) A[i * n + j] -= f * A[k * n + j];
-            b[i] -= f * b[k];
-        }
+// Solve A c = 1 for symmetric A (n×n row-major, n ≤ NM_MAX_DIIS) by the
+// pseudo-inverse c = Q·diag(1/λ)·Qᵀ·1 from a cyclic Jacobi eigenvalue
+// decomposition, FP64.  This is the solve the reference makes with its SVD
+// (SFNewton::Ax, sfnewton.cpp:793-835): near convergence A ≈ 1e-9·(all
+// ones) is numerically singular, and the pseudo-inverse stays finite there
+// because the eigenvectors of the rounding-noise eigenvalues are nearly
+// orthogonal to the ones vector, where an elimination can divide by a zero
+// pivot.
+__host__ __device__ inline void nm_pinv_solve(const double* Ain, double* c, int n) {
+    if (n == 1) { c[0] = 1.0; return; }
+    double a[NM_MAX_DIIS * NM_MAX_DIIS], q[NM_MAX_DIIS * NM_MAX_DIIS];
+    for (int i = 0; i < n * n; i++) a[i] = Ain[i];
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) q[i * n + j] = i == j ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 60; sweep++) {
+        double off = 0, dg = 0;
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) {
+                const double v = a[i * n + j] * a[i * n + j];
+                if (i == j) dg += v; else off += v;
+            }
+        if (off == 0 || off <= 1e-30 * dg) break;
+        for (int p = 0; p < n - 1; p++)
+            for (int r = p + 1; r < n; r++) {
+                const double apr = a[p * n + r];
+                if (apr == 0) continue;
+                // rotation that zeroes a[p][r]: tan of the angle, smaller root
+                const double th = (a[r * n + r] - a[p * n + p]) / (2 * apr);
+                const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1));
+                const double cs = 1 / sqrt(t * t + 1), sn = t * cs;
+                for (int k = 0; k < n; k++) {  // columns p, r
+                    const double u = a[k * n + p], v = a[k * n + r];
+                    a[k * n + p] = cs * u - sn * v;
+                    a[k * n + r] = sn * u + cs * v;
+                }
+                for (int k = 0; k < n; k++) {  // rows p, r
+                    const double u = a[p * n + k], v = a[r * n + k];
+                    a[p * n + k] = cs * u - sn * v;
+                    a[r * n + k] = sn * u + cs * v;
+                }
+                for (int k = 0; k < n; k++) {  // eigenvectors
+                    const double u = q[k * n + p], v = q[k * n + r];
+                    q[k * n + p] = cs * u - sn * v;
+                    q[k * n + r] = sn * u + cs * v;
+                }
+            }
     }
-    for (int i = n - 1; i >= 0; i--) {
-        double v = b[i];
-        for (int j = i + 1; j < n; j++) v -= A[i * n + j] * c[j];
-        c[i] = v / A[i * n + i];
+    for (int i = 0; i < n; i++) c[i] = 0;
+    for (int j = 0; j < n; j++) {
+        double proj = 0;  // (Qᵀ·1)_j
+        for (int k = 0; k < n; k++) proj += q[k * n + j];
+        const double w = proj / a[j * n + j];
+        for (int i = 0; i < n; i++) c[i] += q[i * n + j] * w;
     }
 }
 
@@ -71,12 +93,24 @@ struct ResArgs {
 
 struct MolDev {
     double* Gf = nullptr;   // forward propagators [n_store*M]
+    float* Gf32 = nullptr;  // FP32 forward propagators [n_store*M] (3-D FP32 path)
+    float* rho32 = nullptr; // FP32 composition, Kahan sum and compensation [2*n_molmon*M]
     double* rho = nullptr;  // Σ d·Gf·Gb per molecule segment type [n_molmon*M]
     double* Pc = nullptr;   // P(G_end)·KSAM of each child block [n_blocks*M]
     double* Q = nullptr;    // backward start of each child block [n_blocks*M]
 };
 
 nmdev::Lat make_lat(const nm_plan* p);
+
+// 3-D lattice for the dedicated simple-cubic kernels (ctx3d.cu)
+struct L3 {
+    int MX, MY, MZ, JX, JY;
+    int b1x, bmx, b1y, bmy, b1z, bmz;  // halo source layer per axis side
+};
+struct Ctx;
+L3 make_l3(const nm_plan* p);
+bool ctx3d_eligible(const nm_plan* p, std::string* why);
+int ctx3d_molecule_pass(Ctx& C, int m, bool fp32);
 
 struct Ctx {
     const nm_plan* plan = nullptr;
@@ -97,6 +131,21 @@ struct Ctx {
     double *d_xR = nullptr, *d_xx0 = nullptr, *d_g = nullptr, *d_x = nullptr, *d_Aij = nullptr,
            *d_Ci = nullptr, *d_gram_partial = nullptr;
     std::vector<MolDev> mols;
+    // 3-D simple-cubic path (ctx3d.cu) and its FP32 propagators
+    bool use3d = false;       // dedicated 3-D kernels for every molecule
+    bool fp32 = false;        // context created with NM_FP32 propagators
+    bool phase32 = false;     // the current residual uses FP32 propagators
+    double sw_floor = 0;      // FP32 accuracy floor of ‖g‖ (switch to FP64 near it)
+    L3 l3{};
+    float *d_G1f = nullptr, *d_gb32 = nullptr;
+    unsigned* d_maxbits = nullptr;  // per stored vector: 32 slots with bits of its maximum
+    int* d_E = nullptr;             // per stored vector: power-of-two exponent
+    // the residual's launches captured once per (x, g, precision) and replayed
+    cudaGraphExec_t graph = nullptr;
+    const double* graph_x = nullptr;
+    double* graph_g = nullptr;
+    bool graph_32 = false;
+    long long graph_launches = 0;
     NormArgs norm_args;
     PhiArgs phi_args;
     ResArgs res_args;
@@ -107,6 +156,7 @@ struct Ctx {
     int wsum(const double* X, double* out_dev);
     int molecule_pass(int m);
     int residual(const double* x, double* g);
+    int residual_launches(const double* x, double* g);
     int check_status();
     int solve(double* x, nm_solve_result* res, int max_iter);
     int free_energy(double* F, double* Omega, double* mu);

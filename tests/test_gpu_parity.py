@@ -295,3 +295,59 @@ def test_batched_residual_fp32_stretched_stars():
         _, go = Oracle(p).residual(x[lo:hi])
         assert np.max(np.abs(a64[lo:hi] - go)) < 1e-10, pick[i]
         assert np.linalg.norm(a32[lo:hi] - go) < _fp32_floor(p), (pick[i], np.linalg.norm(a32[lo:hi] - go))
+
+
+def _solve_tight(text: str, tol: str = "1e-10", itlim: int = 3000) -> str:
+    import re
+    text = re.sub(r"newton : isaac : tolerance : \S+", f"newton : isaac : tolerance : {tol}", text)
+    return re.sub(r"newton : isaac : iterationlimit : \S+", f"newton : isaac : iterationlimit : {itlim}", text)
+
+
+def test_context_fp32_3d_matches_oracle():
+    """3-D simple-cubic melt with FP32 propagators (one power-of-two exponent
+    per stored vector, FP64 normalisation, residual and DIIS, FP64 finish)
+    against the FP64 oracle, both solved to ‖g‖ < 1e-10: φ to 1e-6 and F to
+    1e-7 relative (the FP32 tolerances of the hot-path contract).  The FP64
+    context on the same dedicated 3-D kernels is held to 1e-8 / 1e-9."""
+    run = load_golden("melt3d")["runs"]["it0"]
+    plan = Plan(_solve_tight(run["input"]))
+    x0 = np.array(run["x"])
+    orc = Oracle(plan)
+    rc, xo, _, ro = orc.solve(x0.copy())
+    assert rc == 0 and ro < 1e-10
+    Fo, Oo, _ = orc.free_energy()
+    phio = orc.field(0).reshape(plan.n_seg, -1)
+    for prec in (NM_FP32, NM_FP64):
+        ctx = Context(plan, prec)
+        res, phi = ctx.solve_host(x0.copy())
+        assert res.status == 0 and res.residual < 1e-10, (prec, res)
+        F, O, _ = ctx.free_energy()
+        tol_phi, tol_F = (1e-6, 1e-7) if prec == NM_FP32 else (1e-8, 1e-9)
+        assert abs(F - Fo) <= tol_F * max(1, abs(Fo)), (prec, F, Fo)
+        phi = phi.reshape(plan.n_seg, -1)
+        for i in range(plan.n_seg):
+            assert rel_err(interior(plan, phi[i]), interior(plan, phio[i])) < tol_phi, (prec, i)
+
+
+def test_context_fp32_residual_3d_close_to_oracle():
+    """One FP32-propagator residual of the 3-D melt at its seeded start field;
+    the second call replays the captured graph and must give the same g."""
+    run = load_golden("melt3d")["runs"]["it0"]
+    plan = Plan(run["input"])
+    x = np.array(run["x"])
+    _, go = Oracle(plan).residual(x)
+    ctx = Context(plan, NM_FP32)
+    xd, gd = dev(x), torch.zeros(plan.iv, dtype=torch.float64, device="cuda")
+    ctx.residual_dev(xd.data_ptr(), gd.data_ptr())
+    g1 = host(gd).copy()
+    ctx.residual_dev(xd.data_ptr(), gd.data_ptr())
+    g = host(gd)
+    assert np.array_equal(g, g1)
+    assert np.linalg.norm(g - go) < 1e-5 * max(1.0, np.linalg.norm(go)), np.linalg.norm(g - go)
+
+
+def test_context_fp32_rejects_unsupported_plan():
+    from namics_gb300 import NamicsError
+    run = load_golden("brush1d_cfg1")["runs"]["conv"]
+    with pytest.raises(NamicsError):
+        Context(Plan(run["input"]), NM_FP32)
