@@ -12,7 +12,7 @@
 // and per DIIS iteration (sfnewton.cpp:1078-1095, 837-880):
 //   k_diis_step   x -= δ·g, history slot, ‖g‖² partials
 //   k_gram        Gram row of the history (deterministic two-pass sums)
-//   k_diis_solve  small solve A c = 1, c /= Σc  (one thread, FP64)
+//   host          small solve A c = 1 by pseudo-inverse, c /= Σc (FP64)
 //   k_diis_mix    x = Σ c_i xR_i
 // All arithmetic is FP64; all reductions are two-pass with a fixed grid, so
 // repeated runs are bit-identical.
@@ -349,10 +349,11 @@ __global__ void k_gram(int n, const double* __restrict__ xx0, int k, int kd, int
     if (threadIdx.x == 0) partial[(size_t)i * gridDim.x + blockIdx.x] = r;
 }
 
-// one thread: finish the Gram row, slide the window, solve, normalise
-__global__ void k_diis_solve(const double* __restrict__ partial, int nb, int kd_in, int m,
-                             double* __restrict__ Aij, double* __restrict__ Ci, int* __restrict__ status) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// Finish the Gram row from its per-block partial sums (fixed order), slide
+// the m×m window, set row/column kd-1 to ⟨Δx_i, Δx_k⟩ + 1e-9, solve A c = 1
+// by the pseudo-inverse and normalise c /= Σc (SFNewton::DIIS and Ax,
+// sfnewton.cpp:837-880, 793-835).  Host side; Aij is the m×m window.
+static int diis_coefficients(const double* partial, int nb, int kd_in, int m, double* Aij, double* Ci) {
     int kd = kd_in;
     if (kd > m) {
         kd = m;
@@ -368,7 +369,7 @@ __global__ void k_diis_solve(const double* __restrict__ partial, int nb, int kd_
     for (int i = 0; i < kd; i++)
         for (int j = 0; j < kd; j++) {
             double v = Aij[j + m * i];
-            if (v != v) { *status = NM_ERR_NAN_DIIS; return; }
+            if (v != v) { set_error("NaN in the DIIS matrix"); return NM_ERR_NAN_DIIS; }
             A[i * kd + j] = v;
         }
     nm_pinv_solve(A, c, kd);
@@ -376,8 +377,9 @@ __global__ void k_diis_solve(const double* __restrict__ partial, int nb, int kd_
     for (int i = 0; i < kd; i++) normC += c[i];
     for (int i = 0; i < kd; i++) {
         Ci[i] = c[i] / normC;
-        if (Ci[i] != Ci[i]) *status = NM_ERR_NAN_SVD;
+        if (Ci[i] != Ci[i]) { set_error("NaN in the DIIS coefficients"); return NM_ERR_NAN_SVD; }
     }
+    return NM_OK;
 }
 
 __global__ void k_diis_mix(int n, double* __restrict__ x, const double* __restrict__ xR,
@@ -624,6 +626,7 @@ int Ctx::solve(double* x, nm_solve_result* res, int max_iter) {
     phase32 = fp32;
     double best = 1e300;
     int since_best = 0;
+    std::vector<double> Ah((size_t)m * m, 0.0), ci(m), gpart((size_t)m * nb);
     // One residual evaluation.  In the FP32 phase its norm and status are
     // checked before x moves: a failure of the reduced precision (G(N) <= 0,
     // a non-finite residual) hands over to FP64 at the same x.
@@ -664,11 +667,19 @@ int Ctx::solve(double* x, nm_solve_result* res, int max_iter) {
         int kd = k_diis > m ? m : k_diis;
         dim3 gg(nb, kd);
         k_gram<<<gg, RED_THREADS, 0, stream>>>(nvar, d_xx0, k, kd, m, d_gram_partial);
-        k_diis_solve<<<1, 1, 0, stream>>>(d_gram_partial, nb, k_diis, m, d_Aij, d_Ci, d_status);
-        k_diis_mix<<<grid_for(nvar), 256, 0, stream>>>(nvar, x, d_xR, d_Ci, k, k_diis, m);
-        launches += 5;
+        launches += 3;
+        // one synchronisation per iteration: ‖g‖, the status and the Gram row
+        // partials come back; the m×m solve runs on the host (SFNewton::DIIS,
+        // sfnewton.cpp:837-880) and the coefficients go back for the mix
         CK(cudaMemcpyAsync(&resid, d_resid, sizeof(double), cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(gpart.data(), d_gram_partial, sizeof(double) * kd * nb, cudaMemcpyDeviceToHost, stream));
         rc = check_status();
+        if (!rc) rc = diis_coefficients(gpart.data(), nb, k_diis, m, Ah.data(), ci.data());
+        if (!rc) {
+            CK(cudaMemcpyAsync(d_Ci, ci.data(), sizeof(double) * kd, cudaMemcpyHostToDevice, stream));
+            k_diis_mix<<<grid_for(nvar), 256, 0, stream>>>(nvar, x, d_xR, d_Ci, k, k_diis, m);
+            launches++;
+        }
         if (phase32) {
             // FP32 propagators until a stall near their accuracy floor (or an
             // FP32 failure); then FP64 residuals, DIIS history restarted, so
@@ -864,7 +875,6 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
     TRY(dalloc(&d_xx0, (size_t)mm * p->iv));
     TRY(dalloc(&d_g, (size_t)p->iv));
     TRY(dalloc(&d_x, (size_t)p->iv));
-    TRY(dalloc(&d_Aij, (size_t)mm * mm));
     TRY(dalloc(&d_Ci, (size_t)mm));
     TRY(dalloc(&d_gram_partial, (size_t)mm * red_blocks));
     // kernel argument blocks
@@ -898,7 +908,7 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
 Ctx::~Ctx() {
     double* ptrs[] = {d_L, d_lm1, d_l0, d_l1, d_ksam, d_gmask, d_phi_frozen, d_G1, d_phi, d_phi_side,
                       d_phitot, d_alpha, d_mol_phitot, d_gb, d_tmpF, d_tmpGP, d_sc, d_seg_phibulk,
-                      d_partial, d_resid, d_xR, d_xx0, d_g, d_x, d_Aij, d_Ci, d_gram_partial};
+                      d_partial, d_resid, d_xR, d_xx0, d_g, d_x, d_Ci, d_gram_partial};
     for (double* q : ptrs) if (q) cudaFree(q);
     if (d_seg_it) cudaFree(d_seg_it);
     if (d_seg_frozen) cudaFree(d_seg_frozen);

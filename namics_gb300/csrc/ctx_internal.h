@@ -128,7 +128,7 @@ struct Ctx {
            *d_alpha = nullptr, *d_mol_phitot = nullptr, *d_gb = nullptr, *d_tmpF = nullptr,
            *d_tmpGP = nullptr, *d_sc = nullptr, *d_seg_phibulk = nullptr, *d_partial = nullptr,
            *d_resid = nullptr;
-    double *d_xR = nullptr, *d_xx0 = nullptr, *d_g = nullptr, *d_x = nullptr, *d_Aij = nullptr,
+    double *d_xR = nullptr, *d_xx0 = nullptr, *d_g = nullptr, *d_x = nullptr,
            *d_Ci = nullptr, *d_gram_partial = nullptr;
     std::vector<MolDev> mols;
     // 3-D simple-cubic path (ctx3d.cu) and its FP32 propagators
