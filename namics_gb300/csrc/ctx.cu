@@ -53,9 +53,15 @@ __global__ void k_g1(Lat L, int ns, const double* __restrict__ x, const int* __r
         for (int i = 0; i < ns; i++) {
             int it = seg_it[i];
             double u = it >= 0 ? x[(size_t)it * M + src] : 0.0;
-            double v = exp(-u) * gmask[(size_t)i * M + s];
-            G1[(size_t)i * M + s] = v;
-            if (G1f) G1f[(size_t)i * M + s] = (float)v;  // FP32 propagators (3-D path)
+            if (G1f) {
+                // FP32 phase: one FP32 exp serves both copies (the FP64 copy,
+                // used by φ = ρ/G1, then matches the propagators' G1 exactly)
+                float v = expf(-(float)u) * (float)gmask[(size_t)i * M + s];
+                G1f[(size_t)i * M + s] = v;
+                G1[(size_t)i * M + s] = (double)v;
+            } else {
+                G1[(size_t)i * M + s] = exp(-u) * gmask[(size_t)i * M + s];
+            }
         }
     }
 }
@@ -655,7 +661,7 @@ int Ctx::solve(double* x, nm_solve_result* res, int max_iter) {
     CK(cudaMemcpyAsync(&resid, d_resid, sizeof(double), cudaMemcpyDeviceToHost, stream));
     rc = check_status();
     if (rc) { res->iterations = 0; res->residual = resid; res->status = rc; return rc; }
-    while (resid > tol && it < max_iter) {
+    while (!(resid <= tol) && it < max_iter) {  // a NaN residual never counts as converged
         it++;
         rc = eval();
         if (rc) return rc;
@@ -695,6 +701,7 @@ int Ctx::solve(double* x, nm_solve_result* res, int max_iter) {
                 continue;
             }
         }
+        if (!rc && !std::isfinite(resid)) { set_error("non-finite residual"); rc = NM_ERR_NAN_DIIS; }
         if (rc) break;
     }
     phase32 = fp32;

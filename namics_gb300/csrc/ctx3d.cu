@@ -71,11 +71,11 @@ __global__ void __launch_bounds__(128) k3_prop(L3 L, const T* __restrict__ in, c
     }
     const int Eout = FP32 ? ((MODE == 1 || MODE == 2) ? 0 : E[sin] + e) : 0;
     float vmax = 0.f;
+#pragma unroll
     for (int yy = 0; yy < C3_RY; yy++) {
         const int y = blockIdx.y * C3_RY + yy + 1;
-        if (y > L.MY) break;
         T v = 0;
-        if (z <= L.MZ) {
+        if (z <= L.MZ && y <= L.MY) {
             const int s = x * L.JX + y * L.JY + z;
             if (MODE == 1 || MODE == 2) {
                 v = G1[s];

