@@ -307,6 +307,100 @@ def run_melt3d(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def ads2d_text(n: int = 100, N: int = 200) -> str:
+    """Config 5, 25% of requests: 2-D planar n×n adsorption of (A)N from a
+    bulk at phi_b = 1e-3 onto a surface with chi_AS = -1, monomeric solvent."""
+    return "\n".join([
+        "lat : flat : gradients : 2", f"lat : flat : n_layers_x : {n}", f"lat : flat : n_layers_y : {n}",
+        "lat : flat : geometry : planar", "lat : flat : lattice_type : simple_cubic",
+        "lat : flat : lowerbound_x : surface", "lat : flat : upperbound_x : mirror",
+        "lat : flat : lowerbound_y : mirror", "lat : flat : upperbound_y : mirror",
+        "mon : S : freedom : frozen", "mon : S : frozen_range : lowerbound",
+        "mon : A : freedom : free", "mon : W : freedom : free", "mon : A : chi_S : -1",
+        f"mol : pol : composition : (A){N}", "mol : pol : freedom : free", "mol : pol : phibulk : 1e-3",
+        "mol : water : composition : (W)1", "mol : water : freedom : solvent",
+        "newton : isaac : method : DIIS", "newton : isaac : tolerance : 1e-7",
+        "newton : isaac : iterationlimit : 1000", "newton : isaac : deltamax : 0.1", "newton : isaac : m : 10",
+    ]) + "\n"
+
+
+def melt3d_small_text(n: int = 64, a: int = 20, chi: float = 0.4) -> str:
+    """Config 5, 5% of requests: n³ periodic (A)a(B)a melt at chi_AB."""
+    return melt3d_text(n, 1000).replace("chi_B : 0.3", f"chi_B : {chi}").replace(
+        "(A)50(B)50", f"(A){a}(B){a}")
+
+
+def run_served(args) -> None:
+    """Config 5: a Poisson request stream served on one GPU by nm_server
+    (continuous batching: 1-gradient requests waiting together share one
+    batched launch, others get a device context each; W workers with one
+    stream each; admission by device footprint).  Mix: 70% config-4 brushes,
+    25% 2-D 100×100 (A)200 adsorption, 5% 3-D 64³ (A)20(B)20 melts at
+    chi 0.4, all from seeded fields.  Reported: converged solves/s over the
+    span from the first submit to the last completion, p50/p99 of the
+    submit-to-completion time, for FP32 propagators and for plain FP64."""
+    import torch  # noqa: F401  (device initialisation)
+    from namics_gb300 import build as b
+    b.build_product()
+    from namics_gb300 import NM_FP32, NM_FP64, Plan, Server
+    rng = np.random.default_rng(SEED + 7)
+    n_req = args.requests
+    brush_texts = workload(max(1, int(0.7 * n_req) + 8))
+    kinds = rng.choice(3, size=n_req, p=[0.70, 0.25, 0.05])
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, size=n_req))
+    ads, melt = Plan(ads2d_text()), Plan(melt3d_small_text())
+    reqs, bi = [], 0
+    for k in kinds:
+        if k == 0:
+            p = Plan(brush_texts[bi]); bi += 1
+            x = rng.uniform(*FIELD, size=p.iv)
+        elif k == 1:
+            p = ads
+            x = rng.uniform(-0.01, 0.01, size=p.iv)
+        else:
+            p = melt
+            u = rng.uniform(-0.1, 0.1, size=p.M)
+            x = np.concatenate([u, -u])
+        reqs.append((int(k), p, x))
+    out = {}
+    for prec, name in ((NM_FP32, "fp32"), (NM_FP64, "fp64")):
+        srv = Server(precision=prec, workers=args.workers, max_batch=64, memory_budget=64 << 30)
+        t0 = time.perf_counter()
+        ids = []
+        for (k, p, x), ta in zip(reqs, arrivals):
+            now = time.perf_counter() - t0
+            if ta > now:
+                time.sleep(ta - now)
+            ids.append((k, srv.submit(p, x)))
+        lat, ok, by_kind = [], 0, {0: [], 1: [], 2: []}
+        for k, rid in ids:
+            res, _, sec = srv.wait(rid)
+            lat.append(sec)
+            by_kind[k].append(sec)
+            ok += res.status == 0
+        span = time.perf_counter() - t0
+        launches = srv.launch_count()
+        srv.close()
+        lat = np.array(lat) * 1e3
+        out[name] = {"value": ok / span, "unit": "solves/s", "converged": int(ok), "requests": n_req,
+                     "span_s": span, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                     "p50_ms_by_kind": {kn: (float(np.percentile(np.array(v) * 1e3, 50)) if v else None)
+                                        for kn, v in zip(("brush1d", "ads2d", "melt3d"), by_kind.values())},
+                     "gpu_launches": launches}
+    f32 = out["fp32"]
+    line = {
+        "metric": METRIC, "value": f32["value"], "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 0,
+        "ms_per_step": f32["span_s"] * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded request stream)",
+        "config": {"workload": f"config 5: Poisson stream, {args.rate:g} requests/s, {n_req} requests; 70% "
+                               "config-4 brushes, 25% 2-D 100x100 (A)200 adsorption, 5% 3-D 64^3 (A)20(B)20 melts",
+                   "workers": args.workers, "max_batch": 64, "memory_budget_gb": 64},
+        "latency": {"p50_ms": f32["p50_ms"], "p99_ms": f32["p99_ms"], "what": "submit to completion"},
+        "fp32": f32, "fp64_gpu": out["fp64"],
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -316,8 +410,12 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU comparison")
-    ap.add_argument("--workload", default="brush1d", choices=["brush1d", "melt3d"],
-                    help="brush1d: config 4, the headline; melt3d: config 2 (DIIS iterations/s)")
+    ap.add_argument("--workload", default="brush1d", choices=["brush1d", "melt3d", "served"],
+                    help="brush1d: config 4, the headline; melt3d: config 2 (DIIS iterations/s); "
+                         "served: config 5 (request stream)")
+    ap.add_argument("--rate", type=float, default=20.0, help="served: arrivals per second")
+    ap.add_argument("--requests", type=int, default=200, help="served: requests in the stream")
+    ap.add_argument("--workers", type=int, default=8, help="served: concurrent solves")
     ap.add_argument("--iters", type=int, default=20, help="melt3d: DIIS iterations per step")
     ap.add_argument("--n3d", type=int, default=128, help="melt3d: box edge")
     ap.add_argument("--instances", type=int, default=N_INSTANCES)
@@ -327,6 +425,9 @@ def main():
         return
     if args.workload == "melt3d":
         run_melt3d(args)
+        return
+    if args.workload == "served":
+        run_served(args)
         return
     ws, rank, local = dist_env()
     import torch

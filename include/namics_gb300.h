@@ -239,6 +239,39 @@ int nm_batch_times(nm_batch* b, double* seconds);
 int nm_batch_free_energy(nm_batch* b, double* F, double* Omega);
 long long nm_batch_launch_count(nm_batch* b);
 
+/* ---- request server (continuous batching on one GPU) ----------------------
+ * No single counterpart in the reference (it runs one Solve at a time): a
+ * stream of independent solves of any gradient count, served while others
+ * run.  `workers` threads, one CUDA stream each, take requests from one
+ * FIFO queue; 1-gradient requests waiting together are solved in one
+ * batched launch (up to max_batch), others one per device context.  Work is
+ * admitted by estimated device footprint against memory_budget bytes.
+ * precision: NM_FP32 or NM_FP64 propagators (FP32 where the solver for the
+ * request supports it, FP64 otherwise). */
+typedef struct nm_server nm_server;
+typedef struct nm_server_options {
+    int    precision;        /* enum nm_precision                            */
+    int    device;           /* CUDA device ordinal                          */
+    int    workers;          /* concurrent solves (streams)                  */
+    int    max_batch;        /* most 1-gradient requests per batched launch  */
+    size_t memory_budget;    /* device bytes admitted requests may hold      */
+} nm_server_options;
+int nm_server_create(const nm_server_options* opt, nm_server** out);
+/* Queue one solve from the field x_host (plan->iv values, copied).  The plan
+ * must stay alive until the request has been waited for.  NM_ERR_NOMEM if
+ * the request alone exceeds the memory budget. */
+int nm_server_submit(nm_server* srv, const nm_plan* plan, const double* x_host,
+                     long long* request_id);
+/* Block until the request is done: the solved field (may be NULL), the solve
+ * result and the seconds from submit to completion.  Returns the request's
+ * status (a solve that hit its iteration limit returns NM_OK with
+ * res->status = NM_ERR_NOT_CONVERGED). */
+int nm_server_wait(nm_server* srv, long long request_id, double* x_host,
+                   nm_solve_result* res, double* seconds);
+long long nm_server_launch_count(nm_server* srv);
+/* Finishes every queued request, then stops the workers. */
+int nm_server_destroy(nm_server* srv);
+
 /* ---- allocation-free single-problem solve --------------------------------
  * No counterpart in the reference.  For callers that must not allocate
  * device memory when they solve (a fixed memory budget carved up front, a

@@ -16,7 +16,7 @@ import numpy as np
 from . import _abi
 from ._abi import NM_FP32, NM_FP64  # noqa: F401
 
-__all__ = ["Plan", "Context", "Batch", "NamicsError", "load_library", "NM_FP32", "NM_FP64"]
+__all__ = ["Plan", "Context", "Batch", "Server", "NamicsError", "load_library", "NM_FP32", "NM_FP64"]
 
 
 class NamicsError(RuntimeError):
@@ -268,3 +268,47 @@ class Batch:
 
     def launch_count(self) -> int:
         return int(_abi.load().nm_batch_launch_count(self._h))
+
+
+class Server:
+    """Continuous-batching request server on one GPU (nm_server_*)."""
+
+    def __init__(self, precision: int = NM_FP32, workers: int = 4, max_batch: int = 64,
+                 memory_budget: int = 64 << 30, device: int = 0):
+        lib = _abi.load()
+        opt = _abi.nm_server_options(precision, device, workers, max_batch, memory_budget)
+        h = C.c_void_p()
+        _check(lib.nm_server_create(C.byref(opt), C.byref(h)))
+        self._h = h
+        self._plans = {}
+
+    def submit(self, plan: Plan, x: np.ndarray) -> int:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        rid = C.c_longlong()
+        _check(_abi.load().nm_server_submit(self._h, plan.ptr, _dptr(x), C.byref(rid)))
+        self._plans[rid.value] = plan  # kept alive until waited for
+        return rid.value
+
+    def wait(self, rid: int):
+        plan = self._plans[rid]
+        x = np.empty(plan.iv)
+        r = _abi.nm_solve_result()
+        sec = C.c_double()
+        rc = _abi.load().nm_server_wait(self._h, rid, _dptr(x), C.byref(r), C.byref(sec))
+        del self._plans[rid]
+        _check(rc)
+        return SolveResult(r.iterations, r.residual, r.status), x, sec.value
+
+    def launch_count(self) -> int:
+        return int(_abi.load().nm_server_launch_count(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _abi.load().nm_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

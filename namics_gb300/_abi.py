@@ -65,6 +65,11 @@ class nm_solve_result(C.Structure):
 
 P_plan = C.POINTER(nm_plan)
 
+
+class nm_server_options(C.Structure):
+    _fields_ = [("precision", C.c_int), ("device", C.c_int), ("workers", C.c_int),
+                ("max_batch", C.c_int), ("memory_budget", C.c_size_t)]
+
 # (name, restype, argtypes) for every entry point declared in the header
 SIGNATURES = [
     ("nm_plan_create", C.c_int, [C.c_char_p, C.POINTER(P_plan)]),
@@ -92,6 +97,11 @@ SIGNATURES = [
     ("nm_batch_times", C.c_int, [C.c_void_p, dp]),
     ("nm_batch_free_energy", C.c_int, [C.c_void_p, dp, dp]),
     ("nm_batch_launch_count", C.c_longlong, [C.c_void_p]),
+    ("nm_server_create", C.c_int, [C.POINTER(nm_server_options), C.POINTER(C.c_void_p)]),
+    ("nm_server_submit", C.c_int, [C.c_void_p, P_plan, dp, C.POINTER(C.c_longlong)]),
+    ("nm_server_wait", C.c_int, [C.c_void_p, C.c_longlong, dp, C.POINTER(nm_solve_result), C.POINTER(C.c_double)]),
+    ("nm_server_launch_count", C.c_longlong, [C.c_void_p]),
+    ("nm_server_destroy", C.c_int, [C.c_void_p]),
     ("nm_solve1d_noalloc", C.c_int, [P_plan, C.c_void_p, C.c_int, C.c_void_p, C.POINTER(nm_solve_result)]),
 ]
 

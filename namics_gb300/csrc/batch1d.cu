@@ -20,6 +20,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -832,25 +833,28 @@ struct Batch {
     bool own_stream = false;
     long long launches = 0;
 
+    // stream-ordered device memory (see nm_pool_setup): no device-wide
+    // synchronisation when a batch is created or destroyed
     template <typename X>
     int alloc(X** p, size_t n) {
         if (n == 0) n = 1;
-        cudaError_t e = cudaMalloc((void**)p, sizeof(X) * n);
-        if (e != cudaSuccess) { set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e)); return NM_ERR_NOMEM; }
+        cudaError_t e = cudaMallocAsync((void**)p, sizeof(X) * n, stream);
+        if (e != cudaSuccess) { set_error(std::string("cudaMallocAsync: ") + cudaGetErrorString(e)); return NM_ERR_NOMEM; }
         allocs.push_back((void*)*p);
-        cudaMemset(*p, 0, sizeof(X) * n);
+        cudaMemsetAsync(*p, 0, sizeof(X) * n, stream);
         return NM_OK;
     }
     template <typename X>
     int upload(X** p, const X* h, size_t n) {
         int rc = alloc(p, n);
         if (rc) return rc;
-        cudaError_t e = cudaMemcpy(*p, h, sizeof(X) * n, cudaMemcpyHostToDevice);
+        // pageable source: staged before the call returns, so h may go away
+        cudaError_t e = cudaMemcpyAsync(*p, h, sizeof(X) * n, cudaMemcpyHostToDevice, stream);
         if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
         return NM_OK;
     }
     ~Batch() {
-        for (void* p : allocs) cudaFree(p);
+        for (void* p : allocs) cudaFreeAsync(p, stream);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
 };
@@ -862,6 +866,7 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
     int dev = opt ? opt->device : 0;
     cudaError_t e = cudaSetDevice(dev);
     if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
+    nm_pool_setup(dev);
     if (opt && opt->stream) B.stream = (cudaStream_t)opt->stream;
     else { cudaStreamCreateWithFlags(&B.stream, cudaStreamNonBlocking); B.own_stream = true; }
     long long off = 0;
@@ -956,8 +961,18 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
     TRYB(B.alloc(&B.d_probs, (size_t)n));
     B.smem = maxsmem;
     if (maxsmem > 220 * 1024) { set_error("problem too large for the batched solver's shared memory"); return NM_ERR_INPUT; }
-    cudaError_t e1 = cudaFuncSetAttribute(k_batch1d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxsmem);
-    if (e1 != cudaSuccess) { set_error("cudaFuncSetAttribute failed"); return NM_ERR_CUDA; }
+    // the kernel's dynamic shared-memory limit only ever rises, so batches
+    // created on other threads cannot lower it under a running launch
+    static std::mutex smem_mu;
+    static size_t smem_set[64] = {};
+    {
+        std::lock_guard<std::mutex> lk(smem_mu);
+        if (dev >= 0 && dev < 64 && maxsmem > smem_set[dev]) {
+            cudaError_t e1 = cudaFuncSetAttribute(k_batch1d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxsmem);
+            if (e1 != cudaSuccess) { set_error("cudaFuncSetAttribute failed"); return NM_ERR_CUDA; }
+            smem_set[dev] = maxsmem;
+        }
+    }
     return NM_OK;
 }
 

@@ -581,15 +581,10 @@ int Ctx::residual_launches(const double* x, double* g) {
     return NM_OK;
 }
 
-// One residual evaluation.  The 3-D path issues about two launches per chain
-// segment with nothing returning to the host, so its launches are captured
-// into a CUDA graph once per (x, g, precision) and replayed after that.
+// One residual evaluation.  It issues about two launches per chain segment
+// with nothing returning to the host, so its launches are captured into a
+// CUDA graph once per (x, g, precision) and replayed after that.
 int Ctx::residual(const double* x, double* g) {
-    if (!use3d) {
-        int rc = residual_launches(x, g);
-        if (!rc) have_state = true;
-        return rc;
-    }
     if (!graph || graph_x != x || graph_g != g || graph_32 != phase32) {
         if (graph) { cudaGraphExecDestroy(graph); graph = nullptr; }
         long long l0 = launches;
@@ -771,13 +766,29 @@ int Ctx::free_energy(double* F, double* Omega, double* mu) {
     return NM_OK;
 }
 
+// Device memory of contexts and batches is stream-ordered (cudaMallocAsync /
+// cudaFreeAsync on the object's own stream): creating and destroying them
+// never synchronises the device, so solves on other streams keep running
+// (the request server overlaps many).  Freed memory stays in the device's
+// default pool for the next object instead of going back to the driver.
+void nm_pool_setup(int dev) {
+    static bool done[64] = {};
+    if (dev < 0 || dev >= 64 || done[dev]) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        unsigned long long keep = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    done[dev] = true;
+}
+
 template <typename T>
-static int dalloc(T** p, size_t n) {
+static int dalloc(T** p, size_t n, cudaStream_t st) {
     if (n == 0) n = 1;
-    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * n);
-    if (e != cudaSuccess) { set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e)); return NM_ERR_NOMEM; }
-    e = cudaMemset(*p, 0, sizeof(T) * n);
-    if (e != cudaSuccess) { set_error(std::string("cudaMemset: ") + cudaGetErrorString(e)); return NM_ERR_CUDA; }
+    cudaError_t e = cudaMallocAsync((void**)p, sizeof(T) * n, st);
+    if (e != cudaSuccess) { set_error(std::string("cudaMallocAsync: ") + cudaGetErrorString(e)); return NM_ERR_NOMEM; }
+    e = cudaMemsetAsync(*p, 0, sizeof(T) * n, st);
+    if (e != cudaSuccess) { set_error(std::string("cudaMemsetAsync: ") + cudaGetErrorString(e)); return NM_ERR_CUDA; }
     return NM_OK;
 }
 
@@ -792,6 +803,7 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
     }
     int dev = opt ? opt->device : 0;
     CK(cudaSetDevice(dev));
+    nm_pool_setup(dev);
     if (opt && opt->stream) { stream = (cudaStream_t)opt->stream; own_stream = false; }
     else { CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking)); own_stream = true; }
     int M = p->M, ns = p->n_seg;
@@ -815,75 +827,75 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
     interior = p->gradients == 1 ? p->MX : (p->gradients == 2 ? p->MX * p->MY : p->MX * p->MY * p->MZ);
     red_blocks = 2 * 152;
     // constants
-    TRY(dalloc(&d_L, M));
-    CK(cudaMemcpy(d_L, p->L, sizeof(double) * M, cudaMemcpyHostToDevice));
+    TRY(dalloc(&d_L, M, stream));
+    CK(cudaMemcpyAsync(d_L, p->L, sizeof(double) * M, cudaMemcpyHostToDevice, stream));
     if (p->lambda_1) {
-        TRY(dalloc(&d_lm1, M)); TRY(dalloc(&d_l0, M)); TRY(dalloc(&d_l1, M));
-        CK(cudaMemcpy(d_lm1, p->lambda_1, sizeof(double) * M, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d_l0, p->lambda0, sizeof(double) * M, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(d_l1, p->lambda1, sizeof(double) * M, cudaMemcpyHostToDevice));
+        TRY(dalloc(&d_lm1, M, stream)); TRY(dalloc(&d_l0, M, stream)); TRY(dalloc(&d_l1, M, stream));
+        CK(cudaMemcpyAsync(d_lm1, p->lambda_1, sizeof(double) * M, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(d_l0, p->lambda0, sizeof(double) * M, cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(d_l1, p->lambda1, sizeof(double) * M, cudaMemcpyHostToDevice, stream));
         lat.lm1 = d_lm1; lat.l0 = d_l0; lat.l1 = d_l1;
     }
     std::vector<double> ks(M);
     for (int s = 0; s < M; s++) ks[s] = p->ksam[s];
-    TRY(dalloc(&d_ksam, M));
-    CK(cudaMemcpy(d_ksam, ks.data(), sizeof(double) * M, cudaMemcpyHostToDevice));
-    TRY(dalloc(&d_gmask, (size_t)ns * M));
-    CK(cudaMemcpy(d_gmask, p->seg_gmask, sizeof(double) * ns * M, cudaMemcpyHostToDevice));
-    TRY(dalloc(&d_phi_frozen, (size_t)ns * M));
-    CK(cudaMemcpy(d_phi_frozen, p->seg_phi_frozen, sizeof(double) * ns * M, cudaMemcpyHostToDevice));
-    TRY(dalloc(&d_seg_it, ns));
-    CK(cudaMemcpy(d_seg_it, p->seg_it, sizeof(int) * ns, cudaMemcpyHostToDevice));
+    TRY(dalloc(&d_ksam, M, stream));
+    CK(cudaMemcpyAsync(d_ksam, ks.data(), sizeof(double) * M, cudaMemcpyHostToDevice, stream));
+    TRY(dalloc(&d_gmask, (size_t)ns * M, stream));
+    CK(cudaMemcpyAsync(d_gmask, p->seg_gmask, sizeof(double) * ns * M, cudaMemcpyHostToDevice, stream));
+    TRY(dalloc(&d_phi_frozen, (size_t)ns * M, stream));
+    CK(cudaMemcpyAsync(d_phi_frozen, p->seg_phi_frozen, sizeof(double) * ns * M, cudaMemcpyHostToDevice, stream));
+    TRY(dalloc(&d_seg_it, ns, stream));
+    CK(cudaMemcpyAsync(d_seg_it, p->seg_it, sizeof(int) * ns, cudaMemcpyHostToDevice, stream));
     std::vector<int> sf(ns);
     for (int i = 0; i < ns; i++) sf[i] = p->seg_freedom[i] == NM_SEG_FROZEN;
-    TRY(dalloc(&d_seg_frozen, ns));
-    CK(cudaMemcpy(d_seg_frozen, sf.data(), sizeof(int) * ns, cudaMemcpyHostToDevice));
+    TRY(dalloc(&d_seg_frozen, ns, stream));
+    CK(cudaMemcpyAsync(d_seg_frozen, sf.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, stream));
     // state
-    TRY(dalloc(&d_G1, (size_t)ns * M));
-    TRY(dalloc(&d_phi, (size_t)ns * M));
-    TRY(dalloc(&d_phi_side, (size_t)ns * M));
-    TRY(dalloc(&d_phitot, M));
-    TRY(dalloc(&d_alpha, M));
-    TRY(dalloc(&d_mol_phitot, (size_t)p->n_mol * M));
-    TRY(dalloc(&d_gb, 2 * (size_t)M));
-    TRY(dalloc(&d_tmpF, M));
-    TRY(dalloc(&d_tmpGP, M));
-    TRY(dalloc(&d_sc, 5 * (size_t)p->n_mol));
-    TRY(dalloc(&d_seg_phibulk, ns));
-    TRY(dalloc(&d_status, 1));
-    TRY(dalloc(&d_partial, (size_t)red_blocks));
-    TRY(dalloc(&d_resid, 4));
+    TRY(dalloc(&d_G1, (size_t)ns * M, stream));
+    TRY(dalloc(&d_phi, (size_t)ns * M, stream));
+    TRY(dalloc(&d_phi_side, (size_t)ns * M, stream));
+    TRY(dalloc(&d_phitot, M, stream));
+    TRY(dalloc(&d_alpha, M, stream));
+    TRY(dalloc(&d_mol_phitot, (size_t)p->n_mol * M, stream));
+    TRY(dalloc(&d_gb, 2 * (size_t)M, stream));
+    TRY(dalloc(&d_tmpF, M, stream));
+    TRY(dalloc(&d_tmpGP, M, stream));
+    TRY(dalloc(&d_sc, 5 * (size_t)p->n_mol, stream));
+    TRY(dalloc(&d_seg_phibulk, ns, stream));
+    TRY(dalloc(&d_status, 1, stream));
+    TRY(dalloc(&d_partial, (size_t)red_blocks, stream));
+    TRY(dalloc(&d_resid, 4, stream));
     mols.resize(p->n_mol);
     int max_store = 1;
     for (int m = 0; m < p->n_mol; m++) max_store = std::max(max_store, p->mols[m].n_store);
     if (use3d) {
-        TRY(dalloc(&d_maxbits, 2 * 32 * (size_t)max_store));  // 32 slots per stored vector
-        TRY(dalloc(&d_E, 2 * (size_t)max_store));
+        TRY(dalloc(&d_maxbits, 2 * 32 * (size_t)max_store, stream));  // 32 slots per stored vector
+        TRY(dalloc(&d_E, 2 * (size_t)max_store, stream));
     }
     if (fp32) {
-        TRY(dalloc(&d_G1f, (size_t)ns * M));
-        TRY(dalloc(&d_gb32, 2 * (size_t)M));
+        TRY(dalloc(&d_G1f, (size_t)ns * M, stream));
+        TRY(dalloc(&d_gb32, 2 * (size_t)M, stream));
         for (int m = 0; m < p->n_mol; m++) {
             const nm_molecule& mol = p->mols[m];
-            TRY(dalloc(&mols[m].Gf32, (size_t)mol.n_store * M));
-            TRY(dalloc(&mols[m].rho32, 2 * (size_t)mol.n_molmon * M));
+            TRY(dalloc(&mols[m].Gf32, (size_t)mol.n_store * M, stream));
+            TRY(dalloc(&mols[m].rho32, 2 * (size_t)mol.n_molmon * M, stream));
         }
     }
     for (int m = 0; m < p->n_mol; m++) {
         const nm_molecule& mol = p->mols[m];
-        TRY(dalloc(&mols[m].Gf, (size_t)mol.n_store * M));
-        TRY(dalloc(&mols[m].rho, (size_t)mol.n_molmon * M));
-        TRY(dalloc(&mols[m].Pc, (size_t)mol.n_blocks * M));
-        TRY(dalloc(&mols[m].Q, (size_t)mol.n_blocks * M));
+        TRY(dalloc(&mols[m].Gf, (size_t)mol.n_store * M, stream));
+        TRY(dalloc(&mols[m].rho, (size_t)mol.n_molmon * M, stream));
+        TRY(dalloc(&mols[m].Pc, (size_t)mol.n_blocks * M, stream));
+        TRY(dalloc(&mols[m].Q, (size_t)mol.n_blocks * M, stream));
     }
     // DIIS
     int mm = p->diis_m;
-    TRY(dalloc(&d_xR, (size_t)mm * p->iv));
-    TRY(dalloc(&d_xx0, (size_t)mm * p->iv));
-    TRY(dalloc(&d_g, (size_t)p->iv));
-    TRY(dalloc(&d_x, (size_t)p->iv));
-    TRY(dalloc(&d_Ci, (size_t)mm));
-    TRY(dalloc(&d_gram_partial, (size_t)mm * red_blocks));
+    TRY(dalloc(&d_xR, (size_t)mm * p->iv, stream));
+    TRY(dalloc(&d_xx0, (size_t)mm * p->iv, stream));
+    TRY(dalloc(&d_g, (size_t)p->iv, stream));
+    TRY(dalloc(&d_x, (size_t)p->iv, stream));
+    TRY(dalloc(&d_Ci, (size_t)mm, stream));
+    TRY(dalloc(&d_gram_partial, (size_t)mm * red_blocks, stream));
     // kernel argument blocks
     std::memset(&norm_args, 0, sizeof(norm_args));
     std::memset(&phi_args, 0, sizeof(phi_args));
@@ -908,7 +920,7 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
     res_args.ns = ns; res_args.nit = p->n_it;
     for (int i = 0; i < p->n_it; i++) res_args.it_seg[i] = p->it_seg[i];
     for (int i = 0; i < ns * ns; i++) res_args.chi[i] = p->chi[i];
-    CK(cudaDeviceSynchronize());
+    CK(cudaStreamSynchronize(stream));
     return NM_OK;
 }
 
@@ -916,19 +928,19 @@ Ctx::~Ctx() {
     double* ptrs[] = {d_L, d_lm1, d_l0, d_l1, d_ksam, d_gmask, d_phi_frozen, d_G1, d_phi, d_phi_side,
                       d_phitot, d_alpha, d_mol_phitot, d_gb, d_tmpF, d_tmpGP, d_sc, d_seg_phibulk,
                       d_partial, d_resid, d_xR, d_xx0, d_g, d_x, d_Ci, d_gram_partial};
-    for (double* q : ptrs) if (q) cudaFree(q);
-    if (d_seg_it) cudaFree(d_seg_it);
-    if (d_seg_frozen) cudaFree(d_seg_frozen);
-    if (d_status) cudaFree(d_status);
+    for (double* q : ptrs) if (q) cudaFreeAsync(q, stream);
+    if (d_seg_it) cudaFreeAsync(d_seg_it, stream);
+    if (d_seg_frozen) cudaFreeAsync(d_seg_frozen, stream);
+    if (d_status) cudaFreeAsync(d_status, stream);
     for (auto& D : mols) {
-        cudaFree(D.Gf); cudaFree(D.rho); cudaFree(D.Pc); cudaFree(D.Q);
-        if (D.Gf32) cudaFree(D.Gf32);
-        if (D.rho32) cudaFree(D.rho32);
+        cudaFreeAsync(D.Gf, stream); cudaFreeAsync(D.rho, stream); cudaFreeAsync(D.Pc, stream); cudaFreeAsync(D.Q, stream);
+        if (D.Gf32) cudaFreeAsync(D.Gf32, stream);
+        if (D.rho32) cudaFreeAsync(D.rho32, stream);
     }
-    if (d_G1f) cudaFree(d_G1f);
-    if (d_gb32) cudaFree(d_gb32);
-    if (d_maxbits) cudaFree(d_maxbits);
-    if (d_E) cudaFree(d_E);
+    if (d_G1f) cudaFreeAsync(d_G1f, stream);
+    if (d_gb32) cudaFreeAsync(d_gb32, stream);
+    if (d_maxbits) cudaFreeAsync(d_maxbits, stream);
+    if (d_E) cudaFreeAsync(d_E, stream);
     if (graph) cudaGraphExecDestroy(graph);
     if (own_stream && stream) cudaStreamDestroy(stream);
 }

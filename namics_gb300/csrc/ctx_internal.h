@@ -108,6 +108,7 @@ struct L3 {
     int b1x, bmx, b1y, bmy, b1z, bmz;  // halo source layer per axis side
 };
 struct Ctx;
+void nm_pool_setup(int dev);  // keep freed stream-ordered memory in the device's pool
 L3 make_l3(const nm_plan* p);
 bool ctx3d_eligible(const nm_plan* p, std::string* why);
 int ctx3d_molecule_pass(Ctx& C, int m, bool fp32);

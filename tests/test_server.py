@@ -1,0 +1,76 @@
+"""Request server (nm_server_*): continuous batching of mixed solves.
+
+Each request's result must be the same when it is solved in the mix
+(batched with other 1-gradient requests, overlapping on other streams,
+admitted under a memory budget) as when it is solved alone through the
+existing entry points: bit-identical here, because every reduction on the
+device has a fixed order and a batched problem's CTA does not depend on its
+neighbours.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+from namics_gb300 import NM_FP32, NM_FP64, Batch, Context, Plan, Server  # noqa: E402
+
+
+def _cases():
+    out = []
+    for n in golden_names():
+        runs = load_golden(n)["runs"]
+        run = runs.get("conv") or runs.get("it5")
+        if run is None:
+            continue
+        plan = Plan(run["input"])
+        if plan.c.gradients == 3 and plan.c.lattice_type != 0:
+            continue  # 3-D hexagonal: FP64 generic path, slow to converge; not needed here
+        out.append((n, plan, np.array(run["x"])))
+    return out
+
+
+def _alone(plan, x, precision):
+    if plan.c.gradients == 1:
+        xx = x.copy()
+        its, res, st = Batch([plan], precision).solve_host(xx)
+        return int(its[0]), float(res[0]), int(st[0]), xx
+    # the server uses FP32 propagators in a context only where it has them (3-D)
+    prec = precision if (precision == NM_FP64 or plan.c.gradients == 3) else NM_FP64
+    ctx = Context(plan, prec)
+    xx = x.copy()
+    r, _ = ctx.solve_host(xx)
+    return r.iterations, r.residual, r.status, xx
+
+
+@pytest.mark.parametrize("precision", [NM_FP32, NM_FP64])
+def test_server_results_equal_alone_and_in_the_mix(precision):
+    cases = _cases()
+    kinds = {c[1].c.gradients for c in cases}
+    assert kinds == {1, 2, 3}, kinds
+    # a budget that holds only part of the mix at once, so requests queue
+    srv = Server(precision=precision, workers=4, max_batch=8, memory_budget=256 << 20)
+    ids = [(n, plan, x, srv.submit(plan, x)) for n, plan, x in cases for _ in range(2)]
+    results = [(n, plan, x) + srv.wait(rid) for n, plan, x, rid in ids]
+    assert srv.launch_count() > 0
+    srv.close()
+    for n, plan, x, res, xs, sec in results:
+        its, resid, st, xa = _alone(plan, x, precision)
+        assert res.status == st and res.iterations == its, (n, res, its, st)
+        assert res.residual == resid, n
+        assert np.array_equal(xs, xa), n
+        assert sec > 0
+
+
+def test_server_rejects_request_beyond_budget():
+    from namics_gb300 import NamicsError
+    n, plan, x = _cases()[0]
+    srv = Server(precision=NM_FP64, workers=1, memory_budget=1 << 10)
+    with pytest.raises(NamicsError):
+        srv.submit(plan, x)
+    srv.close()
