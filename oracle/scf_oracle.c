@@ -22,6 +22,7 @@ struct orc_state {
     double **Gf, **rho, **jGb, **Pc, **Qb;
     double *gb;
     double *GN, *norm, *mol_n, *mol_theta, *mol_phibulk, *seg_phibulk;
+    double *psi, *EE, *q, *eps, *X;  /* electrostatics (charged systems) */
     int have_state;
 };
 
@@ -347,18 +348,202 @@ static void mol_backward_block(orc_state* st, int m, int b, double* Q) {
     }
 }
 
+/* ---- electrostatics (charged systems) ------------------------------------
+ * Constants of namics.cpp:44-49; the lattice routines of LG1Planar.cpp:162-200,
+ * LGrad1.cpp:593-680 and 820-833, LG2Planar.cpp:1130-1175, LGrad2.cpp:
+ * 1392-1440 and 1702-1740 (fjc = 1; the fixed-ψ0 branches are not covered). */
+#define ORC_E 1.60217e-19
+#define ORC_KBT (1.38065e-23 * 298.15)
+#define ORC_EPS0 8.85418e-12
+#define ORC_PIE 3.14159265
+
+/* mirror bounds on every side */
+static void set_M_bounds(orc_state* st, double* X) {
+    const nm_plan* P = st->P;
+    int MX = P->MX;
+    if (P->gradients == 1) { X[0] = X[1]; X[MX + 1] = X[MX]; return; }
+    int MY = P->MY, JX = P->JX;
+    for (int x = 1; x < MX + 1; x++) { X[x * JX + 0] = X[x * JX + 1]; X[x * JX + MY + 1] = X[x * JX + MY]; }
+    for (int y = 1; y < MY + 1; y++) { X[0 + y] = X[1 * JX + y]; X[(MX + 1) * JX + y] = X[MX * JX + y]; }
+    X[0] = X[1]; X[MY + 1] = X[MY];
+    X[(MX + 1) * JX + 0] = X[(MX + 1) * JX + 1]; X[(MX + 1) * JX + MY + 1] = X[(MX + 1) * JX + MY];
+}
+
+/* EE: the field-energy density weight of each site (Lattice::UpdateEE) */
+static void update_EE(orc_state* st, double* EE, double* psi) {
+    const nm_plan* P = st->P;
+    int M = st->M, MX = P->MX;
+    double pf = 0.5 * ORC_EPS0 * P->bond_length / ORC_KBT * (ORC_KBT / ORC_E) * (ORC_KBT / ORC_E);
+    const double* L = P->L;
+    set_M_bounds(st, psi);
+    Zero(EE, M);
+    if (P->gradients == 1) {
+        if (P->geometry == NM_PLANAR) {
+            pf = pf / 2.0 * 1 * 1;
+            double Exmin, Explus = psi[0] - psi[1];
+            Explus *= Explus;
+            for (int x = 1; x < MX + 1; x++) {
+                Exmin = Explus;
+                Explus = psi[x] - psi[x + 1];
+                Explus *= Explus;
+                EE[x] = pf * (Exmin + Explus);
+            }
+        } else if (P->geometry == NM_CYLINDRICAL) {
+            int r = (int)(P->offset_first_layer * 1);
+            pf = pf * ORC_PIE;
+            for (int x = 1; x < MX + 1; x++) {
+                r++;
+                double Exmin = psi[x] - psi[x - 1];
+                Exmin *= (r - 1) * Exmin;
+                double Explus = psi[x] - psi[x + 1];
+                Explus *= (r) * Explus;
+                EE[x] = pf * (Exmin + Explus) / L[x];
+            }
+        } else {
+            pf = pf * ORC_PIE * 2 / 1;
+            int r = (int)(P->offset_first_layer * 1 + 1.0);
+            double Exmin, Explus = r * (psi[1] - psi[2]);
+            Explus *= Explus;
+            EE[1] = pf * Explus / (L[1]);
+            for (int x = 2; x < MX + 1; x++) {
+                r += 1.0;
+                Exmin = Explus;
+                Explus = r * (psi[x] - psi[x + 1]);
+                Explus *= Explus;
+                EE[x] = pf * (Exmin + Explus) / L[x];
+            }
+        }
+        return;
+    }
+    int MY = P->MY, JX = P->JX;
+    pf = pf / 2;  /* both 2-D lattices halve pf once */
+    if (P->geometry == NM_PLANAR) {
+        for (int x = 1; x < MX + 1; x++)
+            for (int y = 1; y < MY + 1; y++) {
+                int z = x * JX + y;
+                double Exmin = psi[z] - psi[z - JX]; Exmin *= Exmin;
+                double Explus = psi[z] - psi[z + JX]; Explus *= Explus;
+                double Eymin = psi[z] - psi[z - 1]; Eymin *= Eymin;
+                double Eyplus = psi[z] - psi[z + 1]; Eyplus *= Eyplus;
+                EE[x * JX + y] = pf * (Exmin + Explus + Eymin + Eyplus);
+            }
+        return;
+    }
+    int r = (int)(P->offset_first_layer * 1);
+    for (int x = 1; x < MX + 1; x++) {
+        r++;
+        for (int y = 1; y < MY + 1; y++) {
+            int z = x * JX + y;
+            double Exmin = psi[z] - psi[z - JX];
+            Exmin *= (r - 0.5) * Exmin * 2 * ORC_PIE;
+            double Explus = psi[z] - psi[z + JX];
+            Explus *= (r + 0.5) * Explus * 2 * ORC_PIE;
+            double Eymin = (psi[z] - psi[z - 1]) * 1;
+            Eymin *= Eymin;
+            double Eyplus = (psi[z] - psi[z + 1]) * 1;
+            Eyplus *= Eyplus;
+            EE[z] = pf * ((Exmin + Explus) / L[z] + Eymin + Eyplus);
+        }
+    }
+}
+
+/* g -= X(ψ), X the Poisson update of ψ from the charge density q and the
+ * relative permittivity eps (Lattice::UpdatePsi, not-fixed-ψ0 branch) */
+static void update_psi(orc_state* st, double* g, const double* psi, const double* q, const double* eps) {
+    const nm_plan* P = st->P;
+    int M = st->M, MX = P->MX;
+    const double* L = P->L;
+    double* X = st->X;
+    double C = ORC_E * ORC_E / (ORC_EPS0 * ORC_KBT * P->bond_length);
+    if (P->gradients == 1) {
+        if (P->geometry == NM_PLANAR) {
+            C = C * 2.0 / 1 / 1;
+            double epsXmin, epsXplus = eps[0] + eps[1];
+            for (int x = 1; x < MX + 1; x++) {
+                epsXmin = epsXplus;
+                epsXplus = eps[x] + eps[x + 1];
+                double a = x == 1 ? psi[0] : X[x - 1];  /* upwind */
+                X[x] = (epsXmin * a + C * q[x] + epsXplus * psi[x + 1]) / (epsXmin + epsXplus);
+            }
+        } else if (P->geometry == NM_CYLINDRICAL) {
+            C = C / ORC_PIE;
+            double r = P->offset_first_layer * 1;
+            double epsXmin, epsXplus = r * (eps[0] + eps[1]);
+            for (int x = 1; x < MX + 1; x++) {
+                r++;
+                epsXmin = epsXplus;
+                epsXplus = r * (eps[x] + eps[x + 1]);
+                double a = x == 1 ? psi[0] : X[x - 1];  /* upwind */
+                X[x] = (epsXmin * a + C * q[x] + epsXplus * psi[x + 1]) / (epsXmin + epsXplus);
+            }
+        } else {
+            C = C / (2.0 * ORC_PIE) * 1;
+            double r = P->offset_first_layer * 1;
+            double epsXmin, epsXplus = r * r * (eps[0] + eps[1]);
+            double a = 0, b = psi[0], c = psi[1];
+            for (int x = 1; x < MX + 1; x++) {
+                epsXmin = epsXplus;
+                r++;
+                epsXplus = r * r * (eps[x] + eps[x + 1]);
+                a = b; b = c; c = psi[x + 1];
+                X[x] = (epsXmin * a + C * q[x] * L[x] + epsXplus * c) / (epsXmin + epsXplus);
+            }
+        }
+    } else if (P->geometry == NM_PLANAR) {
+        int MY = P->MY, JX = P->JX;
+        C = C * 2.0 / 1 / 1;
+        for (int x = 1; x < MX + 1; x++)
+            for (int y = 1; y < MY + 1; y++) {
+                int i = x * JX + y;
+                double epsXmin = eps[i] + eps[i - JX], epsXplus = eps[i] + eps[i + JX];
+                double epsYmin = eps[i] + eps[i - 1], epsYplus = eps[i] + eps[i + 1];
+                double ax = x == 1 ? psi[i - JX] : X[i - JX];  /* upwind */
+                double ay = y == 1 ? psi[i - 1] : X[i - 1];
+                X[i] = (C * q[i] + epsXmin * ax + epsXplus * psi[i + JX] + epsYmin * ay + epsYplus * psi[i + 1]) /
+                       (epsXmin + epsXplus + epsYmin + epsYplus);
+            }
+    } else {
+        int MY = P->MY, JX = P->JX;
+        C = C / 2 / 1 / 1;
+        double r = P->offset_first_layer * 1;
+        for (int x = 1; x < MX + 1; x++) {
+            r++;
+            for (int y = 1; y < MY + 1; y++) {
+                int i = x * JX + y;
+                double epsXmin = 2 * ORC_PIE * (r - 1) * (eps[i] + eps[i - JX]) / L[i] * 1 * 1;
+                double epsXplus = 2 * ORC_PIE * r * (eps[i] + eps[i + JX]) / L[i] * 1 * 1;
+                double epsYmin = eps[i] + eps[i - 1], epsYplus = eps[i] + eps[i + 1];
+                X[i] = (C * q[i] + epsXmin * psi[i - JX] + epsXplus * psi[i + JX] + epsYmin * psi[i - 1] +
+                        epsYplus * psi[i + 1]) /
+                       (epsXmin + epsXplus + epsYmin + epsYplus);
+            }
+        }
+    }
+    for (int i = 0; i < M; i++) g[i] = g[i] - X[i];  /* YisAminB */
+}
+
 /* ---- residual ------------------------------------------------------------ */
 static int compute_phis(orc_state* st, const double* x) {
     const nm_plan* P = st->P;
     int M = st->M, ns = P->n_seg;
     /* PutU (system.cpp:1987-2085) + Segment::PrepareForCalculations
      * (segment.cpp:835-879): u = x[it(seg)], set_bounds(u), G1 = exp(-u),
-     * times MASK (pinned) and KSAM. */
+     * times MASK (pinned) and KSAM.  Charged: ψ is the last block of x and
+     * u += -ε·EE + v·ψ (system.cpp:2001-2030). */
+    if (P->charged) {
+        Cp(st->psi, x + (size_t)P->n_it * M, M);
+        update_EE(st, st->EE, st->psi);
+    }
     for (int i = 0; i < ns; i++) {
         double* u = st->u + (size_t)i * M;
         double* G1 = st->G1 + (size_t)i * M;
-        if (P->seg_it[i] >= 0) Cp(u, x + (size_t)P->seg_it[i] * M, M);
-        else Zero(u, M);
+        if (P->seg_it[i] >= 0) {
+            Cp(u, x + (size_t)P->seg_it[i] * M, M);
+            if (P->charged) {
+                YplusisCtimesX(u, st->EE, -1.0 * P->seg_epsilon[i], M);
+                if (P->seg_valence[i] != 0) YplusisCtimesX(u, st->psi, P->seg_valence[i], M);
+            }
+        } else Zero(u, M);
         set_bounds(st, u);
         for (int s = 0; s < M; s++) G1[s] = exp(-u[s]);
         Times(G1, G1, P->seg_gmask + (size_t)i * M, M);
@@ -414,6 +599,21 @@ static int compute_phis(orc_state* st, const double* x) {
             if (norm > 0) Norm(phi, norm, M);
         }
     }
+    if (P->charged && P->neutralizer >= 0) {
+        /* the neutraliser takes the bulk volume fraction that makes the bulk
+         * neutral (system.cpp:2487-2515, 2560-2570) */
+        int nt = P->neutralizer;
+        const nm_molecule* mol = &P->mols[nt];
+        double qs = P->solvent >= 0 ? P->mols[P->solvent].charge : 0;
+        if (mol->charge != qs) st->mol_phibulk[nt] = ((B - 1.0) * qs - A) / (mol->charge - qs);
+        B += st->mol_phibulk[nt];
+        double norm = st->mol_phibulk[nt] / mol->chainlength;
+        st->mol_n[nt] = norm * st->GN[nt];
+        st->mol_theta[nt] = st->mol_n[nt] * mol->chainlength;
+        st->norm[nt] = norm;
+        for (int k = 0; k < mol->n_molmon; k++)
+            if (norm > 0) Norm(st->rho[nt] + (size_t)k * M, norm, M);
+    }
     if (P->solvent >= 0) {
         int sv = P->solvent;
         const nm_molecule* mol = &P->mols[sv];
@@ -446,7 +646,7 @@ static int compute_phis(orc_state* st, const double* x) {
 int orc_residual(orc_state* st, const double* x, double* g) {
     const nm_plan* P = st->P;
     int M = st->M, ns = P->n_seg, nit = P->n_it;
-    if (P->charged) return NM_ERR_INPUT;
+    if (P->charged && P->gradients == 3) return NM_ERR_INPUT;
     /* System::Classical_residual (system.cpp:2087-2189) */
     Cp(g, x, P->iv);
     int rc = compute_phis(st, x);
@@ -475,6 +675,28 @@ int orc_residual(orc_state* st, const double* x, double* g) {
         }
         remove_bounds(st, gi);
         for (int s = 0; s < M; s++) gi[s] *= P->ksam[s];
+    }
+    if (P->charged) {
+        /* the ψ block: DoElectrostatics (system.cpp:1920-1953), then
+         * g = ψ - UpdatePsi(ψ) (system.cpp:2161-2170) */
+        double* gp = g + (size_t)nit * M;
+        Zero(st->q, M);
+        Zero(st->eps, M);
+        for (int i = 0; i < ns; i++) {
+            double* phi = st->phi + (size_t)i * M;
+            YplusisCtimesX(st->q, phi, P->seg_valence[i], M);
+            set_bounds(st, phi);
+            YplusisCtimesX(st->eps, phi, P->seg_epsilon[i], M);
+        }
+        Div(st->q, st->phitot, M);
+        Div(st->eps, st->phitot, M);
+        Cp(st->psi, x + (size_t)nit * M, M);
+        Cp(gp, st->psi, M);
+        set_M_bounds(st, st->psi);
+        set_M_bounds(st, st->psi);
+        st->psi[0] = st->psi[1];
+        update_psi(st, gp, st->psi, st->q, st->eps);
+        remove_bounds(st, gp);
     }
     return NM_OK;
 }
@@ -685,6 +907,12 @@ int orc_free_energy(orc_state* st, double* Fout, double* Omega, double* mu) {
         Add(F, T, M);
     }
     for (int s = 0; s < M; s++) F[s] *= P->ksam[s];
+    if (P->charged) {  /* system.cpp:3020-3028 */
+        Zero(T, M);
+        AddTimes(T, st->q, st->psi, M);
+        Norm(T, 0.5, M);
+        Add(F, T, M);
+    }
     double Fv = weighted_sum(st, F);
     /* grand potential */
     double* GP = F;
@@ -710,7 +938,22 @@ int orc_free_energy(orc_state* st, double* Fout, double* Omega, double* mu) {
         }
     }
     Norm(GP, -1.0, M);
-    for (int s = 0; s < M; s++) GP[s] *= P->ksam[s];
+    if (P->charged) {  /* system.cpp:3225-3238 */
+        Zero(T, M);
+        Times(T, st->EE, st->eps, M);
+        Norm(T, -2.0, M);
+        AddTimes(T, st->q, st->psi, M);
+        Norm(T, -1.0 / 2.0, M);
+        Add(GP, T, M);
+        for (int s = 0; s < M; s++) GP[s] *= P->ksam[s];
+        for (int s = 0; s < M; s++) T[s] = st->q[s] * P->ksam[s];
+        for (int s = 0; s < M; s++) T[s] = st->q[s] - T[s];
+        Times(T, T, st->psi, M);
+        Norm(T, 0.5, M);
+        Add(GP, T, M);
+    } else {
+        for (int s = 0; s < M; s++) GP[s] *= P->ksam[s];
+    }
     double Ov = weighted_sum(st, GP);
     free(F);
     if (Fout) *Fout = Fv;
@@ -775,6 +1018,11 @@ orc_state* orc_create(const nm_plan* P) {
     st->mol_theta = calloc((size_t)nm, sizeof(double));
     st->mol_phibulk = calloc((size_t)nm, sizeof(double));
     st->seg_phibulk = calloc((size_t)ns, sizeof(double));
+    st->psi = calloc((size_t)M, sizeof(double));
+    st->EE = calloc((size_t)M, sizeof(double));
+    st->q = calloc((size_t)M, sizeof(double));
+    st->eps = calloc((size_t)M, sizeof(double));
+    st->X = calloc((size_t)M, sizeof(double));
     return st;
 }
 
@@ -788,5 +1036,6 @@ void orc_destroy(orc_state* st) {
     free(st->alpha); free(st->tmp); free(st->unity); free(st->gb); free(st->mol_phitot);
     free(st->GN); free(st->norm); free(st->mol_n); free(st->mol_theta); free(st->mol_phibulk);
     free(st->seg_phibulk);
+    free(st->psi); free(st->EE); free(st->q); free(st->eps); free(st->X);
     free(st);
 }
