@@ -843,6 +843,9 @@ int orc_get_field(orc_state* st, int which, double* out) {
         case 3: Cp(out, st->phitot, M); return NM_OK;
         case 4: Cp(out, st->mol_phitot, P->n_mol * M); return NM_OK;
         case 5: Cp(out, st->phi_side, P->n_seg * M); return NM_OK;
+        case 6: if (!P->charged) return NM_ERR_ARG; Cp(out, st->psi, M); return NM_OK;
+        case 7: if (!P->charged) return NM_ERR_ARG; Cp(out, st->q, M); return NM_OK;
+        case 8: if (!P->charged) return NM_ERR_ARG; Cp(out, st->eps, M); return NM_OK;
     }
     return NM_ERR_ARG;
 }
@@ -857,7 +860,8 @@ int orc_get_molecule(orc_state* st, int m, double* GN, double* n, double* theta,
 }
 
 /* GetFreeEnergy (system.cpp:2809-3029), GetGrandPotential (:3038-3244),
- * CreateMu (:3246-3400) for uncharged, state-free systems. */
+ * CreateMu (:3246-3400) for state-free systems, with the electrostatic
+ * terms where the system is charged. */
 int orc_free_energy(orc_state* st, double* Fout, double* Omega, double* mu) {
     const nm_plan* P = st->P;
     int M = st->M, ns = P->n_seg;

@@ -140,6 +140,34 @@ def cases() -> list[dict]:
         "mol : pol : composition : (A)12", "mol : pol : freedom : free", "mol : pol : phibulk : 0.1",
         "mol : water : composition : (W)1", "mol : water : freedom : solvent"]
     C.append(dict(name="sol3d_hex", lines=lines, field=(-0.1, 0.1), seed=11, modes=["it0", "it5"]))
+    # charged grafted polyelectrolyte brushes (valence -0.1 on A) with a
+    # neutralising counter-ion (Na) and added salt (Cl at phi_b 0.01), on the
+    # four lattices the electrostatics covers (configuration-3 class, reduced)
+    def charged_lines(comp, n):
+        return ["lat : flat : bondlength : 5e-10",
+                "mon : S : freedom : frozen", "mon : S : frozen_range : lowerbound",
+                "mon : X : freedom : pinned", "mon : X : pinned_range : firstlayer",
+                "mon : A : freedom : free", "mon : A : valence : -0.1",
+                "mon : W : freedom : free",
+                "mon : Na : freedom : free", "mon : Na : valence : 1",
+                "mon : Cl : freedom : free", "mon : Cl : valence : -1",
+                "mon : A : chi_W : 0.5", "mon : X : chi_W : 0.5",
+                f"mol : pol : composition : {comp}", "mol : pol : freedom : restricted", f"mol : pol : n : {n}",
+                "mol : water : composition : (W)1", "mol : water : freedom : solvent",
+                "mol : Na : composition : (Na)1", "mol : Na : freedom : neutralizer",
+                "mol : Cl : composition : (Cl)1", "mol : Cl : freedom : free", "mol : Cl : phibulk : 0.01"]
+    C.append(dict(name="charged1d", lines=lat1d(40) + charged_lines("(X)1(A)39", 0.05),
+                  field=(-0.01, 0.01), seed=20, modes=["it0", "conv"], conv_itlim=5000))
+    C.append(dict(name="charged1d_cyl", lines=lat1d(30, geom="cylindrical", offset=10) +
+                  charged_lines("(X)1(A)29", 3.0), field=(-0.01, 0.01), seed=21, modes=["it0", "conv"],
+                  conv_itlim=5000, split_tol=1e-4))
+    C.append(dict(name="charged2d", lines=lat2d(16, 10, ["surface", "mirror", "mirror", "mirror"]) +
+                  charged_lines("(X)1(A)29", 0.5), field=(-0.01, 0.01), seed=22, modes=["it0", "it5", "conv"],
+                  newton=dict(tol=1e-6), conv_itlim=5000, path_tol=1e-7))
+    C.append(dict(name="charged2d_cyl", lines=lat2d(16, 10, ["surface", "mirror", "mirror", "mirror"],
+                  geom="cylindrical", offset=10) + charged_lines("(X)1(A)29", 10.0),
+                  field=(-0.01, 0.01), seed=23, modes=["it0", "it5", "conv"], newton=dict(tol=1e-6),
+                  conv_itlim=5000, split_tol=1e-2))
     # configuration-4 sample: random 1-gradient brushes (seeded), 10% stars
     rng = np.random.default_rng(2024)
     for i in range(6):
@@ -166,6 +194,8 @@ def outputs_block(plan: Plan) -> list[str]:
     for name in plan.seg_names:
         s.append(f"pro : mon : {name} : G1")
     s.append("pro : sys : noname : alpha")
+    if plan.c.charged:
+        s += ["pro : sys : noname : psi", "pro : sys : noname : q", "pro : sys : noname : eps"]
     s.append("output : kal : append : false")
     s += ["kal : sys : noname : free_energy", "kal : sys : noname : grand_potential",
           "kal : newton : isaac : residual", "kal : newton : isaac : iterations"]
@@ -196,7 +226,7 @@ def write_guess(path: Path, plan: Plan, x: np.ndarray) -> None:
     with open(path, "w") as f:
         f.write("DIIS\n")
         f.write(f" {c.MX}\t{my}\t{mz}\t1\n")
-        f.write("false\n")
+        f.write("true\n" if c.charged else "false\n")
         f.write(f"{len(names)}\n")
         for n in names:
             f.write(n + "\n")
@@ -228,7 +258,7 @@ def run_case(case: dict, mode: str, workdir: Path) -> dict:
     MOLNAMES = [ln.split(":")[1].strip() for ln in body if ln.startswith("mol")]
     MOLNAMES = list(dict.fromkeys(MOLNAMES))
     x = make_field(plan, *case["field"], case["seed"], case.get("antisym", False))
-    itlim = {"it0": 0, "it5": 5, "conv": 1000}[mode]
+    itlim = {"it0": 0, "it5": 5, "conv": case.get("conv_itlim", 1000)}[mode]
     nw["itlim"] = itlim
     text = "\n".join(body + newton(**nw)) + "\n"
     tag = f"{case['name']}_{mode}"
@@ -260,7 +290,8 @@ def main():
         for case in cases():
             if only and case["name"] not in only:
                 continue
-            res = {"name": case["name"], "runs": {}}
+            res = {"name": case["name"], "runs": {}, "split_tol": case.get("split_tol", 1e-5),
+                   "path_tol": case.get("path_tol", 1e-8)}
             for mode in case["modes"]:
                 res["runs"][mode] = run_case(case, mode, wd)
                 k = res["runs"][mode]["kal"]

@@ -23,3 +23,25 @@ def rel_err(a: np.ndarray, b: np.ndarray, floor: float = 1e-300) -> float:
     b = np.asarray(b, dtype=np.float64)
     scale = np.maximum(np.max(np.abs(b)), floor)
     return float(np.max(np.abs(a - b)) / scale)
+
+
+def newton_tolerance(run: dict) -> float:
+    """The `newton : … : tolerance` the run's input text sets (1e-7 if none)."""
+    for ln in run["input"].splitlines():
+        parts = [t.strip() for t in ln.split(":")]
+        if len(parts) == 4 and parts[0] == "newton" and parts[2] == "tolerance":
+            return float(parts[3])
+    return 1e-7
+
+
+def charge_scale(plan, run: dict) -> float:
+    """max over sites of Σ_s |valence_s|·φ_s from the run's .pro columns: the
+    size of the ion densities whose near-cancelling sum is the charge q, so
+    the scale q's error is measured against."""
+    c = plan.c
+    tot = 0.0
+    for i, seg in enumerate(plan.seg_names):
+        v = abs(c.seg_valence[i])
+        if v:
+            tot = tot + v * np.abs(pro_column(run, f"mon_{seg}_phi"))
+    return float(np.max(tot))

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from conftest import golden_names, load_golden
-from helpers import interior, pro_column, rel_err
+from helpers import charge_scale, interior, newton_tolerance, pro_column, rel_err
 
 from namics_gb300 import Plan
 from orc import Oracle
@@ -41,9 +41,15 @@ def test_oracle_matches_reference(name):
         # path is the same (same iteration count); where the small DIIS solve
         # (Jacobi here, SVD in the reference) rounds an ill-conditioned
         # history differently the paths split, and both end within the
-        # convergence ball ‖g‖ < 1e-7 of the same solution.
+        # convergence ball of the same solution.  How far apart two points of
+        # that ball can lie depends on the problem's conditioning: 1e-5 for
+        # most, wider (the fixture's split_tol) for the charged cylindrical
+        # cases, whose potential direction is weakly constrained.
         same_path = mode == "it0" or its == int(k["newton_isaac_iterations"])
-        tol = 1e-12 if mode == "it0" else (1e-8 if same_path else 1e-5)
+        # Along the same path, rounding still drifts over hundreds of
+        # iterations by the fixture's path_tol (1e-8; 1e-7 for the 2-D
+        # charged brush, 883 iterations).
+        tol = 1e-12 if mode == "it0" else (g.get("path_tol", 1e-8) if same_path else g.get("split_tol", 1e-5))
         if mode.startswith("it") and mode != "it0":
             tol = 1e-7  # fixed iteration count on an unstable start
         phi = orc.field(0).reshape(plan.n_seg, plan.M)
@@ -54,6 +60,13 @@ def test_oracle_matches_reference(name):
                 assert rel_err(interior(plan, g1[i]), pro_column(run, f"mon_{seg}_G1")) < tol, (mode, seg)
         alpha = orc.field(2)
         assert rel_err(interior(plan, alpha), pro_column(run, "sys_noname_alpha")) < max(tol, 1e-12)
+        if plan.c.charged:
+            # potential (field 6), and charge density (field 7) against the
+            # ion densities it is the near-cancelling sum of
+            psi = pro_column(run, "sys_noname_psi")
+            assert rel_err(interior(plan, orc.field(6)), psi) < max(tol, 1e-12), mode
+            dq = np.max(np.abs(interior(plan, orc.field(7)) - pro_column(run, "sys_noname_q")))
+            assert dq <= max(tol, 1e-12) * charge_scale(plan, run), mode
         F, O, mu = orc.free_energy()
         assert abs(F - k["sys_noname_free_energy"]) <= tol * max(1.0, abs(k["sys_noname_free_energy"]))
         assert abs(O - k["sys_noname_grand_potential"]) <= tol * max(1.0, abs(k["sys_noname_grand_potential"]))
@@ -63,4 +76,4 @@ def test_oracle_matches_reference(name):
             assert abs(mu[m] - k[f"mol_{mn}_Mu"]) <= tol * max(1.0, abs(k[f"mol_{mn}_Mu"]))
         if mode == "conv":
             assert abs(its - int(k["newton_isaac_iterations"])) <= max(2, its)  # both converged
-            assert run["kal"]["newton_isaac_residual"] < 1e-7
+            assert run["kal"]["newton_isaac_residual"] < newton_tolerance(run)
