@@ -184,7 +184,9 @@ int nm_solve_host(nm_ctx* ctx, double* x_host, double* phi_host,
 
 /* Results of the last residual evaluation (device -> host copies).
  * which: 0 segment φ [n_seg*M], 1 G1 [n_seg*M], 2 α [M], 3 φ_tot [M],
- * 4 molecule φ_tot [n_mol*M], 5 φ_side [n_seg*M]. */
+ * 4 molecule φ_tot [n_mol*M], 5 φ_side [n_seg*M]; charged systems also
+ * 6 ψ with mirror bounds [M], 7 charge density q [M], 8 relative
+ * permittivity ε [M] (every site, halo layers included). */
 int nm_get_field(nm_ctx* ctx, int which, double* out_host);
 
 /* Per-molecule scalars of the last residual: GN, n, θ, φ_bulk, norm. */

@@ -9,6 +9,8 @@
 //   k_norms       normalisation of every molecule (system.cpp:2368-2560)
 //   k_phi         φ = rho/G1·norm, φ_tot       (system.cpp:2438-2610)
 //   k_residual    φ_side stencil + χ terms + α + incompressibility + KSAM
+// and, for a charged system (elec.cu), k_field (ψ bounds, EE) before k_g1
+// and k_charge + the Poisson update (ψ block of g) after k_residual.
 // and per DIIS iteration (sfnewton.cpp:1078-1095, 837-880):
 //   k_diis_step   x -= δ·g, history slot, ‖g‖² partials
 //   k_gram        Gram row of the history (deterministic two-pass sums)
@@ -45,14 +47,21 @@ static const int RED_THREADS = 256;
 
 // ---------------------------------------------------------------- kernels --
 
+// u = x (+ the charged terms −ε·EE + v·ψ, system.cpp:2001-2030) at the
+// set_bounds source of each site; G1 = exp(−u)·mask·KSAM
 __global__ void k_g1(Lat L, int ns, const double* __restrict__ x, const int* __restrict__ seg_it,
-                     const double* __restrict__ gmask, double* __restrict__ G1, float* __restrict__ G1f) {
+                     const double* __restrict__ gmask, double* __restrict__ G1, float* __restrict__ G1f,
+                     ChgArgs chg, const double* __restrict__ EE, const double* __restrict__ psi) {
     int M = L.M;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < M; s += gridDim.x * blockDim.x) {
         int src = nmdev::bc_source(L, s);
         for (int i = 0; i < ns; i++) {
             int it = seg_it[i];
             double u = it >= 0 ? x[(size_t)it * M + src] : 0.0;
+            if (chg.on && it >= 0) {
+                u += -1.0 * chg.eps[i] * EE[src];
+                if (chg.val[i] != 0) u += chg.val[i] * psi[src];
+            }
             if (G1f) {
                 // FP32 phase: one FP32 exp serves both copies (the FP64 copy,
                 // used by φ = ρ/G1, then matches the propagators' G1 exactly)
@@ -80,13 +89,25 @@ __global__ void k_prop(Lat L, const double* __restrict__ in, const double* __res
     }
 }
 
-// backward step fused with composition: out = stencil(in)·G1; rho += d·Gf·out
+// backward step fused with composition: out = stencil(in)·G1; rho += d·Gf·out.
+// nh > 0 (charged systems): also the halo part of rho, the flat-array step
+// at each halo site times the bounded Gf there (out's halo is not stored:
+// the next step reads it through set_bounds).
 __global__ void k_prop_back(Lat L, const double* __restrict__ in, const double* __restrict__ G1,
                             double* __restrict__ out, const double* __restrict__ Gf,
-                            double* __restrict__ rho, double d) {
+                            double* __restrict__ rho, double d, int nh) {
     int n = nmdev::interior_count(L);
     nmdev::GLoad<double> ld{in};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n + nh; i += gridDim.x * blockDim.x) {
+        if (i >= n) {
+            const int h = nmdev::halo_site(L, i - n);
+            nmdev::BLoad bl{in, L};
+            const double v = nmdev::flat_prop_at(L, bl, h) * G1[h];
+            const double gf = Gf[nmdev::bc_source(L, h)];
+            if (d == 1.0) rho[h] += gf * v;
+            else rho[h] += d * gf * v;
+            continue;
+        }
         int x, y, z;
         nmdev::site_coords(L, i, x, y, z);
         int s = x * L.JX + y * L.JY + z;
@@ -199,6 +220,19 @@ __global__ void k_norms(NormArgs a, double* __restrict__ sc, double* __restrict_
         } else s[4] = 0;
         s[1] = norm;
     }
+    if (a.neutralizer >= 0) {
+        // the neutraliser's bulk fraction makes the bulk neutral
+        // (system.cpp:2487-2515, 2560-2570)
+        const MolScal& Nt = a.mol[a.neutralizer];
+        double* s = sc + 5 * a.neutralizer;
+        const double qs = a.solvent >= 0 ? a.mol[a.solvent].charge : 0.0;
+        if (Nt.charge != qs) s[4] = ((B - 1.0) * qs - A) / (Nt.charge - qs);
+        B += s[4];
+        double norm = s[4] / Nt.N;
+        s[2] = norm * s[0];
+        s[3] = s[2] * Nt.N;
+        s[1] = norm;
+    }
     if (a.solvent >= 0) {
         double* s = sc + 5 * a.solvent;
         s[4] = 1.0 - B;
@@ -213,10 +247,13 @@ __global__ void k_norms(NormArgs a, double* __restrict__ sc, double* __restrict_
     if (st) *status = st;
 }
 
+// φ = frozen + rho/G1·norm and φ_tot.  halo != 0 (charged systems): φ_tot
+// at halo sites also takes the halo part of rho, as the reference's flat
+// arrays do (φ itself is read through set_bounds there).
 __global__ void k_phi(Lat L, PhiArgs a, const double* __restrict__ sc, const double* __restrict__ G1,
                       const double* __restrict__ phi_frozen, const int* __restrict__ seg_frozen,
                       double* __restrict__ phi, double* __restrict__ phitot,
-                      double* __restrict__ mol_phitot) {
+                      double* __restrict__ mol_phitot, int halo) {
     int M = L.M;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < M; s += gridDim.x * blockDim.x) {
         bool in = nmdev::is_interior(L, s);
@@ -237,6 +274,15 @@ __global__ void k_phi(Lat L, PhiArgs a, const double* __restrict__ sc, const dou
                 phi[(size_t)sg * M + s] += v;
                 pt += v;
                 mol_phitot[(size_t)m * M + s] += v;
+            }
+        } else if (halo) {
+            for (int k = 0; k < a.n_mm; k++) {
+                int sg = a.mm_seg[k], m = a.mm_mol[k];
+                double g1 = G1[(size_t)sg * M + s];
+                double v = g1 != 0 ? a.mm_rho[k][s] / g1 : 0.0;
+                double norm = sc[5 * m + 1];
+                if (norm > 0) v *= norm;
+                pt += v;
             }
         }
         phitot[s] = pt;
@@ -404,7 +450,8 @@ __global__ void k_diis_mix(int n, double* __restrict__ x, const double* __restri
 
 // free-energy and grand-potential densities (system.cpp:2809-3244)
 struct FeArgs {
-    int ns, n_mol;
+    int ns, n_mol, charged;
+    const double *q, *psi, *EE, *eps;  // charged systems
     int seg_frozen[NM_MAX_SEG], seg_in_mol[NM_MAX_SEG];
     double chi[NM_MAX_SEG * NM_MAX_SEG];
     double cF[NM_MAX_MOL], cF2[NM_MAX_MOL], invN[NM_MAX_MOL];
@@ -438,6 +485,7 @@ __global__ void k_fe_density(Lat L, FeArgs a, const double* __restrict__ sc, con
         for (int m = 0; m < a.n_mol; m++) f += a.cF2[m] * mol_phitot[(size_t)m * M + s];
         double km = ksam[s];
         F[s] = f * km;
+        if (a.charged) F[s] += a.q[s] * a.psi[s] * 0.5;  // system.cpp:3020-3028
         for (int m = 0; m < a.n_mol; m++) gp += (mol_phitot[(size_t)m * M + s] + (-sc[5 * m + 4])) * a.invN[m];
         gp += alpha[s];
         for (int j = 0; j < a.ns; j++) {
@@ -450,7 +498,14 @@ __global__ void k_fe_density(Lat L, FeArgs a, const double* __restrict__ sc, con
                 gp += chi * (pj * phi_side[(size_t)k * M + s] + (-pbA * seg_phibulk[k]));
             }
         }
-        GP[s] = (-gp) * km;
+        if (a.charged) {  // system.cpp:3225-3238
+            double t = a.EE[s] * a.eps[s] * -2.0;
+            t = (t + a.q[s] * a.psi[s]) * (-1.0 / 2.0);
+            double qs = a.q[s];
+            GP[s] = ((-gp) + t) * km + (qs - qs * km) * a.psi[s] * 0.5;
+        } else {
+            GP[s] = (-gp) * km;
+        }
     }
 }
 
@@ -483,7 +538,7 @@ int Ctx::molecule_pass(int m) {
     MolDev& D = mols[m];
     size_t M = plan->M;
     int n = interior;
-    int gb = grid_for(n);
+    int gb = grid_for(n), gbh = grid_for(n + nh);
     CK(cudaMemsetAsync(D.rho, 0, sizeof(double) * M * mol.n_molmon, stream));
     // forward
     for (int b = 0; b < mol.n_blocks; b++) {
@@ -534,11 +589,11 @@ int Ctx::molecule_pass(int m) {
         if (B.parent < 0) {
             k_back_init<<<gb, 256, 0, stream>>>(lat, G1, cur, D.Gf + (size_t)s * M, rho, B.degeneracy);
         } else {
-            k_prop_back<<<gb, 256, 0, stream>>>(lat, D.Q + (size_t)b * M, G1, cur, D.Gf + (size_t)s * M, rho, B.degeneracy);
+            k_prop_back<<<gbh, 256, 0, stream>>>(lat, D.Q + (size_t)b * M, G1, cur, D.Gf + (size_t)s * M, rho, B.degeneracy, nh);
         }
         launches++;
         for (s = s - 1; s >= B.s0; s--) {
-            k_prop_back<<<gb, 256, 0, stream>>>(lat, cur, G1, nxt, D.Gf + (size_t)s * M, rho, B.degeneracy);
+            k_prop_back<<<gbh, 256, 0, stream>>>(lat, cur, G1, nxt, D.Gf + (size_t)s * M, rho, B.degeneracy, nh);
             launches++;
             double* t = cur; cur = nxt; nxt = t;
         }
@@ -568,16 +623,20 @@ int Ctx::molecule_pass(int m) {
 // by residual() on the 3-D path).
 int Ctx::residual_launches(const double* x, double* g) {
     int M = plan->M;
-    k_g1<<<grid_for(M), 256, 0, stream>>>(lat, plan->n_seg, x, d_seg_it, d_gmask, d_G1, phase32 ? d_G1f : nullptr);
+    if (charged) elec_field(x);
+    k_g1<<<grid_for(M), 256, 0, stream>>>(lat, plan->n_seg, x, d_seg_it, d_gmask, d_G1, phase32 ? d_G1f : nullptr,
+                                          chg, d_EE, d_psi);
     launches++;
     for (int m = 0; m < plan->n_mol; m++) {
         int rc = use3d ? ctx3d_molecule_pass(*this, m, phase32) : molecule_pass(m);
         if (rc) return rc;
     }
     k_norms<<<1, 32, 0, stream>>>(norm_args, d_sc, d_seg_phibulk, d_status);
-    k_phi<<<grid_for(M), 256, 0, stream>>>(lat, phi_args, d_sc, d_G1, d_phi_frozen, d_seg_frozen, d_phi, d_phitot, d_mol_phitot);
+    k_phi<<<grid_for(M), 256, 0, stream>>>(lat, phi_args, d_sc, d_G1, d_phi_frozen, d_seg_frozen, d_phi, d_phitot,
+                                           d_mol_phitot, charged ? 1 : 0);
     k_residual<<<grid_for(M), 256, 0, stream>>>(lat, res_args, x, d_phi, d_phitot, d_seg_phibulk, d_ksam, g, d_alpha, d_phi_side);
     launches += 3;
+    if (charged) elec_residual(x, g);
     return NM_OK;
 }
 
@@ -716,6 +775,8 @@ int Ctx::free_energy(double* F, double* Omega, double* mu) {
     FeArgs a;
     std::memset(&a, 0, sizeof(a));
     a.ns = ns; a.n_mol = plan->n_mol;
+    a.charged = charged;
+    a.q = d_q; a.psi = d_psi; a.EE = d_EE; a.eps = d_eps;
     for (int i = 0; i < ns; i++) {
         a.seg_frozen[i] = plan->seg_freedom[i] == NM_SEG_FROZEN;
         a.seg_in_mol[i] = plan->seg_it[i] >= 0;
@@ -796,7 +857,6 @@ static int dalloc(T** p, size_t n, cudaStream_t st) {
 
 int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
     plan = p;
-    if (p->charged) { set_error("charged systems (electrostatics) are not supported by the device path"); return NM_ERR_INPUT; }
     if (p->n_seg > NM_MAX_SEG || p->n_mol > NM_MAX_MOL || p->diis_m > NM_MAX_DIIS) {
         set_error("problem exceeds the device path's compiled limits (segments, molecules, DIIS m)");
         return NM_ERR_INPUT;
@@ -865,6 +925,7 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
     TRY(dalloc(&d_status, 1, stream));
     TRY(dalloc(&d_partial, (size_t)red_blocks, stream));
     TRY(dalloc(&d_resid, 4, stream));
+    if (p->charged) TRY(elec_init());
     mols.resize(p->n_mol);
     int max_store = 1;
     for (int m = 0; m < p->n_mol; m++) max_store = std::max(max_store, p->mols[m].n_store);
@@ -901,6 +962,7 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
     std::memset(&phi_args, 0, sizeof(phi_args));
     std::memset(&res_args, 0, sizeof(res_args));
     norm_args.n_mol = p->n_mol; norm_args.solvent = p->solvent; norm_args.ns = ns;
+    norm_args.neutralizer = p->charged ? p->neutralizer : -1;
     phi_args.ns = ns; phi_args.n_mol = p->n_mol;
     int k = 0;
     for (int m = 0; m < p->n_mol; m++) {
@@ -927,7 +989,8 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
 Ctx::~Ctx() {
     double* ptrs[] = {d_L, d_lm1, d_l0, d_l1, d_ksam, d_gmask, d_phi_frozen, d_G1, d_phi, d_phi_side,
                       d_phitot, d_alpha, d_mol_phitot, d_gb, d_tmpF, d_tmpGP, d_sc, d_seg_phibulk,
-                      d_partial, d_resid, d_xR, d_xx0, d_g, d_x, d_Ci, d_gram_partial};
+                      d_partial, d_resid, d_xR, d_xx0, d_g, d_x, d_Ci, d_gram_partial,
+                      d_EE, d_psi, d_q, d_eps, d_X};
     for (double* q : ptrs) if (q) cudaFreeAsync(q, stream);
     if (d_seg_it) cudaFreeAsync(d_seg_it, stream);
     if (d_seg_frozen) cudaFreeAsync(d_seg_frozen, stream);
@@ -1015,6 +1078,7 @@ int nm_solve_host(nm_ctx* ctx, double* x_host, double* phi_host, nm_solve_result
 int nm_get_field(nm_ctx* ctx, int which, double* out_host) {
     Ctx* c = reinterpret_cast<Ctx*>(ctx);
     if (!c || !out_host || !c->have_state) { nm::set_error("nm_get_field: no state"); return NM_ERR_ARG; }
+    if (which >= 6 && which <= 8 && !c->charged) { nm::set_error("nm_get_field: ψ, q and ε exist only for charged systems"); return NM_ERR_ARG; }
     size_t M = c->plan->M, ns = c->plan->n_seg;
     const double* src = nullptr;
     size_t n = 0;
@@ -1025,6 +1089,9 @@ int nm_get_field(nm_ctx* ctx, int which, double* out_host) {
         case 3: src = c->d_phitot; n = M; break;
         case 4: src = c->d_mol_phitot; n = c->plan->n_mol * M; break;
         case 5: src = c->d_phi_side; n = ns * M; break;
+        case 6: src = c->d_psi; n = M; break;
+        case 7: src = c->d_q; n = M; break;
+        case 8: src = c->d_eps; n = M; break;
         default: nm::set_error("nm_get_field: unknown field"); return NM_ERR_ARG;
     }
     cudaError_t e = cudaMemcpyAsync(out_host, src, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream);

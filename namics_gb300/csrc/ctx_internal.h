@@ -75,6 +75,7 @@ __host__ __device__ inline void nm_pinv_solve(const double* Ain, double* c, int 
 struct MolScal { int freedom, pinned; double n_in, theta_in, phibulk_in, N, charge; };
 struct NormArgs {
     int n_mol, solvent, ns;
+    int neutralizer;  // molecule index (charged systems) or -1
     MolScal mol[NM_MAX_MOL];
     int n_mm;
     int mm_mol[NM_MAX_MM], mm_seg[NM_MAX_MM];
@@ -89,6 +90,23 @@ struct ResArgs {
     int ns, nit;
     int it_seg[NM_MAX_SEG];
     double chi[NM_MAX_SEG * NM_MAX_SEG];
+};
+
+// Charged systems: per-segment relative permittivity and valence, for the
+// u += -ε·EE + v·ψ terms of PutU (system.cpp:2001-2030).
+struct ChgArgs {
+    int on;
+    double eps[NM_MAX_SEG], val[NM_MAX_SEG];
+};
+
+// Constants of the electrostatics (namics.cpp:44-49 and the lattice's
+// UpdateEE / UpdatePsi prefactors), evaluated on the host in the reference's
+// operation order.
+struct ElecConst {
+    double pf;      // UpdateEE prefactor, geometry factors included
+    double C;       // UpdatePsi prefactor, geometry factors included
+    double offset;  // offset_first_layer
+    const double* Lv;  // site volume L (device)
 };
 
 struct MolDev {
@@ -150,6 +168,13 @@ struct Ctx {
     NormArgs norm_args;
     PhiArgs phi_args;
     ResArgs res_args;
+    // electrostatics (charged systems, 1 and 2 gradients): ψ is the last
+    // block of x; halo sites of the composition are evaluated (nh of them)
+    bool charged = false;
+    int nh = 0;
+    ChgArgs chg{};
+    ElecConst ec{};
+    double *d_EE = nullptr, *d_psi = nullptr, *d_q = nullptr, *d_eps = nullptr, *d_X = nullptr;
 
     int init(const nm_plan* p, const nm_ctx_options* opt);
     ~Ctx();
@@ -161,6 +186,9 @@ struct Ctx {
     int check_status();
     int solve(double* x, nm_solve_result* res, int max_iter);
     int free_energy(double* F, double* Omega, double* mu);
+    int elec_init();                                // constants and buffers
+    int elec_field(const double* x);                // ψ with mirror bounds, EE
+    int elec_residual(const double* x, double* g);  // q, ε, ψ block of g
 };
 
 }  // namespace nm

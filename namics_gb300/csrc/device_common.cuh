@@ -117,6 +117,95 @@ __device__ __forceinline__ bool is_interior(const Lat& L, int s) {
     return x >= 1 && x <= L.MX && y >= 1 && y <= L.MY && z >= 1 && z <= L.MZ;
 }
 
+// ---- halo sites (1 and 2 gradients) --------------------------------------
+// The reference keeps its propagators as flat padded arrays and applies the
+// neighbour sum to every element, halo layers included.  The values it leaves
+// in the halo are overwritten by set_bounds before any propagator is read
+// again, with one exception that reaches the result: the halo part of the
+// composition rho, which flows into φ_tot at halo sites and from there into
+// the relative permittivity ε = Σ ε_i φ_i / φ_tot that the Poisson update
+// reads at its boundary neighbours.  Charged systems therefore evaluate the
+// flat-array neighbour sum at the halo sites as well.
+
+__device__ __forceinline__ int halo_count(const Lat& L) {
+    return L.g == 1 ? 2 : 2 * L.JX + 2 * L.MX;
+}
+
+// j-th halo site: 1-D {0, MX+1}; 2-D the rows x = 0 and x = MX+1, then the
+// columns y = 0 and y = MY+1 of x = 1..MX.
+__device__ __forceinline__ int halo_site(const Lat& L, int j) {
+    if (L.g == 1) return j == 0 ? 0 : L.MX + 1;
+    const int JX = L.JX;
+    if (j < JX) return j;
+    j -= JX;
+    if (j < JX) return (L.MX + 1) * JX + j;
+    j -= JX;
+    return (j / 2 + 1) * JX + ((j & 1) ? L.MY + 1 : 0);
+}
+
+// Lattice::propagate's neighbour sum at site s of the flat array (every
+// term whose write and read positions lie inside the array, in the order
+// the reference accumulates them): LG1Planar.cpp:138-159, LGrad1.cpp:
+// 432-454, LG2Planar.cpp:1039-1127, LGrad2.cpp:1053-1090.  `g` loads an
+// element of the already bounded input.
+template <typename LD>
+__device__ __forceinline__ double flat_prop_at(const Lat& L, const LD& g, int s) {
+    const int M = L.M, JX = L.JX;
+    if (L.g == 1) {
+        if (L.geom == 0) {
+            double v = 0;
+            if (s >= 1) v += L.lam * g(s - 1);
+            v += (1.0 - 2.0 * L.lam) * g(s);
+            if (s < M - 1) v += L.lam * g(s + 1);
+            return v;
+        }
+        double v = g(s) * L.l0[s];
+        if (s >= 1) v += g(s - 1) * L.lm1[s];
+        if (s < M - 1) v += g(s + 1) * L.l1[s];
+        return v;
+    }
+    if (L.geom == 0) {
+        if (L.lat == 0) {
+            const double C1 = 16.0 / 36.0, C2 = 4.0 / 36.0, C3 = 1.0 / 36.0;
+            double v = C1 * g(s);
+            if (s >= 1) v += C2 * g(s - 1);
+            if (s < M - 1) v += C2 * g(s + 1);
+            if (s >= JX) v += C2 * g(s - JX);
+            if (s < M - JX) v += C2 * g(s + JX);
+            if (s >= JX + 1) v += C3 * g(s - JX - 1);
+            if (s >= JX) v += C3 * g(s - JX + 1);
+            if (s >= 1 && s < M - JX + 1) v += C3 * g(s + JX - 1);
+            if (s < M - JX - 1) v += C3 * g(s + JX + 1);
+            return v;
+        }
+        double v = 2.0 * g(s);
+        if (s >= JX) v += g(s - JX);
+        if (s < M - JX) v += g(s + JX);
+        if (s >= 1) v += g(s - 1);
+        if (s < M - 1) v += g(s + 1);
+        v *= 2.0;
+        if (s >= JX + 1) v += g(s - JX - 1);
+        if (s < M - JX - 1) v += g(s + JX + 1);
+        if (s >= JX && s < M - 1) v += g(s - JX + 1);
+        if (s >= 1 && s < M - JX) v += g(s + JX - 1);
+        return v * (1.0 / 16.0);
+    }
+    double C1, C2, C3;
+    if (L.lat == 0) { C1 = 4.0 / 6.0; C2 = 1.0 / 6.0; C3 = 4.0; }
+    else { C1 = 0.5; C2 = 0.25; C3 = 2.0; }
+    double v = C1 * g(s);
+    if (s >= JX) v += g(s - JX) * L.lm1[s];
+    if (s < M - JX) v += g(s + JX) * L.l1[s];
+    if (s >= 1) v += C2 * g(s - 1);
+    if (s < M - 1) v += C2 * g(s + 1);
+    v *= C3;
+    if (s >= JX + 1) v += g(s - JX - 1) * L.lm1[s];
+    if (s >= JX && s < M - 1) v += g(s - JX + 1) * L.lm1[s];
+    if (s >= 1 && s < M - JX) v += g(s + JX - 1) * L.l1[s];
+    if (s < M - JX - 1) v += g(s + JX + 1) * L.l1[s];
+    return v * C2;
+}
+
 // Source site that set_bounds copies into site s (s itself when interior).
 __device__ __forceinline__ int bc_source(const Lat& L, int s) {
     if (L.g == 1) return bmap(s, L.MX, L.b1[0], L.bm[0]);
@@ -128,5 +217,13 @@ __device__ __forceinline__ int bc_source(const Lat& L, int s) {
     return bmap(x, L.MX, L.b1[0], L.bm[0]) * L.JX + bmap(y, L.MY, L.b1[1], L.bm[1]) * L.JY +
            bmap(z, L.MZ, L.b1[2], L.bm[2]);
 }
+
+// Element i of an array after set_bounds: the halo takes its source site's
+// value (a surface halo keeps its own, zero in every stored propagator).
+struct BLoad {
+    const double* __restrict__ p;
+    Lat L;
+    __device__ __forceinline__ double operator()(int i) const { return p[bc_source(L, i)]; }
+};
 
 }  // namespace nmdev

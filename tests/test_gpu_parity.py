@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from conftest import golden_names, load_golden
-from helpers import interior, pro_column, rel_err
+from helpers import interior, newton_tolerance, pro_column, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -61,6 +61,14 @@ def test_residual_matches_oracle(name):
     assert abs(O - Oo) <= 1e-10 * max(1, abs(Oo))
     assert np.allclose(mu, muo, rtol=1e-10, atol=1e-10)
     assert ctx.launch_count() > 0
+    if plan.c.charged:
+        # ψ, and q and ε at every site: ε at the halo layers comes from the
+        # reference's flat-array composition there and feeds the Poisson update
+        # (element-wise: ε reaches ~1e8 at halo sites where φ_tot is tiny)
+        assert rel_err(interior(plan, ctx.field(6)), interior(plan, orc.field(6))) < 1e-10
+        for which in (7, 8):
+            a, b = ctx.field(which), orc.field(which)
+            assert np.allclose(a, b, rtol=1e-9, atol=1e-10), (which, np.max(np.abs(a - b)))
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -75,8 +83,12 @@ def test_solve_matches_reference(name):
         k = run["kal"]
         same = res.iterations == int(k["newton_isaac_iterations"])
         if mode == "conv":
-            assert res.status == 0 and res.residual < 1e-7
-        tol = 1e-8 if same else 1e-6
+            assert res.status == 0 and res.residual < newton_tolerance(run)
+        # along the reference's DIIS path: 1e-8 (the fixture's path_tol where
+        # rounding drifts further); on a split path the convergence ball, which
+        # the weakly constrained charged cylindrical fixtures widen (split_tol)
+        split = g.get("split_tol", 1e-5)
+        tol = g.get("path_tol", 1e-8) if same else (split if split > 1e-5 else 1e-6)
         if mode != "conv":
             tol = 1e-6  # a few iterations from an unstable start
         phi = phi.reshape(plan.n_seg, plan.M)
@@ -93,7 +105,7 @@ def _batch_cases():
         g = load_golden(n)
         if "conv" in g["runs"]:
             p = Plan(g["runs"]["conv"]["input"])
-            if p.c.gradients == 1:
+            if p.c.gradients == 1 and not p.c.charged:  # the batched solver is uncharged
                 out.append(n)
     return out
 

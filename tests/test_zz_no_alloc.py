@@ -29,7 +29,7 @@ def _one_gradient_cases():
         runs = load_golden(n)["runs"]
         if "conv" in runs:
             plan = Plan(runs["conv"]["input"])  # keep alive while reading it
-            if plan.c.gradients == 1:
+            if plan.c.gradients == 1 and not plan.c.charged:
                 out.append((plan.M, runs["conv"]))
     return out
 
