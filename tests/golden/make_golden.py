@@ -163,7 +163,7 @@ def cases() -> list[dict]:
                   conv_itlim=5000, split_tol=1e-4))
     C.append(dict(name="charged2d", lines=lat2d(16, 10, ["surface", "mirror", "mirror", "mirror"]) +
                   charged_lines("(X)1(A)29", 0.5), field=(-0.01, 0.01), seed=22, modes=["it0", "it5", "conv"],
-                  newton=dict(tol=1e-6), conv_itlim=5000, path_tol=1e-7))
+                  newton=dict(tol=1e-6), conv_itlim=5000, path_tol=3e-6))
     C.append(dict(name="charged2d_cyl", lines=lat2d(16, 10, ["surface", "mirror", "mirror", "mirror"],
                   geom="cylindrical", offset=10) + charged_lines("(X)1(A)29", 10.0),
                   field=(-0.01, 0.01), seed=23, modes=["it0", "it5", "conv"], newton=dict(tol=1e-6),
