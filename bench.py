@@ -330,6 +330,116 @@ def melt3d_small_text(n: int = 64, a: int = 20, chi: float = 0.4) -> str:
         "(A)50(B)50", f"(A){a}(B){a}")
 
 
+def cyl2d_text(nx: int = 200, ny: int = 200, N: int = 500, n: float = 1.0, chi: float = 0.5,
+               itlim: int = 20, tol: float = 1e-7) -> str:
+    """Config 3: 2-D cylindrical nx (r) × ny (z) lattice, offset_first_layer
+    10 (inner cylinder of radius 10, a frozen wall below x = 1), (X)1(A)N-1
+    pinned at the first layer with n chains, chi_AS = chi; A carries valence
+    -0.1, monovalent ions: Na the neutraliser, Cl free at phi_b 0.01; water
+    the solvent; bondlength 5e-10 m."""
+    return "\n".join([
+        "lat : flat : gradients : 2", f"lat : flat : n_layers_x : {nx}", f"lat : flat : n_layers_y : {ny}",
+        "lat : flat : geometry : cylindrical", "lat : flat : lattice_type : simple_cubic",
+        "lat : flat : offset_first_layer : 10", "lat : flat : bondlength : 5e-10",
+        "lat : flat : lowerbound_x : surface", "lat : flat : upperbound_x : mirror",
+        "lat : flat : lowerbound_y : mirror", "lat : flat : upperbound_y : mirror",
+        "mon : S : freedom : frozen", "mon : S : frozen_range : lowerbound",
+        "mon : X : freedom : pinned", "mon : X : pinned_range : firstlayer",
+        "mon : A : freedom : free", "mon : A : valence : -0.1", "mon : W : freedom : free",
+        "mon : Na : freedom : free", "mon : Na : valence : 1", "mon : Cl : freedom : free", "mon : Cl : valence : -1",
+        f"mon : A : chi_W : {chi}", f"mon : X : chi_W : {chi}",
+        f"mol : pol : composition : (X)1(A){N - 1}", "mol : pol : freedom : restricted", f"mol : pol : n : {n!r}",
+        "mol : water : composition : (W)1", "mol : water : freedom : solvent",
+        "mol : Na : composition : (Na)1", "mol : Na : freedom : neutralizer",
+        "mol : Cl : composition : (Cl)1", "mol : Cl : freedom : free", "mol : Cl : phibulk : 0.01",
+        "newton : isaac : method : DIIS", f"newton : isaac : tolerance : {tol}",
+        f"newton : isaac : iterationlimit : {itlim}", "newton : isaac : deltamax : 0.1", "newton : isaac : m : 10",
+    ]) + "\n"
+
+
+def cyl2d_plan(nx: int, ny: int, N: int, sigma: float, chi: float, itlim: int, tol: float = 1e-7):
+    """The config-3 plan with n = sigma × (sites of the first layer, Σ_y L(x=1))."""
+    from namics_gb300 import Plan
+    probe = Plan(cyl2d_text(nx, ny, N, 1.0, chi, itlim, tol))
+    c = probe.c
+    first = sum(c.L[1 * c.JX + y] for y in range(1, ny + 1))
+    return Plan(cyl2d_text(nx, ny, N, sigma * first, chi, itlim, tol))
+
+
+def run_cyl2d(args) -> None:
+    """Config 3 on one GPU: DIIS iterations of the 200×200 cylindrical charged
+    brush (A_500, sigma 0.02, chi_AS 0.5) from a seeded field x ~ U(-0.01,
+    0.01), ψ included.  A step is `--iters` DIIS iterations (residual +
+    Poisson update + field update), timed with CUDA events on the context's
+    stream; L2 is flushed between steps.  Also reported: the max |Δφ| of one
+    GPU residual at the seeded field against the CPU oracle's."""
+    import torch
+    from namics_gb300 import build as b
+    b.build_product()
+    from namics_gb300 import NM_FP64, Context
+    nx = ny = args.n2d
+    plan = cyl2d_plan(nx, ny, 500, 0.02, 0.5, args.iters)
+    rng = np.random.default_rng(SEED)
+    x0h = rng.uniform(-0.01, 0.01, size=plan.iv)
+    x0 = torch.from_numpy(x0h).cuda()
+    flush = torch.empty(int(256e6) // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    out = {}
+    for prec, name in ((NM_FP64, "fp64"),):
+        ctx = Context(plan, prec, stream=stream.cuda_stream)
+        xw = torch.empty_like(x0)
+        times = []
+        clocks = ClockSampler(0)
+        with clocks:
+            for k in range(args.warmup + args.steps):
+                flush.zero_()
+                xw.copy_(x0)
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                r = ctx.solve_dev(xw.data_ptr())
+                e1.record(stream)
+                e1.synchronize()
+                if k >= args.warmup:
+                    times.append(e0.elapsed_time(e1))
+        ms = statistics.mean(times)
+        its = r.iterations + 1
+        out[name] = {"ms_per_step": ms, "residuals_per_step": its, "ms_per_residual_and_update": ms / its,
+                     "residual_after_step": r.residual, "launches": ctx.launch_count(), "clocks": clocks.summary()}
+        # φ of one residual at the seeded field against the oracle
+        gd = torch.zeros_like(x0)
+        ctx.residual_dev(x0.data_ptr(), gd.data_ptr())
+        out[name]["phi"] = ctx.field(0)
+        ctx.close()
+    dphi = None
+    if not args.no_cpu:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        b.build_oracle()
+        from orc import Oracle
+        orc = Oracle(plan)
+        rc, _ = orc.residual(x0h)
+        if rc == 0:
+            mask = np.tile(plan.interior_mask(), plan.n_seg)
+            dphi = float(np.max(np.abs(out["fp64"]["phi"][mask] - orc.field(0)[mask])))
+    f64 = out["fp64"]
+    updates = float(plan.segment_updates())
+    line = {
+        "metric": "SCF DIIS iterations/s, 200x200 cylindrical charged brush A500 (FP64 GPU)",
+        "value": 1000.0 / f64["ms_per_residual_and_update"], "unit": "iterations/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": f64["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded field)",
+        "config": {"workload": f"config 3: {nx}x{ny} cylindrical, offset 10, (X)1(A)499 pinned, sigma 0.02, "
+                               "chi_AS 0.5, A valence -0.1, Na neutraliser, Cl phi_b 0.01, bondlength 5e-10",
+                   "iterations_per_step": args.iters, "l2": "flushed between steps (256 MB write)",
+                   "segment_site_updates_per_residual": updates, "parallelism": "one GPU"},
+        "updates_per_s": updates / (f64["ms_per_residual_and_update"] / 1000.0),
+        "max_abs_dphi_vs_oracle_fp64": dphi,
+        "fp64_gpu": {k: v for k, v in f64.items() if k != "phi"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_served(args) -> None:
     """Config 5: a Poisson request stream served on one GPU by nm_server
     (continuous batching: 1-gradient requests waiting together share one
@@ -410,9 +520,11 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU comparison")
-    ap.add_argument("--workload", default="brush1d", choices=["brush1d", "melt3d", "served"],
+    ap.add_argument("--workload", default="brush1d", choices=["brush1d", "melt3d", "cyl2d", "served"],
                     help="brush1d: config 4, the headline; melt3d: config 2 (DIIS iterations/s); "
+                         "cyl2d: config 3 (charged cylindrical brush, DIIS iterations/s); "
                          "served: config 5 (request stream)")
+    ap.add_argument("--n2d", type=int, default=200, help="cyl2d: lattice edge (r and z)")
     ap.add_argument("--rate", type=float, default=20.0, help="served: arrivals per second")
     ap.add_argument("--requests", type=int, default=200, help="served: requests in the stream")
     ap.add_argument("--workers", type=int, default=8, help="served: concurrent solves")
@@ -428,6 +540,9 @@ def main():
         return
     if args.workload == "served":
         run_served(args)
+        return
+    if args.workload == "cyl2d":
+        run_cyl2d(args)
         return
     ws, rank, local = dist_env()
     import torch
