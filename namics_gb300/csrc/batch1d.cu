@@ -18,6 +18,7 @@
 // normalisation, residual and DIIS stay FP64.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -624,8 +625,12 @@ __device__ __forceinline__ unsigned long long b1_clock() {
     return t;
 }
 
-__global__ void __launch_bounds__(B1_THREADS, 4) k_batch1d(B1Prob* __restrict__ probs, int mode) {
-    B1Prob& P = probs[blockIdx.x];
+// order (may be null): CTA b solves problem order[b].  The batch lists its
+// problems by descending steps per residual, so the block scheduler spreads
+// the longest solves one per SM before it doubles any of them up.
+__global__ void __launch_bounds__(B1_THREADS, 4) k_batch1d(B1Prob* __restrict__ probs, int mode,
+                                                          const int* __restrict__ order) {
+    B1Prob& P = probs[order ? order[blockIdx.x] : blockIdx.x];
     if (threadIdx.x == 0) P.t_begin = b1_clock();
     extern __shared__ double sm[];
     const int M = P.M, ns = P.ns, iv = P.iv, n_mm = P.n_mm, m = P.m;
@@ -823,6 +828,7 @@ struct Batch {
     std::vector<const nm_plan*> plans;
     std::vector<B1Prob> hp;
     B1Prob* d_probs = nullptr;
+    int* d_order = nullptr;  // CTA -> problem, longest solves first
     std::vector<void*> allocs;
     double* d_x = nullptr;
     double* d_g = nullptr;
@@ -959,6 +965,20 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
     TRYB(B.alloc(&B.d_g, (size_t)off));
     for (int p = 0; p < n; p++) { B.hp[p].x = B.d_x + B.offsets[p]; B.hp[p].g = B.d_g + B.offsets[p]; }
     TRYB(B.alloc(&B.d_probs, (size_t)n));
+    {
+        // a step's latency hardly depends on the lattice size (each thread
+        // owns at most 4 sites), so a solve's length follows its steps per
+        // residual, Σ n_store; larger lattices first among equals
+        std::vector<long long> steps(n, 0);
+        for (int p = 0; p < n; p++)
+            for (int m = 0; m < plans[p]->n_mol; m++) steps[p] += plans[p]->mols[m].n_store;
+        std::vector<int> ord(n);
+        for (int p = 0; p < n; p++) ord[p] = p;
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+            return steps[a] != steps[b] ? steps[a] > steps[b] : plans[a]->MX > plans[b]->MX;
+        });
+        TRYB(B.upload(&B.d_order, ord.data(), (size_t)n));
+    }
     B.smem = maxsmem;
     if (maxsmem > 220 * 1024) { set_error("problem too large for the batched solver's shared memory"); return NM_ERR_INPUT; }
     // the kernel's dynamic shared-memory limit only ever rises, so batches
@@ -981,7 +1001,7 @@ static int batch_run(Batch& B) {
     cudaError_t e = cudaMemcpyAsync(B.d_probs, B.hp.data(), sizeof(B1Prob) * n, cudaMemcpyHostToDevice, B.stream);
     if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
     // one CTA per problem; FP32 problems switch to FP64 inside their CTA
-    k_batch1d<<<n, B1_THREADS, B.smem, B.stream>>>(B.d_probs, B.precision == NM_FP32 ? 1 : 0);
+    k_batch1d<<<n, B1_THREADS, B.smem, B.stream>>>(B.d_probs, B.precision == NM_FP32 ? 1 : 0, B.d_order);
     B.launches++;
     e = cudaGetLastError();
     if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
@@ -1065,7 +1085,7 @@ int nm_batch_residual_dev(nm_batch* b, const double* x_dev, double* g_dev, int p
     for (int p = 0; p < np; p++) B->hp[p].eval_only = 1;
     e = cudaMemcpyAsync(B->d_probs, B->hp.data(), sizeof(nm::B1Prob) * np, cudaMemcpyHostToDevice, B->stream);
     if (e != cudaSuccess) { nm::set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
-    nm::k_batch1d<<<np, B1_THREADS, B->smem, B->stream>>>(B->d_probs, precision == NM_FP32 ? 1 : 0);
+    nm::k_batch1d<<<np, B1_THREADS, B->smem, B->stream>>>(B->d_probs, precision == NM_FP32 ? 1 : 0, B->d_order);
     B->launches++;
     e = cudaMemcpyAsync(g_dev, B->d_g, sizeof(double) * n, cudaMemcpyDeviceToDevice, B->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(B->stream);
@@ -1295,7 +1315,7 @@ extern "C" int nm_solve1d_noalloc(const nm_plan* plan, double* x_dev, int precis
         e = cudaMemcpyAsync(copies[i].dst, copies[i].src, copies[i].bytes, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_prob, &H, sizeof(B1Prob), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
-    k_batch1d<<<1, B1_THREADS, smem, st>>>(d_prob, precision == NM_FP32 ? 1 : 0);
+    k_batch1d<<<1, B1_THREADS, smem, st>>>(d_prob, precision == NM_FP32 ? 1 : 0, nullptr);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaMemcpyAsync(&H, d_prob, sizeof(B1Prob), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
