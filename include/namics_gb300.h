@@ -50,6 +50,7 @@ extern "C" {
 #define NM_ERR_ARG        -12   /* bad argument                             */
 #define NM_ERR_NOMEM      -13   /* device allocation failed                 */
 #define NM_ERR_NOT_CONVERGED -14 /* iteration limit reached (solve only)   */
+#define NM_ERR_TIMEOUT    -15   /* a bounded device wait gave up            */
 
 /* ---- enumerations (values are part of the ABI) -------------------------- */
 enum nm_geometry  { NM_PLANAR = 0, NM_CYLINDRICAL = 1, NM_SPHERICAL = 2 };
@@ -161,6 +162,13 @@ typedef struct nm_ctx_options {
  * (solve_scf.cpp:67-106, system.cpp:100-190, molecule.cpp:130-270). */
 int nm_ctx_create(const nm_plan* plan, const nm_ctx_options* opt, nm_ctx** out);
 int nm_ctx_destroy(nm_ctx* ctx);
+
+/* Context options.  NM_OPT_SWEEP2D (default 1): 2-gradient linear-chain
+ * problems run each propagator sweep as one persistent cooperative launch
+ * instead of one launch per segment step; 0 selects the per-step kernels
+ * (same arithmetic, same results). */
+#define NM_OPT_SWEEP2D 1
+int nm_ctx_set_option(nm_ctx* ctx, int option, int value);
 
 /* One residual evaluation g(x) on device buffers of length plan->iv.
  * Replaces Solve_scf::residuals -> System::Classical_residual

@@ -195,6 +195,9 @@ class Context:
     def launch_count(self) -> int:
         return int(_abi.load().nm_ctx_launch_count(self._h))
 
+    def set_option(self, option: int, value: int) -> None:
+        _check(_abi.load().nm_ctx_set_option(self._h, option, value))
+
 
 class Batch:
     """Many independent 1-gradient problems solved in one persistent launch."""

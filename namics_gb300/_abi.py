@@ -17,6 +17,8 @@ NM_ERR_CUDA = -11
 NM_ERR_ARG = -12
 NM_ERR_NOMEM = -13
 NM_ERR_NOT_CONVERGED = -14
+NM_ERR_TIMEOUT = -15
+NM_OPT_SWEEP2D = 1
 
 NM_FP64, NM_FP32 = 0, 1
 
@@ -78,6 +80,7 @@ SIGNATURES = [
     ("nm_version", C.c_char_p, []),
     ("nm_ctx_create", C.c_int, [P_plan, C.POINTER(nm_ctx_options), C.POINTER(C.c_void_p)]),
     ("nm_ctx_destroy", C.c_int, [C.c_void_p]),
+    ("nm_ctx_set_option", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     ("nm_residual_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("nm_solve_dev", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(nm_solve_result)]),
     ("nm_solve_host", C.c_int, [C.c_void_p, dp, dp, C.POINTER(nm_solve_result)]),

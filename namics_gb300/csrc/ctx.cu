@@ -628,7 +628,10 @@ int Ctx::residual_launches(const double* x, double* g) {
                                           chg, d_EE, d_psi);
     launches++;
     for (int m = 0; m < plan->n_mol; m++) {
-        int rc = use3d ? ctx3d_molecule_pass(*this, m, phase32) : molecule_pass(m);
+        int rc;
+        if (use3d) rc = ctx3d_molecule_pass(*this, m, phase32);
+        else if (use2d && sweep2d && plan->mols[m].n_store > 1) rc = ctx2d_molecule_pass(*this, m);
+        else rc = molecule_pass(m);
         if (rc) return rc;
     }
     k_norms<<<1, 32, 0, stream>>>(norm_args, d_sc, d_seg_phibulk, d_status);
@@ -926,6 +929,7 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
     TRY(dalloc(&d_partial, (size_t)red_blocks, stream));
     TRY(dalloc(&d_resid, 4, stream));
     if (p->charged) TRY(elec_init());
+    if (ctx2d_eligible(p)) TRY(ctx2d_init(*this));
     mols.resize(p->n_mol);
     int max_store = 1;
     for (int m = 0; m < p->n_mol; m++) max_store = std::max(max_store, p->mols[m].n_store);
@@ -1004,6 +1008,12 @@ Ctx::~Ctx() {
     if (d_gb32) cudaFreeAsync(d_gb32, stream);
     if (d_maxbits) cudaFreeAsync(d_maxbits, stream);
     if (d_E) cudaFreeAsync(d_E, stream);
+    for (auto& T : sw_tabs) {
+        if (T.seg) cudaFreeAsync(T.seg, stream);
+        if (T.mm) cudaFreeAsync(T.mm, stream);
+        if (T.deg) cudaFreeAsync(T.deg, stream);
+    }
+    if (d_flags) cudaFreeAsync(d_flags, stream);
     if (graph) cudaGraphExecDestroy(graph);
     if (own_stream && stream) cudaStreamDestroy(stream);
 }
@@ -1042,6 +1052,18 @@ int nm_ctx_create(const nm_plan* plan, const nm_ctx_options* opt, nm_ctx** out) 
 
 int nm_ctx_destroy(nm_ctx* ctx) {
     delete reinterpret_cast<Ctx*>(ctx);
+    return NM_OK;
+}
+
+int nm_ctx_set_option(nm_ctx* ctx, int option, int value) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c) { nm::set_error("nm_ctx_set_option: null context"); return NM_ERR_ARG; }
+    if (option != NM_OPT_SWEEP2D) { nm::set_error("nm_ctx_set_option: unknown option"); return NM_ERR_ARG; }
+    c->sweep2d = value != 0;
+    if (c->graph) {  // the captured residual used the other kernels
+        cudaGraphExecDestroy(c->graph);
+        c->graph = nullptr;
+    }
     return NM_OK;
 }
 

@@ -130,6 +130,11 @@ void nm_pool_setup(int dev);  // keep freed stream-ordered memory in the device'
 L3 make_l3(const nm_plan* p);
 bool ctx3d_eligible(const nm_plan* p, std::string* why);
 int ctx3d_molecule_pass(Ctx& C, int m, bool fp32);
+// persistent 2-D sweeps (ctx2d.cu)
+bool ctx2d_eligible(const nm_plan* p);
+int ctx2d_init(Ctx& C);
+int ctx2d_molecule_pass(Ctx& C, int m);
+struct SweepTab { int* seg = nullptr; int* mm = nullptr; double* deg = nullptr; };
 
 struct Ctx {
     const nm_plan* plan = nullptr;
@@ -175,6 +180,12 @@ struct Ctx {
     ChgArgs chg{};
     ElecConst ec{};
     double *d_EE = nullptr, *d_psi = nullptr, *d_q = nullptr, *d_eps = nullptr, *d_X = nullptr;
+    // persistent 2-D sweeps: one cooperative launch per sweep (ctx2d.cu)
+    bool use2d = false;      // eligible and set up
+    bool sweep2d = true;     // nm_ctx_set_option(NM_OPT_SWEEP2D)
+    int sw_rows = 0, sw_ctas = 0;
+    int* d_flags = nullptr;  // per-CTA step published
+    std::vector<SweepTab> sw_tabs;
 
     int init(const nm_plan* p, const nm_ctx_options* opt);
     ~Ctx();
