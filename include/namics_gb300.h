@@ -163,10 +163,11 @@ typedef struct nm_ctx_options {
 int nm_ctx_create(const nm_plan* plan, const nm_ctx_options* opt, nm_ctx** out);
 int nm_ctx_destroy(nm_ctx* ctx);
 
-/* Context options.  NM_OPT_SWEEP2D (default 1): 2-gradient linear-chain
- * problems run each propagator sweep as one persistent cooperative launch
- * instead of one launch per segment step; 0 selects the per-step kernels
- * (same arithmetic, same results). */
+/* Context options.  NM_OPT_SWEEP2D (default 0): 1 runs each propagator
+ * sweep of a 2-gradient linear-chain problem as one persistent cooperative
+ * launch (CTAs synchronised per step through neighbour progress flags)
+ * instead of one launch per segment step.  Same arithmetic, same results;
+ * on GB300 the per-step launches are the faster of the two. */
 #define NM_OPT_SWEEP2D 1
 int nm_ctx_set_option(nm_ctx* ctx, int option, int value);
 

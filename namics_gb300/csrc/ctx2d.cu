@@ -1,8 +1,12 @@
-// Persistent 2-D sweeps for the generic context (FP64, linear chains).
+// Persistent 2-D sweeps for the generic context (FP64, linear chains), an
+// option (NM_OPT_SWEEP2D, off by default).
 //
 // A 2-D step touches MX·MY sites (40 804 for a 200×200 lattice), about 8
 // warps per SM, so a step launched on its own costs a launch plus a memory
-// round trip, ~4.4 µs, for well under a microsecond of work.  Here one
+// round trip, ~4.4 µs.  Measured on GB300 the sweep below is slower still
+// (7.2 µs per step on that lattice): a release/acquire hand-off between
+// neighbouring CTAs costs more than a kernel boundary, and the FP64 work of a
+// step concentrates on fewer SMs.  Here one
 // cooperative launch runs a whole sweep: CTA c owns rows x ∈ [x0, x1] and,
 // per step, waits only for the CTAs that own the rows its stencil reads
 // (x0-R .. x1+R; R = 1, or 2 when the halo composition of a charged system
@@ -11,11 +15,12 @@
 // (`stencil_at`, `flat_prop_at`, the same fused composition), so results
 // are bit-identical to the per-step path.
 //
-// Ordering: a CTA stores its rows, bar.sync, then one thread fences and
-// stores the step number with release semantics; a waiting CTA's thread 0
-// loads the flags with acquire semantics, bar.sync, and every thread reads
-// the neighbours' rows with ld.global.cg (L2; L1 is not coherent across
-// SMs).  The backward sweep ping-pongs two buffers: writing step j into a
+// Ordering: a CTA stores its rows, bar.sync, then one thread stores the
+// step number with release semantics (cumulative over the writes the
+// barrier ordered before it); in a waiting CTA one thread per neighbour
+// loads that neighbour's flag with acquire semantics, bar.sync, and every
+// thread reads the neighbours' rows with ld.global.cg (L2; L1 is not
+// coherent across SMs).  The backward sweep ping-pongs two buffers: writing step j into a
 // buffer that neighbours read at step j-1 is safe because step j begins by
 // waiting for their step j-1.
 //
@@ -80,36 +85,31 @@ struct Sw2 {
 
 __device__ __forceinline__ void publish(const Sw2& a, int step) {
     __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        st_release(a.flags + blockIdx.x, step);
-    }
+    if (threadIdx.x == 0) st_release(a.flags + blockIdx.x, step);
 }
 
-// wait until every CTA owning rows x0-R .. x1+R has published `step`
+// wait until every CTA owning rows x0-R .. x1+R has published `step`; thread
+// t polls the t-th of those CTAs, so the waits overlap
 __device__ bool wait_for(const Sw2& a, int x0, int x1, int step) {
-    __shared__ int ok;
-    if (threadIdx.x == 0) {
-        int good = 1;
-        const int lo = max(x0 - a.R, 1), hi = min(x1 + a.R, a.L.MX);
-        const int c0 = (lo - 1) / a.rows, c1 = (hi - 1) / a.rows;
+    const int lo = max(x0 - a.R, 1), hi = min(x1 + a.R, a.L.MX);
+    const int c0 = (lo - 1) / a.rows, c1 = (hi - 1) / a.rows;
+    const int c = c0 + (int)threadIdx.x;
+    int good = 1;
+    if (c <= c1 && c != (int)blockIdx.x) {
         const unsigned long long t0 = gtimer();
-        for (int c = c0; c <= c1 && good; c++) {
-            if (c == (int)blockIdx.x) continue;
-            long long polls = 0;
-            while (ld_acquire(a.flags + c) < step) {
+        long long polls = 0;
+        while (ld_acquire(a.flags + c) < step) {
+            if ((++polls & 63) == 0) {
                 if (*(volatile int*)a.status == NM_ERR_TIMEOUT) { good = 0; break; }
-                if (++polls > (1LL << 26) || gtimer() - t0 > 2000000000ull) {
+                if (polls > (1LL << 26) || gtimer() - t0 > 2000000000ull) {
                     atomicCAS(a.status, 0, NM_ERR_TIMEOUT);
                     good = 0;
                     break;
                 }
             }
         }
-        ok = good;
     }
-    __syncthreads();
-    return ok != 0;
+    return __syncthreads_and(good) != 0;
 }
 
 __global__ void __launch_bounds__(256) k2_fwd(Sw2 a) {
@@ -232,6 +232,9 @@ int ctx2d_init(Ctx& C) {
     if (per_sm < 1) return NM_OK;
     const int MX = p->MX;
     C.sw_rows = (MX + sms * per_sm - 1) / (sms * per_sm);
+    // a charged system's halo composition reads two rows out: with two rows
+    // per CTA those still belong to the adjacent CTAs only
+    if (C.nh && C.sw_rows < 2) C.sw_rows = 2;
     C.sw_ctas = (MX + C.sw_rows - 1) / C.sw_rows;
     // per molecule: segment, rho slot and degeneracy of every stored s
     C.sw_tabs.resize(p->n_mol);

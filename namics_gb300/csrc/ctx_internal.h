@@ -182,7 +182,7 @@ struct Ctx {
     double *d_EE = nullptr, *d_psi = nullptr, *d_q = nullptr, *d_eps = nullptr, *d_X = nullptr;
     // persistent 2-D sweeps: one cooperative launch per sweep (ctx2d.cu)
     bool use2d = false;      // eligible and set up
-    bool sweep2d = true;     // nm_ctx_set_option(NM_OPT_SWEEP2D)
+    bool sweep2d = false;    // nm_ctx_set_option(NM_OPT_SWEEP2D)
     int sw_rows = 0, sw_ctas = 0;
     int* d_flags = nullptr;  // per-CTA step published
     std::vector<SweepTab> sw_tabs;
