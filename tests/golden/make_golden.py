@@ -168,6 +168,18 @@ def cases() -> list[dict]:
                   geom="cylindrical", offset=10) + charged_lines("(X)1(A)29", 10.0),
                   field=(-0.01, 0.01), seed=23, modes=["it0", "it5", "conv"], newton=dict(tol=1e-6),
                   conv_itlim=5000, split_tol=1e-2))
+    # the other Poisson updates and halo stencils: 1-D spherical (Jacobi
+    # update), 2-D hexagonal planar (hexagonal flat halo sums), and a charged
+    # 3-arm star (the halo composition through a branch join)
+    C.append(dict(name="charged1d_sph", lines=lat1d(30, geom="spherical", offset=10) +
+                  charged_lines("(X)1(A)29", 20.0), field=(-0.01, 0.01), seed=24, modes=["it0", "it5", "conv"],
+                  conv_itlim=5000))
+    C.append(dict(name="charged2d_hex", lines=lat2d(16, 10, ["surface", "mirror", "mirror", "mirror"],
+                                                      lattype="hexagonal") + charged_lines("(X)1(A)29", 0.5),
+                  field=(-0.01, 0.01), seed=25, modes=["it0", "it5", "conv"], newton=dict(tol=1e-6),
+                  conv_itlim=5000, path_tol=2e-5))
+    C.append(dict(name="charged_star1d", lines=lat1d(40) + charged_lines("(X)1(A)9[(A)10](A)10", 0.04),
+                  field=(-0.01, 0.01), seed=26, modes=["it0", "it5", "conv"], conv_itlim=5000))
     # configuration-4 sample: random 1-gradient brushes (seeded), 10% stars
     rng = np.random.default_rng(2024)
     for i in range(6):

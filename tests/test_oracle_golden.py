@@ -47,10 +47,10 @@ def test_oracle_matches_reference(name):
         # cases, whose potential direction is weakly constrained.
         same_path = mode == "it0" or its == int(k["newton_isaac_iterations"])
         # Along the same path, rounding still drifts over hundreds of
-        # iterations by up to the fixture's path_tol (1e-8; 3e-6 for the 2-D
-        # charged brush: 883 iterations to a residual of 1e-6 on a problem
-        # whose potential direction is weakly constrained, where the
-        # contracted multiply-adds of the device path drift furthest).
+        # iterations by up to the fixture's path_tol (1e-8; 3e-6 and 2e-5 for
+        # the 2-D planar charged brushes, simple cubic and hexagonal: ~870
+        # iterations to a residual of 1e-6 on problems whose potential
+        # direction is weakly constrained).
         tol = 1e-12 if mode == "it0" else (g.get("path_tol", 1e-8) if same_path else g.get("split_tol", 1e-5))
         if mode.startswith("it") and mode != "it0":
             tol = 1e-7  # fixed iteration count on an unstable start
