@@ -630,6 +630,7 @@ int Ctx::residual_launches(const double* x, double* g) {
     for (int m = 0; m < plan->n_mol; m++) {
         int rc;
         if (use3d) rc = ctx3d_molecule_pass(*this, m, phase32);
+        else if (phase32 && use2d32) rc = ctx2d32_molecule_pass(*this, m);
         else if (use2d && sweep2d && plan->mols[m].n_store > 1) rc = ctx2d_molecule_pass(*this, m);
         else rc = molecule_pass(m);
         if (rc) return rc;
@@ -871,14 +872,19 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
     else { CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking)); own_stream = true; }
     int M = p->M, ns = p->n_seg;
     lat = make_lat(p);
+    bool want2d32 = false;
     {
         std::string why;
         use3d = ctx3d_eligible(p, &why);
         fp32 = opt && opt->precision == NM_FP32;
         if (fp32 && !use3d) {
-            set_error("FP32 propagators in a device context: " + why +
-                      " (1-gradient problems take the batched solver, nm_batch_*)");
-            return NM_ERR_INPUT;
+            std::string why2;
+            if (p->gradients == 3 || !ctx2d32_eligible(p, &why2)) {
+                set_error("FP32 propagators in a device context: " + (p->gradients == 2 ? why2 : why) +
+                          " (1-gradient problems take the batched solver, nm_batch_*)");
+                return NM_ERR_INPUT;
+            }
+            want2d32 = true;
         }
         if (use3d) l3 = make_l3(p);
         phase32 = fp32;  // residual calls outside a solve use the context's precision
@@ -930,6 +936,7 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
     TRY(dalloc(&d_resid, 4, stream));
     if (p->charged) TRY(elec_init());
     if (ctx2d_eligible(p)) TRY(ctx2d_init(*this));
+    if (want2d32) TRY(ctx2d32_init(*this));
     mols.resize(p->n_mol);
     int max_store = 1;
     for (int m = 0; m < p->n_mol; m++) max_store = std::max(max_store, p->mols[m].n_store);
@@ -937,7 +944,7 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
         TRY(dalloc(&d_maxbits, 2 * 32 * (size_t)max_store, stream));  // 32 slots per stored vector
         TRY(dalloc(&d_E, 2 * (size_t)max_store, stream));
     }
-    if (fp32) {
+    if (fp32 && use3d) {
         TRY(dalloc(&d_G1f, (size_t)ns * M, stream));
         TRY(dalloc(&d_gb32, 2 * (size_t)M, stream));
         for (int m = 0; m < p->n_mol; m++) {
@@ -1014,6 +1021,9 @@ Ctx::~Ctx() {
         if (T.deg) cudaFreeAsync(T.deg, stream);
     }
     if (d_flags) cudaFreeAsync(d_flags, stream);
+    for (int* q : E2f) if (q) cudaFreeAsync(q, stream);
+    if (d_E2b) cudaFreeAsync(d_E2b, stream);
+    if (d_rowpart) cudaFreeAsync(d_rowpart, stream);
     if (graph) cudaGraphExecDestroy(graph);
     if (own_stream && stream) cudaStreamDestroy(stream);
 }

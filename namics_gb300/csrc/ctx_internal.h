@@ -135,6 +135,10 @@ bool ctx2d_eligible(const nm_plan* p);
 int ctx2d_init(Ctx& C);
 int ctx2d_molecule_pass(Ctx& C, int m);
 struct SweepTab { int* seg = nullptr; int* mm = nullptr; double* deg = nullptr; };
+// FP32 propagators on 2-gradient lattices, one exponent per row (ctx2d32.cu)
+bool ctx2d32_eligible(const nm_plan* p, std::string* why);
+int ctx2d32_init(Ctx& C);
+int ctx2d32_molecule_pass(Ctx& C, int m);
 
 struct Ctx {
     const nm_plan* plan = nullptr;
@@ -186,6 +190,11 @@ struct Ctx {
     int sw_rows = 0, sw_ctas = 0;
     int* d_flags = nullptr;  // per-CTA step published
     std::vector<SweepTab> sw_tabs;
+    // FP32 propagators on 2-gradient lattices (ctx2d32.cu): per-row exponents
+    bool use2d32 = false;
+    int* d_E2b = nullptr;           // [2][MX+2] exponents of the backward pair
+    double* d_rowpart = nullptr;    // [MX+2] per-row partial sums of G(N)
+    std::vector<int*> E2f;          // per molecule [n_store][MX+2]
 
     int init(const nm_plan* p, const nm_ctx_options* opt);
     ~Ctx();
