@@ -936,7 +936,6 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
     TRY(dalloc(&d_resid, 4, stream));
     if (p->charged) TRY(elec_init());
     if (ctx2d_eligible(p)) TRY(ctx2d_init(*this));
-    if (want2d32) TRY(ctx2d32_init(*this));
     mols.resize(p->n_mol);
     int max_store = 1;
     for (int m = 0; m < p->n_mol; m++) max_store = std::max(max_store, p->mols[m].n_store);
@@ -968,6 +967,7 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
     TRY(dalloc(&d_x, (size_t)p->iv, stream));
     TRY(dalloc(&d_Ci, (size_t)mm, stream));
     TRY(dalloc(&d_gram_partial, (size_t)mm * red_blocks, stream));
+    if (want2d32) TRY(ctx2d32_init(*this));  // after the molecules' state exists
     // kernel argument blocks
     std::memset(&norm_args, 0, sizeof(norm_args));
     std::memset(&phi_args, 0, sizeof(phi_args));
