@@ -367,25 +367,29 @@ def cyl2d_plan(nx: int, ny: int, N: int, sigma: float, chi: float, itlim: int, t
 
 
 def run_cyl2d(args) -> None:
-    """Config 3 on one GPU: DIIS iterations of the 200×200 cylindrical charged
-    brush (A_500, sigma 0.02, chi_AS 0.5) from a seeded field x ~ U(-0.01,
-    0.01), ψ included.  A step is `--iters` DIIS iterations (residual +
-    Poisson update + field update), timed with CUDA events on the context's
-    stream; L2 is flushed between steps.  Also reported: the max |Δφ| of one
-    GPU residual at the seeded field against the CPU oracle's."""
+    """Config 3 on one GPU: the 200×200 cylindrical charged brush (A_500, sigma
+    0.02, chi_AS 0.5) from a seeded field x ~ U(-0.01, 0.01), ψ included, with
+    FP32 propagators (one power-of-two exponent per lattice row, FP64
+    composition, Poisson update, residual and DIIS) and with plain FP64.
+    A step is `--iters` DIIS iterations (residual + Poisson update + field
+    update), timed with CUDA events on the context's stream; L2 is flushed
+    between steps.  Also reported per precision: the max |Δφ| of one residual
+    at the seeded field against the CPU oracle's, and one full solve to
+    ‖g‖ < 1e-7 (FP32 first, FP64 finish), timed end to end."""
     import torch
     from namics_gb300 import build as b
     b.build_product()
-    from namics_gb300 import NM_FP64, Context
+    from namics_gb300 import NM_FP32, NM_FP64, Context
     nx = ny = args.n2d
     plan = cyl2d_plan(nx, ny, 500, 0.02, 0.5, args.iters)
+    solve_plan = cyl2d_plan(nx, ny, 500, 0.02, 0.5, 20000)
     rng = np.random.default_rng(SEED)
     x0h = rng.uniform(-0.01, 0.01, size=plan.iv)
     x0 = torch.from_numpy(x0h).cuda()
     flush = torch.empty(int(256e6) // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.Stream()
     out = {}
-    for prec, name in ((NM_FP64, "fp64"),):
+    for prec, name in ((NM_FP32, "fp32"), (NM_FP64, "fp64")):
         ctx = Context(plan, prec, stream=stream.cuda_stream)
         xw = torch.empty_like(x0)
         times = []
@@ -407,12 +411,19 @@ def run_cyl2d(args) -> None:
         its = r.iterations + 1
         out[name] = {"ms_per_step": ms, "residuals_per_step": its, "ms_per_residual_and_update": ms / its,
                      "residual_after_step": r.residual, "launches": ctx.launch_count(), "clocks": clocks.summary()}
-        # φ of one residual at the seeded field against the oracle
+        # φ of one residual at the seeded field (against the oracle below)
         gd = torch.zeros_like(x0)
         ctx.residual_dev(x0.data_ptr(), gd.data_ptr())
         out[name]["phi"] = ctx.field(0)
         ctx.close()
-    dphi = None
+        if not args.no_solve:
+            sctx = Context(solve_plan, prec, stream=stream.cuda_stream)
+            xs = x0h.copy()
+            t0 = time.perf_counter()
+            rs, _ = sctx.solve_host(xs, want_phi=False)
+            out[name]["full_solve"] = {"seconds": time.perf_counter() - t0, "iterations": rs.iterations,
+                                       "residual": rs.residual, "status": rs.status}
+            sctx.close()
     if not args.no_cpu:
         sys.path.insert(0, str(ROOT / "oracle"))
         b.build_oracle()
@@ -421,21 +432,24 @@ def run_cyl2d(args) -> None:
         rc, _ = orc.residual(x0h)
         if rc == 0:
             mask = np.tile(plan.interior_mask(), plan.n_seg)
-            dphi = float(np.max(np.abs(out["fp64"]["phi"][mask] - orc.field(0)[mask])))
-    f64 = out["fp64"]
+            po = orc.field(0)[mask]
+            for name in out:
+                out[name]["max_abs_dphi_vs_oracle"] = float(np.max(np.abs(out[name]["phi"][mask] - po)))
+    f32, f64 = out["fp32"], out["fp64"]
     updates = float(plan.segment_updates())
     line = {
-        "metric": "SCF DIIS iterations/s, 200x200 cylindrical charged brush A500 (FP64 GPU)",
-        "value": 1000.0 / f64["ms_per_residual_and_update"], "unit": "iterations/s", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": f64["ms_per_step"], "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded field)",
+        "metric": "SCF DIIS iterations/s, 200x200 cylindrical charged brush A500 (FP32 propagators vs plain FP64 GPU)",
+        "value": 1000.0 / f32["ms_per_residual_and_update"], "unit": "iterations/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": f32["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded field)",
         "config": {"workload": f"config 3: {nx}x{ny} cylindrical, offset 10, (X)1(A)499 pinned, sigma 0.02, "
                                "chi_AS 0.5, A valence -0.1, Na neutraliser, Cl phi_b 0.01, bondlength 5e-10",
                    "iterations_per_step": args.iters, "l2": "flushed between steps (256 MB write)",
                    "segment_site_updates_per_residual": updates, "parallelism": "one GPU"},
-        "updates_per_s": updates / (f64["ms_per_residual_and_update"] / 1000.0),
-        "max_abs_dphi_vs_oracle_fp64": dphi,
-        "fp64_gpu": {k: v for k, v in f64.items() if k != "phi"},
+        "updates_per_s": updates / (f32["ms_per_residual_and_update"] / 1000.0),
+        "fp32": {k: v for k, v in f32.items() if k != "phi"},
+        "fp64_gpu": dict({k: v for k, v in f64.items() if k != "phi"},
+                         value=1000.0 / f64["ms_per_residual_and_update"], unit="iterations/s"),
     }
     print(json.dumps(line), flush=True)
 
@@ -525,6 +539,7 @@ def main():
                          "cyl2d: config 3 (charged cylindrical brush, DIIS iterations/s); "
                          "served: config 5 (request stream)")
     ap.add_argument("--n2d", type=int, default=200, help="cyl2d: lattice edge (r and z)")
+    ap.add_argument("--no-solve", action="store_true", help="cyl2d: skip the timed full solves")
     ap.add_argument("--rate", type=float, default=20.0, help="served: arrivals per second")
     ap.add_argument("--requests", type=int, default=200, help="served: requests in the stream")
     ap.add_argument("--workers", type=int, default=8, help="served: concurrent solves")
