@@ -7,8 +7,7 @@
 //     (1 gradient), the worker takes it and every other waiting 1-gradient
 //     request, up to max_batch, and solves them in one k_batch1d launch;
 //   - otherwise it takes that request alone into a device context (2-D,
-//     3-D; FP32 propagators where the context supports them: 2-D and 3-D
-//     simple-cubic linear chains).
+//     3-D; FP32 propagators for 3-D simple-cubic linear chains).
 // Work is admitted by device footprint: a request (or group) starts only when
 // its estimated memory fits beside what is already running, so memory never
 // oversubscribes; a request larger than the whole budget is rejected at
@@ -117,10 +116,12 @@ void Server::run_batch(std::vector<Request*>& group, cudaStream_t st) {
 }
 
 void Server::run_single(Request* r, cudaStream_t st) {
-    // FP32 propagators where the context has them (3-D simple-cubic and 2-D
-    // linear chains); FP64 otherwise
+    // FP32 propagators where they are the faster path (3-D simple-cubic
+    // linear chains); FP64 otherwise.  2-D contexts have FP32 propagators
+    // too, but their per-step kernels are latency-bound and measured slower
+    // in FP32 (row maxima per step, a DIIS restart at the handover).
     int prec = opt.precision;
-    if (prec == NM_FP32 && !ctx3d_eligible(r->plan, nullptr) && !ctx2d32_eligible(r->plan, nullptr)) prec = NM_FP64;
+    if (prec == NM_FP32 && !ctx3d_eligible(r->plan, nullptr)) prec = NM_FP64;
     nm_ctx_options o{prec, 0, opt.device, st};
     nm_ctx* c = nullptr;
     int rc = nm_ctx_create(r->plan, &o, &c);

@@ -40,9 +40,9 @@ def _alone(plan, x, precision):
         xx = x.copy()
         its, res, st = Batch([plan], precision).solve_host(xx)
         return int(its[0]), float(res[0]), int(st[0]), xx
-    # the server uses FP32 propagators in a context where it has them (2-D and
-    # 3-D simple-cubic linear chains; the 3-D hexagonal fixture is left out above)
-    prec = precision if (precision == NM_FP64 or plan.c.gradients in (2, 3)) else NM_FP64
+    # the server uses FP32 propagators in a context only for 3-D simple-cubic
+    # linear chains (the 3-D hexagonal fixture is left out above)
+    prec = precision if (precision == NM_FP64 or plan.c.gradients == 3) else NM_FP64
     ctx = Context(plan, prec)
     xx = x.copy()
     r, _ = ctx.solve_host(xx)
