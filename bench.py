@@ -391,9 +391,12 @@ def run_cyl2d(args) -> None:
     chis = (0.0, 0.5)
     plans = [cyl2d_plan(nx, ny, 500, 0.02, c, args.iters) for c in chis]
     solve_plans = [cyl2d_plan(nx, ny, 500, 0.02, c, 20000) for c in chis]
-    rng = np.random.default_rng(SEED)
-    x0h = rng.uniform(-0.01, 0.01, size=plans[0].iv)
-    x0 = torch.from_numpy(x0h).cuda()
+    # one seeded field per plan: the iteration vector's length depends on chi
+    # (at chi_AS = 0 every segment shares one chi row, one iteration species)
+    x0h = [np.random.default_rng(SEED + i).uniform(-0.01, 0.01, size=p.iv) for i, p in enumerate(plans)]
+    for p, sp, xh in zip(plans, solve_plans, x0h):
+        assert p.iv == sp.iv == xh.size
+    x0 = [torch.from_numpy(xh).cuda() for xh in x0h]
     flush = torch.empty(int(256e6) // 4, dtype=torch.float32, device="cuda")
     streams = [torch.cuda.Stream() for _ in chis]
 
@@ -407,15 +410,15 @@ def run_cyl2d(args) -> None:
     out = {}
     for prec, name in ((NM_FP32, "fp32"), (NM_FP64, "fp64")):
         ctxs = [Context(p, prec, stream=st.cuda_stream) for p, st in zip(plans, streams)]
-        xw = [torch.empty_like(x0) for _ in chis]
+        xw = [torch.empty_like(x) for x in x0]
         times, its = [], []
         res = [None, None]
         clocks = ClockSampler(0)
         with clocks:
             for k in range(args.warmup + args.steps):
                 flush.zero_()
-                for w in xw:
-                    w.copy_(x0)
+                for w, x in zip(xw, x0):
+                    w.copy_(x)
                 torch.cuda.synchronize()
                 ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in chis]
                 for (e0, _), st in zip(ev, streams):
@@ -436,14 +439,14 @@ def run_cyl2d(args) -> None:
         out[name] = {"ms_per_step": ms, "residuals_per_step": n_its, "iterations_per_s": 1000.0 * n_its / ms,
                      "residual_after_step": [r.residual for r in res],
                      "launches": sum(c.launch_count() for c in ctxs), "clocks": clocks.summary()}
-        gd = torch.zeros_like(x0)
-        ctxs[1].residual_dev(x0.data_ptr(), gd.data_ptr())
+        gd = torch.zeros_like(x0[1])
+        ctxs[1].residual_dev(x0[1].data_ptr(), gd.data_ptr())
         out[name]["phi"] = ctxs[1].field(0)
         for c in ctxs:
             c.close()
         if not args.no_solve:
             sctx = [Context(p, prec, stream=st.cuda_stream) for p, st in zip(solve_plans, streams)]
-            xs = [x0h.copy() for _ in chis]
+            xs = [xh.copy() for xh in x0h]
             rs = [None, None]
 
             def solve(i):
@@ -461,7 +464,7 @@ def run_cyl2d(args) -> None:
         b.build_oracle()
         from orc import Oracle
         orc = Oracle(plans[1])
-        rc, _ = orc.residual(x0h)
+        rc, _ = orc.residual(x0h[1])
         if rc == 0:
             mask = np.tile(plans[1].interior_mask(), plans[1].n_seg)
             po = orc.field(0)[mask]

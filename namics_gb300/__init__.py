@@ -40,6 +40,12 @@ def _dptr(a: np.ndarray):
     return a.ctypes.data_as(_abi.dp)
 
 
+def _check_len(x: np.ndarray, n: int, what: str) -> None:
+    # the library reads and writes exactly n doubles of a host array
+    if x.size != n:
+        raise ValueError(f"{what}: x has {x.size} entries, the problem needs {n}")
+
+
 class Plan:
     """A compiled problem: Namics input text -> lattice, segments, molecules."""
 
@@ -160,6 +166,7 @@ class Context:
 
     def solve_host(self, x: np.ndarray, want_phi: bool = True) -> tuple[SolveResult, np.ndarray | None]:
         x = np.ascontiguousarray(x, dtype=np.float64)
+        _check_len(x, self.plan.iv, "Context.solve_host")
         phi = np.empty(self.plan.n_seg * self.plan.M) if want_phi else None
         r = _abi.nm_solve_result()
         rc = _abi.load().nm_solve_host(self._h, _dptr(x), _dptr(phi) if want_phi else None, C.byref(r))
@@ -239,6 +246,7 @@ class Batch:
         return it, res, st
 
     def solve_host(self, x: np.ndarray):
+        _check_len(x, self.total, "Batch.solve_host")
         n = len(self.plans)
         it = np.zeros(n, dtype=np.int32)
         res = np.zeros(n)
@@ -287,6 +295,7 @@ class Server:
 
     def submit(self, plan: Plan, x: np.ndarray) -> int:
         x = np.ascontiguousarray(x, dtype=np.float64)
+        _check_len(x, plan.iv, "Server.submit")
         rid = C.c_longlong()
         _check(_abi.load().nm_server_submit(self._h, plan.ptr, _dptr(x), C.byref(rid)))
         self._plans[rid.value] = plan  # kept alive until waited for
