@@ -169,10 +169,6 @@ int nm_ctx_destroy(nm_ctx* ctx);
  * instead of one launch per segment step.  Same arithmetic, same results;
  * on GB300 the per-step launches are the faster of the two. */
 #define NM_OPT_SWEEP2D 1
-/* NM_OPT_MARCH3D (default 1): the FP32 3-D simple-cubic steps march along x
- * with the x neighbours in registers; 0 selects the gather kernel (same
- * arithmetic, same results). */
-#define NM_OPT_MARCH3D 2
 int nm_ctx_set_option(nm_ctx* ctx, int option, int value);
 
 /* One residual evaluation g(x) on device buffers of length plan->iv.

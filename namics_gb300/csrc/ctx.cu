@@ -1068,9 +1068,8 @@ int nm_ctx_destroy(nm_ctx* ctx) {
 int nm_ctx_set_option(nm_ctx* ctx, int option, int value) {
     Ctx* c = reinterpret_cast<Ctx*>(ctx);
     if (!c) { nm::set_error("nm_ctx_set_option: null context"); return NM_ERR_ARG; }
-    if (option == NM_OPT_SWEEP2D) c->sweep2d = value != 0;
-    else if (option == NM_OPT_MARCH3D) c->march3d = value != 0;
-    else { nm::set_error("nm_ctx_set_option: unknown option"); return NM_ERR_ARG; }
+    if (option != NM_OPT_SWEEP2D) { nm::set_error("nm_ctx_set_option: unknown option"); return NM_ERR_ARG; }
+    c->sweep2d = value != 0;
     if (c->graph) {  // the captured residual used the other kernels
         cudaGraphExecDestroy(c->graph);
         c->graph = nullptr;

@@ -123,79 +123,6 @@ __global__ void __launch_bounds__(128) k3_prop(L3 L, const T* __restrict__ in, c
     }
 }
 
-// FP32 steps that march along x (modes 0 and 3 of k3_prop, same arithmetic
-// in the same order, so the same results).  A block owns a C25_TZ × C25_TY
-// column tile of (z, y) and C25_XC consecutive planes x; each thread keeps
-// its column's planes x-1, x and x+1 in registers (the plane after next is
-// loaded one plane ahead), so the x neighbours come from registers instead
-// of two more planes gathered through L2, and the y and z neighbours of the
-// current plane from L1.  Each input element is then fetched from L2 about
-// once per block instead of three times.
-#define C25_TZ 32
-#define C25_TY 8
-#define C25_XC 16
-
-template <int MODE>
-__global__ void __launch_bounds__(C25_TZ * C25_TY) k3f_march(L3 L, const float* __restrict__ in,
-                                                             const float* __restrict__ G1, float* __restrict__ out,
-                                                             unsigned* __restrict__ maxbits, int* __restrict__ E,
-                                                             int sin, int sout, const float* __restrict__ Gf, int sgf,
-                                                             int sroot, float* __restrict__ rhi,
-                                                             float* __restrict__ rlo, float d) {
-    const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * C25_TZ + tz;
-    const int z = blockIdx.x * C25_TZ + tz + 1, y = blockIdx.y * C25_TY + ty + 1;
-    const int xa = blockIdx.z * C25_XC + 1, xb = min(L.MX, xa + C25_XC - 1);
-    const bool act = z <= L.MZ && y <= L.MY;
-    const int zc = min(z, L.MZ), yc = min(y, L.MY);  // inactive threads read valid sites
-    unsigned mb = maxbits[sin * C3_SLOTS + (tid & 31)];
-    for (int o = 16; o > 0; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
-    const int e = c3_expo(__uint_as_float(mb));
-    const float f = c3_p2f(-e) * (1.0f / 6.0f);
-    const int Eout = E[sin] + e;
-    const int zm = c3_map(zc - 1, L.MZ, L.b1z, L.bmz), zp = c3_map(zc + 1, L.MZ, L.b1z, L.bmz);
-    const int ym = c3_map(yc - 1, L.MY, L.b1y, L.bmy), yp = c3_map(yc + 1, L.MY, L.b1y, L.bmy);
-    const int yz = yc * L.JY + zc;
-    const float* col = in + yz;  // this column's element of a plane: col[x·JX]
-    float prev = col[c3_map(xa - 1, L.MX, L.b1x, L.bmx) * L.JX];
-    float cur = col[xa * L.JX];
-    float next = col[c3_map(xa + 1, L.MX, L.b1x, L.bmx) * L.JX];
-    float vmax = 0.f;
-    for (int x = xa; x <= xb; x++) {
-        // the plane after next, one plane ahead of its use
-        const float nn = x + 1 <= xb ? col[c3_map(x + 2, L.MX, L.b1x, L.bmx) * L.JX] : 0.f;
-        const int xz = x * L.JX + zc, xy = x * L.JX + yc * L.JY;
-        const float s6 = ((prev + next) + (in[xz + ym * L.JY] + in[xz + yp * L.JY])) + (in[xy + zm] + in[xy + zp]);
-        const int s = x * L.JX + yz;
-        const float v = s6 * f * G1[s];
-        if (act) {
-            out[s] = v;
-            if (MODE == 3) {
-                const int Es = E[sgf] + Eout - E[sroot], h = Es >> 1;
-                const float sa = c3_p2f(min(h, 127)), sb = c3_p2f(min(Es - h, 127));
-                const float yv = (Gf[s] * sa) * (v * sb * d) - rlo[s];
-                const float t2 = rhi[s] + yv;
-                rlo[s] = (t2 - rhi[s]) - yv;
-                rhi[s] = t2;
-            }
-            vmax = fmaxf(vmax, v);
-        }
-        prev = cur;
-        cur = next;
-        next = nn;
-    }
-    float m = vmax;
-    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    __shared__ float wm[C25_TZ * C25_TY / 32];
-    if ((tid & 31) == 0) wm[tid >> 5] = m;
-    __syncthreads();
-    if (tid == 0) {
-        for (int i = 1; i < C25_TZ * C25_TY / 32; i++) m = fmaxf(m, wm[i]);
-        const int b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-        if (m > 0.f) atomicMax(&maxbits[sout * C3_SLOTS + (b & (C3_SLOTS - 1))], __float_as_uint(m));
-        if (b == 0) E[sout] = Eout;
-    }
-}
-
 // Σ_interior of an FP32 vector (FP64 partial sums), G(N) = Σ·2^E(root), and
 // the true-scale FP64 ρ
 __global__ void k3_wsum32(L3 L, const float* __restrict__ X, double* __restrict__ partial) {
@@ -270,14 +197,6 @@ template <typename T, int MODE>
 static void k3(Ctx& C, const T* in, const T* G1, T* out, int sin, int sout, const T* Gf, int sgf, int sroot, T* rhi,
                T* rlo, double d) {
     const nm_plan* p = C.plan;
-    if (sizeof(T) == 4 && (MODE == 0 || MODE == 3) && C.march3d) {
-        dim3 g((p->MZ + C25_TZ - 1) / C25_TZ, (p->MY + C25_TY - 1) / C25_TY, (p->MX + C25_XC - 1) / C25_XC);
-        k3f_march<MODE == 3 ? 3 : 0><<<g, dim3(C25_TZ, C25_TY), 0, C.stream>>>(
-            C.l3, (const float*)in, (const float*)G1, (float*)out, C.d_maxbits, C.d_E, sin, sout, (const float*)Gf,
-            sgf, sroot, (float*)rhi, (float*)rlo, (float)d);
-        C.launches++;
-        return;
-    }
     dim3 grid((p->MZ + 127) / 128, (p->MY + C3_RY - 1) / C3_RY, p->MX);
     k3_prop<T, MODE><<<grid, 128, 0, C.stream>>>(C.l3, in, G1, out, C.d_maxbits, C.d_E, sin, sout, Gf, sgf, sroot, rhi,
                                                  rlo, (T)d);

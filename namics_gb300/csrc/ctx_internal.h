@@ -187,7 +187,6 @@ struct Ctx {
     // persistent 2-D sweeps: one cooperative launch per sweep (ctx2d.cu)
     bool use2d = false;      // eligible and set up
     bool sweep2d = false;    // nm_ctx_set_option(NM_OPT_SWEEP2D)
-    bool march3d = true;     // nm_ctx_set_option(NM_OPT_MARCH3D): x-marching FP32 3-D steps
     int sw_rows = 0, sw_ctas = 0;
     int* d_flags = nullptr;  // per-CTA step published
     std::vector<SweepTab> sw_tabs;

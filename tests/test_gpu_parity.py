@@ -366,41 +366,3 @@ def test_context_fp32_rejects_unsupported_plan():
     run = load_golden("brush1d_cfg1")["runs"]["conv"]
     with pytest.raises(NamicsError):
         Context(Plan(run["input"]), NM_FP32)
-
-
-def test_context_fp32_3d_march_equals_gather():
-    """The x-marching FP32 3-D step kernels (NM_OPT_MARCH3D, the default) and
-    the gather kernels sum the same values in the same order: residuals and a
-    few DIIS iterations must be bit-identical."""
-    from namics_gb300._abi import NM_OPT_MARCH3D
-    run = load_golden("melt3d")["runs"]["it0"]
-    plan = Plan(_solve_tight(run["input"], tol="1e-9", itlim=8))
-    x0 = np.array(run["x"])
-    out = []
-    for march in (0, 1):
-        ctx = Context(plan, NM_FP32)
-        ctx.set_option(NM_OPT_MARCH3D, march)
-        xd, gd = dev(x0), torch.zeros(plan.iv, dtype=torch.float64, device="cuda")
-        ctx.residual_dev(xd.data_ptr(), gd.data_ptr())
-        g = host(gd).copy()
-        x = x0.copy()
-        r, phi = ctx.solve_host(x)
-        out.append((g, r, x, phi))
-    (g0, r0, x0_, p0), (g1, r1, x1_, p1) = out
-    assert np.array_equal(g0, g1)
-    assert r0.iterations == r1.iterations and r0.residual == r1.residual
-    assert np.array_equal(x0_, x1_) and np.array_equal(p0, p1)
-    # a 40³ periodic box: three x chunks (the last partial) and a partial z tile
-    import bench
-    big = Plan(bench.melt3d_text(40, 3))
-    rng = np.random.default_rng(5)
-    u = rng.uniform(-0.1, 0.1, size=big.M)
-    xb = np.concatenate([u, -u])
-    gs = []
-    for march in (0, 1):
-        ctx = Context(big, NM_FP32)
-        ctx.set_option(NM_OPT_MARCH3D, march)
-        xd, gd = dev(xb), torch.zeros(big.iv, dtype=torch.float64, device="cuda")
-        ctx.residual_dev(xd.data_ptr(), gd.data_ptr())
-        gs.append(host(gd).copy())
-    assert np.array_equal(gs[0], gs[1])
