@@ -47,8 +47,6 @@ struct B1Mol {
     int* epc;            // [n_blocks][128]
     void* Q;             // [n_blocks] vectors: backward start of each block
     int* eq;             // [n_blocks][128]
-    void* Gb;            // [n_store] FP32 backward propagators [128·SP] (FP32 phase)
-    int* eb;             // [n_store][128]
 };
 
 struct B1Prob {
@@ -945,11 +943,6 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
             TRYB(B.alloc(&epc, BC_NT * (size_t)mol.n_blocks));
             TRYB(B.alloc(&eq, BC_NT * (size_t)mol.n_blocks));
             D.ef = ef; D.epc = epc; D.eq = eq;
-            char* gbv;
-            int* ebv;
-            TRYB(B.alloc(&gbv, (size_t)4 * BC_NT * b1_sp(P->MX) * mol.n_store));
-            TRYB(B.alloc(&ebv, BC_NT * (size_t)mol.n_store));
-            D.Gb = gbv; D.eb = ebv;
             for (int j = 0; j < mol.n_molmon; j++) {
                 if (kk >= NM_MAX_MM) { set_error("too many (molecule, segment) pairs"); return NM_ERR_INPUT; }
                 H.mm_mol[kk] = m; H.mm_seg[kk] = mol.molmon_seg[j]; H.mm_frac[kk] = mol.molmon_fraction[j];
@@ -1250,8 +1243,6 @@ static int noalloc_layout(const nm_plan* P, StaticArena& A, double* x_dev, B1Pro
             D.ef = A.take<int>(BC_NT * (size_t)mol.n_store);
             D.epc = A.take<int>(BC_NT * (size_t)mol.n_blocks);
             D.eq = A.take<int>(BC_NT * (size_t)mol.n_blocks);
-            D.Gb = A.take<char>((size_t)4 * BC_NT * b1_sp(P->MX) * mol.n_store);
-            D.eb = A.take<int>(BC_NT * (size_t)mol.n_store);
             if (A.overflow) goto full;
             put(db, mol.blocks, sizeof(nm_block) * mol.n_blocks);
             if (mol.n_blocks > 1) put(dci, mol.child_index, sizeof(int) * nci);

@@ -378,8 +378,6 @@ __device__ void bc_residual(B1Prob& P, const Lat1 L, const Coef<double> C64, B1S
         int* __restrict__ ef = D.ef;    // [n_store][128] thread exponents of Gf
         int* __restrict__ epc = D.epc;  // [n_blocks][128]
         int* __restrict__ eqb = D.eq;   // [n_blocks][128]
-        float* __restrict__ Gbs = (float*)D.Gb;  // [n_store] backward propagators, as Gf
-        int* __restrict__ ebs = D.eb;            // [n_store][128]
         // ---- forward sweep (post-order: children before parents) ----
         for (int b = 0; b < D.n_blocks; b++) {
             const nm_block B = D.blocks[b];
@@ -548,15 +546,12 @@ __device__ void bc_residual(B1Prob& P, const Lat1 L, const Coef<double> C64, B1S
                 acc[j] = 0.f;
                 cmp[j] = 0.f;
             }
-            // The backward sweep stores each Gb(s) with its exponents, as the
-            // forward sweep stores Gf(s); the composition then runs over the
-            // stored rows after the sweep, in the same order with the same
-            // operations, off the step-to-step chain of barriers.
-            float* __restrict__ gbp = Gbs + (size_t)top * Wl + t;
-            int* __restrict__ ebp = ebs + top * BC_NT + t;
+            {
+                float gf0[SP];
 #pragma unroll
-            for (int j = 0; j < SP; j++) gbp[j * BC_NT] = cur[j];
-            *ebp = st.E;
+                for (int j = 0; j < SP; j++) gf0[j] = Gf[(size_t)top * Wl + j * BC_NT + t];
+                bc_comp<SP>(gf0, ef[top * BC_NT + t], cur, winv, st.E, ebase, acc, cmp);
+            }
             float aL[SP], aC[SP], aR[SP];
 #pragma unroll
             for (int j = 0; j < SP; j++) {
@@ -565,21 +560,29 @@ __device__ void bc_residual(B1Prob& P, const Lat1 L, const Coef<double> C64, B1S
                 aR[j] = cRs[j * BC_NT + t] * wr[j];
             }
             // steps k = 1 .. length-1 (segments top-1 down to s0) in groups of
-            // BC_RS, the group's first step settling the previous rescale
+            // BC_RS; each group's stored Gf rows were loaded a group earlier
             const int nsteps = B.length - 1;
-            int k = 0;
-            for (; k + BC_RS <= nsteps; k += BC_RS) {
+            float rows[BC_RS][SP];
+            int erows[BC_RS];
+            bc_rows<SP>(Gf, ef, top - 1, B.s0, Wl, t, rows, erows);
+            int k = 0, s = top - 1;
+            for (; k + BC_RS <= nsteps; k += BC_RS, s -= BC_RS) {
+                float nrows[BC_RS][SP];
+                int nerows[BC_RS];
+                bc_rows<SP>(Gf, ef, s - BC_RS, B.s0, Wl, t, nrows, nerows);
 #pragma unroll
                 for (int i = 0; i < BC_RS; i++) {
                     if (i == 0) bc_xs<SP, PER, true>(cur, aL, aC, aR, G, st, par, X);
                     else bc_xs<SP, PER, false>(cur, aL, aC, aR, G, st, par, X);
                     st.E += eg;
                     if (i == BC_RS - 1) bc_lnorm<SP>(cur, st);
-                    gbp -= Wl;
-                    ebp -= BC_NT;
+                    bc_comp<SP>(rows[i], erows[i], cur, winv, st.E, ebase, acc, cmp);
+                }
 #pragma unroll
-                    for (int j = 0; j < SP; j++) gbp[j * BC_NT] = cur[j];
-                    *ebp = st.E;
+                for (int i = 0; i < BC_RS; i++) {
+                    erows[i] = nerows[i];
+#pragma unroll
+                    for (int j = 0; j < SP; j++) rows[i][j] = nrows[i][j];
                 }
             }
 #pragma unroll
@@ -588,24 +591,8 @@ __device__ void bc_residual(B1Prob& P, const Lat1 L, const Coef<double> C64, B1S
                     if (st.resc) bc_xs<SP, PER, true>(cur, aL, aC, aR, G, st, par, X);
                     else bc_xs<SP, PER, false>(cur, aL, aC, aR, G, st, par, X);
                     st.E += eg;
-                    gbp -= Wl;
-                    ebp -= BC_NT;
-#pragma unroll
-                    for (int j = 0; j < SP; j++) gbp[j * BC_NT] = cur[j];
-                    *ebp = st.E;
+                    bc_comp<SP>(rows[i], erows[i], cur, winv, st.E, ebase, acc, cmp);
                 }
-            }
-            // composition, segments top down to s0 (each thread reads back
-            // only what it stored)
-#pragma unroll 4
-            for (int sg = top; sg >= B.s0; sg--) {
-                float gfv[SP], gbv[SP];
-#pragma unroll
-                for (int j = 0; j < SP; j++) {
-                    gfv[j] = Gf[(size_t)sg * Wl + j * BC_NT + t];
-                    gbv[j] = Gbs[(size_t)sg * Wl + j * BC_NT + t];
-                }
-                bc_comp<SP>(gfv, ef[sg * BC_NT + t], gbv, winv, ebs[sg * BC_NT + t], ebase, acc, cmp);
             }
 #pragma unroll
             for (int j = 0; j < SP; j++) rr[j * BC_NT + t] += acc[j] - cmp[j];
