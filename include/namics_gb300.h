@@ -136,6 +136,8 @@ typedef struct nm_plan {
     /* solver (newton : ... keys) */
     int    diis_m, iterationlimit, max_norm;
     double tolerance, deltamax;
+    /* molecule names, in the order of `mols` (the `mol : <name>` keys) */
+    const char* const* mol_name;
 } nm_plan;
 
 /* Parse Namics input text (the `lat/mon/mol/sys/newton` key subset of the
@@ -205,6 +207,19 @@ int nm_get_molecule(nm_ctx* ctx, int mol, double* GN, double* n,
 /* Free energy, grand potential and chemical potentials (mu: [n_mol]) of
  * the state of the last residual evaluation (system.cpp:2809-3244). */
 int nm_free_energy(nm_ctx* ctx, double* F, double* Omega, double* mu);
+
+/* Outputs of the last residual evaluation in the reference's file layouts
+ * (Output::WriteOutput, output.cpp:385-564; LGrad*::PutProfiles).  items:
+ * the `key : name : property` triples of an input's output block.
+ * nm_write_pro: profiles, interior sites, one row per site ("mon : <seg> :
+ * phi|G1", "mol : <mol> : phi", "sys : <any> : alpha|phitot", charged also
+ * "sys : <any> : psi|q|eps").  nm_write_kal: one header line (unless
+ * append) and one line of scalars ("sys : <any> : free_energy|
+ * grand_potential", "newton : <any> : residual|iterations" from res,
+ * "mol : <mol> : GN|n|theta|phibulk|Mu").  An unknown item is NM_ERR_ARG. */
+int nm_write_pro(nm_ctx* ctx, const char* path, const char* const* items, int n_items);
+int nm_write_kal(nm_ctx* ctx, const char* path, const char* const* items, int n_items,
+                 const nm_solve_result* res, int append);
 
 /* Unit-testable pieces on device arrays of length M.
  * nm_propagate: G_out = Side(set_bounds(G_in))·G1 (Lattice::propagate,

@@ -202,6 +202,22 @@ class Context:
     def launch_count(self) -> int:
         return int(_abi.load().nm_ctx_launch_count(self._h))
 
+    def write_pro(self, path: str, items: list[str]) -> None:
+        """Profiles of the last residual in the reference's .pro layout."""
+        arr = (C.c_char_p * len(items))(*[s.encode() for s in items])
+        _check(_abi.load().nm_write_pro(self._h, str(path).encode(), arr, len(items)))
+
+    def write_kal(self, path: str, items: list[str], result: SolveResult | None = None,
+                  append: bool = False) -> None:
+        """Scalars of the last residual (and of `result`) in the .kal layout."""
+        arr = (C.c_char_p * len(items))(*[s.encode() for s in items])
+        r = None
+        if result is not None:
+            r = _abi.nm_solve_result()
+            r.iterations, r.residual, r.status = result.iterations, result.residual, result.status
+        _check(_abi.load().nm_write_kal(self._h, str(path).encode(), arr, len(items),
+                                        C.byref(r) if r is not None else None, int(append)))
+
     def set_option(self, option: int, value: int) -> None:
         _check(_abi.load().nm_ctx_set_option(self._h, option, value))
 

@@ -53,7 +53,7 @@ class nm_plan(C.Structure):
                 ("iv", C.c_int), ("charged", C.c_int), ("n_mol", C.c_int),
                 ("mols", C.POINTER(nm_molecule)), ("solvent", C.c_int), ("neutralizer", C.c_int),
                 ("diis_m", C.c_int), ("iterationlimit", C.c_int), ("max_norm", C.c_int),
-                ("tolerance", C.c_double), ("deltamax", C.c_double)]
+                ("tolerance", C.c_double), ("deltamax", C.c_double), ("mol_name", C.POINTER(C.c_char_p))]
 
 
 class nm_ctx_options(C.Structure):
@@ -87,6 +87,9 @@ SIGNATURES = [
     ("nm_get_field", C.c_int, [C.c_void_p, C.c_int, dp]),
     ("nm_get_molecule", C.c_int, [C.c_void_p, C.c_int, dp, dp, dp, dp]),
     ("nm_free_energy", C.c_int, [C.c_void_p, dp, dp, dp]),
+    ("nm_write_pro", C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_char_p), C.c_int]),
+    ("nm_write_kal", C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_char_p), C.c_int,
+                               C.POINTER(nm_solve_result), C.c_int]),
     ("nm_propagate_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("nm_side_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("nm_ctx_launch_count", C.c_longlong, [C.c_void_p]),

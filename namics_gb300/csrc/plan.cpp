@@ -832,6 +832,9 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
     }
     P.n_mol = nmol;
     P.mols = H->mols.data();
+    H->mol_names.assign(molnames.begin(), molnames.end());
+    for (auto& s : H->mol_names) H->mol_name_ptrs.push_back(s.c_str());
+    P.mol_name = H->mol_name_ptrs.data();
     return &H->plan;
 }
 

@@ -32,6 +32,8 @@ struct PlanHolder {
     std::vector<double> seg_mask, seg_gmask, seg_phi_frozen, chi, seg_valence, seg_epsilon;
     std::vector<MolBuild> mb;
     std::vector<nm_molecule> mols;
+    std::vector<std::string> mol_names;
+    std::vector<const char*> mol_name_ptrs;
     std::string method_note;
 };
 

@@ -287,14 +287,44 @@ def run_case(case: dict, mode: str, workdir: Path) -> dict:
         raise RuntimeError(f"reference failed on {tag}: {r.stdout[-1500:]} {r.stderr[-500:]}")
     prod = parse_pro(pro, plan.c.gradients)
     kald = parse_kal(kal)
-    return dict(input=text, x=x.tolist(), mode=mode, iterationlimit=itlim,
-                pro_header=prod["header"], pro=prod["data"].tolist(), kal=kald,
-                molnames=MOLNAMES)
+    out = dict(input=text, x=x.tolist(), mode=mode, iterationlimit=itlim,
+               pro_header=prod["header"], pro=prod["data"].tolist(), kal=kald,
+               molnames=MOLNAMES)
+    if case.get("raw"):
+        # the reference's files verbatim, and the output items that made them
+        out["pro_text"] = pro.read_text()
+        out["kal_text"] = kal.read_text()
+        ob = outputs_block(plan)
+        out["pro_items"] = [ln for ln in ob if ln.startswith("pro :")]
+        out["kal_items"] = [ln for ln in ob if ln.startswith("kal :")]
+    return out
+
+
+RAW_CASES = ["brush1d_cfg1", "brush2d_cyl", "melt3d", "charged1d"]
+
+
+def main_raw():
+    """tests/golden/raw_outputs.json: the reference's .pro and .kal files,
+    verbatim, for the single-residual run of a 1-D, a 2-D cylindrical, a 3-D
+    and a charged case (the file-format pin of nm_write_pro/nm_write_kal)."""
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        wd = Path(td)
+        (wd / "output").mkdir()
+        for case in cases():
+            if case["name"] in RAW_CASES:
+                case = dict(case, raw=True)
+                out[case["name"]] = run_case(case, "it0", wd)
+                print(case["name"], len(out[case["name"]]["pro_text"]), flush=True)
+    (GOLDEN / "raw_outputs.json").write_text(json.dumps(out))
 
 
 def main():
     if not REF_BIN.exists():
         sys.exit(f"{REF_BIN} missing: build it with  make -f oracle/Makefile.ref")
+    if sys.argv[1:2] == ["--raw"]:
+        main_raw()
+        return
     only = set(sys.argv[1:])
     with tempfile.TemporaryDirectory() as td:
         wd = Path(td)
