@@ -142,6 +142,7 @@ int nm_write_kal(nm_ctx* ctx, const char* path, const char* const* items, int n_
     double F = 0, Om = 0;
     std::vector<double> mu(p->n_mol);
     bool have_fe = false;
+    std::vector<double> molphi;
     struct Val { bool is_int; int i; double d; };
     std::vector<Val> vals;
     std::vector<std::string> heads;
@@ -172,10 +173,30 @@ int nm_write_kal(nm_ctx* ctx, const char* path, const char* const* items, int n_
                     if (rc) return rc;
                     v.d = mu[m];
                     ok = true;
-                } else if (prop == "GN" || prop == "n" || prop == "theta" || prop == "phibulk") {
+                } else if (prop == "theta") {
+                    // the amount in the system, Σ L·φ over the interior, as the
+                    // reference computes it for its output (molecule.cpp:2006-2009)
+                    const size_t M = p->M;
+                    if (molphi.empty()) {
+                        molphi.resize((size_t)p->n_mol * M);
+                        int rc = nm_get_field(ctx, 4, molphi.data());
+                        if (rc) return rc;
+                    }
+                    const bool w = p->gradients < 3 && p->geometry != NM_PLANAR;
+                    double sum = 0;
+                    const double* ph = molphi.data() + (size_t)m * M;
+                    for (int x = 1; x <= p->MX; x++)
+                        for (int y = (p->gradients > 1 ? 1 : 0); y <= (p->gradients > 1 ? p->MY : 0); y++)
+                            for (int z = (p->gradients > 2 ? 1 : 0); z <= (p->gradients > 2 ? p->MZ : 0); z++) {
+                                const size_t s = (size_t)x * p->JX + (size_t)y * p->JY + z;
+                                sum += w ? ph[s] * p->L[s] : ph[s];
+                            }
+                    v.d = sum;
+                    ok = true;
+                } else if (prop == "GN" || prop == "n" || prop == "phibulk") {
                     int rc = nm_get_molecule(ctx, m, &GN, &n, &th, &pb);
                     if (rc) return rc;
-                    v.d = prop == "GN" ? GN : prop == "n" ? n : prop == "theta" ? th : pb;
+                    v.d = prop == "GN" ? GN : prop == "n" ? n : pb;
                     ok = true;
                 }
             }
