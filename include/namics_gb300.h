@@ -173,6 +173,14 @@ int nm_ctx_destroy(nm_ctx* ctx);
 #define NM_OPT_SWEEP2D 1
 int nm_ctx_set_option(nm_ctx* ctx, int option, int value);
 
+/* Scans (the reference's Variate: variate.cpp, solve_scf.cpp:717-868): change
+ * values of a live context and solve again from its current field (a warm
+ * start).  items: "mon : <seg> : chi_<seg>" (set both ways), "mol : <mol> :
+ * n | theta" (restricted), "mol : <mol> : phibulk" (free).  All are applied,
+ * then checked: χ must keep the iteration species (segments with equal χ
+ * rows) unchanged.  On error nothing changes (NM_ERR_ARG, NM_ERR_INPUT). */
+int nm_ctx_set_values(nm_ctx* ctx, const char* const* items, const double* values, int n);
+
 /* One residual evaluation g(x) on device buffers of length plan->iv.
  * Replaces Solve_scf::residuals -> System::Classical_residual
  * (solve_scf.cpp:752-908, system.cpp:2087-2189). */

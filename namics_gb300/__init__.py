@@ -218,6 +218,13 @@ class Context:
         _check(_abi.load().nm_write_kal(self._h, str(path).encode(), arr, len(items),
                                         C.byref(r) if r is not None else None, int(append)))
 
+    def set_values(self, values: dict[str, float]) -> None:
+        """Change χ or a molecule's amount for the next solve (a scan step)."""
+        items = list(values)
+        arr = (C.c_char_p * len(items))(*[s.encode() for s in items])
+        v = np.ascontiguousarray([float(values[k]) for k in items], dtype=np.float64)
+        _check(_abi.load().nm_ctx_set_values(self._h, arr, _dptr(v), len(items)))
+
     def set_option(self, option: int, value: int) -> None:
         _check(_abi.load().nm_ctx_set_option(self._h, option, value))
 

@@ -81,6 +81,7 @@ SIGNATURES = [
     ("nm_ctx_create", C.c_int, [P_plan, C.POINTER(nm_ctx_options), C.POINTER(C.c_void_p)]),
     ("nm_ctx_destroy", C.c_int, [C.c_void_p]),
     ("nm_ctx_set_option", C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    ("nm_ctx_set_values", C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), dp, C.c_int]),
     ("nm_residual_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("nm_solve_dev", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(nm_solve_result)]),
     ("nm_solve_host", C.c_int, [C.c_void_p, dp, dp, C.POINTER(nm_solve_result)]),

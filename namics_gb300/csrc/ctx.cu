@@ -785,7 +785,7 @@ int Ctx::free_energy(double* F, double* Omega, double* mu) {
         a.seg_frozen[i] = plan->seg_freedom[i] == NM_SEG_FROZEN;
         a.seg_in_mol[i] = plan->seg_it[i] >= 0;
     }
-    for (int i = 0; i < ns * ns; i++) a.chi[i] = plan->chi[i];
+    for (int i = 0; i < ns * ns; i++) a.chi[i] = chi[i];
     for (int m = 0; m < plan->n_mol; m++) {
         const nm_molecule& mol = plan->mols[m];
         double N = mol.chainlength;
@@ -794,7 +794,7 @@ int Ctx::free_energy(double* F, double* Omega, double* mu) {
         for (int j = 0; j < mol.n_molmon; j++)
             for (int k = 0; k < mol.n_molmon; k++)
                 constant -= mol.molmon_fraction[j] * mol.molmon_fraction[k] *
-                            (plan->chi[mol.molmon_seg[j] * ns + mol.molmon_seg[k]] / 2);
+                            (chi[mol.molmon_seg[j] * ns + mol.molmon_seg[k]] / 2);
         a.cF2[m] = constant;
         a.invN[m] = 1.0 / N;
     }
@@ -822,7 +822,7 @@ int Ctx::free_energy(double* F, double* Omega, double* mu) {
                 for (int k = 0; k < ns; k++) {
                     double FB = 0;
                     for (int q = 0; q < mol.n_molmon; q++) if (mol.molmon_seg[q] == k) FB = mol.molmon_fraction[q];
-                    Mu = Mu - NA * (plan->chi[j * ns + k] / 2) * (spb[j] - FA) * (spb[k] - FB);
+                    Mu = Mu - NA * (chi[j * ns + k] / 2) * (spb[j] - FA) * (spb[k] - FB);
                 }
             }
             mu[i] = Mu;
@@ -992,7 +992,8 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
     norm_args.n_mm = k; phi_args.n_mm = k;
     res_args.ns = ns; res_args.nit = p->n_it;
     for (int i = 0; i < p->n_it; i++) res_args.it_seg[i] = p->it_seg[i];
-    for (int i = 0; i < ns * ns; i++) res_args.chi[i] = p->chi[i];
+    chi.assign(p->chi, p->chi + (size_t)ns * ns);
+    for (int i = 0; i < ns * ns; i++) res_args.chi[i] = chi[i];
     CK(cudaStreamSynchronize(stream));
     return NM_OK;
 }
@@ -1062,6 +1063,70 @@ int nm_ctx_create(const nm_plan* plan, const nm_ctx_options* opt, nm_ctx** out) 
 
 int nm_ctx_destroy(nm_ctx* ctx) {
     delete reinterpret_cast<Ctx*>(ctx);
+    return NM_OK;
+}
+
+// Values of a live context for scans (the reference's Variate, variate.cpp,
+// solve_scf.cpp:717-868): χ between two segment types ("mon : A : chi_W",
+// set both ways) and a molecule's amount ("mol : pol : n | theta" for
+// restricted, "mol : pol : phibulk" for free molecules).  All items are
+// applied, then checked: χ must keep the iteration species (segments with
+// equal χ rows, System::IsUnique) as they were, because x's layout follows
+// them.  On any error nothing changes.  The captured residual is dropped;
+// the next solve starts from the context's current field.
+int nm_ctx_set_values(nm_ctx* ctx, const char* const* items, const double* values, int n) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c || (n > 0 && (!items || !values))) { nm::set_error("nm_ctx_set_values: bad argument"); return NM_ERR_ARG; }
+    const nm_plan* p = c->plan;
+    const int ns = p->n_seg;
+    std::vector<double> chi = c->chi;
+    nm::NormArgs na = c->norm_args;
+    auto trim = [](std::string s) {
+        size_t a = s.find_first_not_of(" \t"), b = s.find_last_not_of(" \t");
+        return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+    };
+    for (int i = 0; i < n; i++) {
+        std::string it = items[i] ? items[i] : "";
+        size_t p1 = it.find(':'), p2 = p1 == std::string::npos ? p1 : it.find(':', p1 + 1);
+        if (p2 == std::string::npos) { nm::set_error("nm_ctx_set_values: not a 'key : name : property' item: " + it); return NM_ERR_ARG; }
+        const std::string key = trim(it.substr(0, p1)), name = trim(it.substr(p1 + 1, p2 - p1 - 1)),
+                          prop = trim(it.substr(p2 + 1));
+        const double v = values[i];
+        bool ok = false;
+        if (key == "mon" && prop.rfind("chi_", 0) == 0) {
+            int a = -1, b = -1;
+            for (int k = 0; k < ns; k++) {
+                if (name == p->seg_name[k]) a = k;
+                if (prop.substr(4) == p->seg_name[k]) b = k;
+            }
+            if (a >= 0 && b >= 0 && a != b) { chi[a * ns + b] = chi[b * ns + a] = v; ok = true; }
+        } else if (key == "mol") {
+            for (int m = 0; m < p->n_mol; m++) {
+                if (!p->mol_name || name != p->mol_name[m]) continue;
+                nm::MolScal& S = na.mol[m];
+                if (S.freedom == NM_MOL_RESTRICTED && prop == "n") { S.n_in = v; S.theta_in = v * S.N; ok = true; }
+                else if (S.freedom == NM_MOL_RESTRICTED && prop == "theta") { S.theta_in = v; S.n_in = v / S.N; ok = true; }
+                else if (S.freedom == NM_MOL_FREE && prop == "phibulk") { S.phibulk_in = v; ok = true; }
+            }
+        }
+        if (!ok) { nm::set_error("nm_ctx_set_values: not a value this context can change: " + it); return NM_ERR_ARG; }
+    }
+    // the iteration species must stay: rows of χ equal within a species, different across
+    for (int a = 0; a < ns; a++)
+        for (int b = a + 1; b < ns; b++) {
+            if (p->seg_it[a] < 0 || p->seg_it[b] < 0) continue;
+            bool same = true;
+            for (int k = 0; k < ns; k++) same = same && chi[a * ns + k] == chi[b * ns + k];
+            if (same != (p->seg_it[a] == p->seg_it[b])) {
+                nm::set_error(std::string("nm_ctx_set_values: the new χ changes the iteration species (") +
+                              p->seg_name[a] + ", " + p->seg_name[b] + ")");
+                return NM_ERR_INPUT;
+            }
+        }
+    c->chi = chi;
+    for (int k = 0; k < ns * ns; k++) c->res_args.chi[k] = chi[k];
+    c->norm_args = na;
+    if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
     return NM_OK;
 }
 

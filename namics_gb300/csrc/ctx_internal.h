@@ -177,6 +177,7 @@ struct Ctx {
     NormArgs norm_args;
     PhiArgs phi_args;
     ResArgs res_args;
+    std::vector<double> chi;  // the context's χ (nm_ctx_set_values may change it)
     // electrostatics (charged systems, 1 and 2 gradients): ψ is the last
     // block of x; halo sites of the composition are evaluated (nh of them)
     bool charged = false;
