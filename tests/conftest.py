@@ -15,7 +15,9 @@ def pytest_configure(config):
 
 
 def golden_names():
-    return sorted(p.stem for p in GOLDEN.glob("*.json"))
+    """The per-case fixtures (raw_outputs.json, the reference's output files
+    verbatim, is read by test_outputs.py only)."""
+    return sorted(p.stem for p in GOLDEN.glob("*.json") if p.stem != "raw_outputs")
 
 
 def load_golden(name):
