@@ -518,6 +518,8 @@ static bool setup_lattice(const InputBlock& in, PlanHolder& H, std::string& err)
         } else {
             if (!to_int(get("n_layers_z"), P.MZ) || P.MZ < 1) { err = "lat n_layers_z required"; return false; }
             if (P.geometry != NM_PLANAR) { err = "3 gradients need planar geometry"; return false; }
+            // the reference's input check (lattice.cpp:513-516): a 3-D wall
+            // is a frozen layer inside the system, not a 'surface' bound
             for (int d = 0; d < 6; d++)
                 if (P.bc[d] == NM_BC_SURFACE) { err = "3-gradient lattices take mirror or periodic bounds"; return false; }
             P.JX = (P.MY + 2) * (P.MZ + 2); P.JY = P.MZ + 2; P.M = (P.MX + 2) * (P.MY + 2) * (P.MZ + 2);

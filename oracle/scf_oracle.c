@@ -362,6 +362,22 @@ static void set_M_bounds(orc_state* st, double* X) {
     const nm_plan* P = st->P;
     int MX = P->MX;
     if (P->gradients == 1) { X[0] = X[1]; X[MX + 1] = X[MX]; return; }
+    if (P->gradients == 3) {  /* LGrad3.cpp:1679-1702: the faces only */
+        int MY = P->MY, MZ = P->MZ, JX = P->JX, JY = P->JY;
+        for (int x = 1; x < MX + 1; x++) for (int y = 1; y < MY + 1; y++) {
+            X[x * JX + y * JY + 0] = X[x * JX + y * JY + 1];
+            X[x * JX + y * JY + MZ + 1] = X[x * JX + y * JY + MZ];
+        }
+        for (int y = 1; y < MY + 1; y++) for (int z = 1; z < MZ + 1; z++) {
+            X[0 + y * JY + z] = X[1 * JX + y * JY + z];
+            X[(MX + 1) * JX + y * JY + z] = X[MX * JX + y * JY + z];
+        }
+        for (int z = 1; z < MZ + 1; z++) for (int x = 1; x < MX + 1; x++) {
+            X[x * JX + 0 + z] = X[x * JX + 1 * JY + z];
+            X[x * JX + (MY + 1) * JY + z] = X[x * JX + MY * JY + z];
+        }
+        return;
+    }
     int MY = P->MY, JX = P->JX;
     for (int x = 1; x < MX + 1; x++) { X[x * JX + 0] = X[x * JX + 1]; X[x * JX + MY + 1] = X[x * JX + MY]; }
     for (int y = 1; y < MY + 1; y++) { X[0 + y] = X[1 * JX + y]; X[(MX + 1) * JX + y] = X[MX * JX + y]; }
@@ -413,6 +429,22 @@ static void update_EE(orc_state* st, double* EE, double* psi) {
                 EE[x] = pf * (Exmin + Explus) / L[x];
             }
         }
+        return;
+    }
+    if (P->gradients == 3) {
+        /* LGrad3::UpdateEE (LGrad3.cpp:1131-1139): squared differences along
+         * z, x and y over the flat array (AddGradSquare, tools_host.h:444),
+         * then the prefactor */
+        int JX = P->JX, JY = P->JY;
+        int d3[3] = {1, JX, JY};
+        for (int a = 0; a < 3; a++) {
+            int d = d3[a];
+            for (int i = 0; i < M - 2 * d; i++) {
+                double u = psi[i] - psi[i + d], w = psi[i + d] - psi[i + 2 * d];
+                EE[i + d] += u * u + w * w;
+            }
+        }
+        Norm(EE, pf, M);
         return;
     }
     int MY = P->MY, JX = P->JX;
@@ -489,6 +521,28 @@ static void update_psi(orc_state* st, double* g, const double* psi, const double
                 X[x] = (epsXmin * a + C * q[x] * L[x] + epsXplus * c) / (epsXmin + epsXplus);
             }
         }
+    } else if (P->gradients == 3) {
+        /* LGrad3::UpdatePsi (LGrad3.cpp:1155-1215), not-fixed-ψ0 branch with
+         * an empty mask: a forward and a backward Gauss-Seidel sweep in place
+         * on psi; the backward sweep subtracts the new psi from g */
+        int MY = P->MY, MZ = P->MZ, JX = P->JX, JY = P->JY;
+        double* ps = (double*)psi;
+        for (int pass = 0; pass < 2; pass++) {
+            for (int xi = 1; xi < MX + 1; xi++)
+                for (int yi = 1; yi < MY + 1; yi++)
+                    for (int zi = 1; zi < MZ + 1; zi++) {
+                        int x = pass ? MX + 1 - xi : xi, y = pass ? MY + 1 - yi : yi, z = pass ? MZ + 1 - zi : zi;
+                        int i = x * JX + y * JY + z;
+                        double ezm = eps[i - 1] + eps[i], ezp = eps[i] + eps[i + 1];
+                        double eym = eps[i] + eps[i - JY], eyp = eps[i] + eps[i + JY];
+                        double exm = eps[i] + eps[i - JX], exp_ = eps[i] + eps[i + JX];
+                        ps[i] = (exm * ps[i - JX] + exp_ * ps[i + JX] + eym * ps[i - JY] + eyp * ps[i + JY] +
+                                 ezm * ps[i - 1] + ezp * ps[i + 1] + C * q[i]) /
+                                (exm + exp_ + eym + eyp + ezm + ezp);
+                        if (pass) g[i] -= ps[i];
+                    }
+        }
+        return;
     } else if (P->geometry == NM_PLANAR) {
         int MY = P->MY, JX = P->JX;
         C = C * 2.0 / 1 / 1;
@@ -646,7 +700,6 @@ static int compute_phis(orc_state* st, const double* x) {
 int orc_residual(orc_state* st, const double* x, double* g) {
     const nm_plan* P = st->P;
     int M = st->M, ns = P->n_seg, nit = P->n_it;
-    if (P->charged && P->gradients == 3) return NM_ERR_INPUT;
     /* System::Classical_residual (system.cpp:2087-2189) */
     Cp(g, x, P->iv);
     int rc = compute_phis(st, x);

@@ -180,6 +180,15 @@ def cases() -> list[dict]:
                   conv_itlim=5000, path_tol=2e-5))
     C.append(dict(name="charged_star1d", lines=lat1d(40) + charged_lines("(X)1(A)9[(A)10](A)10", 0.04),
                   field=(-0.01, 0.01), seed=26, modes=["it0", "it5", "conv"], conv_itlim=5000))
+    # 3-gradient charged brush: the 3-D Poisson update (a forward and a
+    # backward Gauss-Seidel sweep) and the 3-D halo sums
+    # (a 3-D wall is a frozen layer inside the box: the reference refuses
+    # 'surface' bounds in 3-D)
+    lat = lat3d((9, 6, 6), bc="mirror")
+    wall = [ln.replace("frozen_range : lowerbound", "frozen_range : 1,1,1;1,6,6")
+            .replace("pinned_range : firstlayer", "pinned_range : 2,1,1;2,6,6") for ln in charged_lines("(X)1(A)15", 1.8)]
+    C.append(dict(name="charged3d", lines=lat + wall, field=(-0.01, 0.01), seed=27,
+                  modes=["it0", "it5", "conv"], conv_itlim=5000, split_tol=2e-4))
     # configuration-4 sample: random 1-gradient brushes (seeded), 10% stars
     rng = np.random.default_rng(2024)
     for i in range(6):
