@@ -100,7 +100,8 @@ __global__ void k_prop_back(Lat L, const double* __restrict__ in, const double* 
     nmdev::GLoad<double> ld{in};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n + nh; i += gridDim.x * blockDim.x) {
         if (i >= n) {
-            const int h = nmdev::halo_site(L, i - n);
+            const int h = L.g == 3 ? i - n : nmdev::halo_site(L, i - n);
+            if (L.g == 3 && nmdev::is_interior(L, h)) continue;
             nmdev::BLoad bl{in, L};
             const double v = nmdev::flat_prop_at(L, bl, h) * G1[h];
             const double gf = Gf[nmdev::bc_source(L, h)];

@@ -180,6 +180,7 @@ L3 make_l3(const nm_plan* p) {
 bool ctx3d_eligible(const nm_plan* p, std::string* why) {
     auto no = [&](const char* w) { if (why) *why = w; return false; };
     if (p->gradients != 3) return no("3-gradient lattices only");
+    if (p->charged) return no("charged systems take the generic kernels (their halo composition)");
     if (p->lattice_type != NM_SIMPLE_CUBIC) return no("simple-cubic lattices only");
     if (p->geometry != NM_PLANAR) return no("planar geometry only");
     for (int m = 0; m < p->n_mol; m++) {

@@ -130,6 +130,7 @@ __device__ __forceinline__ bool is_interior(const Lat& L, int s) {
 __device__ __forceinline__ int halo_count(const Lat& L) {
     return L.g == 1 ? 2 : 2 * L.JX + 2 * L.MX;
 }
+// (3 gradients: the halo part runs over all M sites and skips the interior)
 
 // j-th halo site: 1-D {0, MX+1}; 2-D the rows x = 0 and x = MX+1, then the
 // columns y = 0 and y = MY+1 of x = 1..MX.
@@ -148,9 +149,38 @@ __device__ __forceinline__ int halo_site(const Lat& L, int j) {
 // the reference accumulates them): LG1Planar.cpp:138-159, LGrad1.cpp:
 // 432-454, LG2Planar.cpp:1039-1127, LGrad2.cpp:1053-1090.  `g` loads an
 // element of the already bounded input.
+// one flat-array term: gs[w + i] += g[r + i] for i in [0, n)
+template <typename LD>
+__device__ __forceinline__ void flat_add(double& v, const LD& g, int s, int w, int r, int n) {
+    if (s >= w && s < w + n) v += g(s - w + r);
+}
+
 template <typename LD>
 __device__ __forceinline__ double flat_prop_at(const Lat& L, const LD& g, int s) {
     const int M = L.M, JX = L.JX;
+    if (L.g == 3) {  // LGrad3.cpp:673-782, stencil_full
+        const int JY = L.JY;
+        double v = 0;
+        if (L.lat != 0) v = 2.0 * g(s);
+        flat_add(v, g, s, JX, 0, M - JX); flat_add(v, g, s, 0, JX, M - JX);
+        flat_add(v, g, s, JY, 0, M - JY); flat_add(v, g, s, 0, JY, M - JY);
+        flat_add(v, g, s, 1, 0, M - 1); flat_add(v, g, s, 0, 1, M - 1);
+        if (L.lat == 0) return v * (1.0 / 6.0);
+        v *= 2.0;
+        flat_add(v, g, s, JX + JY, 0, M - JX - JY); flat_add(v, g, s, 0, JX + JY, M - JX - JY);
+        flat_add(v, g, s, JX, JY, M - JX - JY); flat_add(v, g, s, JY, JX, M - JX - JY);
+        flat_add(v, g, s, JX + 1, 0, M - JX - 1); flat_add(v, g, s, 1, JX, M - JX - 1);
+        flat_add(v, g, s, JY + 1, 0, M - JY - 1); flat_add(v, g, s, 1, JY, M - JY - 1);
+        flat_add(v, g, s, JX, 1, M - JX - 1); flat_add(v, g, s, 0, JX + 1, M - JX - 1);
+        flat_add(v, g, s, JY, 1, M - JY - 1); flat_add(v, g, s, 0, JY + 1, M - JY - 1);
+        v *= 2.0;
+        const int n3 = M - JX - JY - 1;
+        flat_add(v, g, s, JX + JY + 1, 0, n3); flat_add(v, g, s, 0, JX + JY + 1, n3);
+        flat_add(v, g, s, JX + JY, 1, n3); flat_add(v, g, s, 1, JX + JY, n3);
+        flat_add(v, g, s, JX + 1, JY, n3); flat_add(v, g, s, JY, JX + 1, n3);
+        flat_add(v, g, s, JY + 1, JX, n3); flat_add(v, g, s, JX, JY + 1, n3);
+        return v * (1.0 / 40.0);
+    }
     if (L.g == 1) {
         if (L.geom == 0) {
             double v = 0;

@@ -1,4 +1,4 @@
-// Electrostatics of a charged system in a device context (1 and 2 gradients).
+// Electrostatics of a charged system in a device context (1, 2 and 3 gradients).
 //
 // ψ is the last block of the iteration vector x.  Per residual evaluation:
 //   before G1   k_field        ψ with mirror bounds on every side and the
@@ -14,7 +14,10 @@
 // and 1-D cylindrical lattices: each site takes the already updated value of
 // its lower neighbours.  It runs as one thread along x in 1-D and as one
 // block over anti-diagonals in 2-D; the spherical and 2-D cylindrical updates
-// read only old values and run over all sites in parallel.
+// read only old values and run over all sites in parallel.  In 3-D it is a
+// forward then a backward Gauss–Seidel sweep in place on ψ (LGrad3.cpp:
+// 1155-1215): one block walks the planes x + y + z = d up, then down, which
+// gives each site exactly the inputs of the reference's sequential sweeps.
 #include <cuda_runtime.h>
 
 #include <string>
@@ -32,9 +35,20 @@ constexpr double K_BT = 1.38065e-23 * 298.15;
 constexpr double EPS0 = 8.85418e-12;
 constexpr double PIE = 3.14159265;
 
-// site of the mirror bounds (set_M_bounds) that halo site s takes
+// site of the mirror bounds (set_M_bounds) that halo site s takes; in 3-D
+// only the faces are set (LGrad3.cpp:1679-1702), edges and corners keep
+// their own value
 __device__ __forceinline__ int mirror_src(const Lat& L, int s) {
     if (L.g == 1) return s == 0 ? 1 : (s == L.MX + 1 ? L.MX : s);
+    if (L.g == 3) {
+        int x = s / L.JX, r = s % L.JX, y = r / L.JY, z = r % L.JY;
+        const int ox = x == 0 || x == L.MX + 1, oy = y == 0 || y == L.MY + 1, oz = z == 0 || z == L.MZ + 1;
+        if (ox + oy + oz != 1) return s;
+        if (ox) x = x == 0 ? 1 : L.MX;
+        if (oy) y = y == 0 ? 1 : L.MY;
+        if (oz) z = z == 0 ? 1 : L.MZ;
+        return x * L.JX + y * L.JY + z;
+    }
     int x = s / L.JX, y = s % L.JX;
     x = x == 0 ? 1 : (x == L.MX + 1 ? L.MX : x);
     y = y == 0 ? 1 : (y == L.MY + 1 ? L.MY : y);
@@ -48,6 +62,21 @@ __global__ void k_field(Lat L, ElecConst c, const double* __restrict__ xpsi, dou
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < M; s += gridDim.x * blockDim.x) {
         psi[s] = P(s);
         double e = 0;
+        if (L.g == 3) {
+            // squared differences along z, x and y over the flat array
+            // (AddGradSquare, tools_host.h:444), at every site that has both
+            // neighbours in the array, then the prefactor
+            const int dd[3] = {1, L.JX, L.JY};
+            for (int k = 0; k < 3; k++) {
+                const int d = dd[k];
+                if (s >= d && s < M - d) {
+                    const double u = P(s - d) - P(s), w = P(s) - P(s + d);
+                    e += u * u + w * w;
+                }
+            }
+            EE[s] = e * c.pf;
+            continue;
+        }
         if (nmdev::is_interior(L, s)) {
             const double pf = c.pf;
             if (L.g == 1) {
@@ -166,6 +195,36 @@ __global__ void k_psi_sweep2(Lat L, ElecConst c, const double* __restrict__ xpsi
         g[s] = nmdev::is_interior(L, s) ? xpsi[s] - X[s] : 0.0;
 }
 
+// 3-D: forward and backward Gauss–Seidel sweeps in place on psi (mirror
+// bounded), one block, plane x + y + z = d at a time; the backward sweep
+// leaves g = x_ψ − ψ_new at interior sites
+__global__ void k_psi_gs3(Lat L, ElecConst c, const double* __restrict__ xpsi, double* __restrict__ psi,
+                          const double* __restrict__ q, const double* __restrict__ eps, double* __restrict__ g) {
+    const int MX = L.MX, MY = L.MY, MZ = L.MZ, JX = L.JX, JY = L.JY, M = L.M;
+    const int D = MX + MY + MZ;
+    for (int pass = 0; pass < 2; pass++) {
+        for (int k = 0; k <= D - 3; k++) {
+            const int d = pass ? D - k : 3 + k;
+            for (int idx = threadIdx.x; idx < MX * MY; idx += blockDim.x) {
+                const int x = idx / MY + 1, y = idx % MY + 1, z = d - x - y;
+                if (z < 1 || z > MZ) continue;
+                const int i = x * JX + y * JY + z;
+                const double ezm = eps[i - 1] + eps[i], ezp = eps[i] + eps[i + 1];
+                const double eym = eps[i] + eps[i - JY], eyp = eps[i] + eps[i + JY];
+                const double exm = eps[i] + eps[i - JX], exp_ = eps[i] + eps[i + JX];
+                const double v = (exm * psi[i - JX] + exp_ * psi[i + JX] + eym * psi[i - JY] + eyp * psi[i + JY] +
+                                  ezm * psi[i - 1] + ezp * psi[i + 1] + c.C * q[i]) /
+                                 (exm + exp_ + eym + eyp + ezm + ezp);
+                psi[i] = v;
+                if (pass) g[i] = xpsi[i] - v;
+            }
+            __syncthreads();
+        }
+    }
+    for (int s = threadIdx.x; s < M; s += blockDim.x)
+        if (!nmdev::is_interior(L, s)) g[s] = 0.0;
+}
+
 // 1-D spherical and 2-D cylindrical: every site from old values
 __global__ void k_psi_jacobi(Lat L, ElecConst c, const double* __restrict__ xpsi, const double* __restrict__ psi,
                              const double* __restrict__ q, const double* __restrict__ eps, double* __restrict__ g) {
@@ -201,10 +260,6 @@ int grid_of(int n) {
 
 int Ctx::elec_init() {
     const nm_plan* p = plan;
-    if (p->gradients == 3) {
-        set_error("charged 3-gradient systems are not supported by the device path");
-        return NM_ERR_INPUT;
-    }
     if (!(p->bond_length > 0)) {
         set_error("charged system needs a positive lattice bondlength");
         return NM_ERR_INPUT;
@@ -219,6 +274,8 @@ int Ctx::elec_init() {
         if (p->geometry == NM_PLANAR) { pf = pf / 2.0; C = C * 2.0; }
         else if (p->geometry == NM_CYLINDRICAL) { pf = pf * PIE; C = C / PIE; }
         else { pf = pf * PIE * 2; C = C / (2.0 * PIE); }
+    } else if (p->gradients == 3) {
+        // planar only, no geometry factors (LGrad3.cpp:1132, 1170)
     } else {
         pf = pf / 2;
         C = p->geometry == NM_PLANAR ? C * 2.0 : C / 2;
@@ -233,7 +290,9 @@ int Ctx::elec_init() {
         if (e == cudaSuccess) e = cudaMemsetAsync(*b, 0, sizeof(double) * M, stream);
         if (e != cudaSuccess) { set_error(std::string("electrostatics buffers: ") + cudaGetErrorString(e)); return NM_ERR_NOMEM; }
     }
-    nh = p->gradients == 1 ? 2 : 2 * p->JX + 2 * p->MX;
+    // halo sites of the composition; in 3-D the halo part runs over all M
+    // sites and skips the interior
+    nh = p->gradients == 1 ? 2 : (p->gradients == 2 ? 2 * p->JX + 2 * p->MX : p->M);
     return NM_OK;
 }
 
@@ -254,6 +313,8 @@ int Ctx::elec_residual(const double* x, double* g) {
         k_psi_sweep1<<<1, 32, 0, stream>>>(lat, ec, xpsi, d_psi, d_q, d_eps, gp);
     else if (plan->gradients == 2 && plan->geometry == NM_PLANAR)
         k_psi_sweep2<<<1, 512, 0, stream>>>(lat, ec, xpsi, d_psi, d_q, d_eps, d_X, gp);
+    else if (plan->gradients == 3)
+        k_psi_gs3<<<1, 1024, 0, stream>>>(lat, ec, xpsi, d_psi, d_q, d_eps, gp);
     else
         k_psi_jacobi<<<grid_of(M), 256, 0, stream>>>(lat, ec, xpsi, d_psi, d_q, d_eps, gp);
     launches += 2;

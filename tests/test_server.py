@@ -42,7 +42,7 @@ def _alone(plan, x, precision):
         return int(its[0]), float(res[0]), int(st[0]), xx
     # the server uses FP32 propagators in a context only for 3-D simple-cubic
     # linear chains (the 3-D hexagonal fixture is left out above)
-    prec = precision if (precision == NM_FP64 or plan.c.gradients == 3) else NM_FP64
+    prec = precision if (precision == NM_FP64 or (plan.c.gradients == 3 and not plan.c.charged)) else NM_FP64
     ctx = Context(plan, prec)
     xx = x.copy()
     r, _ = ctx.solve_host(xx)
