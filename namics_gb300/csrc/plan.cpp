@@ -609,6 +609,13 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
         }
         if (in.has("mon", nm_, "valence")) to_real(in.get("mon", nm_, "valence"), H->seg_valence[i]);
         if (in.has("mon", nm_, "epsilon")) to_real(in.get("mon", nm_, "epsilon"), H->seg_epsilon[i]);
+        if (in.has("mon", nm_, "e.psi0/kT")) {
+            // the reference's fixed-ψ0 residual resets ψ to 0 off the surface at
+            // every evaluation (OverwriteC, tools_host.h:515-517, from
+            // Segment::UpdateValence), so it iterates no potential; not offered
+            err = "mon " + nm_ + ": fixed surface potentials (e.psi0/kT) are not supported";
+            delete H; return nullptr;
+        }
         if (in.has("mon", nm_, "fluctuation_potentials") || in.has("mon", nm_, "state1")) {
             err = "mon " + nm_ + ": external potentials / internal states are not supported"; delete H; return nullptr;
         }
