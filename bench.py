@@ -224,7 +224,7 @@ def run_reference(args) -> None:
 
 
 def melt3d_text(n: int = 128, itlim: int = 20) -> str:
-    """Config 2: n³ box, periodic in all three directions, melt of symmetric
+    """The 3-D melt: n³ box, periodic in all three directions, melt of symmetric
     diblock (A)50(B)50 (N = 100, incompressible), chi_AB = 0.3."""
     return "\n".join([
         "lat : flat : gradients : 3", f"lat : flat : n_layers_x : {n}", f"lat : flat : n_layers_y : {n}",
@@ -238,7 +238,7 @@ def melt3d_text(n: int = 128, itlim: int = 20) -> str:
 
 
 def run_melt3d(args) -> None:
-    """Config 2 on one GPU: DIIS iterations of the 128³ A50B50 melt with FP32
+    """On one GPU: DIIS iterations of the 128³ A50B50 melt with FP32
     propagators (per-vector power-of-two exponents, FP64 DIIS) and with plain
     FP64 propagators, from the same seeded field u_A = -u_B ~ U(-0.1, 0.1).
     A step is `--iters` DIIS iterations (residual + field update), timed with
@@ -294,7 +294,7 @@ def run_melt3d(args) -> None:
         "value": 1000.0 / f32["ms_per_residual_and_update"], "unit": "iterations/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": f32["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded field)",
-        "config": {"workload": f"config 2: {n}^3 periodic, (A)50(B)50 melt, chi_AB 0.3, u_A=-u_B~U(-0.1,0.1)",
+        "config": {"workload": f"{n}^3 periodic (A)50(B)50 melt, chi_AB 0.3, u_A=-u_B~U(-0.1,0.1)",
                    "iterations_per_step": args.iters, "l2": "flushed between steps (256 MB write)",
                    "segment_site_updates_per_residual": updates, "parallelism": "one GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -308,7 +308,7 @@ def run_melt3d(args) -> None:
 
 
 def ads2d_text(n: int = 100, N: int = 200) -> str:
-    """Config 5, 25% of requests: 2-D planar n×n adsorption of (A)N from a
+    """Request stream, 25% of requests: 2-D planar n×n adsorption of (A)N from a
     bulk at phi_b = 1e-3 onto a surface with chi_AS = -1, monomeric solvent."""
     return "\n".join([
         "lat : flat : gradients : 2", f"lat : flat : n_layers_x : {n}", f"lat : flat : n_layers_y : {n}",
@@ -325,14 +325,14 @@ def ads2d_text(n: int = 100, N: int = 200) -> str:
 
 
 def melt3d_small_text(n: int = 64, a: int = 20, chi: float = 0.4) -> str:
-    """Config 5, 5% of requests: n³ periodic (A)a(B)a melt at chi_AB."""
+    """Request stream, 5% of requests: n³ periodic (A)a(B)a melt at chi_AB."""
     return melt3d_text(n, 1000).replace("chi_B : 0.3", f"chi_B : {chi}").replace(
         "(A)50(B)50", f"(A){a}(B){a}")
 
 
 def cyl2d_text(nx: int = 200, ny: int = 200, N: int = 500, n: float = 1.0, chi: float = 0.5,
                itlim: int = 20, tol: float = 1e-7) -> str:
-    """Config 3: 2-D cylindrical nx (r) × ny (z) lattice, offset_first_layer
+    """The charged cylindrical brush: 2-D cylindrical nx (r) × ny (z) lattice, offset_first_layer
     10 (inner cylinder of radius 10, a frozen wall below x = 1), (X)1(A)N-1
     pinned at the first layer with n chains, chi_AS = chi; A carries valence
     -0.1, monovalent ions: Na the neutraliser, Cl free at phi_b 0.01; water
@@ -358,7 +358,7 @@ def cyl2d_text(nx: int = 200, ny: int = 200, N: int = 500, n: float = 1.0, chi: 
 
 
 def cyl2d_plan(nx: int, ny: int, N: int, sigma: float, chi: float, itlim: int, tol: float = 1e-7):
-    """The config-3 plan with n = sigma × (sites of the first layer, Σ_y L(x=1))."""
+    """The charged cylindrical brush with n = sigma × (sites of the first layer, Σ_y L(x=1))."""
     from namics_gb300 import Plan
     probe = Plan(cyl2d_text(nx, ny, N, 1.0, chi, itlim, tol))
     c = probe.c
@@ -367,7 +367,7 @@ def cyl2d_plan(nx: int, ny: int, N: int, sigma: float, chi: float, itlim: int, t
 
 
 def run_cyl2d(args) -> None:
-    """Config 3 on one GPU: the 200×200 cylindrical charged brush (A_500, sigma
+    """On one GPU: the 200×200 cylindrical charged brush (A_500, sigma
     0.02, A valence -0.1, Na neutraliser, Cl phi_b 0.01) at both chi_AS values
     of the configuration, 0 and 0.5, solved side by side: one device context
     and one CUDA stream each, driven from two host threads.  A single solve
@@ -478,7 +478,7 @@ def run_cyl2d(args) -> None:
         "value": f32["iterations_per_s"], "unit": "iterations/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": f32["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded field)",
-        "config": {"workload": f"config 3: {nx}x{ny} cylindrical, offset 10, (X)1(A)499 pinned, sigma 0.02, "
+        "config": {"workload": f"{nx}x{ny} cylindrical charged brush, offset 10, (X)1(A)499 pinned, sigma 0.02, "
                                "chi_AS in {0, 0.5} (two solves side by side), A valence -0.1, Na neutraliser, "
                                "Cl phi_b 0.01, bondlength 5e-10",
                    "iterations_per_step": args.iters, "l2": "flushed between steps (256 MB write)",
@@ -492,10 +492,10 @@ def run_cyl2d(args) -> None:
 
 
 def run_served(args) -> None:
-    """Config 5: a Poisson request stream served on one GPU by nm_server
+    """A Poisson request stream served on one GPU by nm_server
     (continuous batching: 1-gradient requests waiting together share one
     batched launch, others get a device context each; W workers with one
-    stream each; admission by device footprint).  Mix: 70% config-4 brushes,
+    stream each; admission by device footprint).  Mix: 70% 1-D brushes/stars drawn like the batched workload,
     25% 2-D 100×100 (A)200 adsorption, 5% 3-D 64³ (A)20(B)20 melts at
     chi 0.4, all from seeded fields.  Reported: converged solves/s over the
     span from the first submit to the last completion, p50/p99 of the
@@ -553,8 +553,8 @@ def run_served(args) -> None:
         "metric": METRIC, "value": f32["value"], "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 0,
         "ms_per_step": f32["span_s"] * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded request stream)",
-        "config": {"workload": f"config 5: Poisson stream, {args.rate:g} requests/s, {n_req} requests; 70% "
-                               "config-4 brushes, 25% 2-D 100x100 (A)200 adsorption, 5% 3-D 64^3 (A)20(B)20 melts",
+        "config": {"workload": f"Poisson request stream, {args.rate:g} requests/s, {n_req} requests; 70% "
+                               "1-D brushes/stars as in the batched workload, 25% 2-D 100x100 (A)200 adsorption, 5% 3-D 64^3 (A)20(B)20 melts",
                    "workers": args.workers, "max_batch": 64, "memory_budget_gb": 64},
         "latency": {"p50_ms": f32["p50_ms"], "p99_ms": f32["p99_ms"], "what": "submit to completion"},
         "fp32": f32, "fp64_gpu": out["fp64"],
@@ -572,9 +572,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU comparison")
     ap.add_argument("--workload", default="brush1d", choices=["brush1d", "melt3d", "cyl2d", "served"],
-                    help="brush1d: config 4, the headline; melt3d: config 2 (DIIS iterations/s); "
-                         "cyl2d: config 3 (charged cylindrical brush, DIIS iterations/s); "
-                         "served: config 5 (request stream)")
+                    help="brush1d: 512 batched 1-D brushes/stars, the headline; melt3d: 128³ melt (DIIS iterations/s); "
+                         "cyl2d: 200×200 charged cylindrical brushes at two chi values (DIIS iterations/s); "
+                         "served: Poisson request stream of mixed solves")
     ap.add_argument("--n2d", type=int, default=200, help="cyl2d: lattice edge (r and z)")
     ap.add_argument("--no-solve", action="store_true", help="cyl2d: skip the timed full solves")
     ap.add_argument("--rate", type=float, default=20.0, help="served: arrivals per second")

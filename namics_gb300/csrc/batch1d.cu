@@ -618,7 +618,7 @@ __device__ __noinline__ void bc_dispatch(B1Prob& P, const Lat1 L, const Coef<dou
 //   CTA with the DIIS history restarted, so the stopping test ‖g‖ < tol is
 //   always made on an FP64 residual.  A failure of the FP32 evaluation
 //   (G(N) <= 0, a non-finite residual) is a failure of the reduced precision,
-//   not a verdict on the problem: the FP64 phase takes over at the same x.
+//   says nothing about the problem itself: the FP64 phase takes over at the same x.
 __device__ __forceinline__ unsigned long long b1_clock() {
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));

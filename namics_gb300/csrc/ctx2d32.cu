@@ -1,5 +1,5 @@
-// FP32 propagators for 2-gradient contexts (config 3 class: cylindrical and
-// planar lattices, linear chains, neutral or charged), FP64 everything else.
+// FP32 propagators for 2-gradient contexts (cylindrical and planar lattices,
+// linear chains, neutral or charged), FP64 everything else.
 //
 // Block floating point with one power-of-two exponent per lattice row x:
 // G(x, y) = v(x, y)·2^E[x].  A grafted brush's propagators span hundreds of

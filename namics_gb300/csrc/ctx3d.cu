@@ -1,5 +1,5 @@
-// 3-D simple-cubic propagator steps for the generic context (config-2 class
-// problems: 3-gradient planar lattices, linear chains), FP64 or FP32.
+// 3-D simple-cubic propagator steps for the generic context (melts and other
+// 3-gradient planar lattices with linear chains), FP64 or FP32.
 //
 // One step is G_out(x,y,z) = G1·(Σ of the six neighbours)/6
 // (LGrad3::propagate, LGrad3.cpp:673-744, simple-cubic stencil), with the

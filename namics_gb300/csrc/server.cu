@@ -1,4 +1,4 @@
-// Request server: continuous batching of SCF solves on one GPU (config 5).
+// Request server: continuous batching of SCF solves on one GPU.
 //
 // Requests of any gradient count arrive one at a time (nm_server_submit) and
 // are solved on the device while others are running.  W worker threads each

@@ -80,10 +80,10 @@ def newton(tol=1e-7, dmax=0.1, itlim=1000, m=10):
 
 def cases() -> list[dict]:
     C = []
-    # config 1: 1-gradient planar simple-cubic brush, 100 layers, A_100 (X1A99) at σ=0.05
+    # 1-gradient planar simple-cubic brush, 100 layers, A_100 (X1A99) at σ=0.05
     base = lat1d(100) + brush_lines("(X)1(A)99", n=0.05, chi=0.5)
     C.append(dict(name="brush1d_cfg1", lines=base, field=(-0.01, 0.01), seed=1, modes=["it0", "conv"]))
-    # 3-arm star brush (configuration-4 star variant)
+    # 3-arm star brush (the star variant of the batched workload)
     C.append(dict(name="star1d", lines=lat1d(80) + brush_lines("(X)1(A)19[(A)20](A)20", n=0.04, chi=0.4),
                   field=(-0.01, 0.01), seed=2, modes=["it0", "conv"]))
     # hexagonal planar brush with an adsorbing wall
@@ -110,7 +110,7 @@ def cases() -> list[dict]:
                          "mol : pol : freedom : restricted", "mol : pol : theta : 4",
                          "mol : water : composition : (W)1", "mol : water : freedom : solvent"]
     C.append(dict(name="dend1d", lines=lines, field=(-0.05, 0.05), seed=6, modes=["it0", "conv"]))
-    # 2-gradient planar adsorption (configuration-5 2-D class, reduced size)
+    # 2-gradient planar adsorption (the 2-D requests of the request stream, reduced size)
     lines = lat2d(24, 16, ["surface", "mirror", "mirror", "mirror"]) + [
         "mon : S : freedom : frozen", "mon : S : frozen_range : lowerbound",
         "mon : A : freedom : free", "mon : W : freedom : free", "mon : A : chi_S : -1",
@@ -125,11 +125,11 @@ def cases() -> list[dict]:
         "mol : pol : composition : (A)20", "mol : pol : freedom : free", "mol : pol : phibulk : 0.01",
         "mol : water : composition : (W)1", "mol : water : freedom : solvent"]
     C.append(dict(name="ads2d_hex", lines=lines, field=(-0.05, 0.05), seed=8, modes=["it0", "conv"]))
-    # 2-gradient cylindrical brush (configuration-3 geometry, uncharged, reduced)
+    # 2-gradient cylindrical brush (the charged cylindrical brush's geometry, uncharged, reduced)
     lines = lat2d(20, 10, ["surface", "mirror", "mirror", "mirror"], geom="cylindrical", offset=10) + \
         brush_lines("(X)1(A)39", n=12.0, chi=0.5, pinned_range="firstlayer")
     C.append(dict(name="brush2d_cyl", lines=lines, field=(-0.02, 0.02), seed=9, modes=["it0", "conv"]))
-    # 3-gradient periodic diblock melt (configuration-2 class, reduced size)
+    # 3-gradient periodic diblock melt (the 128³ melt, reduced size)
     lines = lat3d((10, 10, 10)) + ["mon : A : freedom : free", "mon : B : freedom : free", "mon : A : chi_B : 0.3",
                                    "mol : AB : composition : (A)10(B)10", "mol : AB : freedom : solvent"]
     C.append(dict(name="melt3d", lines=lines, field=(-0.1, 0.1), seed=10, antisym=True,
@@ -142,7 +142,7 @@ def cases() -> list[dict]:
     C.append(dict(name="sol3d_hex", lines=lines, field=(-0.1, 0.1), seed=11, modes=["it0", "it5"]))
     # charged grafted polyelectrolyte brushes (valence -0.1 on A) with a
     # neutralising counter-ion (Na) and added salt (Cl at phi_b 0.01), on the
-    # four lattices the electrostatics covers (configuration-3 class, reduced)
+    # four lattices the electrostatics covers (the charged cylindrical brush class, reduced)
     def charged_lines(comp, n):
         return ["lat : flat : bondlength : 5e-10",
                 "mon : S : freedom : frozen", "mon : S : frozen_range : lowerbound",
@@ -189,7 +189,7 @@ def cases() -> list[dict]:
             .replace("pinned_range : firstlayer", "pinned_range : 2,1,1;2,6,6") for ln in charged_lines("(X)1(A)15", 1.8)]
     C.append(dict(name="charged3d", lines=lat + wall, field=(-0.01, 0.01), seed=27,
                   modes=["it0", "it5", "conv"], conv_itlim=5000, split_tol=2e-4))
-    # configuration-4 sample: random 1-gradient brushes (seeded), 10% stars
+    # a sample of the batched workload: random 1-gradient brushes (seeded), 10% stars
     rng = np.random.default_rng(2024)
     for i in range(6):
         nl = int(rng.integers(50, 401))
