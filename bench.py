@@ -44,6 +44,10 @@ FIELD = (-0.01, 0.01)
 METRIC = "SCF solves/s at |residual|<1e-7 (served FP32 vs plain FP64 GPU); p50/p99 latency"
 UNIT = "solves/s"
 B_PER_UPDATE_FP32 = 22.0   # algorithmic bytes per segment-site update (FP32 propagators, FP64 φ)
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_batch1d launch on the
+# default 512-instance FP32 workload, from one ncu capture
+# (profiles/k_batch1d_fp32_batch512_launches.md): 17.75 GB + 28.69 GB
+TRAFFIC_BATCH512_FP32 = 4.644e10
 B_PER_UPDATE_FP64 = 36.0
 
 
@@ -718,9 +722,13 @@ def main():
                    "segment_site_updates_per_step": updates, "l2": "flushed between steps (256 MB write)",
                    "parallelism": f"replicas x{ws}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak,
+                     "traffic": (TRAFFIC_BATCH512_FP32 if (prec == NM_FP32 and args.instances == N_INSTANCES)
+                                 else None),
                      "note": f"{bpu:.0f} B per segment-site update x updates / kernel time; peak of measured "
-                             "(MEASURED_PEAKS.json hbm_gbs)"},
+                             "(MEASURED_PEAKS.json hbm_gbs); traffic: DRAM bytes of one launch from an ncu "
+                             "capture of this workload, below the algorithmic bytes because the chains run in "
+                             "registers and shared memory"},
         "e2e": {"value": n_ok * ws / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes},
         "gpu_launches": launches,
