@@ -78,6 +78,7 @@ __global__ void k_g1(Lat L, int ns, const double* __restrict__ x, const int* __r
 // out = stencil(in)·G1 at interior sites (G1 may be null: ≡ 1)
 __global__ void k_prop(Lat L, const double* __restrict__ in, const double* __restrict__ G1,
                        double* __restrict__ out) {
+    nmdev::pdl_begin();
     int n = nmdev::interior_count(L);
     nmdev::GLoad<double> ld{in};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -87,6 +88,7 @@ __global__ void k_prop(Lat L, const double* __restrict__ in, const double* __res
         double v = nmdev::stencil_at(L, ld, x, y, z);
         out[s] = G1 ? v * G1[s] : v;
     }
+    nmdev::pdl_end();
 }
 
 // backward step fused with composition: out = stencil(in)·G1; rho += d·Gf·out.
@@ -96,6 +98,7 @@ __global__ void k_prop(Lat L, const double* __restrict__ in, const double* __res
 __global__ void k_prop_back(Lat L, const double* __restrict__ in, const double* __restrict__ G1,
                             double* __restrict__ out, const double* __restrict__ Gf,
                             double* __restrict__ rho, double d, int nh) {
+    nmdev::pdl_begin();
     int n = nmdev::interior_count(L);
     nmdev::GLoad<double> ld{in};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n + nh; i += gridDim.x * blockDim.x) {
@@ -117,11 +120,13 @@ __global__ void k_prop_back(Lat L, const double* __restrict__ in, const double* 
         if (d == 1.0) rho[s] += Gf[s] * v;
         else rho[s] += d * Gf[s] * v;
     }
+    nmdev::pdl_end();
 }
 
 // root of the backward sweep: out = G1; rho += d·Gf·G1
 __global__ void k_back_init(Lat L, const double* __restrict__ G1, double* __restrict__ out,
                             const double* __restrict__ Gf, double* __restrict__ rho, double d) {
+    nmdev::pdl_begin();
     int n = nmdev::interior_count(L);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         int x, y, z;
@@ -132,9 +137,11 @@ __global__ void k_back_init(Lat L, const double* __restrict__ G1, double* __rest
         if (d == 1.0) rho[s] += Gf[s] * v;
         else rho[s] += d * Gf[s] * v;
     }
+    nmdev::pdl_end();
 }
 
 __global__ void k_copy_interior(Lat L, const double* __restrict__ in, double* __restrict__ out) {
+    nmdev::pdl_begin();
     int n = nmdev::interior_count(L);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         int x, y, z;
@@ -142,10 +149,12 @@ __global__ void k_copy_interior(Lat L, const double* __restrict__ in, double* __
         int s = x * L.JX + y * L.JY + z;
         out[s] = in[s];
     }
+    nmdev::pdl_end();
 }
 
 // out *= a^pow (interior)
 __global__ void k_mul_pow(Lat L, double* __restrict__ out, const double* __restrict__ a, int pw) {
+    nmdev::pdl_begin();
     int n = nmdev::interior_count(L);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         int x, y, z;
@@ -155,6 +164,7 @@ __global__ void k_mul_pow(Lat L, double* __restrict__ out, const double* __restr
         for (int k = 0; k < pw; k++) v *= a[s];
         out[s] = v;
     }
+    nmdev::pdl_end();
 }
 
 __device__ __forceinline__ double block_sum(double v, double* sh) {
@@ -521,7 +531,7 @@ static int grid_for(int n, int threads = 256) {
 
 int Ctx::launch_prop(const double* in, const double* G1, double* out) {
     int n = interior;
-    k_prop<<<grid_for(n), 256, 0, stream>>>(lat, in, G1, out);
+    launch_pdl(k_prop, grid_for(n), 256, stream, lat, in, G1, out);
     launches++;
     return NM_OK;
 }
@@ -547,7 +557,7 @@ int Ctx::molecule_pass(int m) {
         const double* G1 = d_G1 + (size_t)B.seg * M;
         double* out = D.Gf + (size_t)B.s0 * M;
         if (B.n_child == 0) {
-            k_copy_interior<<<gb, 256, 0, stream>>>(lat, G1, out);
+            launch_pdl(k_copy_interior, gb, 256, stream, lat, G1, out);
             launches++;
         } else {
             bool simple = (B.n_child == 1 && mol.blocks[mol.child_index[B.child0]].mult == 1);
@@ -562,10 +572,10 @@ int Ctx::molecule_pass(int m) {
             const nm_block& C0 = mol.blocks[c0];
             launch_prop(D.Gf + (size_t)(C0.s0 + C0.length - 1) * M, G1, out);
             if (!simple) {
-                if (C0.mult > 1) { k_mul_pow<<<gb, 256, 0, stream>>>(lat, out, D.Pc + (size_t)c0 * M, C0.mult - 1); launches++; }
+                if (C0.mult > 1) { launch_pdl(k_mul_pow, gb, 256, stream, lat, out, D.Pc + (size_t)c0 * M, C0.mult - 1); launches++; }
                 for (int c = 1; c < B.n_child; c++) {
                     int cb = mol.child_index[B.child0 + c];
-                    k_mul_pow<<<gb, 256, 0, stream>>>(lat, out, D.Pc + (size_t)cb * M, mol.blocks[cb].mult);
+                    launch_pdl(k_mul_pow, gb, 256, stream, lat, out, D.Pc + (size_t)cb * M, mol.blocks[cb].mult);
                     launches++;
                 }
             }
@@ -588,13 +598,13 @@ int Ctx::molecule_pass(int m) {
         double* nxt = d_gb + M;
         int s = B.s0 + B.length - 1;
         if (B.parent < 0) {
-            k_back_init<<<gb, 256, 0, stream>>>(lat, G1, cur, D.Gf + (size_t)s * M, rho, B.degeneracy);
+            launch_pdl(k_back_init, gb, 256, stream, lat, G1, cur, D.Gf + (size_t)s * M, rho, B.degeneracy);
         } else {
-            k_prop_back<<<gbh, 256, 0, stream>>>(lat, D.Q + (size_t)b * M, G1, cur, D.Gf + (size_t)s * M, rho, B.degeneracy, nh);
+            launch_pdl(k_prop_back, gbh, 256, stream, lat, D.Q + (size_t)b * M, G1, cur, D.Gf + (size_t)s * M, rho, B.degeneracy, nh);
         }
         launches++;
         for (s = s - 1; s >= B.s0; s--) {
-            k_prop_back<<<gbh, 256, 0, stream>>>(lat, cur, G1, nxt, D.Gf + (size_t)s * M, rho, B.degeneracy, nh);
+            launch_pdl(k_prop_back, gbh, 256, stream, lat, cur, G1, nxt, D.Gf + (size_t)s * M, rho, B.degeneracy, nh);
             launches++;
             double* t = cur; cur = nxt; nxt = t;
         }
@@ -602,15 +612,15 @@ int Ctx::molecule_pass(int m) {
         for (int c = 0; c < B.n_child; c++) {
             int cb = mol.child_index[B.child0 + c];
             double* q = D.Q + (size_t)cb * M;
-            k_copy_interior<<<gb, 256, 0, stream>>>(lat, cur, q);
+            launch_pdl(k_copy_interior, gb, 256, stream, lat, cur, q);
             launches++;
             bool simple = (B.n_child == 1 && mol.blocks[cb].mult == 1);
             if (!simple) {
-                if (mol.blocks[cb].mult > 1) { k_mul_pow<<<gb, 256, 0, stream>>>(lat, q, D.Pc + (size_t)cb * M, mol.blocks[cb].mult - 1); launches++; }
+                if (mol.blocks[cb].mult > 1) { launch_pdl(k_mul_pow, gb, 256, stream, lat, q, D.Pc + (size_t)cb * M, mol.blocks[cb].mult - 1); launches++; }
                 for (int o = 0; o < B.n_child; o++) {
                     if (o == c) continue;
                     int ob = mol.child_index[B.child0 + o];
-                    k_mul_pow<<<gb, 256, 0, stream>>>(lat, q, D.Pc + (size_t)ob * M, mol.blocks[ob].mult);
+                    launch_pdl(k_mul_pow, gb, 256, stream, lat, q, D.Pc + (size_t)ob * M, mol.blocks[ob].mult);
                     launches++;
                 }
             }

@@ -58,6 +58,7 @@ __global__ void __launch_bounds__(128) k3_prop(L3 L, const T* __restrict__ in, c
                                                int* __restrict__ E, int sin, int sout,
                                                const T* __restrict__ Gf, int sgf, int sroot,
                                                T* __restrict__ rhi, T* __restrict__ rlo, T d) {
+    nmdev::pdl_begin();
     constexpr bool FP32 = sizeof(T) == 4;
     const int z = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int x = blockIdx.z + 1;
@@ -121,6 +122,7 @@ __global__ void __launch_bounds__(128) k3_prop(L3 L, const T* __restrict__ in, c
             if (b == 0) E[sout] = Eout;
         }
     }
+    nmdev::pdl_end();
 }
 
 // Σ_interior of an FP32 vector (FP64 partial sums), G(N) = Σ·2^E(root), and
@@ -199,8 +201,8 @@ static void k3(Ctx& C, const T* in, const T* G1, T* out, int sin, int sout, cons
                T* rlo, double d) {
     const nm_plan* p = C.plan;
     dim3 grid((p->MZ + 127) / 128, (p->MY + C3_RY - 1) / C3_RY, p->MX);
-    k3_prop<T, MODE><<<grid, 128, 0, C.stream>>>(C.l3, in, G1, out, C.d_maxbits, C.d_E, sin, sout, Gf, sgf, sroot, rhi,
-                                                 rlo, (T)d);
+    launch_pdl(k3_prop<T, MODE>, grid, 128, C.stream, C.l3, in, G1, out, C.d_maxbits, C.d_E, sin, sout, Gf, sgf, sroot,
+               rhi, rlo, (T)d);
     C.launches++;
 }
 

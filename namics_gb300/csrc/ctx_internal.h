@@ -120,6 +120,23 @@ struct MolDev {
 
 nmdev::Lat make_lat(const nm_plan* p);
 
+// launch with programmatic stream serialisation (the kernel calls pdl_begin
+// before it touches memory); also recorded that way in a captured graph
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // 3-D lattice for the dedicated simple-cubic kernels (ctx3d.cu)
 struct L3 {
     int MX, MY, MZ, JX, JY;

@@ -248,6 +248,15 @@ __device__ __forceinline__ int bc_source(const Lat& L, int s) {
            bmap(z, L.MZ, L.b1[2], L.bm[2]);
 }
 
+// Programmatic dependent launch: a step kernel launched with the
+// programmatic-serialisation attribute may be scheduled while its
+// predecessor drains.  It waits for the predecessor's completion (all writes
+// visible) before touching memory, and releases its own successor only after
+// its stores; released at the start instead, chains of waiting grids filled
+// the SMs and 2-D residuals ran twice as long.
+__device__ __forceinline__ void pdl_begin() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_end() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // Element i of an array after set_bounds: the halo takes its source site's
 // value (a surface halo keeps its own, zero in every stored propagator).
 struct BLoad {
