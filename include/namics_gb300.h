@@ -171,10 +171,6 @@ int nm_ctx_destroy(nm_ctx* ctx);
  * instead of one launch per segment step.  Same arithmetic, same results;
  * on GB300 the per-step launches are the faster of the two. */
 #define NM_OPT_SWEEP2D 1
-/* NM_OPT_BAND2D (default 1): FP32 2-gradient contexts run several segment
- * steps per launch on bands of rows held in shared memory; 0 selects one
- * launch per step (same arithmetic, same results). */
-#define NM_OPT_BAND2D 3
 int nm_ctx_set_option(nm_ctx* ctx, int option, int value);
 
 /* Scans (the reference's Variate: variate.cpp, solve_scf.cpp:717-868): change

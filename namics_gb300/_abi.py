@@ -19,7 +19,6 @@ NM_ERR_NOMEM = -13
 NM_ERR_NOT_CONVERGED = -14
 NM_ERR_TIMEOUT = -15
 NM_OPT_SWEEP2D = 1
-NM_OPT_BAND2D = 3
 
 NM_FP64, NM_FP32 = 0, 1
 

@@ -1034,11 +1034,6 @@ Ctx::~Ctx() {
     }
     if (d_flags) cudaFreeAsync(d_flags, stream);
     for (int* q : E2f) if (q) cudaFreeAsync(q, stream);
-    for (auto& T : band_tabs) {
-        if (T.seg) cudaFreeAsync(T.seg, stream);
-        if (T.mm) cudaFreeAsync(T.mm, stream);
-        if (T.deg) cudaFreeAsync(T.deg, stream);
-    }
     if (d_E2b) cudaFreeAsync(d_E2b, stream);
     if (d_rowpart) cudaFreeAsync(d_rowpart, stream);
     if (graph) cudaGraphExecDestroy(graph);
@@ -1149,9 +1144,8 @@ int nm_ctx_set_values(nm_ctx* ctx, const char* const* items, const double* value
 int nm_ctx_set_option(nm_ctx* ctx, int option, int value) {
     Ctx* c = reinterpret_cast<Ctx*>(ctx);
     if (!c) { nm::set_error("nm_ctx_set_option: null context"); return NM_ERR_ARG; }
-    if (option == NM_OPT_SWEEP2D) c->sweep2d = value != 0;
-    else if (option == NM_OPT_BAND2D) c->band_on = value != 0;
-    else { nm::set_error("nm_ctx_set_option: unknown option"); return NM_ERR_ARG; }
+    if (option != NM_OPT_SWEEP2D) { nm::set_error("nm_ctx_set_option: unknown option"); return NM_ERR_ARG; }
+    c->sweep2d = value != 0;
     if (c->graph) {  // the captured residual used the other kernels
         cudaGraphExecDestroy(c->graph);
         c->graph = nullptr;

@@ -22,9 +22,7 @@
 // per row plus, for the halo part, the two x-halo rows.
 #include <cuda_runtime.h>
 
-#include <algorithm>
 #include <climits>
-#include <cstddef>
 #include <string>
 #include <vector>
 
@@ -212,176 +210,6 @@ __global__ void k2f_fill(int* p, int n, int v) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = v;
 }
 
-// ---- several steps per launch: bands of rows in shared memory ------------
-// CTA c owns rows [x0, x0+B-1] and keeps rows [x0-H, x0+B-1+H] of the vector
-// being propagated in shared memory (two buffers and their row exponents).
-// Step j of a launch computes the rows two neighbours in from the previous
-// step's valid range, so after k steps (H = k + 1) its own rows are exact
-// and the halo part of a charged system, which reads two rows out, still
-// finds its input.  Each row is the arithmetic of k2f_step (sten_rows, the
-// row maximum, the renormalisation), so results are the same.  The x bounds
-// must be mirror or surface (a periodic x halo would need the far row).
-#define BAND_B 8
-#define BAND_K 4
-
-struct Band32 {
-    Lat L;
-    int k;              // steps this launch
-    int dir;            // +1 forward, -1 backward
-    int s_first;        // stored index of the first step's output
-    const int* seg;     // [n_store] segment of s
-    const int* mm;      // [n_store] rho slot of s
-    const double* deg;  // [n_store] degeneracy of s
-    const float* G1f;   // [ns][M]
-    const double* G1d;  // [ns][M] (halo part)
-    const float* in;    // input vector and its row exponents
-    const int* Ein;
-    float* Gf;          // [n_store][M]: forward writes, backward reads
-    int* Ef;            // [n_store][MX+2]
-    float* out_last;    // backward: the last step's vector and exponents
-    int* Eout_last;
-    double* rho;        // [n_molmon][M]
-    int nh;
-};
-
-template <int DIR>
-__global__ void __launch_bounds__(512) k2f_band(Band32 a) {
-    extern __shared__ float bsm[];
-    const Lat& L = a.L;
-    const int MX = L.MX, MY = L.MY, JX = L.JX, M = L.M;
-    const int H = a.k + 1, NR = BAND_B + 2 * H;
-    float* buf0 = bsm;
-    float* buf1 = buf0 + NR * JX;
-    int* e0 = (int*)(buf1 + NR * JX);
-    int* e1 = e0 + NR;
-    unsigned* rmax = (unsigned*)(e1 + NR);
-    const int x0 = 1 + (int)blockIdx.x * BAND_B, xlo = x0 - H;
-    // load the input rows (halo rows 0 and MX+1 as stored: zeros, EMPTY)
-    for (int i = threadIdx.x; i < NR * JX; i += blockDim.x) {
-        const int x = xlo + i / JX;
-        const float v = (x >= 0 && x <= MX + 1) ? a.in[x * JX + i % JX] : 0.f;
-        buf0[i] = v;
-        buf1[i] = v;  // halo columns (zero) are never written, in either buffer
-    }
-    for (int r = threadIdx.x; r < NR; r += blockDim.x) {
-        const int x = xlo + r;
-        e0[r] = (x >= 0 && x <= MX + 1) ? a.Ein[x] : E2_EMPTY;
-        e1[r] = E2_EMPTY;
-    }
-    __syncthreads();
-    float *cur = buf0, *nxt = buf1;
-    int *ec = e0, *en = e1;
-    for (int j = 1; j <= a.k; j++) {
-        const int s = a.s_first + (j - 1) * DIR;
-        const float* g1 = a.G1f + (size_t)a.seg[s] * M;
-        const int lo = max(1, xlo + j), hi = min(MX, x0 + BAND_B - 1 + H - j);
-        const int nrow = hi - lo + 1;
-        for (int r = threadIdx.x; r < NR; r += blockDim.x) rmax[r] = 0u;
-        // rows outside the lattice keep their stored state (zero, EMPTY)
-        for (int i = threadIdx.x; i < NR * JX; i += blockDim.x) {
-            const int x = xlo + i / JX;
-            if (x < lo || x > hi) nxt[i] = cur[i];
-        }
-        for (int r = threadIdx.x; r < NR; r += blockDim.x) {
-            const int x = xlo + r;
-            if (x < lo || x > hi) en[r] = ec[r];
-        }
-        __syncthreads();
-        // the step: each (row, y) of the valid range
-        for (int i = threadIdx.x; i < nrow * MY; i += blockDim.x) {
-            const int x = lo + i / MY, y = i % MY + 1;
-            const int xm = nmdev::bmap(x - 1, MX, L.b1[0], L.bm[0]), xp = nmdev::bmap(x + 1, MX, L.b1[0], L.bm[0]);
-            const int el = ec[xm - xlo], ecc = ec[x - xlo], er = ec[xp - xlo];
-            const int Eb = max(el, max(ecc, er));
-            float v = 0.f;
-            if (Eb != E2_EMPTY) {
-                const float fl = el == E2_EMPTY ? 0.f : p2f(el - Eb);
-                const float fc = ecc == E2_EMPTY ? 0.f : p2f(ecc - Eb);
-                const float fr = er == E2_EMPTY ? 0.f : p2f(er - Eb);
-                // sten_rows on the band: base[x*JX + y] is row x's slot
-                const float* base = cur - (ptrdiff_t)xlo * JX;
-                v = sten_rows(L, base, x, y, fl, fc, fr) * g1[x * JX + y];
-            }
-            nxt[(x - xlo) * JX + y] = v;
-            if (v > 0.f) atomicMax(&rmax[x - xlo], __float_as_uint(v));
-        }
-        __syncthreads();
-        // renormalise each row, store, compose
-        for (int i = threadIdx.x; i < nrow * MY; i += blockDim.x) {
-            const int x = lo + i / MY, y = i % MY + 1, r = x - xlo;
-            const float m = __uint_as_float(rmax[r]);
-            const int xm = nmdev::bmap(x - 1, MX, L.b1[0], L.bm[0]), xp = nmdev::bmap(x + 1, MX, L.b1[0], L.bm[0]);
-            const int Eb = max(ec[xm - xlo], max(ec[x - xlo], ec[xp - xlo]));
-            const int e = m > 0.f ? expo_f(m) : 0;
-            const float w = m > 0.f ? nxt[r * JX + y] * p2f(-e) : 0.f;
-            const int Eo = m > 0.f ? Eb + e : E2_EMPTY;
-            nxt[r * JX + y] = w;
-            if (y == 1) en[r] = Eo;
-            const bool own = x >= x0 && x < x0 + BAND_B;
-            if (!own) continue;
-            const int gs = x * JX + y;
-            if (DIR > 0) {
-                a.Gf[(size_t)s * M + gs] = w;
-                if (y == 1) a.Ef[(size_t)s * (MX + 2) + x] = Eo;
-            } else {
-                if (Eo != E2_EMPTY) {
-                    const int ef = a.Ef[(size_t)s * (MX + 2) + x];
-                    if (ef != E2_EMPTY) {
-                        const double t = (double)a.Gf[(size_t)s * M + gs] * (double)w * p2d(ef + Eo);
-                        double* rho = a.rho + (size_t)a.mm[s] * M;
-                        const double d = a.deg[s];
-                        if (d == 1.0) rho[gs] += t;
-                        else rho[gs] += d * t;
-                    }
-                }
-                if (j == a.k) {
-                    a.out_last[gs] = w;
-                    if (y == 1) a.Eout_last[x] = Eo;
-                }
-            }
-        }
-        // halo part of ρ (charged systems, backward): own rows' y-halo sites
-        // and the x-halo rows beside the first and last band, from the
-        // previous step's buffer
-        if (DIR < 0 && a.nh) {
-            const int xa = max(x0, 1), xb = min(x0 + BAND_B - 1, MX);
-            const bool lo_row = x0 == 1, hi_row = x0 + BAND_B - 1 >= MX;
-            const int nown = xb - xa + 1;
-            const int nh = 2 * nown + (lo_row ? JX : 0) + (hi_row ? JX : 0);
-            struct Ld {
-                const float* p; const int* E; int xlo; Lat L;
-                __device__ double operator()(int i) const {
-                    const int src = nmdev::bc_source(L, i), xr = src / L.JX - xlo, e = E[xr];
-                    return e == E2_EMPTY ? 0.0 : (double)p[xr * L.JX + src % L.JX] * p2d(e);
-                }
-            };
-            const Ld bl{cur, ec, xlo, L};
-            const double* g1d = a.G1d + (size_t)a.seg[s] * M;
-            double* rho = a.rho + (size_t)a.mm[s] * M;
-            const double d = a.deg[s];
-            const float* gfv = a.Gf + (size_t)s * M;
-            const int* efv = a.Ef + (size_t)s * (MX + 2);
-            for (int t = threadIdx.x; t < nh; t += blockDim.x) {
-                int h;
-                if (t < 2 * nown) h = (xa + t / 2) * JX + ((t & 1) ? MY + 1 : 0);
-                else {
-                    int q = t - 2 * nown;
-                    if (lo_row && q < JX) h = q;
-                    else h = (MX + 1) * JX + (lo_row ? q - JX : q);
-                }
-                const double vv = nmdev::flat_prop_at(L, bl, h) * g1d[h];
-                const int src = nmdev::bc_source(L, h), ef = efv[src / JX];
-                const double gf = ef == E2_EMPTY ? 0.0 : (double)gfv[src] * p2d(ef);
-                if (d == 1.0) rho[h] += gf * vv;
-                else rho[h] += d * gf * vv;
-            }
-        }
-        __syncthreads();
-        float* tf = cur; cur = nxt; nxt = tf;
-        int* ti = ec; ec = en; en = ti;
-    }
-}
-
 }  // namespace
 
 bool ctx2d32_eligible(const nm_plan* p, std::string* why) {
@@ -397,11 +225,6 @@ bool ctx2d32_eligible(const nm_plan* p, std::string* why) {
         }
     }
     return true;
-}
-
-size_t band_smem(const nm_plan* p) {
-    const int NR = BAND_B + 2 * (BAND_K + 1);
-    return sizeof(float) * 2 * NR * p->JX + sizeof(int) * 3 * NR;
 }
 
 int ctx2d32_init(Ctx& C) {
@@ -425,64 +248,8 @@ int ctx2d32_init(Ctx& C) {
             return NM_ERR_NOMEM;
         }
     }
-    // the band kernels (several steps per launch): x bounds mirror or
-    // surface, and the band's shared memory within the device's limit
-    C.use_band = false;
-    if (p->bc[0] != NM_BC_PERIODIC && p->bc[3] != NM_BC_PERIODIC) {
-        const size_t sm = band_smem(p);
-        int dev = 0, optin = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        if (sm <= (size_t)optin &&
-            cudaFuncSetAttribute(k2f_band<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess &&
-            cudaFuncSetAttribute(k2f_band<-1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess) {
-            C.band_tabs.resize(p->n_mol);
-            for (int m = 0; m < p->n_mol; m++) {
-                const nm_molecule& mol = p->mols[m];
-                std::vector<int> seg(mol.n_store), mm(mol.n_store);
-                std::vector<double> deg(mol.n_store);
-                for (int b = 0; b < mol.n_blocks; b++) {
-                    const nm_block& B = mol.blocks[b];
-                    for (int k = 0; k < B.length; k++) {
-                        seg[B.s0 + k] = B.seg; mm[B.s0 + k] = B.molmon; deg[B.s0 + k] = B.degeneracy;
-                    }
-                }
-                auto& T = C.band_tabs[m];
-                if (!al((void**)&T.seg, sizeof(int) * mol.n_store) || !al((void**)&T.mm, sizeof(int) * mol.n_store) ||
-                    !al((void**)&T.deg, sizeof(double) * mol.n_store)) {
-                    set_error("cudaMallocAsync (2-D FP32 band tables)");
-                    return NM_ERR_NOMEM;
-                }
-                cudaMemcpyAsync(T.seg, seg.data(), sizeof(int) * mol.n_store, cudaMemcpyHostToDevice, C.stream);
-                cudaMemcpyAsync(T.mm, mm.data(), sizeof(int) * mol.n_store, cudaMemcpyHostToDevice, C.stream);
-                cudaMemcpyAsync(T.deg, deg.data(), sizeof(double) * mol.n_store, cudaMemcpyHostToDevice, C.stream);
-            }
-            C.use_band = true;
-        }
-    }
     C.use2d32 = true;
     return NM_OK;
-}
-
-static void band(Ctx& C, int m, int dir, int s_first, int k, const float* in, const int* Ein, float* out_last,
-                 int* Eout_last) {
-    const nm_plan* p = C.plan;
-    Band32 a{};
-    a.L = C.lat;
-    a.k = k;
-    a.dir = dir;
-    a.s_first = s_first;
-    a.seg = C.band_tabs[m].seg; a.mm = C.band_tabs[m].mm; a.deg = C.band_tabs[m].deg;
-    a.G1f = C.d_G1f; a.G1d = C.d_G1;
-    a.in = in; a.Ein = Ein;
-    a.Gf = C.mols[m].Gf32; a.Ef = C.E2f[m];
-    a.out_last = out_last; a.Eout_last = Eout_last;
-    a.rho = C.mols[m].rho;
-    a.nh = C.nh ? 1 : 0;
-    const int blocks = (p->MX + BAND_B - 1) / BAND_B;
-    if (dir > 0) k2f_band<1><<<blocks, 512, band_smem(p), C.stream>>>(a);
-    else k2f_band<-1><<<blocks, 512, band_smem(p), C.stream>>>(a);
-    C.launches++;
 }
 
 template <int MODE>
@@ -524,20 +291,13 @@ int ctx2d32_molecule_pass(Ctx& C, int m) {
     a.out = D.Gf32;
     a.Eout = Ef;
     step<1>(C, a);
-    if (C.band_on && C.use_band) {
-        for (int s = 1; s < ns; s += BAND_K) {
-            const int k = std::min(BAND_K, ns - s);
-            band(C, m, +1, s, k, D.Gf32 + (size_t)(s - 1) * M, Ef + (size_t)(s - 1) * R, nullptr, nullptr);
-        }
-    } else {
-        for (int s = 1; s < ns; s++) {
-            a.in = D.Gf32 + (size_t)(s - 1) * M;
-            a.Ein = Ef + (size_t)(s - 1) * R;
-            a.G1 = C.d_G1f + (size_t)seg[s] * M;
-            a.out = D.Gf32 + (size_t)s * M;
-            a.Eout = Ef + (size_t)s * R;
-            step<0>(C, a);
-        }
+    for (int s = 1; s < ns; s++) {
+        a.in = D.Gf32 + (size_t)(s - 1) * M;
+        a.Ein = Ef + (size_t)(s - 1) * R;
+        a.G1 = C.d_G1f + (size_t)seg[s] * M;
+        a.out = D.Gf32 + (size_t)s * M;
+        a.Eout = Ef + (size_t)s * R;
+        step<0>(C, a);
     }
     // G(N)
     const double* Lv = (p->geometry != NM_PLANAR) ? C.d_L : nullptr;
@@ -556,17 +316,6 @@ int ctx2d32_molecule_pass(Ctx& C, int m) {
     a.rho = D.rho + (size_t)mm[top] * M;
     a.d = deg[top];
     step<2>(C, a);
-    if (C.band_on && C.use_band) {
-        // input: the pair buffer the previous launch wrote; output: the other
-        int cur = top & 1;
-        for (int s = top - 1; s >= 0; s -= BAND_K) {
-            const int k = std::min(BAND_K, s + 1);
-            band(C, m, -1, s, k, C.d_gb32 + (size_t)cur * M, C.d_E2b + (size_t)cur * R,
-                 C.d_gb32 + (size_t)(cur ^ 1) * M, C.d_E2b + (size_t)(cur ^ 1) * R);
-            cur ^= 1;
-        }
-        return NM_OK;
-    }
     for (int s = top - 1; s >= 0; s--) {
         a.in = C.d_gb32 + (size_t)((s + 1) & 1) * M;
         a.Ein = C.d_E2b + (size_t)((s + 1) & 1) * R;

@@ -213,9 +213,6 @@ struct Ctx {
     int* d_E2b = nullptr;           // [2][MX+2] exponents of the backward pair
     double* d_rowpart = nullptr;    // [MX+2] per-row partial sums of G(N)
     std::vector<int*> E2f;          // per molecule [n_store][MX+2]
-    bool use_band = false;          // several FP32 steps per launch (band kernels)
-    bool band_on = true;            // nm_ctx_set_option(NM_OPT_BAND2D)
-    std::vector<SweepTab> band_tabs;
 
     int init(const nm_plan* p, const nm_ctx_options* opt);
     ~Ctx();

@@ -106,31 +106,3 @@ def test_fp32_2d_matches_oracle_tight(name):
     phi = phi.reshape(plan.n_seg, -1)
     for i in range(plan.n_seg):
         assert rel_err(interior(plan, phi[i]), interior(plan, phio[i])) < 1e-6, i
-
-
-@pytest.mark.parametrize("name", CASES)
-def test_fp32_2d_bands_equal_single_steps(name):
-    """Several FP32 steps per launch on bands of rows (NM_OPT_BAND2D, the
-    default) against one launch per step: the same arithmetic per row, so
-    the residual and a whole solve are bit-identical."""
-    from namics_gb300._abi import NM_OPT_BAND2D
-    runs = load_golden(name)["runs"]
-    run = runs.get("it5") or runs.get("conv")
-    plan = Plan(run["input"])
-    out = []
-    for band in (0, 1):
-        ctx = Context(plan, NM_FP32)
-        ctx.set_option(NM_OPT_BAND2D, band)
-        x0 = np.array(run["x"])
-        xd = torch.from_numpy(x0).cuda()
-        gd = torch.zeros_like(xd)
-        ctx.residual_dev(xd.data_ptr(), gd.data_ptr())
-        torch.cuda.synchronize()
-        g = gd.cpu().numpy().copy()
-        x = x0.copy()
-        r, phi = ctx.solve_host(x)
-        out.append((g, r, x, phi, ctx.launch_count()))
-    (g0, r0, x0_, p0, l0), (g1, r1, x1_, p1, l1) = out
-    assert np.array_equal(g0, g1)
-    assert r0.iterations == r1.iterations and r0.residual == r1.residual
-    assert np.array_equal(x0_, x1_) and np.array_equal(p0, p1)
