@@ -48,7 +48,10 @@ std::vector<std::string> split(const std::string& s, char c) {
     return out;
 }
 
-struct Entry { std::string cls, name, key, value; };
+struct Entry {
+    std::string cls, name, key, value;
+    mutable bool used = false;  // read by the compiler
+};
 
 // Keyed view of one `start` block of the input (input.cpp:3-78).
 struct InputBlock {
@@ -61,13 +64,16 @@ struct InputBlock {
         return names;
     }
     bool has(const std::string& cls, const std::string& name, const std::string& key) const {
-        for (auto& e : entries) if (e.cls == cls && e.name == name && e.key == key) return true;
-        return false;
+        bool found = false;
+        for (auto& e : entries)
+            if (e.cls == cls && e.name == name && e.key == key) { e.used = true; found = true; }
+        return found;
     }
     std::string get(const std::string& cls, const std::string& name, const std::string& key,
                     const std::string& dflt = "") const {
         std::string v = dflt;  // last occurrence wins
-        for (auto& e : entries) if (e.cls == cls && e.name == name && e.key == key) v = e.value;
+        for (auto& e : entries)
+            if (e.cls == cls && e.name == name && e.key == key) { v = e.value; e.used = true; }
         return v;
     }
 };
@@ -574,6 +580,49 @@ static bool setup_lattice(const InputBlock& in, PlanHolder& H, std::string& err)
     return true;
 }
 
+// Keys the compiler did not read.  The reference refuses a key outside each
+// class's list (Input::CheckParameters, input.cpp:366-431).  Here a key of
+// the reference's lists is accepted unread only where it cannot change a DIIS
+// solve of this path: verbosity, the storage schedule, output requests, the
+// guess files (the caller passes the field), the parameters of the other
+// Newton methods (sfnewton.cpp; iterate_DIIS reads none of them) and of the
+// outer loop of constraints (refused themselves).  Any other key is refused
+// by name, so an input that relies on a feature this build does not have
+// cannot run with it silently dropped.
+static bool no_effect(const Entry& e) {
+    static const char* const newton_keys[] = {
+        "x_info", "e_info", "s_info", "i_info", "t_info", "hs_info", "super_e_info", "super_s_info",
+        "super_i_info", "super_tolerance", "super_iterationlimit", "super_deltamax", "deltamin",
+        "linesearchlimit", "samehessian", "max_accuracy_for_hessian_scaling", "n_iterations_for_hessian",
+        "small_alpha", "target_function", "max_n_small_alpha", "min_accuracy_for_hessian",
+        "max_fr_reverse_direction", "print_hessian_at_it"};
+    static const char* const sys_keys[] = {"GPU", "initial_guess", "guess_inputfile", "final_guess",
+                                           "guess_outputfile"};
+    if (e.cls == "output") return true;
+    if (e.cls == "mol") return e.key == "save_memory";
+    if (e.cls == "newton") {
+        if (e.key == "gradient_type") return e.value == "classical";
+        for (const char* k : newton_keys) if (e.key == k) return true;
+        return false;
+    }
+    if (e.cls == "sys") {
+        if (e.key == "calculation_type") return e.value == "equilibrium";
+        for (const char* k : sys_keys) if (e.key == k) return true;
+        return false;
+    }
+    return false;
+}
+
+static bool check_unread(const InputBlock& in, std::string& err) {
+    for (auto& e : in.entries) {
+        if (e.used || no_effect(e)) continue;
+        err = "input key not supported here (it would change the solve or needs a feature outside this path): '" +
+              e.cls + " : " + e.name + " : " + e.key + "'";
+        return false;
+    }
+    return true;
+}
+
 static nm_plan* build_plan(const InputBlock& in, std::string& err) {
     PlanHolder* H = new PlanHolder();
     nm_plan& P = H->plan;
@@ -859,6 +908,11 @@ int nm_plan_create(const char* input_text, nm_plan** out) {
     std::string err;
     nm_plan* p = nm::build_plan(blk, err);
     if (!p) { nm::set_error(err); return NM_ERR_INPUT; }
+    if (!nm::check_unread(blk, err)) {
+        nm_plan_destroy(p);
+        nm::set_error(err);
+        return NM_ERR_INPUT;
+    }
     *out = p;
     return NM_OK;
 }

@@ -10,6 +10,8 @@ replay the same problem through the oracle and the GPU path without the
 reference present.
 
 Run from the repository root:  python tests/golden/make_golden.py
+(--raw: the verbatim output files; --keys: which input keys the reference
+accepts)
 """
 from __future__ import annotations
 
@@ -328,11 +330,63 @@ def main_raw():
     (GOLDEN / "raw_outputs.json").write_text(json.dumps(out))
 
 
+KEY_BASE = """lat : flat : n_layers : 20
+lat : flat : lattice_type : simple_cubic
+lat : flat : lowerbound : surface
+mon : S : freedom : frozen
+mon : S : frozen_range : lowerbound
+mon : X : freedom : pinned
+mon : X : pinned_range : firstlayer
+mon : A : freedom : free
+mon : W : freedom : free
+mon : A : chi_W : 0.5
+mon : X : chi_W : 0.5
+mol : pol : composition : (X)1(A)19
+mol : pol : freedom : restricted
+mol : pol : n : 0.05
+mol : water : composition : (W)1
+mol : water : freedom : solvent
+newton : isaac : method : DIIS
+newton : isaac : iterationlimit : 0
+"""
+
+# one extra input line per case: keys the reference does not know, keys it
+# knows that cannot change a DIIS solve, and keys it knows that do
+KEY_LINES = [
+    "mon : A : chi_Y : 1", "mon : A : bogus : 1", "lat : flat : bogus : 1", "mol : pol : bogus : 1",
+    "newton : isaac : bogus : 1", "mol : pol : save_memory : true", "newton : isaac : s_info : true",
+    "newton : isaac : e_info : false", "newton : isaac : deltamin : 0.01", "sys : noname : GPU : false",
+    "sys : noname : calculation_type : equilibrium", "lat : flat : lambda : 0.2",
+    "mol : pol : restricted_range : 1;3", "sys : noname : overflow_protection : true",
+]
+
+
+def main_keys():
+    """tests/golden/key_checks.json: whether the reference accepts the base
+    brush input with each line of KEY_LINES added (Input::CheckParameters
+    refuses a key outside the class's list and the run stops)."""
+    out = {"base": KEY_BASE, "cases": []}
+    with tempfile.TemporaryDirectory() as td:
+        wd = Path(td)
+        (wd / "output").mkdir()
+        for i, line in enumerate(KEY_LINES):
+            text = KEY_BASE + line + "\noutput : kal : append : false\nkal : mol : pol : theta\nstart\n"
+            (wd / f"k{i}.in").write_text(text)
+            r = subprocess.run([str(REF_BIN), f"k{i}.in"], cwd=wd, capture_output=True, text=True, timeout=120)
+            refused = "is unknown" in r.stdout or not (wd / "output" / f"k{i}.kal").exists()
+            out["cases"].append({"line": line, "reference": "refused" if refused else "accepted"})
+            print(f"{line:50s} {out['cases'][-1]['reference']}", flush=True)
+    (GOLDEN / "key_checks.json").write_text(json.dumps(out, indent=1))
+
+
 def main():
     if not REF_BIN.exists():
         sys.exit(f"{REF_BIN} missing: build it with  make -f oracle/Makefile.ref")
     if sys.argv[1:2] == ["--raw"]:
         main_raw()
+        return
+    if sys.argv[1:2] == ["--keys"]:
+        main_keys()
         return
     only = set(sys.argv[1:])
     with tempfile.TemporaryDirectory() as td:
