@@ -628,7 +628,10 @@ __device__ __forceinline__ unsigned long long b1_clock() {
 // order (may be null): CTA b solves problem order[b].  The batch lists its
 // problems by descending steps per residual, so the block scheduler spreads
 // the longest solves one per SM before it doubles any of them up.
-__global__ void __launch_bounds__(B1_THREADS, 4) k_batch1d(B1Prob* __restrict__ probs, int mode,
+// Three CTAs per SM (168 registers a thread): at four (128 registers) the
+// FP32 residual spilled inside its step loops and a batch took 8% longer;
+// at two the batch time is the same and the median solve waits longer.
+__global__ void __launch_bounds__(B1_THREADS, 3) k_batch1d(B1Prob* __restrict__ probs, int mode,
                                                           const int* __restrict__ order) {
     B1Prob& P = probs[order ? order[blockIdx.x] : blockIdx.x];
     if (threadIdx.x == 0) P.t_begin = b1_clock();
