@@ -576,9 +576,8 @@ namespace nm {
 // the FP64 phase (G1 [ns·M], cur [M], nxt [M]) and the FP32 phase (G1s, rhos
 // [ns+n_mm][Wl] and three weight rows of Wl floats, Wl = 128·SP); then
 // reduction and DIIS scratch.
-__host__ __device__ inline int b1_sp(int MX) {  // sites per thread: 1, 2 or 4
-    const int sp = (MX + BC_NT - 1) / BC_NT;
-    return sp <= 2 ? sp : 4;
+__host__ __device__ inline int b1_sp(int MX) {  // sites per thread: 1 to 4 (MX <= 512)
+    return (MX + BC_NT - 1) / BC_NT;
 }
 __host__ __device__ inline size_t b1_uni_doubles(int ns, int n_mm, int M, int MX) {
     size_t f64 = (size_t)(ns + 2) * M;
@@ -605,6 +604,7 @@ __device__ __noinline__ void bc_dispatch(B1Prob& P, const Lat1 L, const Coef<dou
     switch (sp) {
         case 1: BC_CALL(1) break;
         case 2: BC_CALL(2) break;
+        case 3: BC_CALL(3) break;
         default: BC_CALL(4) break;
     }
 #undef BC_CALL

@@ -1,7 +1,7 @@
 // FP32 phase of the batched 1-gradient solver: one residual evaluation
 // g(x) with FP32 block-floating-point propagators, 128 threads per problem.
 //
-// Thread t owns the contiguous sites x = t·SP+1 .. t·SP+SP (SP = 1, 2 or 4,
+// Thread t owns the contiguous sites x = t·SP+1 .. t·SP+SP (SP = 1 to 4,
 // so MX <= 512), kept in registers across the whole chain.  A propagation step
 // is register arithmetic plus the two neighbour values of the thread's
 // chunk: shuffles inside a warp, one shared-memory slot per warp edge across
