@@ -46,8 +46,8 @@ UNIT = "solves/s"
 B_PER_UPDATE_FP32 = 22.0   # algorithmic bytes per segment-site update (FP32 propagators, FP64 φ)
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_batch1d launch on the
 # default 512-instance FP32 workload, from one ncu capture
-# (profiles/k_batch1d_fp32_batch512_launches.md): 17.46 GB + 28.26 GB
-TRAFFIC_BATCH512_FP32 = 4.572e10
+# (profiles/k_batch1d_fp32_batch512_launches.md): 15.15 GB + 25.50 GB
+TRAFFIC_BATCH512_FP32 = 4.065e10
 B_PER_UPDATE_FP64 = 36.0
 
 
