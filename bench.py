@@ -103,6 +103,21 @@ def dist_env():
     return ws, rank, local
 
 
+def reduce_over_ranks(ms: float, e2e_s: float, n_ok: int, device="cuda"):
+    """Whole-job figures of N replicas: the slowest rank's step time and
+    end-to-end time (max over ranks) and the converged solves of all ranks
+    (sum).  Without a process group, or with one rank, the figures as given."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return ms, e2e_s, n_ok
+    t = torch.tensor([ms, e2e_s], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    n = torch.tensor([n_ok], dtype=torch.int64, device=device)
+    dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    return float(t[0]), float(t[1]), int(n[0])
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -680,12 +695,7 @@ def main():
         fp64 = {"value": n64 / (ms64 / 1000.0), "unit": UNIT, "ms_per_step": ms64, "converged": n64,
                 "steps": len(t64), "warmup": 1}
         b64.close()
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
     n_ok = int((st == 0).sum())
-    value = n_ok * ws / (ms / 1000.0)
     # end to end through the C ABI with host buffers
     xh = np.concatenate(xs)
     e2e_times = []
@@ -697,6 +707,9 @@ def main():
         e2e_times.append(time.perf_counter() - t0)
     e2e_s = statistics.mean(e2e_times)
     nbytes = xh.nbytes
+    # N replicas: slowest rank's times, all ranks' solves
+    ms, e2e_s, n_all = reduce_over_ranks(ms, e2e_s, n_ok)
+    value = n_all / (ms / 1000.0)
     # roofline: algorithmic bytes of the propagator work of one launch
     updates = 0.0
     for i, p in enumerate(plans):
@@ -717,7 +730,7 @@ def main():
         "data": "synthetic (seeded brush/star instances)",
         "config": {"workload": "batched 1-gradient brushes/stars (512, seeded): n_layers U{50..400}, "
                                "N U{20..500}, sigma U[0.01,0.1], chi U[0,1], 10% 3-arm stars",
-                   "instances": args.instances, "converged": n_ok, "precision": args.precision,
+                   "instances": args.instances * ws, "converged": n_all, "precision": args.precision,
                    "iterations_mean": float(np.mean(its_all)), "iterations_max": int(np.max(its_all)),
                    "segment_site_updates_per_step": updates, "l2": "flushed between steps (256 MB write)",
                    "parallelism": f"replicas x{ws}"},
@@ -729,8 +742,8 @@ def main():
                              "(MEASURED_PEAKS.json hbm_gbs); traffic: DRAM bytes of one launch from an ncu "
                              "capture of this workload, below the algorithmic bytes because the chains run in "
                              "registers and shared memory"},
-        "e2e": {"value": n_ok * ws / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nbytes,
-                "d2h_bytes_per_step": nbytes},
+        "e2e": {"value": n_all / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nbytes * ws,
+                "d2h_bytes_per_step": nbytes * ws},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "latency": latency,
