@@ -84,7 +84,7 @@ def cases() -> list[dict]:
     C = []
     # 1-gradient planar simple-cubic brush, 100 layers, A_100 (X1A99) at σ=0.05
     base = lat1d(100) + brush_lines("(X)1(A)99", n=0.05, chi=0.5)
-    C.append(dict(name="brush1d_cfg1", lines=base, field=(-0.01, 0.01), seed=1, modes=["it0", "conv"]))
+    C.append(dict(name="brush1d_x100", lines=base, field=(-0.01, 0.01), seed=1, modes=["it0", "conv"]))
     # 3-arm star brush (the star variant of the batched workload)
     C.append(dict(name="star1d", lines=lat1d(80) + brush_lines("(X)1(A)19[(A)20](A)20", n=0.04, chi=0.4),
                   field=(-0.01, 0.01), seed=2, modes=["it0", "conv"]))
@@ -205,7 +205,7 @@ def cases() -> list[dict]:
         else:
             comp = f"(X)1(A){N - 1}"
         nl = min(nl, 200)  # keep the reference run short
-        C.append(dict(name=f"cfg4_{i}", lines=lat1d(nl) + brush_lines(comp, n=round(sig, 6), chi=round(chi, 6)),
+        C.append(dict(name=f"brushmix_{i}", lines=lat1d(nl) + brush_lines(comp, n=round(sig, 6), chi=round(chi, 6)),
                       field=(-0.01, 0.01), seed=100 + i, modes=["conv"]))
     return C
 
@@ -311,7 +311,7 @@ def run_case(case: dict, mode: str, workdir: Path) -> dict:
     return out
 
 
-RAW_CASES = ["brush1d_cfg1", "brush2d_cyl", "melt3d", "charged1d"]
+RAW_CASES = ["brush1d_x100", "brush2d_cyl", "melt3d", "charged1d"]
 
 
 def main_raw():

@@ -363,6 +363,6 @@ def test_context_fp32_residual_3d_close_to_oracle():
 
 def test_context_fp32_rejects_unsupported_plan():
     from namics_gb300 import NamicsError
-    run = load_golden("brush1d_cfg1")["runs"]["conv"]
+    run = load_golden("brush1d_x100")["runs"]["conv"]
     with pytest.raises(NamicsError):
         Context(Plan(run["input"]), NM_FP32)

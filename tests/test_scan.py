@@ -28,7 +28,7 @@ def _solve(ctx, x):
     return r, x, F
 
 
-@pytest.mark.parametrize("name", ["brush1d_cfg1", "brush2d_cyl"])
+@pytest.mark.parametrize("name", ["brush1d_x100", "brush2d_cyl"])
 def test_scan_step_equals_fresh_context(name):
     run = load_golden(name)["runs"]["conv"]
     text = run["input"]
@@ -60,7 +60,7 @@ def test_scan_step_equals_fresh_context(name):
 
 
 def test_scan_refuses_splitting_an_iteration_species():
-    run = load_golden("brush1d_cfg1")["runs"]["conv"]
+    run = load_golden("brush1d_x100")["runs"]["conv"]
     plan = Plan(run["input"])
     ctx = Context(plan, NM_FP64)
     r0, xa, Fa = _solve(ctx, np.array(run["x"]))
