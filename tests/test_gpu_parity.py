@@ -366,3 +366,39 @@ def test_context_fp32_rejects_unsupported_plan():
     run = load_golden("brush1d_x100")["runs"]["conv"]
     with pytest.raises(NamicsError):
         Context(Plan(run["input"]), NM_FP32)
+
+
+@pytest.mark.parametrize("nl,N,star", [(300, 240, False), (450, 300, False), (300, 240, True)])
+def test_batched_fp32_wide_lattices(nl, N, star):
+    """Lattices of 256 < MX <= 512, where the FP32 residual keeps three and
+    four sites per thread (the golden fixtures stop at MX 200): one residual
+    at the seeded field within the FP32 floor of the oracle, and an
+    FP32-first solve to ‖g‖ < 1e-10 against the FP64 oracle solved as far,
+    φ to 1e-6 and F to 1e-7."""
+    import bench
+    plan = Plan(_tight(bench.instance_text(nl, N, 0.05, 0.5, star)))
+    assert plan.c.MX == nl
+    x0 = bench.fields([plan])[0]
+    b = Batch([plan], NM_FP32)
+    xd = dev(x0)
+    g32 = torch.zeros_like(xd)
+    b.residual_dev(xd.data_ptr(), g32.data_ptr(), NM_FP32)
+    orc = Oracle(plan)
+    _, go = orc.residual(x0)
+    assert np.linalg.norm(host(g32) - go) < _fp32_floor(plan) * max(1.0, np.linalg.norm(go))
+    x = x0.copy()
+    its, res, st = b.solve_host(x)
+    assert st[0] == 0 and res[0] < 1e-10, (its, res, st)
+    F, _ = b.free_energy()
+    rc, xo, _, ro = orc.solve(x0.copy())
+    assert rc == 0 and ro < 1e-10
+    Fo, _, _ = orc.free_energy()
+    assert abs(F[0] - Fo) <= 1e-7 * max(1, abs(Fo)), (F[0], Fo)
+    ctx = Context(plan, NM_FP64)
+    xd = dev(x)
+    gd = torch.zeros_like(xd)
+    ctx.residual_dev(xd.data_ptr(), gd.data_ptr())
+    phi = ctx.field(0).reshape(plan.n_seg, -1)
+    phio = orc.field(0).reshape(plan.n_seg, -1)
+    for j in range(plan.n_seg):
+        assert rel_err(interior(plan, phi[j]), interior(plan, phio[j])) < 1e-6, j
