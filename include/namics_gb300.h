@@ -138,6 +138,17 @@ typedef struct nm_plan {
     double tolerance, deltamax;
     /* molecule names, in the order of `mols` (the `mol : <name>` keys) */
     const char* const* mol_name;
+    /* a search (`var` keys; Solve_scf::SuperIterate, solve_scf.cpp:717-750):
+     * search_mol < 0 when the input defines none.  search_what: 0 θ, 1 n,
+     * 2 φ_bulk of molecule search_mol.  target_kind: 0 the free energy, 1
+     * the grand potential, 2 a molecule's quantity (target_mol,
+     * target_what: 0 θ, 1 n, 2 φ_bulk, 3 μ); target_value its value.
+     * super_* are the `newton : … : super_*` keys with the reference's
+     * defaults (tolerance·10, iterationlimit/10, 0.5; solve_scf.cpp:153-177). */
+    int    search_mol, search_what, target_kind, target_mol, target_what;
+    double target_value;
+    double super_tolerance, super_deltamax;
+    int    super_iterationlimit;
 } nm_plan;
 
 /* Parse Namics input text (the `lat/mon/mol/sys/newton` key subset of the
@@ -195,6 +206,24 @@ typedef struct nm_solve_result {
 /* DIIS solve from the field x (device, length iv; updated in place).
  * Replaces SFNewton::iterate_DIIS (sfnewton.cpp:1037-1130). */
 int nm_solve_dev(nm_ctx* ctx, double* x_dev, nm_solve_result* res);
+
+typedef struct nm_search_result {
+    double value;            /* the search variable at exit                 */
+    double error;            /* the target's error there (Var->GetError)    */
+    int    iterations;       /* the reference's search iteration count      */
+    int    solves;           /* SCF solves run (evaluations of the error)   */
+    int    status;           /* NM_OK, NM_ERR_NOT_CONVERGED or an error     */
+} nm_search_result;
+
+/* The plan's search: one molecule quantity varied until the target's error
+ * is below super_tolerance.  Replaces Solve_scf::SuperIterate with
+ * SFNewton::iterate_RF (sfnewton.cpp:1132-1185): the damped regula falsi on
+ * the variable's scale relative to its value at each (re)start, every
+ * evaluation a solve from the current field x (device, updated in place) to
+ * super_tolerance.  The molecule's value is left at the search's result,
+ * as nm_ctx_set_values would leave it.  NM_ERR_ARG when the plan has no
+ * search. */
+int nm_ctx_search(nm_ctx* ctx, double* x_dev, nm_search_result* res);
 
 /* Same solve with host buffers: copies x in, solves, copies x back and the
  * per-segment volume fractions out (phi_host: [n_seg*M], may be NULL). */

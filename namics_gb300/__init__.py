@@ -128,6 +128,15 @@ class SolveResult:
     status: int
 
 
+@dataclass
+class SearchResult:
+    value: float       # the searched molecule quantity at exit
+    error: float       # the target's error there
+    iterations: int
+    solves: int
+    status: int
+
+
 class Context:
     """Device state for one problem (nm_ctx)."""
 
@@ -163,6 +172,15 @@ class Context:
         if rc not in (0, _abi.NM_ERR_NOT_CONVERGED) and r.status == 0:
             _check(rc)
         return SolveResult(r.iterations, r.residual, r.status if r.status else rc)
+
+    def search(self, x_ptr: int) -> SearchResult:
+        """The plan's search (`var` keys) from the device field at x_ptr,
+        updated in place; the molecule's value is left at the result."""
+        r = _abi.nm_search_result()
+        rc = _abi.load().nm_ctx_search(self._h, C.c_void_p(x_ptr), C.byref(r))
+        if rc not in (0, _abi.NM_ERR_NOT_CONVERGED):
+            _check(rc)
+        return SearchResult(r.value, r.error, r.iterations, r.solves, r.status)
 
     def solve_host(self, x: np.ndarray, want_phi: bool = True) -> tuple[SolveResult, np.ndarray | None]:
         x = np.ascontiguousarray(x, dtype=np.float64)

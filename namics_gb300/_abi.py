@@ -53,7 +53,11 @@ class nm_plan(C.Structure):
                 ("iv", C.c_int), ("charged", C.c_int), ("n_mol", C.c_int),
                 ("mols", C.POINTER(nm_molecule)), ("solvent", C.c_int), ("neutralizer", C.c_int),
                 ("diis_m", C.c_int), ("iterationlimit", C.c_int), ("max_norm", C.c_int),
-                ("tolerance", C.c_double), ("deltamax", C.c_double), ("mol_name", C.POINTER(C.c_char_p))]
+                ("tolerance", C.c_double), ("deltamax", C.c_double), ("mol_name", C.POINTER(C.c_char_p)),
+                ("search_mol", C.c_int), ("search_what", C.c_int), ("target_kind", C.c_int),
+                ("target_mol", C.c_int), ("target_what", C.c_int), ("target_value", C.c_double),
+                ("super_tolerance", C.c_double), ("super_deltamax", C.c_double),
+                ("super_iterationlimit", C.c_int)]
 
 
 class nm_ctx_options(C.Structure):
@@ -63,6 +67,11 @@ class nm_ctx_options(C.Structure):
 
 class nm_solve_result(C.Structure):
     _fields_ = [("iterations", C.c_int), ("residual", C.c_double), ("status", C.c_int)]
+
+
+class nm_search_result(C.Structure):
+    _fields_ = [("value", C.c_double), ("error", C.c_double), ("iterations", C.c_int),
+                ("solves", C.c_int), ("status", C.c_int)]
 
 
 P_plan = C.POINTER(nm_plan)
@@ -84,6 +93,7 @@ SIGNATURES = [
     ("nm_ctx_set_values", C.c_int, [C.c_void_p, C.POINTER(C.c_char_p), dp, C.c_int]),
     ("nm_residual_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("nm_solve_dev", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(nm_solve_result)]),
+    ("nm_ctx_search", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(nm_search_result)]),
     ("nm_solve_host", C.c_int, [C.c_void_p, dp, dp, C.POINTER(nm_solve_result)]),
     ("nm_get_field", C.c_int, [C.c_void_p, C.c_int, dp]),
     ("nm_get_molecule", C.c_int, [C.c_void_p, C.c_int, dp, dp, dp, dp]),

@@ -694,7 +694,7 @@ int Ctx::check_status() {
 
 int Ctx::solve(double* x, nm_solve_result* res, int max_iter) {
     int nvar = plan->iv, m = plan->diis_m;
-    double dmax = plan->deltamax, tol = plan->tolerance;
+    double dmax = plan->deltamax, tol = tol_override > 0 ? tol_override : plan->tolerance;
     int nb = red_blocks;
     int it = 0, k_diis = 0;
     double resid = 0;
@@ -1165,6 +1165,102 @@ int nm_solve_dev(nm_ctx* ctx, double* x_dev, nm_solve_result* res) {
     if (!ctx || !x_dev || !res) { nm::set_error("nm_solve_dev: null argument"); return NM_ERR_ARG; }
     Ctx* c = reinterpret_cast<Ctx*>(ctx);
     return c->solve(x_dev, res, c->plan->iterationlimit);
+}
+
+int nm_ctx_search(nm_ctx* ctx, double* x_dev, nm_search_result* out) {
+    Ctx* c = reinterpret_cast<Ctx*>(ctx);
+    if (!c || !x_dev || !out) { nm::set_error("nm_ctx_search: null argument"); return NM_ERR_ARG; }
+    const nm_plan* p = c->plan;
+    if (p->search_mol < 0) { nm::set_error("nm_ctx_search: the plan defines no search ('var' keys)"); return NM_ERR_ARG; }
+    static const char* const what[] = {"theta", "n", "phibulk", "mu"};
+    const std::string item = std::string("mol : ") + p->mol_name[p->search_mol] + " : " + what[p->search_what];
+    const char* items[1] = {item.c_str()};
+    const double tol = p->super_tolerance, dmax = p->super_deltamax;
+    const int itlim = p->super_iterationlimit;
+    nm_search_result r{};
+    // inner solves to the search tolerance (solve_scf.cpp:839-846)
+    struct TolGuard {
+        Ctx* c; double old;
+        ~TolGuard() { c->tol_override = old; }
+    } guard{c, c->tol_override};
+    c->tol_override = tol;
+    nm_solve_result sr{};
+    // the target's error (System::GetError, system.cpp:1405-1425;
+    // Molecule::GetError, molecule.cpp:942-968)
+    auto error_now = [&](double& g) -> int {
+        const double t = p->target_value;
+        std::vector<double> mu(p->n_mol);
+        double F = 0, O = 0;
+        if (p->target_kind <= 1 || p->target_what == 3) {
+            int rc = c->free_energy(&F, &O, mu.data());
+            if (rc) return rc;
+        }
+        if (p->target_kind == 0) { g = F - t; return NM_OK; }
+        if (p->target_kind == 1) { g = -(O - t); return NM_OK; }
+        double n = 0, th = 0, pb = 0;
+        int rc = nm_get_molecule(ctx, p->target_mol, nullptr, &n, &th, &pb);
+        if (rc) return rc;
+        const double v = p->target_what == 0 ? th : p->target_what == 1 ? n : p->target_what == 2 ? pb : mu[p->target_mol];
+        g = t != 0 ? v / t - 1.0 : v;
+        if (p->target_what == 2) g = -g;
+        return NM_OK;
+    };
+    // one evaluation: set the variable, solve from the current field, error
+    auto R = [&](double v, double& g) -> int {
+        int rc = nm_ctx_set_values(ctx, items, &v, 1);
+        if (rc) return rc;
+        rc = c->solve(x_dev, &sr, p->iterationlimit);
+        r.solves++;
+        if (rc && rc != NM_ERR_NOT_CONVERGED) return rc;
+        return error_now(g);
+    };
+#define NM_TRY(e) do { int rc_ = (e); if (rc_) { r.status = rc_; *out = r; return rc_; } } while (0)
+    // the variable's current value (the input's, or the last set_values);
+    // the first evaluation solves there (namics.cpp:571-574 goes straight
+    // to SuperIterate)
+    const nm::MolScal& S0 = c->norm_args.mol[p->search_mol];
+    double x = p->search_what == 0 ? S0.theta_in : p->search_what == 1 ? S0.n_in : S0.phibulk_in;
+    // damped regula falsi on the scale of the variable relative to its value
+    // at each (re)start (SFNewton::iterate_RF, sfnewton.cpp:1132-1185),
+    // including its iteration count, which adds the inner steps of the
+    // previous pass again at every restart
+    double a = 0, b = 0, cc = 0, fa = 0, fb = 0, fc = 0, res = 100.0;
+    int k = 0, it = 0;
+    while (it < itlim && std::fabs(res) > tol) {
+        const double xs = x;
+        NM_TRY(R(x, fa));
+        a = 1;
+        x = (a + dmax) * xs;
+        NM_TRY(R(x, fb));
+        b = x / xs;
+        cc = a - 0.5 * ((fa * (a - b)) / (fa - fb));
+        x = cc * xs;
+        NM_TRY(R(x, fc));
+        res = fc;
+        it += k;
+        k = 0;
+        while (k < itlim / 10 && std::fabs(res) > tol) {
+            cc = a - 0.5 * ((fa * (a - b)) / (fa - fb));
+            x = cc * xs;
+            NM_TRY(R(x, fc));
+            if (fc * fb < 0) {
+                b = cc; x = b * xs; NM_TRY(R(x, fb)); res = fb;
+            } else {
+                a = cc; x = a * xs; NM_TRY(R(x, fa)); res = fa;
+            }
+            k++;
+            it++;
+        }
+        if (!std::isfinite(res)) break;
+    }
+#undef NM_TRY
+    r.value = x;
+    r.error = res;
+    r.iterations = it;
+    r.status = std::fabs(res) <= tol ? NM_OK : NM_ERR_NOT_CONVERGED;
+    *out = r;
+    if (r.status) nm::set_error("nm_ctx_search: the target was not reached within super_iterationlimit");
+    return r.status;
 }
 
 int nm_solve_host(nm_ctx* ctx, double* x_host, double* phi_host, nm_solve_result* res) {

@@ -223,6 +223,7 @@ struct Ctx {
     int residual_launches(const double* x, double* g);
     int check_status();
     int solve(double* x, nm_solve_result* res, int max_iter);
+    double tol_override = 0;        // > 0: the solve's tolerance (a search's inner solves)
     int free_energy(double* F, double* Omega, double* mu);
     int elec_init();                                // constants and buffers
     int elec_field(const double* x);                // ψ with mirror bounds, EE

@@ -867,6 +867,78 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
         if (P.diis_m < 1 || P.diis_m > 100) P.diis_m = 10;
         if (P.iterationlimit < 0 || P.iterationlimit > 1000000) P.iterationlimit = 1000;
     }
+    // the outer (search) iteration's controls, defaults of solve_scf.cpp:153-177
+    P.super_tolerance = 10.0 * P.tolerance;
+    P.super_iterationlimit = P.iterationlimit / 10;
+    P.super_deltamax = 0.5;
+    if (!newt.empty()) {
+        const std::string& nn = newt[0];
+        double v; int iv;
+        if (in.has("newton", nn, "super_tolerance") && to_real(in.get("newton", nn, "super_tolerance"), v))
+            P.super_tolerance = v;
+        if (in.has("newton", nn, "super_iterationlimit") && to_int(in.get("newton", nn, "super_iterationlimit"), iv))
+            P.super_iterationlimit = iv;
+        if (in.has("newton", nn, "super_deltamax") && to_real(in.get("newton", nn, "super_deltamax"), v))
+            P.super_deltamax = v;
+    }
+    // ---- a search: `var : mol-<name> : search : theta|n|phibulk` and one
+    // target, `var : sys-<name> : free_energy|grand_potential : <value>` or
+    // `var : mol-<name> : theta|n|phibulk|mu : <value>` (Variate::CheckInput,
+    // variate.cpp:60-200; Molecule::PutVarInfo, molecule.cpp:679-740) ----
+    P.search_mol = -1; P.search_what = -1;
+    P.target_kind = -1; P.target_mol = -1; P.target_what = -1; P.target_value = 0;
+    {
+        static const char* const what[] = {"theta", "n", "phibulk", "mu"};
+        for (const std::string& vn : in.order("var")) {
+            const size_t dash = vn.find('-');
+            if (dash == std::string::npos || vn.find('-', dash + 1) != std::string::npos) {
+                err = "var '" + vn + "': the name is <item>-<name>, e.g. mol-pol";
+                delete H; return nullptr;
+            }
+            const std::string item = vn.substr(0, dash), name = vn.substr(dash + 1);
+            auto set_target = [&](int kind, int mol, int w, const std::string& val) {
+                if (P.target_kind >= 0) { err = "a search takes one target"; return false; }
+                double t;
+                if (!to_real(val, t)) { err = "var '" + vn + "': the target value '" + val + "' is not a number"; return false; }
+                P.target_kind = kind; P.target_mol = mol; P.target_what = w; P.target_value = t;
+                return true;
+            };
+            if (item == "mol") {
+                int mi = -1;
+                for (int m = 0; m < nmol; m++) if (molnames[m] == name) mi = m;
+                if (mi < 0) { err = "var '" + vn + "': no molecule " + name; delete H; return nullptr; }
+                if (in.has("var", vn, "search")) {
+                    const std::string sv = in.get("var", vn, "search");
+                    int w = -1;
+                    for (int k = 0; k < 3; k++) if (sv == what[k]) w = k;
+                    if (w < 0) { err = "var '" + vn + "': search takes theta, n or phibulk"; delete H; return nullptr; }
+                    if (P.search_mol >= 0) { err = "one search per input"; delete H; return nullptr; }
+                    const int fr = H->mb[mi].mol.freedom;
+                    if ((w < 2 && fr != NM_MOL_RESTRICTED) || (w == 2 && fr != NM_MOL_FREE)) {
+                        err = "var '" + vn + "': theta and n are searched on a restricted molecule, phibulk on a free one";
+                        delete H; return nullptr;
+                    }
+                    P.search_mol = mi; P.search_what = w;
+                }
+                for (int k = 0; k < 4; k++)
+                    if (in.has("var", vn, what[k]) && !set_target(2, mi, k, in.get("var", vn, what[k]))) {
+                        delete H; return nullptr;
+                    }
+            } else if (item == "sys") {
+                if (in.has("var", vn, "free_energy") && !set_target(0, -1, -1, in.get("var", vn, "free_energy"))) {
+                    delete H; return nullptr;
+                }
+                if (in.has("var", vn, "grand_potential") &&
+                    !set_target(1, -1, -1, in.get("var", vn, "grand_potential"))) {
+                    delete H; return nullptr;
+                }
+            }
+        }
+        if ((P.search_mol >= 0) != (P.target_kind >= 0)) {
+            err = "a search needs one 'search' and one target";
+            delete H; return nullptr;
+        }
+    }
     // ---- publish pointers ----
     for (auto& s : H->seg_names) H->seg_name_ptrs.push_back(s.c_str());
     P.seg_name = H->seg_name_ptrs.data();

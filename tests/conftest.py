@@ -17,8 +17,10 @@ def pytest_configure(config):
 def golden_names():
     """The per-case fixtures (raw_outputs.json, the reference's output files
     verbatim, is read by test_outputs.py only; key_checks.json, the input keys
-    the reference accepts, by test_input_keys.py)."""
-    return sorted(p.stem for p in GOLDEN.glob("*.json") if p.stem not in ("raw_outputs", "key_checks"))
+    the reference accepts, by test_input_keys.py; search_*.json, the
+    reference's searches, by test_search.py)."""
+    return sorted(p.stem for p in GOLDEN.glob("*.json")
+                  if p.stem not in ("raw_outputs", "key_checks") and not p.stem.startswith("search_"))
 
 
 def load_golden(name):

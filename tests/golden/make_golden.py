@@ -11,7 +11,7 @@ reference present.
 
 Run from the repository root:  python tests/golden/make_golden.py
 (--raw: the verbatim output files; --keys: which input keys the reference
-accepts)
+accepts; --search: the reference's `var` searches)
 """
 from __future__ import annotations
 
@@ -379,6 +379,43 @@ def main_keys():
     (GOLDEN / "key_checks.json").write_text(json.dumps(out, indent=1))
 
 
+# searches: (fixture name, extra input lines); the base is the 1-D
+# (X)1(A)99 brush fixture with its seeded field
+SEARCHES = [
+    ("search_theta_omega", ["var : mol-pol : search : theta", "var : sys-noname : grand_potential : -0.4"]),
+    ("search_theta_F", ["var : mol-pol : search : theta", "var : sys-noname : free_energy : -2.4"]),
+]
+
+
+def main_search():
+    """tests/golden/search_*.json: the reference's `var` searches (θ of the
+    brush for a target grand potential or free energy), run from the brush
+    fixture's seeded field, with the .kal values at the search's end."""
+    case = next(c for c in cases() if c["name"] == "brush1d_x100")
+    with tempfile.TemporaryDirectory() as td:
+        wd = Path(td)
+        (wd / "output").mkdir()
+        for name, extra in SEARCHES:
+            body = list(case["lines"]) + extra
+            text = "\n".join(body + newton()) + "\n"
+            plan = Plan(text)
+            x = make_field(plan, *case["field"], case["seed"], False)
+            write_guess(wd / f"{name}.guess", plan, x)
+            full = text + "sys : noname : initial_guess : file\n" + f"sys : noname : guess_inputfile : {name}.guess\n"
+            full += "output : kal : append : false\n" + "\n".join(
+                f"kal : {k}" for k in ("mol : pol : theta", "mol : pol : n", "sys : noname : grand_potential",
+                                       "sys : noname : free_energy")) + "\nstart\n"
+            (wd / f"{name}.in").write_text(full)
+            r = subprocess.run([str(REF_BIN), f"{name}.in"], cwd=wd, capture_output=True, text=True, timeout=600)
+            kal = wd / "output" / f"{name}.kal"
+            if r.returncode != 0 or not kal.exists():
+                raise RuntimeError(f"reference failed on {name}: {r.stdout[-1500:]}")
+            out = dict(input=text, x=x.tolist(), kal=parse_kal(kal),
+                       super_iterations=[ln for ln in r.stdout.splitlines() if ln.startswith("s_it")])
+            (GOLDEN / f"{name}.json").write_text(json.dumps(out))
+            print(name, out["kal"], flush=True)
+
+
 def main():
     if not REF_BIN.exists():
         sys.exit(f"{REF_BIN} missing: build it with  make -f oracle/Makefile.ref")
@@ -387,6 +424,9 @@ def main():
         return
     if sys.argv[1:2] == ["--keys"]:
         main_keys()
+        return
+    if sys.argv[1:2] == ["--search"]:
+        main_search()
         return
     only = set(sys.argv[1:])
     with tempfile.TemporaryDirectory() as td:

@@ -1,0 +1,92 @@
+"""Searches (`var` keys): one molecule quantity varied until a target is met.
+
+tests/golden/search_*.json (make_golden.py --search) hold the reference's
+searches of θ of the 1-D (X)1(A)99 brush for a target grand potential and a
+target free energy, run from the brush fixture's seeded field, with the .kal
+values at the end (Solve_scf::SuperIterate, SFNewton::iterate_RF).
+
+- CPU: the plan compiler reads the `var` keys and the `super_*` controls
+  with the reference's defaults, and refuses searches it cannot run.
+- GPU: nm_ctx_search ends with the target's error below super_tolerance,
+  at the reference's θ (both searches stop inside the same tolerance, so the
+  θ agree to the tolerance over the slope of the target, about 1e-5
+  relative here), and with the grand potential and free energy of the
+  reference's end point.
+"""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from namics_gb300 import NM_FP64, NamicsError, Plan, _abi
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+CASES = sorted(p.stem for p in GOLDEN.glob("search_*.json"))
+
+
+def _load(name):
+    return json.loads((GOLDEN / f"{name}.json").read_text())
+
+
+def test_search_keys_are_read():
+    g = _load("search_theta_omega")
+    plan = Plan(g["input"])  # keep alive while reading it
+    p = plan.c
+    mols = [p.mol_name[m].decode() for m in range(p.n_mol)]
+    assert (p.search_mol, p.search_what) == (mols.index("pol"), 0)
+    assert (p.target_kind, p.target_value) == (1, -0.4)
+    assert p.super_tolerance == pytest.approx(10 * p.tolerance)
+    assert p.super_iterationlimit == p.iterationlimit // 10
+    assert p.super_deltamax == 0.5
+    qplan = Plan(g["input"] + "newton : isaac : super_tolerance : 1e-5\nnewton : isaac : super_deltamax : 0.2\n")
+    assert (qplan.c.super_tolerance, qplan.c.super_deltamax) == (1e-5, 0.2)
+    fplan = Plan(_load("search_theta_F")["input"])
+    assert fplan.c.target_kind == 0
+    base = g["input"].replace("var : mol-pol : search : theta\n", "").replace(
+        "var : sys-noname : grand_potential : -0.4\n", "")
+    bplan = Plan(base)
+    assert bplan.c.search_mol == -1
+
+
+@pytest.mark.parametrize("extra", [
+    "var : mol-pol : search : theta\n",                                    # no target
+    "var : sys-noname : grand_potential : -0.4\n",                         # no search
+    "var : mol-pol : search : theta\nvar : sys-noname : free_energy : -2\nvar : sys-noname : grand_potential : 0\n",
+    "var : mol-water : search : theta\nvar : sys-noname : free_energy : -2\n",   # the solvent
+    "var : mol-pol : search : phibulk\nvar : sys-noname : free_energy : -2\n",   # restricted: theta or n
+    "var : mol-pol : scan : theta\n",                                      # scans are nm_ctx_set_values
+    "var : pol : search : theta\nvar : sys-noname : free_energy : -2\n",   # not item-name
+])
+def test_unrunnable_searches_are_refused(extra):
+    g = _load("search_theta_omega")
+    base = g["input"].replace("var : mol-pol : search : theta\n", "").replace(
+        "var : sys-noname : grand_potential : -0.4\n", "")
+    with pytest.raises(NamicsError) as ei:
+        Plan(base + extra)
+    assert ei.value.code == _abi.NM_ERR_INPUT
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CASES)
+def test_search_matches_reference(name):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from namics_gb300 import Context
+    g = _load(name)
+    plan = Plan(g["input"])
+    ctx = Context(plan, NM_FP64)
+    x = torch.from_numpy(np.array(g["x"])).cuda()
+    r = ctx.search(x.data_ptr())
+    tol = plan.c.super_tolerance
+    assert r.status == 0 and abs(r.error) <= tol, r
+    k = g["kal"]
+    assert abs(r.value - k["mol_pol_theta"]) <= 1e-4 * k["mol_pol_theta"], (r.value, k["mol_pol_theta"])
+    F, O, _ = ctx.free_energy()
+    if plan.c.target_kind == 1:
+        assert abs(O - plan.c.target_value) <= tol
+    else:
+        assert abs(F - plan.c.target_value) <= tol
+    assert abs(O - k["sys_noname_grand_potential"]) <= 1e-5 and abs(F - k["sys_noname_free_energy"]) <= 1e-5
+    assert ctx.molecule(plan.c.search_mol)["theta"] == pytest.approx(r.value, rel=1e-12)
