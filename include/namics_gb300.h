@@ -149,6 +149,12 @@ typedef struct nm_plan {
     double target_value;
     double super_tolerance, super_deltamax;
     int    super_iterationlimit;
+    /* a scan (`var : mol-<name> : scan : theta|n|phibulk` with step,
+     * end_value, scale, steps; Molecule::PutVarScan, molecule.cpp:785-815):
+     * scan_mol < 0 when the input defines none; steps k = 0 .. scan_n, the
+     * values from nm_plan_scan_value */
+    int    scan_mol, scan_what, scan_n, scan_exponential;
+    double scan_start, scan_end, scan_step;
 } nm_plan;
 
 /* Parse Namics input text (the `lat/mon/mol/sys/newton` key subset of the
@@ -183,6 +189,13 @@ int nm_ctx_destroy(nm_ctx* ctx);
  * on GB300 the per-step launches are the faster of the two. */
 #define NM_OPT_SWEEP2D 1
 int nm_ctx_set_option(nm_ctx* ctx, int option, int value);
+
+/* The value of step k (0 .. plan->scan_n) of the plan's scan
+ * (Molecule::UpdateVarInfo, molecule.cpp:884-930): start + k·step, or on the
+ * exponential scale 10^((1 - k/n)·log10(start) + (k/n)·log10(end)).  The
+ * caller sets it with nm_ctx_set_values and solves, one step at a time.
+ * NM_ERR_ARG without a scan or with k out of range. */
+int nm_plan_scan_value(const nm_plan* plan, int k, double* value);
 
 /* Scans (the reference's Variate: variate.cpp, solve_scf.cpp:717-868): change
  * values of a live context and solve again from its current field (a warm

@@ -111,6 +111,19 @@ class Plan:
         m[tuple(slice(1, -1) for _ in self.shape)] = True
         return m.reshape(-1)
 
+    def scan_values(self) -> list[float]:
+        """The values of the input's scan (`var : … : scan`), step 0 first;
+        empty without a scan."""
+        c = self.c
+        if c.scan_mol < 0:
+            return []
+        out = []
+        for k in range(c.scan_n + 1):
+            v = C.c_double()
+            _check(_abi.load().nm_plan_scan_value(self._p, k, C.byref(v)))
+            out.append(v.value)
+        return out
+
     def chainlength(self, mol: int) -> float:
         return self.c.mols[mol].chainlength
 

@@ -57,7 +57,10 @@ class nm_plan(C.Structure):
                 ("search_mol", C.c_int), ("search_what", C.c_int), ("target_kind", C.c_int),
                 ("target_mol", C.c_int), ("target_what", C.c_int), ("target_value", C.c_double),
                 ("super_tolerance", C.c_double), ("super_deltamax", C.c_double),
-                ("super_iterationlimit", C.c_int)]
+                ("super_iterationlimit", C.c_int),
+                ("scan_mol", C.c_int), ("scan_what", C.c_int), ("scan_n", C.c_int),
+                ("scan_exponential", C.c_int), ("scan_start", C.c_double), ("scan_end", C.c_double),
+                ("scan_step", C.c_double)]
 
 
 class nm_ctx_options(C.Structure):
@@ -94,6 +97,7 @@ SIGNATURES = [
     ("nm_residual_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("nm_solve_dev", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(nm_solve_result)]),
     ("nm_ctx_search", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(nm_search_result)]),
+    ("nm_plan_scan_value", C.c_int, [P_plan, C.c_int, dp]),
     ("nm_solve_host", C.c_int, [C.c_void_p, dp, dp, C.POINTER(nm_solve_result)]),
     ("nm_get_field", C.c_int, [C.c_void_p, C.c_int, dp]),
     ("nm_get_molecule", C.c_int, [C.c_void_p, C.c_int, dp, dp, dp, dp]),

@@ -885,6 +885,8 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
     // target, `var : sys-<name> : free_energy|grand_potential : <value>` or
     // `var : mol-<name> : theta|n|phibulk|mu : <value>` (Variate::CheckInput,
     // variate.cpp:60-200; Molecule::PutVarInfo, molecule.cpp:679-740) ----
+    P.scan_mol = -1; P.scan_what = -1; P.scan_n = 0; P.scan_exponential = 0;
+    P.scan_start = P.scan_end = P.scan_step = 0;
     P.search_mol = -1; P.search_what = -1;
     P.target_kind = -1; P.target_mol = -1; P.target_what = -1; P.target_value = 0;
     {
@@ -924,6 +926,47 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
                     if (in.has("var", vn, what[k]) && !set_target(2, mi, k, in.get("var", vn, what[k]))) {
                         delete H; return nullptr;
                     }
+                if (in.has("var", vn, "scan")) {
+                    // Variate::CheckInput (variate.cpp:280-336), Molecule::PutVarScan
+                    const std::string sv = in.get("var", vn, "scan");
+                    int w = -1;
+                    for (int k = 0; k < 3; k++) if (sv == what[k]) w = k;
+                    const nm_molecule& mol = H->mb[mi].mol;
+                    const bool fits = (w < 2 && mol.freedom == NM_MOL_RESTRICTED) || (w == 2 && mol.freedom == NM_MOL_FREE);
+                    if (w < 0 || !fits) {
+                        err = "var '" + vn + "': scan takes theta or n of a restricted molecule, phibulk of a free one";
+                        delete H; return nullptr;
+                    }
+                    if (P.scan_mol >= 0) { err = "one scan per input"; delete H; return nullptr; }
+                    double end = 0, step = 0;
+                    if (!in.has("var", vn, "end_value") || !to_real(in.get("var", vn, "end_value"), end)) {
+                        err = "var '" + vn + "': a scan needs a numeric end_value"; delete H; return nullptr;
+                    }
+                    const std::string scale = in.get("var", vn, "scale", "linear");
+                    const double start = w == 0 ? mol.theta : w == 1 ? mol.n : mol.phibulk;
+                    int nsteps = 0;
+                    if (scale == "exponential") {
+                        int steps = 1;
+                        if (in.has("var", vn, "steps") && (!to_int(in.get("var", vn, "steps"), steps) || steps < 1)) {
+                            err = "var '" + vn + "': steps (per decade) must be a positive integer"; delete H; return nullptr;
+                        }
+                        if (end * start < 0) { err = "var '" + vn + "': end_value·start < 0"; delete H; return nullptr; }
+                        nsteps = (int)(end > start ? steps * std::log10(end / start) : steps * std::log10(start / end));
+                        P.scan_exponential = 1;
+                    } else if (scale == "linear") {
+                        if (!in.has("var", vn, "step") || !to_real(in.get("var", vn, "step"), step) || step == 0) {
+                            err = "var '" + vn + "': a linear scan needs a nonzero step"; delete H; return nullptr;
+                        }
+                        nsteps = (int)((end - start) / step);
+                        if ((end - start) / step < 0) {
+                            err = "var '" + vn + "': (end_value - start)/step is negative"; delete H; return nullptr;
+                        }
+                    } else {
+                        err = "var '" + vn + "': scale is linear or exponential"; delete H; return nullptr;
+                    }
+                    P.scan_mol = mi; P.scan_what = w; P.scan_n = nsteps;
+                    P.scan_start = start; P.scan_end = end; P.scan_step = step;
+                }
             } else if (item == "sys") {
                 if (in.has("var", vn, "free_energy") && !set_target(0, -1, -1, in.get("var", vn, "free_energy"))) {
                     delete H; return nullptr;
@@ -986,6 +1029,21 @@ int nm_plan_create(const char* input_text, nm_plan** out) {
         return NM_ERR_INPUT;
     }
     *out = p;
+    return NM_OK;
+}
+
+int nm_plan_scan_value(const nm_plan* plan, int k, double* value) {
+    if (!plan || !value || plan->scan_mol < 0 || k < 0 || k > plan->scan_n) {
+        nm::set_error("nm_plan_scan_value: no scan, or step out of range");
+        return NM_ERR_ARG;
+    }
+    const double a = plan->scan_start, b = plan->scan_end;
+    if (!plan->scan_exponential) *value = a + k * plan->scan_step;
+    else if (plan->scan_n == 0) *value = a;
+    else {
+        const double f = 1.0 * k / plan->scan_n;
+        *value = std::pow(10.0, (1 - f) * std::log10(a) + f * std::log10(b));
+    }
     return NM_OK;
 }
 

@@ -18,9 +18,9 @@ def golden_names():
     """The per-case fixtures (raw_outputs.json, the reference's output files
     verbatim, is read by test_outputs.py only; key_checks.json, the input keys
     the reference accepts, by test_input_keys.py; search_*.json, the
-    reference's searches, by test_search.py)."""
+    reference's searches, and scan_*.json, its scans, by test_search.py)."""
     return sorted(p.stem for p in GOLDEN.glob("*.json")
-                  if p.stem not in ("raw_outputs", "key_checks") and not p.stem.startswith("search_"))
+                  if p.stem not in ("raw_outputs", "key_checks") and not p.stem.startswith(("search_", "scan_")))
 
 
 def load_golden(name):

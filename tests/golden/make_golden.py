@@ -11,7 +11,7 @@ reference present.
 
 Run from the repository root:  python tests/golden/make_golden.py
 (--raw: the verbatim output files; --keys: which input keys the reference
-accepts; --search: the reference's `var` searches)
+accepts; --search, --scan: the reference's `var` searches and scans)
 """
 from __future__ import annotations
 
@@ -416,6 +416,47 @@ def main_search():
             print(name, out["kal"], flush=True)
 
 
+# scans: (fixture name, extra input lines) on the same brush
+SCANS = [
+    ("scan_theta_linear", ["var : mol-pol : scan : theta", "var : mol-pol : step : 0.5", "var : mol-pol : end_value : 7"]),
+    ("scan_theta_truncated", ["var : mol-pol : scan : theta", "var : mol-pol : step : 0.1",
+                              "var : mol-pol : end_value : 5.3"]),
+    ("scan_theta_exponential", ["var : mol-pol : scan : theta", "var : mol-pol : scale : exponential",
+                                "var : mol-pol : steps : 2", "var : mol-pol : end_value : 50"]),
+]
+
+
+def main_scan():
+    """tests/golden/scan_*.json: the reference's `var` scans of θ of the
+    brush (linear, linear with a step count the division truncates, and
+    exponential), run from the brush fixture's seeded field, with one .kal
+    row per step."""
+    case = next(c for c in cases() if c["name"] == "brush1d_x100")
+    with tempfile.TemporaryDirectory() as td:
+        wd = Path(td)
+        (wd / "output").mkdir()
+        for name, extra in SCANS:
+            body = list(case["lines"]) + extra
+            text = "\n".join(body + newton()) + "\n"
+            plan = Plan(text)
+            x = make_field(plan, *case["field"], case["seed"], False)
+            write_guess(wd / f"{name}.guess", plan, x)
+            full = text + "sys : noname : initial_guess : file\n" + f"sys : noname : guess_inputfile : {name}.guess\n"
+            full += "output : kal : append : true\n" + "\n".join(
+                f"kal : {k}" for k in ("mol : pol : theta", "sys : noname : grand_potential",
+                                       "sys : noname : free_energy")) + "\nstart\n"
+            (wd / f"{name}.in").write_text(full)
+            r = subprocess.run([str(REF_BIN), f"{name}.in"], cwd=wd, capture_output=True, text=True, timeout=600)
+            kal = wd / "output" / f"{name}.kal"
+            if r.returncode != 0 or not kal.exists():
+                raise RuntimeError(f"reference failed on {name}: {r.stdout[-1500:]}")
+            lines = kal.read_text().strip().splitlines()
+            head = lines[0].split("\t")
+            rows = [dict(zip(head, (float(t) for t in ln.split("\t")))) for ln in lines[1:]]
+            (GOLDEN / f"{name}.json").write_text(json.dumps(dict(input=text, x=x.tolist(), rows=rows)))
+            print(name, [round(rw["mol_pol_theta"], 6) for rw in rows], flush=True)
+
+
 def main():
     if not REF_BIN.exists():
         sys.exit(f"{REF_BIN} missing: build it with  make -f oracle/Makefile.ref")
@@ -427,6 +468,9 @@ def main():
         return
     if sys.argv[1:2] == ["--search"]:
         main_search()
+        return
+    if sys.argv[1:2] == ["--scan"]:
+        main_scan()
         return
     only = set(sys.argv[1:])
     with tempfile.TemporaryDirectory() as td:

@@ -1,4 +1,4 @@
-"""Searches (`var` keys): one molecule quantity varied until a target is met.
+"""Searches and scans (`var` keys) of a molecule quantity.
 
 tests/golden/search_*.json (make_golden.py --search) hold the reference's
 searches of θ of the 1-D (X)1(A)99 brush for a target grand potential and a
@@ -90,3 +90,57 @@ def test_search_matches_reference(name):
         assert abs(F - plan.c.target_value) <= tol
     assert abs(O - k["sys_noname_grand_potential"]) <= 1e-5 and abs(F - k["sys_noname_free_energy"]) <= 1e-5
     assert ctx.molecule(plan.c.search_mol)["theta"] == pytest.approx(r.value, rel=1e-12)
+
+
+SCANS = sorted(p.stem for p in GOLDEN.glob("scan_*.json"))
+
+
+@pytest.mark.parametrize("name", SCANS)
+def test_scan_values_are_the_reference_steps(name):
+    """tests/golden/scan_*.json (make_golden.py --scan): the reference's scans
+    of θ, one .kal row per step.  The plan's step values are the reference's
+    (the step count truncated like its integer division)."""
+    g = _load(name)
+    plan = Plan(g["input"])
+    vals = plan.scan_values()
+    ref = [r["mol_pol_theta"] for r in g["rows"]]
+    assert len(vals) == len(ref)
+    assert np.allclose(vals, ref, rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("extra", [
+    "var : mol-pol : scan : theta\nvar : mol-pol : step : 0.5\n",                               # no end_value
+    "var : mol-pol : scan : theta\nvar : mol-pol : end_value : 7\n",                            # no step
+    "var : mol-pol : scan : theta\nvar : mol-pol : step : -0.5\nvar : mol-pol : end_value : 7\n",  # wrong way
+    "var : mol-pol : scan : phibulk\nvar : mol-pol : step : 0.5\nvar : mol-pol : end_value : 7\n",
+    "var : mol-pol : scan : theta\nvar : mol-pol : scale : log\nvar : mol-pol : end_value : 7\n",
+])
+def test_unrunnable_scans_are_refused(extra):
+    g = _load("scan_theta_linear")
+    base = "\n".join(ln for ln in g["input"].splitlines() if not ln.startswith("var")) + "\n"
+    with pytest.raises(NamicsError) as ei:
+        Plan(base + extra)
+    assert ei.value.code == _abi.NM_ERR_INPUT
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", SCANS)
+def test_scan_matches_reference(name):
+    """Each step: the step's value set on the live context, a solve warm-started
+    from the previous step's field; F and Ω of every step match the
+    reference's rows (both solved to ‖g‖ < 1e-7)."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from namics_gb300 import Context
+    g = _load(name)
+    plan = Plan(g["input"])
+    ctx = Context(plan, NM_FP64)
+    x = torch.from_numpy(np.array(g["x"])).cuda()
+    for v, row in zip(plan.scan_values(), g["rows"]):
+        ctx.set_values({"mol : pol : theta": v})
+        r = ctx.solve_dev(x.data_ptr())
+        assert r.status == 0, (v, r)
+        F, O, _ = ctx.free_energy()
+        for got, want in ((F, row["sys_noname_free_energy"]), (O, row["sys_noname_grand_potential"])):
+            assert abs(got - want) <= 1e-6 * max(1.0, abs(want)), (v, got, want)
