@@ -870,7 +870,27 @@ struct Batch {
 
 #define TRYB(x) do { int r_ = (x); if (r_) return r_; } while (0)
 
+// what the batched solver takes (host checks, before the device is touched)
+static int batch_check(const nm_plan* P) {
+    if (P->gradients != 1) { set_error("batched solver takes 1-gradient problems only"); return NM_ERR_INPUT; }
+    if (P->search_mol >= 0 || P->scan_mol >= 0) {
+        set_error("a search or scan runs on a device context (nm_ctx_search, nm_plan_scan_value), not in a batch");
+        return NM_ERR_INPUT;
+    }
+    if (P->MX > B1_KS * B1_THREADS) { set_error("batched solver takes at most 512 layers"); return NM_ERR_INPUT; }
+    if (P->charged) { set_error("charged systems are not supported by the batched solver"); return NM_ERR_INPUT; }
+    if (P->n_seg > NM_MAX_SEG || P->n_mol > NM_MAX_MOL || P->diis_m > B1_MAXM) {
+        set_error("problem exceeds the batched solver's limits (segments, molecules, DIIS m <= 12)");
+        return NM_ERR_INPUT;
+    }
+    return NM_OK;
+}
+
 static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx_options* opt) {
+    for (int p = 0; p < n; p++) {
+        if (!plans[p]) { set_error("nm_batch_create: null plan"); return NM_ERR_ARG; }
+        if (int rc = batch_check(plans[p])) return rc;
+    }
     B.precision = opt ? opt->precision : NM_FP64;
     int dev = opt ? opt->device : 0;
     cudaError_t e = cudaSetDevice(dev);
@@ -885,13 +905,6 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
     for (int p = 0; p < n; p++) {
         const nm_plan* P = plans[p];
         B.plans.push_back(P);
-        if (P->gradients != 1) { set_error("batched solver takes 1-gradient problems only"); return NM_ERR_INPUT; }
-        if (P->MX > B1_KS * B1_THREADS) { set_error("batched solver takes at most 512 layers"); return NM_ERR_INPUT; }
-        if (P->charged) { set_error("charged systems are not supported by the batched solver"); return NM_ERR_INPUT; }
-        if (P->n_seg > NM_MAX_SEG || P->n_mol > NM_MAX_MOL || P->diis_m > B1_MAXM) {
-            set_error("problem exceeds the batched solver's limits (segments, molecules, DIIS m <= 12)");
-            return NM_ERR_INPUT;
-        }
         B1Prob& H = B.hp[p];
         std::memset(&H, 0, sizeof(H));
         int M = P->M;
@@ -1182,6 +1195,10 @@ struct NoallocCopy { void* dst; const void* src; size_t bytes; };
 static int noalloc_layout(const nm_plan* P, StaticArena& A, double* x_dev, B1Prob& H, size_t& smem,
                           std::vector<double>& ks, std::vector<NoallocCopy>& copies) {
     if (P->gradients != 1) { set_error("nm_solve1d_noalloc: 1-gradient problems only"); return NM_ERR_INPUT; }
+    if (P->search_mol >= 0 || P->scan_mol >= 0) {
+        set_error("nm_solve1d_noalloc: a search or scan runs on a device context");
+        return NM_ERR_INPUT;
+    }
     if (P->MX > B1_KS * B1_THREADS) { set_error("nm_solve1d_noalloc: at most 512 layers"); return NM_ERR_INPUT; }
     if (P->charged) { set_error("nm_solve1d_noalloc: charged systems are not supported"); return NM_ERR_INPUT; }
     if (P->n_seg > NM_MAX_SEG || P->n_mol > NM_MAX_MOL || P->diis_m > B1_MAXM) {

@@ -211,6 +211,10 @@ int nm_server_create(const nm_server_options* opt, nm_server** out) {
 int nm_server_submit(nm_server* srv, const nm_plan* plan, const double* x_host, long long* request_id) {
     Server* s = reinterpret_cast<Server*>(srv);
     if (!s || !plan || !x_host || !request_id) { nm::set_error("nm_server_submit: bad argument"); return NM_ERR_ARG; }
+    if (plan->search_mol >= 0 || plan->scan_mol >= 0) {
+        nm::set_error("nm_server_submit: a search or scan runs on a device context (nm_ctx_search, nm_plan_scan_value)");
+        return NM_ERR_INPUT;
+    }
     auto* r = new nm::Request();
     r->plan = plan;
     r->x.assign(x_host, x_host + plan->iv);

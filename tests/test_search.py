@@ -144,3 +144,21 @@ def test_scan_matches_reference(name):
         F, O, _ = ctx.free_energy()
         for got, want in ((F, row["sys_noname_free_energy"]), (O, row["sys_noname_grand_potential"])):
             assert abs(got - want) <= 1e-6 * max(1.0, abs(want)), (v, got, want)
+
+
+def test_batch_refuses_searches_and_scans_before_the_device():
+    """A plan with a search or a scan needs several solves on one context;
+    the batched solver refuses it (and any plan it cannot take) with
+    NM_ERR_INPUT before it touches the device, so this holds on a CPU host."""
+    from namics_gb300 import Batch
+    for name in ("search_theta_omega", "scan_theta_linear"):
+        plan = Plan(_load(name)["input"])
+        with pytest.raises(NamicsError) as ei:
+            Batch([plan])
+        assert ei.value.code == _abi.NM_ERR_INPUT
+        assert "search or scan" in str(ei.value)
+    text2d = (GOLDEN / "ads2d.json").read_text()
+    plan2d = Plan(json.loads(text2d)["runs"]["conv"]["input"])
+    with pytest.raises(NamicsError) as ei:
+        Batch([plan2d])
+    assert ei.value.code == _abi.NM_ERR_INPUT
