@@ -33,6 +33,8 @@ def load() -> C.CDLL:
         lib.orc_free_energy.argtypes = [C.c_void_p, dp, dp, dp]
         lib.orc_propagate.argtypes = [C.c_void_p, dp, dp, dp]
         lib.orc_side.argtypes = [C.c_void_p, dp, dp]
+        lib.orc_set_amount.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double]
+        lib.orc_search.argtypes = [C.c_void_p, dp, dp, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         _lib = lib
     return _lib
 
@@ -71,6 +73,20 @@ class Oracle:
         else:
             rc = load().orc_solve_n(self._h, _p(x), max_iter, C.byref(it), C.byref(res))
         return rc, x, it.value, res.value
+
+    def set_amount(self, mol: int, what: int, value: float) -> None:
+        """A molecule amount for the next solves (what: 0 θ, 1 n, 2 φ_bulk)."""
+        rc = load().orc_set_amount(self._h, mol, what, value)
+        if rc:
+            raise RuntimeError(f"orc_set_amount rc={rc}")
+
+    def search(self, x: np.ndarray):
+        """The plan's search from x: (rc, x, value, error, iterations, solves)."""
+        x = np.ascontiguousarray(x, dtype=np.float64).copy()
+        v, e = C.c_double(), C.c_double()
+        it, ns = C.c_int(), C.c_int()
+        rc = load().orc_search(self._h, _p(x), C.byref(v), C.byref(e), C.byref(it), C.byref(ns))
+        return rc, x, v.value, e.value, it.value, ns.value
 
     def field(self, which: int) -> np.ndarray:
         p = self.plan

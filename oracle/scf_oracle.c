@@ -24,6 +24,11 @@ struct orc_state {
     double *GN, *norm, *mol_n, *mol_theta, *mol_phibulk, *seg_phibulk;
     double *psi, *EE, *q, *eps, *X;  /* electrostatics (charged systems) */
     int have_state;
+    /* molecule amounts in force (the plan's, until orc_set_amount changes
+     * them, as a Variate scan or search step does) and a search's inner
+     * tolerance (> 0 overrides the plan's) */
+    double *amt_n, *amt_theta, *amt_phibulk;
+    double tol_override;
 };
 
 /* ---- L0 primitives (tools_host.h:185-470) ------------------------------ */
@@ -630,15 +635,16 @@ static int compute_phis(orc_state* st, const double* x) {
         const nm_molecule* mol = &P->mols[m];
         double N = mol->chainlength;
         double norm = 0;
-        st->mol_n[m] = mol->n; st->mol_theta[m] = mol->theta;
+        const double a_n = st->amt_n[m], a_theta = st->amt_theta[m], a_phibulk = st->amt_phibulk[m];
+        st->mol_n[m] = a_n; st->mol_theta[m] = a_theta;
         if (mol->freedom == NM_MOL_FREE) {
-            st->mol_phibulk[m] = mol->phibulk;
-            norm = mol->phibulk / N;
+            st->mol_phibulk[m] = a_phibulk;
+            norm = a_phibulk / N;
             st->mol_n[m] = norm * st->GN[m];
-            A += mol->phibulk * mol->charge; B += mol->phibulk;
+            A += a_phibulk * mol->charge; B += a_phibulk;
         } else if (mol->freedom == NM_MOL_RESTRICTED) {
             if (st->GN[m] > 0) {
-                norm = mol->n / st->GN[m];
+                norm = a_n / st->GN[m];
                 if (mol->pinned) st->mol_phibulk[m] = 0;
                 else {
                     st->mol_phibulk[m] = N * norm;
@@ -817,7 +823,7 @@ static double resid_norm(const double* g, int n, int max_norm) {
 int orc_solve_n(orc_state* st, double* x, int max_iter, int* iterations, double* residual) {
     const nm_plan* P = st->P;
     int nvar = P->iv, m = P->diis_m;
-    double dmax = P->deltamax, tol = P->tolerance;
+    double dmax = P->deltamax, tol = st->tol_override > 0 ? st->tol_override : P->tolerance;
     double* xR = calloc((size_t)m * nvar, sizeof(double));
     double* x_x0 = calloc((size_t)m * nvar, sizeof(double));
     double* x0 = calloc((size_t)nvar, sizeof(double));
@@ -1045,6 +1051,12 @@ orc_state* orc_create(const nm_plan* P) {
     int M = P->M, ns = P->n_seg, nm = P->n_mol;
     st->P = P; st->M = M;
     bc_sources(st);
+    st->amt_n = calloc((size_t)nm, sizeof(double));
+    st->amt_theta = calloc((size_t)nm, sizeof(double));
+    st->amt_phibulk = calloc((size_t)nm, sizeof(double));
+    for (int m = 0; m < nm; m++) {
+        st->amt_n[m] = P->mols[m].n; st->amt_theta[m] = P->mols[m].theta; st->amt_phibulk[m] = P->mols[m].phibulk;
+    }
     st->u = calloc((size_t)ns * M, sizeof(double));
     st->G1 = calloc((size_t)ns * M, sizeof(double));
     st->phi = calloc((size_t)ns * M, sizeof(double));
@@ -1083,7 +1095,109 @@ orc_state* orc_create(const nm_plan* P) {
     return st;
 }
 
+/* A scan or search step's value change (Molecule::PutValue,
+ * molecule.cpp:995-1010): what 0 θ (n = θ/N), 1 n (θ = n·N), 2 φ_bulk. */
+int orc_set_amount(orc_state* st, int m, int what, double v) {
+    const nm_plan* P = st->P;
+    if (m < 0 || m >= P->n_mol) return NM_ERR_ARG;
+    const double N = P->mols[m].chainlength;
+    if (what == 0) { st->amt_theta[m] = v; st->amt_n[m] = v / N; }
+    else if (what == 1) { st->amt_n[m] = v; st->amt_theta[m] = v * N; }
+    else if (what == 2) st->amt_phibulk[m] = v;
+    else return NM_ERR_ARG;
+    return NM_OK;
+}
+
+/* The plan's search (Solve_scf::SuperIterate, solve_scf.cpp:717-750): the
+ * damped regula falsi of SFNewton::iterate_RF (sfnewton.cpp:1132-1185) on
+ * the variable's scale relative to its value at each (re)start, every
+ * evaluation a DIIS solve from the current x to super_tolerance; the error
+ * of System::GetError (system.cpp:1405-1425) or Molecule::GetError
+ * (molecule.cpp:942-968). */
+static int search_error(orc_state* st, double* g) {
+    const nm_plan* P = st->P;
+    const double t = P->target_value;
+    double F = 0, O = 0;
+    double* mu = calloc((size_t)P->n_mol, sizeof(double));
+    int rc = orc_free_energy(st, &F, &O, mu);
+    if (rc == NM_OK) {
+        if (P->target_kind == 0) *g = F - t;
+        else if (P->target_kind == 1) *g = -(O - t);
+        else {
+            const int m = P->target_mol;
+            const double v = P->target_what == 0 ? st->mol_theta[m] : P->target_what == 1 ? st->mol_n[m]
+                           : P->target_what == 2 ? st->mol_phibulk[m] : mu[m];
+            *g = t != 0 ? v / t - 1.0 : v;
+            if (P->target_what == 2) *g = -*g;
+        }
+    }
+    free(mu);
+    return rc;
+}
+
+static int search_eval(orc_state* st, double* x, double v, double* g, int* solves) {
+    const nm_plan* P = st->P;
+    int its; double res;
+    orc_set_amount(st, P->search_mol, P->search_what, v);
+    int rc = orc_solve(st, x, &its, &res);
+    (*solves)++;
+    if (rc) return rc;
+    return search_error(st, g);
+}
+
+int orc_search(orc_state* st, double* x, double* value, double* error, int* iterations, int* solves) {
+    const nm_plan* P = st->P;
+    if (P->search_mol < 0) return NM_ERR_ARG;
+    const double tol = P->super_tolerance, dmax = P->super_deltamax;
+    const int itlim = P->super_iterationlimit;
+    const int m = P->search_mol;
+    double xv = P->search_what == 0 ? st->amt_theta[m] : P->search_what == 1 ? st->amt_n[m] : st->amt_phibulk[m];
+    double a = 0, b = 0, c = 0, fa = 0, fb = 0, fc = 0, res = 100.0;
+    int k = 0, it = 0, rc = NM_OK;
+    *solves = 0;
+    st->tol_override = tol;
+    while (it < itlim && fabs(res) > tol) {
+        const double xs = xv;
+        if ((rc = search_eval(st, x, xv, &fa, solves))) goto done;
+        a = 1;
+        xv = (a + dmax) * xs;
+        if ((rc = search_eval(st, x, xv, &fb, solves))) goto done;
+        b = xv / xs;
+        c = a - 0.5 * ((fa * (a - b)) / (fa - fb));
+        xv = c * xs;
+        if ((rc = search_eval(st, x, xv, &fc, solves))) goto done;
+        res = fc;
+        it += k;  /* the reference counts the previous pass's steps again */
+        k = 0;
+        while (k < itlim / 10 && fabs(res) > tol) {
+            c = a - 0.5 * ((fa * (a - b)) / (fa - fb));
+            xv = c * xs;
+            if ((rc = search_eval(st, x, xv, &fc, solves))) goto done;
+            if (fc * fb < 0) {
+                b = c; xv = b * xs;
+                if ((rc = search_eval(st, x, xv, &fb, solves))) goto done;
+                res = fb;
+            } else {
+                a = c; xv = a * xs;
+                if ((rc = search_eval(st, x, xv, &fa, solves))) goto done;
+                res = fa;
+            }
+            k++;
+            it++;
+        }
+        if (!(res == res)) break;
+    }
+done:
+    st->tol_override = 0;
+    *value = xv;
+    *error = res;
+    *iterations = it;
+    if (rc) return rc;
+    return fabs(res) <= tol ? NM_OK : NM_ERR_NOT_CONVERGED;
+}
+
 void orc_destroy(orc_state* st) {
+    if (st) { free(st->amt_n); free(st->amt_theta); free(st->amt_phibulk); }
     if (!st) return;
     for (int m = 0; m < st->P->n_mol; m++) {
         free(st->Gf[m]); free(st->rho[m]); free(st->jGb[m]); free(st->Pc[m]); free(st->Qb[m]);

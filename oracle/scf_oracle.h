@@ -32,6 +32,10 @@ int orc_get_field(orc_state* st, int which, double* out);
 int orc_get_molecule(orc_state* st, int mol, double* GN, double* n, double* theta,
                      double* phibulk);
 int orc_free_energy(orc_state* st, double* F, double* Omega, double* mu);
+/* a molecule amount in force for the next solves (what: 0 θ, 1 n, 2 φ_bulk),
+ * and the plan's search from x (updated in place) */
+int orc_set_amount(orc_state* st, int mol, int what, double value);
+int orc_search(orc_state* st, double* x, double* value, double* error, int* iterations, int* solves);
 /* Lattice::propagate and Lattice::Side on one array of length M */
 void orc_propagate(orc_state* st, double* G_in, const double* G1, double* G_out);
 void orc_side(orc_state* st, double* X, double* X_side);

@@ -6,7 +6,10 @@ target free energy, run from the brush fixture's seeded field, with the .kal
 values at the end (Solve_scf::SuperIterate, SFNewton::iterate_RF).
 
 - CPU: the plan compiler reads the `var` keys and the `super_*` controls
-  with the reference's defaults, and refuses searches it cannot run.
+  with the reference's defaults, and refuses searches it cannot run.  The
+  oracle's restatement of the search (orc_search) takes the reference's path
+  (θ, F and Ω to 1e-9), and stepping the oracle through the plan's scan
+  values gives the reference's rows.
 - GPU: nm_ctx_search ends with the target's error below super_tolerance,
   at the reference's θ (both searches stop inside the same tolerance, so the
   θ agree to the tolerance over the slope of the target, about 1e-5
@@ -162,3 +165,45 @@ def test_batch_refuses_searches_and_scans_before_the_device():
     with pytest.raises(NamicsError) as ei:
         Batch([plan2d])
     assert ei.value.code == _abi.NM_ERR_INPUT
+
+
+def _oracle(plan):
+    import sys
+    sys.path.insert(0, str(GOLDEN.parents[1] / "oracle"))
+    from orc import Oracle
+    return Oracle(plan)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_search_follows_the_reference(name):
+    """The oracle's restatement of the search (orc_search) takes the
+    reference's path: the same θ, F and Ω at its end to 1e-9."""
+    g = _load(name)
+    plan = Plan(g["input"])
+    orc = _oracle(plan)
+    rc, _, value, error, _, _ = orc.search(np.array(g["x"]))
+    assert rc == 0 and abs(error) <= plan.c.super_tolerance
+    k = g["kal"]
+    assert abs(value - k["mol_pol_theta"]) <= 1e-9 * k["mol_pol_theta"]
+    F, O, _ = orc.free_energy()
+    assert abs(F - k["sys_noname_free_energy"]) <= 1e-9 * abs(k["sys_noname_free_energy"])
+    assert abs(O - k["sys_noname_grand_potential"]) <= 1e-9 * abs(k["sys_noname_grand_potential"])
+
+
+@pytest.mark.parametrize("name", SCANS)
+def test_oracle_scan_follows_the_reference(name):
+    """The oracle stepping through the plan's scan values, each solve warm
+    from the last, gives the reference's F and Ω at every step to 1e-7
+    (a long step, as 15.8 -> 50 on the exponential scale, can end at another
+    point of the ‖g‖ < 1e-7 ball: 7e-9 relative in F there)."""
+    g = _load(name)
+    plan = Plan(g["input"])
+    orc = _oracle(plan)
+    x = np.array(g["x"])
+    for v, row in zip(plan.scan_values(), g["rows"]):
+        orc.set_amount(plan.c.scan_mol, plan.c.scan_what, v)
+        rc, x, _, res = orc.solve(x)
+        assert rc == 0 and res < plan.c.tolerance
+        F, O, _ = orc.free_energy()
+        assert abs(F - row["sys_noname_free_energy"]) <= 1e-7 * max(1.0, abs(row["sys_noname_free_energy"])), v
+        assert abs(O - row["sys_noname_grand_potential"]) <= 1e-7 * max(1.0, abs(row["sys_noname_grand_potential"])), v
