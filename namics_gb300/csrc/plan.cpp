@@ -981,6 +981,13 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
             err = "a search needs one 'search' and one target";
             delete H; return nullptr;
         }
+        // a free molecule's θ or n as the target: the reference's search
+        // ends in NaN (its error does not follow the variable), so it is
+        // refused rather than run
+        if (P.target_kind == 2 && P.target_what <= 1 && H->mb[P.target_mol].mol.freedom == NM_MOL_FREE) {
+            err = "a search for a free molecule's theta or n is not supported (the reference's ends in NaN)";
+            delete H; return nullptr;
+        }
     }
     // ---- publish pointers ----
     for (auto& s : H->seg_names) H->seg_name_ptrs.push_back(s.c_str());

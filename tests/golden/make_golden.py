@@ -379,23 +379,24 @@ def main_keys():
     (GOLDEN / "key_checks.json").write_text(json.dumps(out, indent=1))
 
 
-# searches: (fixture name, extra input lines); the base is the 1-D
-# (X)1(A)99 brush fixture with its seeded field
+# searches: (fixture name, base fixture whose lines and seeded field are
+# used, extra input lines)
 SEARCHES = [
-    ("search_theta_omega", ["var : mol-pol : search : theta", "var : sys-noname : grand_potential : -0.4"]),
-    ("search_theta_F", ["var : mol-pol : search : theta", "var : sys-noname : free_energy : -2.4"]),
+    ("search_theta_omega", "brush1d_x100",
+     ["var : mol-pol : search : theta", "var : sys-noname : grand_potential : -0.4"]),
+    ("search_theta_F", "brush1d_x100", ["var : mol-pol : search : theta", "var : sys-noname : free_energy : -2.4"]),
 ]
 
 
 def main_search():
     """tests/golden/search_*.json: the reference's `var` searches (θ of the
-    brush for a target grand potential or free energy), run from the brush
+    brush for a target grand potential or free energy), run from the base
     fixture's seeded field, with the .kal values at the search's end."""
-    case = next(c for c in cases() if c["name"] == "brush1d_x100")
     with tempfile.TemporaryDirectory() as td:
         wd = Path(td)
         (wd / "output").mkdir()
-        for name, extra in SEARCHES:
+        for name, base_name, extra in SEARCHES:
+            case = next(c for c in cases() if c["name"] == base_name)
             body = list(case["lines"]) + extra
             text = "\n".join(body + newton()) + "\n"
             plan = Plan(text)
@@ -403,8 +404,8 @@ def main_search():
             write_guess(wd / f"{name}.guess", plan, x)
             full = text + "sys : noname : initial_guess : file\n" + f"sys : noname : guess_inputfile : {name}.guess\n"
             full += "output : kal : append : false\n" + "\n".join(
-                f"kal : {k}" for k in ("mol : pol : theta", "mol : pol : n", "sys : noname : grand_potential",
-                                       "sys : noname : free_energy")) + "\nstart\n"
+                f"kal : {k}" for k in ("mol : pol : theta", "mol : pol : n", "mol : pol : phibulk",
+                                       "sys : noname : grand_potential", "sys : noname : free_energy")) + "\nstart\n"
             (wd / f"{name}.in").write_text(full)
             r = subprocess.run([str(REF_BIN), f"{name}.in"], cwd=wd, capture_output=True, text=True, timeout=600)
             kal = wd / "output" / f"{name}.kal"

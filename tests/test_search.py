@@ -207,3 +207,13 @@ def test_oracle_scan_follows_the_reference(name):
         F, O, _ = orc.free_energy()
         assert abs(F - row["sys_noname_free_energy"]) <= 1e-7 * max(1.0, abs(row["sys_noname_free_energy"])), v
         assert abs(O - row["sys_noname_grand_potential"]) <= 1e-7 * max(1.0, abs(row["sys_noname_grand_potential"])), v
+
+
+def test_free_molecule_theta_target_is_refused():
+    """φ_bulk of a free polymer searched for a target θ: the reference's run
+    of this search ends in NaN for every value tried, so the plan refuses it."""
+    g = json.loads((GOLDEN / "ads1d_cyl_hex.json").read_text())["runs"]["conv"]
+    text = g["input"] + "var : mol-pol : search : phibulk\nvar : mol-pol : theta : 56\n"
+    with pytest.raises(NamicsError) as ei:
+        Plan(text)
+    assert ei.value.code == _abi.NM_ERR_INPUT
