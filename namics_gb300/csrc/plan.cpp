@@ -981,9 +981,9 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
             err = "a search needs one 'search' and one target";
             delete H; return nullptr;
         }
-        // a free molecule's θ or n as the target: the reference's search
-        // ends in NaN (its error does not follow the variable), so it is
-        // refused rather than run
+        // a free molecule's θ or n as the target: the reference's run of
+        // such a search (φ_bulk of an adsorbing free polymer for a target θ)
+        // ends in NaN, so it is refused rather than run
         if (P.target_kind == 2 && P.target_what <= 1 && H->mb[P.target_mol].mol.freedom == NM_MOL_FREE) {
             err = "a search for a free molecule's theta or n is not supported (the reference's ends in NaN)";
             delete H; return nullptr;
