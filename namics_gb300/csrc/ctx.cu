@@ -221,6 +221,7 @@ __global__ void k_norms(NormArgs a, double* __restrict__ sc, double* __restrict_
             s[4] = M.phibulk_in;
             norm = M.phibulk_in / M.N;
             s[2] = norm * GN;
+            s[3] = s[2] * M.N;  // θ = n·N, as for the solvent below
             A += M.phibulk_in * M.charge; B += M.phibulk_in;
         } else if (M.freedom == NM_MOL_RESTRICTED) {
             if (GN > 0) {

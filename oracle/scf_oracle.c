@@ -641,6 +641,7 @@ static int compute_phis(orc_state* st, const double* x) {
             st->mol_phibulk[m] = a_phibulk;
             norm = a_phibulk / N;
             st->mol_n[m] = norm * st->GN[m];
+            st->mol_theta[m] = st->mol_n[m] * N;  /* θ = n·N (Molecule::theta of a free molecule) */
             A += a_phibulk * mol->charge; B += a_phibulk;
         } else if (mol->freedom == NM_MOL_RESTRICTED) {
             if (st->GN[m] > 0) {

@@ -76,6 +76,11 @@ def test_oracle_matches_reference(name):
             mol = orc.molecule(m)
             assert abs(mol["GN"] - k[f"mol_{mn}_GN"]) <= tol * abs(k[f"mol_{mn}_GN"])
             assert abs(mu[m] - k[f"mol_{mn}_Mu"]) <= tol * max(1.0, abs(k[f"mol_{mn}_Mu"]))
+            # amounts: free molecules' n and θ follow from G(N), restricted
+            # ones' bulk fraction from the normalisation
+            for q in ("n", "theta", "phibulk"):
+                assert abs(mol[q] - k[f"mol_{mn}_{q}"]) <= max(tol, 1e-12) * max(1.0, abs(k[f"mol_{mn}_{q}"])), \
+                    (mode, mn, q, mol[q], k[f"mol_{mn}_{q}"])
         if mode == "conv":
             assert abs(its - int(k["newton_isaac_iterations"])) <= max(2, its)  # both converged
             assert run["kal"]["newton_isaac_residual"] < newton_tolerance(run)
