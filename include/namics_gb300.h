@@ -250,7 +250,9 @@ int nm_solve_host(nm_ctx* ctx, double* x_host, double* phi_host,
  * permittivity ε [M] (every site, halo layers included). */
 int nm_get_field(nm_ctx* ctx, int which, double* out_host);
 
-/* Per-molecule scalars of the last residual: GN, n, θ, φ_bulk, norm. */
+/* Per-molecule scalars of the last residual: GN, n, θ, φ_bulk.  Restricted
+ * molecules report their input n and θ; free ones, the solvent and the
+ * neutraliser n = norm·GN and θ = n·N (the reference's Molecule::n, theta). */
 int nm_get_molecule(nm_ctx* ctx, int mol, double* GN, double* n,
                     double* theta, double* phibulk);
 
