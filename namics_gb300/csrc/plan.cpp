@@ -950,17 +950,24 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
                         if (in.has("var", vn, "steps") && (!to_int(in.get("var", vn, "steps"), steps) || steps < 1)) {
                             err = "var '" + vn + "': steps (per decade) must be a positive integer"; delete H; return nullptr;
                         }
-                        if (end * start < 0) { err = "var '" + vn + "': end_value·start < 0"; delete H; return nullptr; }
-                        nsteps = (int)(end > start ? steps * std::log10(end / start) : steps * std::log10(start / end));
+                        if (!(end > 0 && start > 0)) {
+                            err = "var '" + vn + "': an exponential scan needs a positive start and end_value";
+                            delete H; return nullptr;
+                        }
+                        const double ns_real = end > start ? steps * std::log10(end / start) : steps * std::log10(start / end);
+                        if (!(ns_real < 1e6)) { err = "var '" + vn + "': more than 10^6 scan steps"; delete H; return nullptr; }
+                        nsteps = (int)ns_real;
                         P.scan_exponential = 1;
                     } else if (scale == "linear") {
                         if (!in.has("var", vn, "step") || !to_real(in.get("var", vn, "step"), step) || step == 0) {
                             err = "var '" + vn + "': a linear scan needs a nonzero step"; delete H; return nullptr;
                         }
-                        nsteps = (int)((end - start) / step);
-                        if ((end - start) / step < 0) {
+                        const double ns_real = (end - start) / step;
+                        if (ns_real < 0) {
                             err = "var '" + vn + "': (end_value - start)/step is negative"; delete H; return nullptr;
                         }
+                        if (!(ns_real < 1e6)) { err = "var '" + vn + "': more than 10^6 scan steps"; delete H; return nullptr; }
+                        nsteps = (int)ns_real;
                     } else {
                         err = "var '" + vn + "': scale is linear or exponential"; delete H; return nullptr;
                     }

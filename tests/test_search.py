@@ -117,6 +117,8 @@ def test_scan_values_are_the_reference_steps(name):
     "var : mol-pol : scan : theta\nvar : mol-pol : step : -0.5\nvar : mol-pol : end_value : 7\n",  # wrong way
     "var : mol-pol : scan : phibulk\nvar : mol-pol : step : 0.5\nvar : mol-pol : end_value : 7\n",
     "var : mol-pol : scan : theta\nvar : mol-pol : scale : log\nvar : mol-pol : end_value : 7\n",
+    "var : mol-pol : scan : theta\nvar : mol-pol : scale : exponential\nvar : mol-pol : end_value : 0\n",
+    "var : mol-pol : scan : theta\nvar : mol-pol : step : 1e-9\nvar : mol-pol : end_value : 7\n",  # 2e9 steps
 ])
 def test_unrunnable_scans_are_refused(extra):
     g = _load("scan_theta_linear")
