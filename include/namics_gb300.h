@@ -351,9 +351,11 @@ long long nm_server_launch_count(nm_server* srv);
 int nm_server_destroy(nm_server* srv);
 
 /* ---- allocation-free single-problem solve --------------------------------
- * No counterpart in the reference.  For callers that must not allocate
- * device memory when they solve (a fixed memory budget carved up front, a
- * sequence about to be captured, a re-solve on a latency-critical path):
+ * No counterpart in the reference.  For callers that cannot call the
+ * device allocator when they solve: a host that hands out a fixed device
+ * memory budget before work starts and owns every byte of it, or a
+ * re-solve on a latency-critical path where an allocation could stall or
+ * fail.  It
  * solves one 1-gradient problem with the batched solver's kernels, its
  * whole device scratch (descriptor, lattice arrays, stored propagators,
  * DIIS history, residual) carved from one static device array of
@@ -363,8 +365,9 @@ int nm_server_destroy(nm_server* srv);
  * that device current; make that first call before any stream capture.
  * All calls share the array: calls that overlap in time race on it.
  * x_dev: the plan's iteration vector (length iv), updated in place.
- * stream: cudaStream_t or NULL for the default stream; the call returns
- * after the stream has finished the solve.  Returns res->status (NM_OK,
+ * stream: cudaStream_t or NULL for the default stream; the call
+ * synchronises that stream and returns the result on the host, after the
+ * stream has finished the solve.  Returns res->status (NM_OK,
  * NM_ERR_NOT_CONVERGED or an error). */
 #define NM_NOALLOC_SCRATCH_BYTES (8u << 20)
 int nm_solve1d_noalloc(const nm_plan* plan, double* x_dev, int precision,

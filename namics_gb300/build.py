@@ -92,13 +92,16 @@ def build_oracle(verbose: bool = False) -> Path:
     return lib
 
 
-def build_reference(ref: str = "/root/reference") -> Path | None:
-    """Compile the unmodified reference program into oracle/_ref (only where
-    its sources are present; the recipe is oracle/Makefile.ref)."""
-    if not Path(ref, "src").is_dir():
+def build_reference(ref: str | None = None) -> Path | None:
+    """Compile the unmodified reference program into oracle/_ref, only where
+    its sources are present.  The sources' location is `ref`, else the
+    environment variable NAMICS_REFERENCE, else the recipe's own default
+    (oracle/Makefile.ref, REF)."""
+    ref = ref or os.environ.get("NAMICS_REFERENCE")
+    mk = ["make", "-s", "-f", str(ORACLE / "Makefile.ref")] + ([f"REF={ref}"] if ref else [])
+    if subprocess.run(mk + ["have-sources"], capture_output=True).returncode != 0:
         return None
-    jobs = str(os.cpu_count() or 4)
-    _run(["make", "-s", "-f", str(ORACLE / "Makefile.ref"), f"REF={ref}", "-j", jobs])
+    _run(mk + ["-j", str(os.cpu_count() or 4)])
     return ORACLE / "_ref" / "namics"
 
 

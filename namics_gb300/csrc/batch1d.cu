@@ -870,6 +870,21 @@ struct Batch {
 
 #define TRYB(x) do { int r_ = (x); if (r_) return r_; } while (0)
 
+// Raise k_batch1d's dynamic shared-memory limit on device `dev` (current) to
+// at least `bytes`.  The limit only ever rises, and every path that launches
+// k_batch1d (batches, the server's workers, the allocation-free solve) goes
+// through this one lock, so no caller can lower it under another's launch.
+static cudaError_t b1_raise_smem(int dev, size_t bytes) {
+    static std::mutex mu;
+    static size_t set[64] = {};
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (bytes <= set[dev]) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(k_batch1d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) set[dev] = bytes;
+    return e;
+}
+
 // what the batched solver takes (host checks, before the device is touched)
 static int batch_check(const nm_plan* P) {
     if (P->gradients != 1) { set_error("batched solver takes 1-gradient problems only"); return NM_ERR_INPUT; }
@@ -997,17 +1012,9 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
     }
     B.smem = maxsmem;
     if (maxsmem > 220 * 1024) { set_error("problem too large for the batched solver's shared memory"); return NM_ERR_INPUT; }
-    // the kernel's dynamic shared-memory limit only ever rises, so batches
-    // created on other threads cannot lower it under a running launch
-    static std::mutex smem_mu;
-    static size_t smem_set[64] = {};
-    {
-        std::lock_guard<std::mutex> lk(smem_mu);
-        if (dev >= 0 && dev < 64 && maxsmem > smem_set[dev]) {
-            cudaError_t e1 = cudaFuncSetAttribute(k_batch1d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)maxsmem);
-            if (e1 != cudaSuccess) { set_error("cudaFuncSetAttribute failed"); return NM_ERR_CUDA; }
-            smem_set[dev] = maxsmem;
-        }
+    if (cudaError_t e1 = b1_raise_smem(dev, maxsmem)) {
+        set_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e1));
+        return NM_ERR_CUDA;
     }
     return NM_OK;
 }
@@ -1154,15 +1161,16 @@ long long nm_batch_launch_count(nm_batch* b) {
 // Allocation-free single-problem solve.
 //
 // Some callers cannot allocate device memory at the point where they solve:
-// a host that owns a fixed memory budget sliced before work begins, a
-// sequence about to be captured into a CUDA graph, or a signal-time
-// re-solve that must not touch the allocator.  nm_solve1d_noalloc runs the
+// a host that owns a fixed device memory budget sliced before work begins,
+// or a re-solve on a latency-critical path that must not touch the
+// allocator.  nm_solve1d_noalloc runs the
 // same kernel as nm_batch_solve_dev on one 1-gradient problem, with every piece of device scratch
 // carved from one file-scope array compiled into the library.  The array's
 // address is looked up once per device (cudaGetSymbolAddress, with that
 // device current) on the first call for that device; make that first call
 // before any stream capture.  The scratch is shared, so calls that overlap
-// in time (two host threads, or two streams in flight) race on it.
+// in time (two host threads, or two streams in flight) race on it.  Each
+// call synchronises its stream and returns its result on the host.
 // ======================================================================
 namespace nm {
 
@@ -1291,16 +1299,6 @@ full:
     return NM_ERR_INPUT;
 }
 
-// raise (never lower) a kernel's dynamic shared-memory limit
-template <typename K>
-static cudaError_t noalloc_smem(K kernel, size_t bytes) {
-    cudaFuncAttributes fa;
-    cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
-    if (e != cudaSuccess) return e;
-    if ((size_t)fa.maxDynamicSharedSizeBytes >= bytes) return cudaSuccess;
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-}
-
 }  // namespace nm
 
 extern "C" int nm_solve1d_noalloc(const nm_plan* plan, double* x_dev, int precision, void* stream,
@@ -1327,7 +1325,7 @@ extern "C" int nm_solve1d_noalloc(const nm_plan* plan, double* x_dev, int precis
     std::vector<NoallocCopy> copies;
     int rc = noalloc_layout(plan, A, x_dev, H, smem, ks, copies);
     if (rc) return rc;
-    e = noalloc_smem(k_batch1d, smem);
+    e = b1_raise_smem(dev, smem);
     if (e != cudaSuccess) { set_error(std::string("nm_solve1d_noalloc: ") + cudaGetErrorString(e)); return NM_ERR_CUDA; }
     // what the batch path's zero-filled allocations start from
     e = cudaMemsetAsync(A.base, 0, A.used, st);

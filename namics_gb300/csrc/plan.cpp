@@ -962,12 +962,18 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
                         if (!in.has("var", vn, "step") || !to_real(in.get("var", vn, "step"), step) || step == 0) {
                             err = "var '" + vn + "': a linear scan needs a nonzero step"; delete H; return nullptr;
                         }
+                        // the step count is (end - start)/step truncated to an
+                        // int first, as the reference assigns it
+                        // (molecule.cpp:807-812): a ratio in (-1, 0) is a
+                        // zero-step scan, a truncated count below 0 is refused
                         const double ns_real = (end - start) / step;
-                        if (ns_real < 0) {
+                        if (!(ns_real < 1e6 && ns_real > -1e6)) {
+                            err = "var '" + vn + "': more than 10^6 scan steps"; delete H; return nullptr;
+                        }
+                        nsteps = (int)ns_real;
+                        if (nsteps < 0) {
                             err = "var '" + vn + "': (end_value - start)/step is negative"; delete H; return nullptr;
                         }
-                        if (!(ns_real < 1e6)) { err = "var '" + vn + "': more than 10^6 scan steps"; delete H; return nullptr; }
-                        nsteps = (int)ns_real;
                     } else {
                         err = "var '" + vn + "': scale is linear or exponential"; delete H; return nullptr;
                     }

@@ -128,6 +128,16 @@ def test_unrunnable_scans_are_refused(extra):
     assert ei.value.code == _abi.NM_ERR_INPUT
 
 
+def test_scan_ratio_truncating_to_zero_steps_is_accepted():
+    """(end - start)/step = (4.8 - 5)/0.5 = -0.4: the reference assigns the
+    ratio to an int first (molecule.cpp:807-812), so the scan has zero steps
+    and runs once at the start value (the reference's own run of this input
+    writes one .kal row at θ = 5)."""
+    g = _load("scan_theta_linear")
+    plan = Plan(g["input"].replace("end_value : 7", "end_value : 4.8"))
+    assert plan.scan_values() == pytest.approx([5.0], rel=1e-12)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", SCANS)
 def test_scan_matches_reference(name):
