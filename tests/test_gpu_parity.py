@@ -210,20 +210,37 @@ def test_propagate_and_side_match_oracle(name):
     rng = np.random.default_rng(7)
     G = rng.uniform(0.5, 1.5, plan.M)
     G1 = rng.uniform(0.5, 1.5, plan.M)
-    # the reference keeps a frozen wall at 'surface' halo layers
+    X = rng.uniform(0, 1, plan.M)
+    # a 'surface' halo layer is a frozen wall: set_bounds leaves it alone and
+    # every propagator of a solve is 0 there (G1 = 0 on frozen sites), so the
+    # inputs carry that 0; φ_side reads the wall's frozen volume fraction,
+    # which any value stands for
+    wall = _surface_halo(plan)
+    G[wall] = 0.0
     mask = plan.interior_mask()
-    c = plan.c
     ref = orc.propagate(G * 1.0, G1)
     Gd, G1d, out = dev(G), dev(G1), torch.zeros(plan.M, dtype=torch.float64, device="cuda")
-    surf = any(c.bc[i] == 2 for i in range(6))
-    if not surf:
-        ctx.propagate_dev(Gd.data_ptr(), G1d.data_ptr(), out.data_ptr())
-        assert rel_err(host(out)[mask], ref[mask]) < 1e-12
-        X = rng.uniform(0, 1, plan.M)
-        side_ref = orc.side(orc_bounds(orc, X))
-        out2 = torch.zeros_like(out)
-        ctx.side_dev(dev(X).data_ptr(), out2.data_ptr())
-        assert rel_err(host(out2)[mask], side_ref[mask]) < 1e-12
+    ctx.propagate_dev(Gd.data_ptr(), G1d.data_ptr(), out.data_ptr())
+    assert rel_err(host(out)[mask], ref[mask]) < 1e-12
+    side_ref = orc.side(orc_bounds(orc, X))
+    out2 = torch.zeros_like(out)
+    ctx.side_dev(dev(X).data_ptr(), out2.data_ptr())
+    assert rel_err(host(out2)[mask], side_ref[mask]) < 1e-12
+
+
+def _surface_halo(plan):
+    """Boolean [M]: the halo sites of faces whose boundary is 'surface'
+    (bc order x-low, y-low, z-low, x-high, y-high, z-high)."""
+    c = plan.c
+    shape = plan.shape
+    m = np.zeros(shape, dtype=bool)
+    for ax in range(len(shape)):
+        for side, k in ((0, ax), (1, ax + 3)):
+            if c.bc[k] == 2:
+                sl = [slice(None)] * len(shape)
+                sl[ax] = 0 if side == 0 else shape[ax] - 1
+                m[tuple(sl)] = True
+    return m.reshape(-1)
 
 
 def orc_bounds(orc, X):

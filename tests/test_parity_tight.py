@@ -1,0 +1,125 @@
+"""Converged parity at 1e-10: the FP64 device path and the oracle reach the
+same fixed point of the SCF equations.
+
+Both sides start from the golden fixture's seeded field.  Each first runs its
+own solver, the reference's DIIS (sfnewton.cpp:1037-1130), to the input's
+tolerance: the device context through the C ABI, the oracle in C.  Then each
+is driven below ‖g‖₂ = 1e-12 by the same Anderson mixer over its OWN residual
+function (tests/helpers.anderson_polish).  The reference's DIIS cannot go that
+far: its Gram matrix carries +1e-9 in every entry (sfnewton.cpp:863), so below
+‖g‖ ≈ 1e-11 the small solve is left with about one significant digit and
+stalls or diverges, on the oracle and on the reference alike.
+
+At ‖g‖ ≤ 1e-12 two solves of the oracle from different starts agree to a few
+1e-13 on φ and F for every fixture listed in TIGHT, so 1e-10 relative is a
+meaningful bar for the device path against the oracle:
+  φ of every segment type (interior sites, relative to its largest value),
+  F and Ω (relative to max(1, |F|)), and GN, n, θ of every molecule.
+
+Fixtures whose residual map has a noise floor above 1e-12 are held to what
+their fixed point is defined to (FLOORED, each with the two-start spread of
+the oracle itself).  The 2-D charged planar and cylindrical brushes stall
+near ‖g‖ = 1e-7 in the reference, the oracle and here: the permittivity at
+halo sites reaches ~1e8 (the flat-array composition there) and amplifies
+rounding in the Poisson update.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from helpers import anderson_polish, interior, rel_err
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+from namics_gb300 import NM_FP64, Context, Plan  # noqa: E402
+from orc import Oracle  # noqa: E402
+
+# name -> (polish target ‖g‖, φ tolerance, F tolerance); measured two-start
+# spread of the oracle at that residual in the comments
+FLOORED = {
+    "charged2d": (2e-7, 5e-3, 1e-6),       # oracle spread φ 6.5e-4, F 4.6e-8
+    "charged2d_cyl": (1e-6, 1e-2, 1e-5),   # oracle spread φ 1.0e-3, F 3.6e-6
+    "charged2d_hex": (1e-12, 2e-8, 1e-10),  # oracle spread φ 2.8e-9, F 4.2e-12
+    "charged3d": (1e-12, 1e-9, 1e-10),     # oracle spread φ 9.0e-11, F 2.6e-12
+}
+CASES = golden_names()
+TIGHT = [n for n in CASES if n not in FLOORED]
+
+
+def _first_run(name):
+    g = load_golden(name)
+    return g["runs"].get("conv") or next(iter(g["runs"].values()))
+
+
+def _gpu_resid(ctx, plan):
+    xd = torch.zeros(plan.iv, dtype=torch.float64, device="cuda")
+    gd = torch.zeros_like(xd)
+
+    def f(x):
+        xd.copy_(torch.from_numpy(x))
+        ctx.residual_dev(xd.data_ptr(), gd.data_ptr())
+        torch.cuda.synchronize()
+        return gd.cpu().numpy()
+    return f
+
+
+def _orc_resid(orc):
+    def f(x):
+        rc, g = orc.residual(x)
+        return g if rc == 0 else np.full_like(x, np.nan)
+    return f
+
+
+def _fixed_points(name, target):
+    run = _first_run(name)
+    plan = Plan(run["input"])
+    x0 = np.array(run["x"])
+    ctx = Context(plan, NM_FP64)
+    xg = x0.copy()
+    res, _ = ctx.solve_host(xg, want_phi=False)
+    assert res.status in (0, -14), res  # converged, or the iteration limit (it0/it5 fixtures)
+    xg, rg, _ = anderson_polish(_gpu_resid(ctx, plan), xg, tol=target / 10)
+    orc = Oracle(plan)
+    rc, xo, _, _ = orc.solve(x0.copy())
+    assert rc == 0, rc
+    xo, ro, _ = anderson_polish(_orc_resid(orc), xo, tol=target / 10)
+    # leave both objects at their fixed point's state
+    _gpu_resid(ctx, plan)(xg)
+    assert orc.residual(xo)[0] == 0
+    return plan, ctx, orc, rg, ro
+
+
+def _compare(plan, ctx, orc, tol_phi, tol_F):
+    phi = ctx.field(0).reshape(plan.n_seg, -1)
+    phio = orc.field(0).reshape(plan.n_seg, -1)
+    for i in range(plan.n_seg):
+        a, b = interior(plan, phi[i]), interior(plan, phio[i])
+        if np.max(np.abs(b)) > 0:
+            assert rel_err(a, b) < tol_phi, (plan.seg_names[i], rel_err(a, b))
+    F, O, mu = ctx.free_energy()
+    Fo, Oo, muo = orc.free_energy()
+    assert abs(F - Fo) <= tol_F * max(1, abs(Fo)), (F, Fo)
+    assert abs(O - Oo) <= tol_F * max(1, abs(Oo)), (O, Oo)
+    for m in range(plan.n_mol):
+        d, do = ctx.molecule(m), orc.molecule(m)
+        for k in ("GN", "n", "theta"):
+            assert abs(d[k] - do[k]) <= tol_F * max(abs(do[k]), 1e-300), (m, k, d[k], do[k])
+
+
+@pytest.mark.parametrize("name", TIGHT)
+def test_fp64_fixed_point_matches_oracle_1e10(name):
+    plan, ctx, orc, rg, ro = _fixed_points(name, 1e-12)
+    assert rg <= 1e-12 and ro <= 1e-12, (rg, ro)
+    _compare(plan, ctx, orc, 1e-10, 1e-10)
+
+
+@pytest.mark.parametrize("name", sorted(FLOORED))
+def test_fp64_fixed_point_matches_oracle_at_noise_floor(name):
+    target, tol_phi, tol_F = FLOORED[name]
+    plan, ctx, orc, rg, ro = _fixed_points(name, target)
+    assert rg <= target and ro <= target, (rg, ro)
+    _compare(plan, ctx, orc, tol_phi, tol_F)
