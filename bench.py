@@ -1,15 +1,17 @@
-"""Benchmark: SCF solves/s at |residual| < 1e-7 on the batched brush workload.
+"""Benchmark: SCF solves/s at |residual| < 1e-7 on a stream of batched brushes.
 
 Workload (one "step"): 512 independent 1-gradient planar brushes solved to
-‖g‖₂ < 1e-7 from seeded fields u ~ U(-0.01, 0.01), drawn from a fixed seed:
-n_layers ~ U{50..400}, N ~ U{20..500}, σ ~ U[0.01, 0.1], χ_AS ~ U[0, 1];
-every 10th instance is a 3-arm star with arms of N/3 joined at a branch point.
-All 512 solves run in one launch (one 128-thread CTA per problem, DIIS on
-the device): FP32 block-floating-point propagators, FP64 normalisation,
-residual and DIIS, and an FP64-propagator finish inside the same CTA.  The
-plain FP64 path (the same kernel with FP64 propagators throughout) is timed
-in the same run and reported beside it (`fp64_gpu`), and so are the p50/p99
-of the per-problem time to convergence inside the launch (device timer).
+‖g‖₂ < 1e-7, drawn from a fixed seed: n_layers ~ U{50..400}, N ~ U{20..500},
+σ ~ U[0.01, 0.1], χ_AS ~ U[0, 1]; every 10th instance is a 3-arm star with
+arms of N/3 joined at a branch point.  Every step solves them from a fresh
+seeded start field u ~ U(-0.01, 0.01).  The K timed steps run through one
+device-resident work loop (resident 128-thread CTAs taking problems from a
+queue, DIIS on the device): FP32 block-floating-point propagators, FP64
+normalisation, residual and DIIS, and an FP64-propagator finish in the same
+CTA.  Beside it: the same stream with FP64 propagators throughout
+(`fp64_gpu`), the plain FP64 GPU path that solves one problem at a time
+through a device context (`fp64_gpu_unbatched`), and the p50/p99 of the
+per-problem time to convergence (device timer).
 
 Contract: `python bench.py --gpus N --steps K --warmup W` prints one JSON
 line.  `value` times the kernel with inputs resident in HBM (CUDA events);
@@ -44,10 +46,6 @@ FIELD = (-0.01, 0.01)
 METRIC = "SCF solves/s at |residual|<1e-7 (served FP32 vs plain FP64 GPU); p50/p99 latency"
 UNIT = "solves/s"
 B_PER_UPDATE_FP32 = 22.0   # algorithmic bytes per segment-site update (FP32 propagators, FP64 φ)
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_batch1d launch on the
-# default 512-instance FP32 workload, from one ncu capture
-# (profiles/k_batch1d_fp32_batch512_launches.md): 15.15 GB + 25.50 GB
-TRAFFIC_BATCH512_FP32 = 4.065e10
 B_PER_UPDATE_FP64 = 36.0
 
 
@@ -181,7 +179,7 @@ def cpu_baseline(texts, xs, budget_s: float = 15.0, threads: int | None = None) 
     from orc import Oracle
     threads = threads or os.cpu_count() or 1
     lock = threading.Lock()
-    state = {"next": 0, "done": 0, "its": 0}
+    state = {"next": 0, "done": 0, "ok": 0, "its": 0}
     t0 = time.perf_counter()
     deadline = t0 + budget_s
 
@@ -196,6 +194,7 @@ def cpu_baseline(texts, xs, budget_s: float = 15.0, threads: int | None = None) 
             rc, _, its, res = Oracle(p).solve(xs[i])
             with lock:
                 state["done"] += 1
+                state["ok"] += rc == 0 and res <= p.c.tolerance  # converged solves only
                 state["its"] += its
 
     ts = [threading.Thread(target=worker) for _ in range(threads)]
@@ -204,8 +203,9 @@ def cpu_baseline(texts, xs, budget_s: float = 15.0, threads: int | None = None) 
     for t in ts:
         t.join()
     dt = time.perf_counter() - t0
-    return {"value": state["done"] / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"first {state['done']} of {len(texts)} instances, one solve per thread, {dt:.1f} s wall",
+    return {"value": state["ok"] / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {state['done']} of {len(texts)} instances ({state['ok']} converged), one solve "
+                      f"per thread, {dt:.1f} s wall",
             "seconds": dt}
 
 
@@ -615,6 +615,56 @@ def main():
     if args.workload == "cyl2d":
         run_cyl2d(args)
         return
+    run_brush1d(args)
+
+
+def stream_fields(plans, steps: int, seed0: int):
+    """Start fields of `steps` consecutive steps of the stream: every step
+    solves the same instances from a fresh seeded field (step k: seed0 + k)."""
+    return [x for k in range(steps) for x in fields(plans, seed=seed0 + k)]
+
+
+def plain_fp64_sample(plans, xs, budget_s: float = 6.0, stream=None):
+    """The plain FP64 GPU path: one solve at a time through a device context
+    (nm_solve_dev: the reference's Solve loop, FP64 propagators, one problem
+    on the whole GPU), over the first instances for about budget_s.  Returns
+    converged solves/s and the sample."""
+    import torch
+    from namics_gb300 import NM_FP64, Context
+    done, ok, t_gpu = 0, 0, 0.0
+    t0 = time.perf_counter()
+    for p, x in zip(plans, xs):
+        if time.perf_counter() - t0 > budget_s:
+            break
+        ctx = Context(p, NM_FP64, stream=stream.cuda_stream if stream else None)
+        xd = torch.from_numpy(x.copy()).cuda()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        st = stream or torch.cuda.current_stream()
+        e0.record(st)
+        r = ctx.solve_dev(xd.data_ptr())
+        e1.record(st)
+        e1.synchronize()
+        t_gpu += e0.elapsed_time(e1) / 1000.0
+        ctx.close()
+        done += 1
+        ok += r.status == 0
+    return {"value": ok / t_gpu if t_gpu > 0 else None, "unit": UNIT, "converged": ok, "solves": done,
+            "seconds": t_gpu, "what": "one solve at a time, device context, FP64 propagators, DIIS with a host "
+                                      "sync per iteration (nm_solve_dev); first instances of the workload"}
+
+
+def run_brush1d(args) -> None:
+    """The headline: a sustained stream of batched 1-D brush/star solves.
+
+    Every step brings the 512 instances of the workload with a fresh seeded
+    start field (step k draws its fields from seed SEED + 1 + k).  The K timed
+    steps (K × 512 solves) go through ONE device-resident work loop
+    (nm_batch_solve_dev): resident CTAs, one per slot, take the next problem
+    from the queue as soon as their last one converged, so a long or
+    non-converging solve holds one slot, not the step.  value = converged
+    solves / time of the K steps; ms_per_step = that time / K."""
     ws, rank, local = dist_env()
     import torch
     if ws > 1:
@@ -631,90 +681,85 @@ def main():
 
     texts = workload(args.instances)
     plans = [Plan(t) for t in texts]
-    xs = fields(plans)
+    K, W = args.steps, args.warmup
     prec = NM_FP32 if args.precision == "fp32" else NM_FP64
     stream = torch.cuda.Stream()
-    batch = Batch(plans, prec, device=local, stream=stream.cuda_stream)
+    flush = torch.empty(int(256e6) // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
+    xs = stream_fields(plans, K, SEED + 1)
     x0 = torch.from_numpy(np.concatenate(xs)).cuda()
     xw = torch.empty_like(x0)
-    flush = torch.empty(int(256e6) // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
-
-    def step():
-        xw.copy_(x0)
-        torch.cuda.synchronize()
-        return batch.solve_dev(xw.data_ptr())
-
-    for _ in range(args.warmup):
-        step()
-    # timed: per-step CUDA events on the launching stream, L2 flushed between steps
-    launches0 = batch.launch_count()
-    times, its_all = [], None
+    job = Batch(plans * K, prec, device=local, stream=stream.cuda_stream)
+    # untimed warm-up: W steps of the same stream (their own seeds)
+    if W > 0:
+        xwu = np.concatenate(stream_fields(plans, W, SEED + 1001))
+        warm = Batch(plans * W, prec, device=local, stream=stream.cuda_stream)
+        warm.solve_host(xwu)
+        warm.close()
+    # timed: the K steps in one work loop, inputs resident in HBM, L2 flushed
+    xw.copy_(x0)
+    flush.zero_()
+    launches0 = job.launch_count()
     if ws > 1:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            flush.zero_()
-            xw.copy_(x0)
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            its, res, st = batch.solve_dev(xw.data_ptr())
-            e1.record(stream)
-            e1.synchronize()
-            times.append(e0.elapsed_time(e1))
-            its_all = its
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        its_all, res, st = job.solve_dev(xw.data_ptr())
+        e1.record(stream)
+        e1.synchronize()
     torch.cuda.synchronize()
-    launches = batch.launch_count() - launches0
-    ms = statistics.mean(times)
-    lat = batch.times() * 1e3  # ms per problem, last timed step
+    if ws > 1:
+        dist.barrier()
+    total_ms = e0.elapsed_time(e1)
+    launches = job.launch_count() - launches0
+    queued, solving = job.timings()
     ok = st == 0
-    latency = {"p50_ms": float(np.percentile(lat[ok], 50)) if ok.any() else None,
-               "p99_ms": float(np.percentile(lat[ok], 99)) if ok.any() else None,
-               "unit": "ms", "what": "per-problem time to convergence inside the launch (converged problems)"}
-    # the plain FP64 GPU path on the same instances (same kernel, FP64 propagators throughout)
+    n_ok = int(ok.sum())
+    latency = {"p50_ms": float(np.percentile(solving[ok] * 1e3, 50)) if ok.any() else None,
+               "p99_ms": float(np.percentile(solving[ok] * 1e3, 99)) if ok.any() else None,
+               "queue_wait_p50_ms": float(np.percentile(queued * 1e3, 50)),
+               "queue_wait_p99_ms": float(np.percentile(queued * 1e3, 99)),
+               "unit": "ms", "what": "per converged problem: time to convergence in its slot (device timer); "
+                                     "queue wait from the work loop's start to the problem's start"}
+    # roofline: algorithmic bytes of the propagator work of the launch
+    updates = 0.0
+    per_it = [p.segment_updates() for p in plans]
+    for i in range(len(its_all)):
+        updates += per_it[i % len(plans)] * (int(its_all[i]) + 1)
+    # the same stream with FP64 propagators throughout (same work loop)
     fp64 = None
     if prec == NM_FP32 and not args.no_fp64:
-        b64 = Batch(plans, NM_FP64, device=local, stream=stream.cuda_stream)
-        t64 = []
-        for k in range(3):
-            flush.zero_()
-            xw.copy_(x0)
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            _, _, st64 = b64.solve_dev(xw.data_ptr())
-            e1.record(stream)
-            e1.synchronize()
-            if k > 0:
-                t64.append(e0.elapsed_time(e1))
-        ms64 = statistics.mean(t64)
-        n64 = int((st64 == 0).sum())
-        fp64 = {"value": n64 / (ms64 / 1000.0), "unit": UNIT, "ms_per_step": ms64, "converged": n64,
-                "steps": len(t64), "warmup": 1}
-        b64.close()
-    n_ok = int((st == 0).sum())
-    # end to end through the C ABI with host buffers
-    xh = np.concatenate(xs)
-    e2e_times = []
-    for _ in range(max(2, min(args.steps, 3))):
-        xh2 = xh.copy()
+        K64 = max(1, min(K, 4))
+        j64 = Batch(plans * K64, NM_FP64, device=local, stream=stream.cuda_stream)
+        x64 = torch.from_numpy(np.concatenate(xs[:K64 * len(plans)])).cuda()
+        flush.zero_()
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        batch.solve_host(xh2)
-        e2e_times.append(time.perf_counter() - t0)
-    e2e_s = statistics.mean(e2e_times)
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        _, _, st64 = j64.solve_dev(x64.data_ptr())
+        a1.record(stream)
+        a1.synchronize()
+        ms64 = a0.elapsed_time(a1)
+        n64 = int((st64 == 0).sum())
+        fp64 = {"value": n64 / (ms64 / 1000.0), "unit": UNIT, "ms_per_step": ms64 / K64, "converged": n64,
+                "steps": K64, "what": "the same stream and work loop, FP64 propagators throughout"}
+        j64.close()
+    plain64 = None
+    if rank == 0 and not args.no_fp64:
+        plain64 = plain_fp64_sample(plans, xs[:len(plans)], budget_s=6.0, stream=stream)
+    # end to end through the C ABI with host buffers: the K steps' fields in,
+    # solved fields out, copies inside the timed region
+    xh = np.concatenate(xs)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    job.solve_host(xh)
+    e2e_s = time.perf_counter() - t0
     nbytes = xh.nbytes
-    # N replicas: slowest rank's times, all ranks' solves
-    ms, e2e_s, n_all = reduce_over_ranks(ms, e2e_s, n_ok)
+    ms, e2e_s, n_all = reduce_over_ranks(total_ms, e2e_s, n_ok)
     value = n_all / (ms / 1000.0)
-    # roofline: algorithmic bytes of the propagator work of one launch
-    updates = 0.0
-    for i, p in enumerate(plans):
-        per_it = p.segment_updates()
-        updates += per_it * (int(its_all[i]) + 1)
     bpu = B_PER_UPDATE_FP32 if prec == NM_FP32 else B_PER_UPDATE_FP64
     peaks = {}
     try:
@@ -722,35 +767,38 @@ def main():
     except Exception:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    achieved = updates * bpu / (ms / 1000.0) / 1e9
+    achieved = updates * bpu / (total_ms / 1000.0) / 1e9
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K,
+        "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32" if prec == NM_FP32 else "f64",
-        "data": "synthetic (seeded brush/star instances)",
-        "config": {"workload": "batched 1-gradient brushes/stars (512, seeded): n_layers U{50..400}, "
-                               "N U{20..500}, sigma U[0.01,0.1], chi U[0,1], 10% 3-arm stars",
-                   "instances": args.instances * ws, "converged": n_all, "precision": args.precision,
+        "data": "synthetic (seeded brush/star instances, a fresh seeded start field every step)",
+        "config": {"workload": "stream of batched 1-gradient brushes/stars: 512 seeded instances per step "
+                               "(n_layers U{50..400}, N U{20..500}, sigma U[0.01,0.1], chi U[0,1], 10% 3-arm "
+                               "stars), each step from fresh seeded fields; the K steps in one device-resident "
+                               "work loop",
+                   "instances_per_step": args.instances, "solves": len(its_all) * ws, "converged": n_all,
+                   "precision": args.precision, "slots": job.slots,
                    "iterations_mean": float(np.mean(its_all)), "iterations_max": int(np.max(its_all)),
-                   "segment_site_updates_per_step": updates, "l2": "flushed between steps (256 MB write)",
+                   "segment_site_updates": updates,
+                   "l2": "flushed once before the timed region (256 MB write); the K steps' inputs "
+                         f"({nbytes / 1e6:.0f} MB of fields) are written to HBM before it",
                    "parallelism": f"replicas x{ws}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak,
-                     "traffic": (TRAFFIC_BATCH512_FP32 if (prec == NM_FP32 and args.instances == N_INSTANCES)
-                                 else None),
-                     "note": f"{bpu:.0f} B per segment-site update x updates / kernel time; peak of measured "
-                             "(MEASURED_PEAKS.json hbm_gbs); traffic: DRAM bytes of one launch from an ncu "
-                             "capture of this workload, below the algorithmic bytes because the chains run in "
-                             "registers and shared memory"},
-        "e2e": {"value": n_all / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nbytes * ws,
-                "d2h_bytes_per_step": nbytes * ws},
+                     "frac": achieved / peak, "traffic": None,
+                     "note": f"{bpu:.0f} B per segment-site update x updates / work-loop time; peak of measured "
+                             "(MEASURED_PEAKS.json hbm_gbs, burst copy); traffic: not measured in this run "
+                             "(the ncu capture of the work loop is summarised beside the kernel's profile)"},
+        "e2e": {"value": n_all / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nbytes * ws // K,
+                "d2h_bytes_per_step": nbytes * ws // K},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "latency": latency,
         "fp64_gpu": fp64,
+        "fp64_gpu_unbatched": plain64,
     }
     if rank == 0 and not args.no_cpu and ws == 1:
-        line["cpu_baseline"] = cpu_baseline(texts, xs, budget_s=15.0)
+        line["cpu_baseline"] = cpu_baseline(texts, xs[:len(plans)], budget_s=15.0)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

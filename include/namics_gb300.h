@@ -288,7 +288,12 @@ long long nm_ctx_launch_count(nm_ctx* ctx);
 
 /* ---- batched 1-gradient solver ------------------------------------------
  * Many independent 1-gradient problems solved to convergence in one
- * persistent launch (one CTA per problem, DIIS on the device). */
+ * persistent launch: a device-resident work loop of resident CTAs ("slots",
+ * as many as fit on the device, at most one per problem), each taking the
+ * next problem from a queue in device memory (longest first) as soon as its
+ * previous one converged, with DIIS on the device.  Stored propagators and
+ * DIIS histories live in the slot's scratch; fields x and residuals g are
+ * per problem. */
 typedef struct nm_batch nm_batch;
 
 int nm_batch_create(const nm_plan* const* plans, int n_plans,
@@ -313,6 +318,15 @@ int nm_batch_stats(nm_batch* b, int* fp32_iterations);
  * start of the batch's first CTA to the end of the problem's CTA (device
  * global timer), [n_plans] host array */
 int nm_batch_times(nm_batch* b, double* seconds);
+/* per-problem seconds of the last solve (device global timer): from the
+ * start of the work loop to the problem's start in a slot (queued), and
+ * from its start to its convergence (solving); either may be NULL */
+int nm_batch_timings(nm_batch* b, double* queued, double* solving);
+/* resident CTAs (slots) of the batch's work loop; nm_batch_set_slots runs
+ * later solves on fewer of them (1 .. the number fixed at creation: as many
+ * as fit on the device, at most one per problem) with identical results */
+int nm_batch_slots(nm_batch* b);
+int nm_batch_set_slots(nm_batch* b, int slots);
 /* per-problem free energy / grand potential of the final state */
 int nm_batch_free_energy(nm_batch* b, double* F, double* Omega);
 long long nm_batch_launch_count(nm_batch* b);

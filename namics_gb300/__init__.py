@@ -261,7 +261,8 @@ class Context:
 
 
 class Batch:
-    """Many independent 1-gradient problems solved in one persistent launch."""
+    """Many independent 1-gradient problems solved in one persistent launch
+    (a device-resident work loop: resident CTAs take problems from a queue)."""
 
     def __init__(self, plans: list[Plan], precision: int = NM_FP64, device: int = 0, stream: int | None = None):
         lib = _abi.load()
@@ -323,6 +324,24 @@ class Batch:
         out = np.zeros(len(self.plans))
         _check(_abi.load().nm_batch_times(self._h, _dptr(out)))
         return out
+
+    def timings(self) -> tuple[np.ndarray, np.ndarray]:
+        """Per-problem seconds of the last solve: waiting in the queue (from
+        the work loop's start to the problem's start in a slot) and solving
+        (from that start to convergence)."""
+        q = np.zeros(len(self.plans))
+        s = np.zeros(len(self.plans))
+        _check(_abi.load().nm_batch_timings(self._h, _dptr(q), _dptr(s)))
+        return q, s
+
+    @property
+    def slots(self) -> int:
+        """Resident CTAs of the work loop."""
+        return int(_abi.load().nm_batch_slots(self._h))
+
+    @slots.setter
+    def slots(self, k: int) -> None:
+        _check(_abi.load().nm_batch_set_slots(self._h, int(k)))
 
     def free_energy(self):
         n = len(self.plans)

@@ -116,6 +116,9 @@ SIGNATURES = [
     ("nm_batch_residual_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     ("nm_batch_stats", C.c_int, [C.c_void_p, ip]),
     ("nm_batch_times", C.c_int, [C.c_void_p, dp]),
+    ("nm_batch_timings", C.c_int, [C.c_void_p, dp, dp]),
+    ("nm_batch_slots", C.c_int, [C.c_void_p]),
+    ("nm_batch_set_slots", C.c_int, [C.c_void_p, C.c_int]),
     ("nm_batch_free_energy", C.c_int, [C.c_void_p, dp, dp]),
     ("nm_batch_launch_count", C.c_longlong, [C.c_void_p]),
     ("nm_server_create", C.c_int, [C.POINTER(nm_server_options), C.POINTER(C.c_void_p)]),

@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -68,6 +69,10 @@ struct B1Prob {
     unsigned long long t_begin, t_end;  // %globaltimer (ns) at the CTA's start and end
     double sc[5 * NM_MAX_MOL];  // GN, norm, n, theta, phibulk per molecule
     double seg_phibulk[NM_MAX_SEG];
+    // byte offsets of the stored propagators and the DIIS history inside a
+    // slot of the work loop's scratch (k_batch1d_queue), per molecule
+    struct { unsigned long long gf, pc, q, ef, epc, eq; } so[NM_MAX_MOL];
+    unsigned long long so_xR, so_xx0;
 };
 
 // ---------------------------------------------------------------- helpers
@@ -625,15 +630,8 @@ __device__ __forceinline__ unsigned long long b1_clock() {
     return t;
 }
 
-// order (may be null): CTA b solves problem order[b].  The batch lists its
-// problems by descending steps per residual, so the block scheduler spreads
-// the longest solves one per SM before it doubles any of them up.
-// Three CTAs per SM (168 registers a thread): at four (128 registers) the
-// FP32 residual spilled inside its step loops and a batch took 8% longer;
-// at two the batch time is the same and the median solve waits longer.
-__global__ void __launch_bounds__(B1_THREADS, 3) k_batch1d(B1Prob* __restrict__ probs, int mode,
-                                                          const int* __restrict__ order) {
-    B1Prob& P = probs[order ? order[blockIdx.x] : blockIdx.x];
+// The whole solve of one problem by one CTA (the body of both kernels below).
+__device__ __forceinline__ void b1_solve(B1Prob& P, const int mode) {
     if (threadIdx.x == 0) P.t_begin = b1_clock();
     extern __shared__ double sm[];
     const int M = P.M, ns = P.ns, iv = P.iv, n_mm = P.n_mm, m = P.m;
@@ -817,6 +815,56 @@ __global__ void __launch_bounds__(B1_THREADS, 3) k_batch1d(B1Prob* __restrict__ 
     }
 }
 
+// One CTA per problem: CTA b solves problem order[b] (order may be null).
+// Three CTAs per SM (168 registers a thread): at four (128 registers) the
+// FP32 residual spilled inside its step loops and a batch took 8% longer;
+// at two the batch time is the same and the median solve waits longer.
+__global__ void __launch_bounds__(B1_THREADS, 3) k_batch1d(B1Prob* __restrict__ probs, int mode,
+                                                          const int* __restrict__ order) {
+    b1_solve(probs[order ? order[blockIdx.x] : blockIdx.x], mode);
+}
+
+// The device-resident work loop: a persistent grid of resident CTAs, one per
+// slot.  Each CTA takes the next problem from the queue (atomic head over
+// order[0..n)), points the problem's stored propagators and DIIS history at
+// its slot's scratch, solves it to convergence and takes the next one at
+// once, so a long or non-converging problem holds one slot, not the batch.
+// The batch lists its problems by descending steps per residual, so the
+// longest solves start first.
+__device__ __forceinline__ void b1_rebase(B1Prob& P, unsigned char* base) {
+    for (int m = 0; m < P.nmol; m++) {
+        B1Mol& D = P.mol[m];
+        D.Gf = base + P.so[m].gf;
+        D.Pc = base + P.so[m].pc;
+        D.Q = base + P.so[m].q;
+        D.ef = (int*)(base + P.so[m].ef);
+        D.epc = (int*)(base + P.so[m].epc);
+        D.eq = (int*)(base + P.so[m].eq);
+    }
+    P.xR = (double*)(base + P.so_xR);
+    P.xx0 = (double*)(base + P.so_xx0);
+}
+
+__global__ void __launch_bounds__(B1_THREADS, 3) k_batch1d_queue(B1Prob* __restrict__ probs, int n, int mode,
+                                                                const int* __restrict__ order,
+                                                                unsigned char* __restrict__ slots,
+                                                                unsigned long long slot_bytes,
+                                                                unsigned int* __restrict__ head) {
+    __shared__ unsigned int s_idx;
+    unsigned char* base = slots + (size_t)blockIdx.x * slot_bytes;
+    for (;;) {
+        if (threadIdx.x == 0) s_idx = atomicAdd(head, 1u);
+        __syncthreads();
+        const unsigned int idx = s_idx;
+        if (idx >= (unsigned int)n) break;  // the same idx in every thread
+        B1Prob& P = probs[order ? order[idx] : (int)idx];
+        if (threadIdx.x == 0) b1_rebase(P, base);
+        __syncthreads();
+        b1_solve(P, mode);
+        __syncthreads();  // every thread is done with s_idx and the slot
+    }
+}
+
 // ------------------------------------------------------------------ host
 // Accuracy floor of an FP32-propagator residual: G1 held in FP32 is the exact
 // G1 of a field perturbed by ~6e-8 per site, which a chain of N segments
@@ -831,12 +879,17 @@ struct Batch {
     std::vector<const nm_plan*> plans;
     std::vector<B1Prob> hp;
     B1Prob* d_probs = nullptr;
-    int* d_order = nullptr;  // CTA -> problem, longest solves first
+    int* d_order = nullptr;  // queue order: longest solves first
+    unsigned char* d_slots = nullptr;  // work-loop scratch, slots × slot_bytes
+    unsigned int* d_head = nullptr;    // work-loop queue head
+    size_t slot_bytes = 0;
+    int slots = 0;                     // resident CTAs of the work loop
     std::vector<void*> allocs;
     double* d_x = nullptr;
     double* d_g = nullptr;
     std::vector<long long> offsets;
     int precision = NM_FP64;
+    int slots_cap = 0;  // slots the scratch holds: as many CTAs as fit, at most one per problem
     size_t smem = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -870,8 +923,8 @@ struct Batch {
 
 #define TRYB(x) do { int r_ = (x); if (r_) return r_; } while (0)
 
-// Raise k_batch1d's dynamic shared-memory limit on device `dev` (current) to
-// at least `bytes`.  The limit only ever rises, and every path that launches
+// Raise the dynamic shared-memory limit of k_batch1d and k_batch1d_queue on
+// device `dev` (current) to at least `bytes`.  The limit only ever rises, and every path that launches
 // k_batch1d (batches, the server's workers, the allocation-free solve) goes
 // through this one lock, so no caller can lower it under another's launch.
 static cudaError_t b1_raise_smem(int dev, size_t bytes) {
@@ -881,6 +934,8 @@ static cudaError_t b1_raise_smem(int dev, size_t bytes) {
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     if (bytes <= set[dev]) return cudaSuccess;
     cudaError_t e = cudaFuncSetAttribute(k_batch1d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_batch1d_queue, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e == cudaSuccess) set[dev] = bytes;
     return e;
 }
@@ -917,6 +972,15 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
     size_t maxsmem = 0;
     B.hp.resize(n);
     B.offsets.resize(n + 1);
+    // device copies of a plan's constant arrays, shared by every problem of
+    // the batch that uses the same plan
+    struct PlanDev {
+        const double *lm1 = nullptr, *l0 = nullptr, *l1 = nullptr, *L = nullptr, *ksam = nullptr, *gmask = nullptr,
+                     *phi_frozen = nullptr;
+        const nm_block* blocks[NM_MAX_MOL] = {};
+        const int* child_index[NM_MAX_MOL] = {};
+    };
+    std::map<const nm_plan*, PlanDev> pdev;
     for (int p = 0; p < n; p++) {
         const nm_plan* P = plans[p];
         B.plans.push_back(P);
@@ -930,19 +994,45 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
         H.max_norm = P->max_norm; H.iv = P->iv; H.lam = P->lambda; H.tol = P->tolerance; H.dmax = P->deltamax;
         H.b1 = P->bc[0] == NM_BC_MIRROR ? 1 : P->bc[0] == NM_BC_PERIODIC ? P->MX : 0;
         H.bm = P->bc[3] == NM_BC_MIRROR ? P->MX : P->bc[3] == NM_BC_PERIODIC ? 1 : P->MX + 1;
-        double *dL, *dk, *dg, *dpf;
-        if (P->geometry != NM_PLANAR) {
-            double *a, *b, *c;
-            TRYB(B.upload(&a, P->lambda_1, M)); TRYB(B.upload(&b, P->lambda0, M)); TRYB(B.upload(&c, P->lambda1, M));
-            H.lm1 = a; H.l0 = b; H.l1 = c;
-            TRYB(B.upload(&dL, P->L, M));
-            H.L = dL;
-        } else H.L = nullptr;
-        std::vector<double> ks(M);
-        for (int s = 0; s < M; s++) ks[s] = P->ksam[s];
-        TRYB(B.upload(&dk, ks.data(), M)); H.ksam = dk;
-        TRYB(B.upload(&dg, P->seg_gmask, (size_t)P->n_seg * M)); H.gmask = dg;
-        TRYB(B.upload(&dpf, P->seg_phi_frozen, (size_t)P->n_seg * M)); H.phi_frozen = dpf;
+        auto found = pdev.find(P);
+        if (found == pdev.end()) {
+            PlanDev D;
+            if (P->geometry != NM_PLANAR) {
+                double *a, *b, *c, *dL;
+                TRYB(B.upload(&a, P->lambda_1, M)); TRYB(B.upload(&b, P->lambda0, M)); TRYB(B.upload(&c, P->lambda1, M));
+                TRYB(B.upload(&dL, P->L, M));
+                D.lm1 = a; D.l0 = b; D.l1 = c; D.L = dL;
+            }
+            double *dk, *dg, *dpf;
+            std::vector<double> ks(M);
+            for (int s = 0; s < M; s++) ks[s] = P->ksam[s];
+            TRYB(B.upload(&dk, ks.data(), M));
+            TRYB(B.upload(&dg, P->seg_gmask, (size_t)P->n_seg * M));
+            TRYB(B.upload(&dpf, P->seg_phi_frozen, (size_t)P->n_seg * M));
+            D.ksam = dk; D.gmask = dg; D.phi_frozen = dpf;
+            for (int m = 0; m < P->n_mol; m++) {
+                const nm_molecule& mol = P->mols[m];
+                if (mol.n_blocks > B1_MAXB) { set_error("molecule has too many blocks for the batched solver"); return NM_ERR_INPUT; }
+                nm_block* db; int* dci;
+                TRYB(B.upload(&db, mol.blocks, mol.n_blocks));
+                std::vector<int> ci(mol.child_index, mol.child_index + (mol.n_blocks > 1 ? mol.n_blocks - 1 : 0));
+                if (ci.empty()) ci.push_back(0);
+                TRYB(B.upload(&dci, ci.data(), ci.size()));
+                D.blocks[m] = db; D.child_index[m] = dci;
+            }
+            found = pdev.emplace(P, D).first;
+        }
+        const PlanDev& PD = found->second;
+        H.lm1 = PD.lm1; H.l0 = PD.l0; H.l1 = PD.l1; H.L = PD.L;
+        H.ksam = PD.ksam; H.gmask = PD.gmask; H.phi_frozen = PD.phi_frozen;
+        // this problem's scratch inside one slot of the work loop (256-byte
+        // aligned pieces); the slot is sized for the batch's largest layout
+        size_t used = 0;
+        auto take = [&used](size_t bytes) {
+            size_t o = (used + 255) & ~(size_t)255;
+            used = o + std::max<size_t>(bytes, 1);
+            return (unsigned long long)o;
+        };
         for (int i = 0; i < P->n_seg; i++) {
             H.seg_it[i] = P->seg_it[i];
             H.seg_frozen[i] = P->seg_freedom[i] == NM_SEG_FROZEN;
@@ -953,27 +1043,18 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
         int kk = 0;
         for (int m = 0; m < P->n_mol; m++) {
             const nm_molecule& mol = P->mols[m];
-            if (mol.n_blocks > B1_MAXB) { set_error("molecule has too many blocks for the batched solver"); return NM_ERR_INPUT; }
             B1Mol& D = H.mol[m];
             D.freedom = mol.freedom; D.pinned = mol.pinned; D.n_blocks = mol.n_blocks; D.n_store = mol.n_store;
             D.n_molmon = mol.n_molmon; D.mm0 = kk;
             D.n_in = mol.n; D.theta_in = mol.theta; D.phibulk_in = mol.phibulk; D.N = mol.chainlength;
-            nm_block* db; int* dci;
-            TRYB(B.upload(&db, mol.blocks, mol.n_blocks));
-            std::vector<int> ci(mol.child_index, mol.child_index + (mol.n_blocks > 1 ? mol.n_blocks - 1 : 0));
-            if (ci.empty()) ci.push_back(0);
-            TRYB(B.upload(&dci, ci.data(), ci.size()));
-            D.blocks = db; D.child_index = dci;
-            char *gf, *pc, *q;
-            TRYB(B.alloc(&gf, tsz * (size_t)mol.n_store)); D.Gf = gf;
-            TRYB(B.alloc(&pc, tsz * (size_t)mol.n_blocks)); D.Pc = pc;
-            TRYB(B.alloc(&q, tsz * (size_t)mol.n_blocks)); D.Q = q;
-            int *ef, *epc, *eq;
+            D.blocks = PD.blocks[m]; D.child_index = PD.child_index[m];
+            H.so[m].gf = take(tsz * (size_t)mol.n_store);
+            H.so[m].pc = take(tsz * (size_t)mol.n_blocks);
+            H.so[m].q = take(tsz * (size_t)mol.n_blocks);
             // power-of-two exponents: one per thread (128) per stored vector
-            TRYB(B.alloc(&ef, BC_NT * (size_t)mol.n_store));
-            TRYB(B.alloc(&epc, BC_NT * (size_t)mol.n_blocks));
-            TRYB(B.alloc(&eq, BC_NT * (size_t)mol.n_blocks));
-            D.ef = ef; D.epc = epc; D.eq = eq;
+            H.so[m].ef = take(sizeof(int) * BC_NT * (size_t)mol.n_store);
+            H.so[m].epc = take(sizeof(int) * BC_NT * (size_t)mol.n_blocks);
+            H.so[m].eq = take(sizeof(int) * BC_NT * (size_t)mol.n_blocks);
             for (int j = 0; j < mol.n_molmon; j++) {
                 if (kk >= NM_MAX_MM) { set_error("too many (molecule, segment) pairs"); return NM_ERR_INPUT; }
                 H.mm_mol[kk] = m; H.mm_seg[kk] = mol.molmon_seg[j]; H.mm_frac[kk] = mol.molmon_fraction[j];
@@ -981,9 +1062,9 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
             }
         }
         H.n_mm = kk;
-        double *xR, *xx0;
-        TRYB(B.alloc(&xR, (size_t)P->diis_m * P->iv)); TRYB(B.alloc(&xx0, (size_t)P->diis_m * P->iv));
-        H.xR = xR; H.xx0 = xx0;
+        H.so_xR = take(sizeof(double) * (size_t)P->diis_m * P->iv);
+        H.so_xx0 = take(sizeof(double) * (size_t)P->diis_m * P->iv);
+        B.slot_bytes = std::max(B.slot_bytes, (used + 255) & ~(size_t)255);
         B.offsets[p] = off;
         off += P->iv;
         H.sw_tol = 2e-6;
@@ -1016,17 +1097,38 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
         set_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e1));
         return NM_ERR_CUDA;
     }
+    // the work loop: as many slots as CTAs of k_batch1d_queue fit on the
+    // device at once with this shared memory, at most one per problem
+    int per_sm = 0, sms = 0;
+    cudaError_t e2 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch1d_queue, B1_THREADS, maxsmem);
+    if (e2 == cudaSuccess) e2 = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e2 != cudaSuccess || per_sm < 1) {
+        set_error(std::string("batched solver occupancy: ") + cudaGetErrorString(e2));
+        return NM_ERR_CUDA;
+    }
+    B.slots = B.slots_cap = std::min(n, per_sm * sms);
+    TRYB(B.alloc(&B.d_slots, B.slot_bytes * (size_t)B.slots_cap));
+    TRYB(B.alloc(&B.d_head, 1));
     return NM_OK;
+}
+
+// the work loop over every problem of the batch; FP32 problems switch to FP64
+// inside their CTA
+static cudaError_t b1_launch(Batch& B, int mode) {
+    int n = (int)B.hp.size();
+    cudaError_t e = cudaMemsetAsync(B.d_head, 0, sizeof(unsigned int), B.stream);
+    if (e != cudaSuccess) return e;
+    k_batch1d_queue<<<B.slots, B1_THREADS, B.smem, B.stream>>>(B.d_probs, n, mode, B.d_order, B.d_slots,
+                                                              (unsigned long long)B.slot_bytes, B.d_head);
+    B.launches++;
+    return cudaGetLastError();
 }
 
 static int batch_run(Batch& B) {
     int n = (int)B.hp.size();
     cudaError_t e = cudaMemcpyAsync(B.d_probs, B.hp.data(), sizeof(B1Prob) * n, cudaMemcpyHostToDevice, B.stream);
     if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
-    // one CTA per problem; FP32 problems switch to FP64 inside their CTA
-    k_batch1d<<<n, B1_THREADS, B.smem, B.stream>>>(B.d_probs, B.precision == NM_FP32 ? 1 : 0, B.d_order);
-    B.launches++;
-    e = cudaGetLastError();
+    e = b1_launch(B, B.precision == NM_FP32 ? 1 : 0);
     if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
     e = cudaMemcpyAsync(B.hp.data(), B.d_probs, sizeof(B1Prob) * n, cudaMemcpyDeviceToHost, B.stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(B.stream);
@@ -1108,9 +1210,8 @@ int nm_batch_residual_dev(nm_batch* b, const double* x_dev, double* g_dev, int p
     for (int p = 0; p < np; p++) B->hp[p].eval_only = 1;
     e = cudaMemcpyAsync(B->d_probs, B->hp.data(), sizeof(nm::B1Prob) * np, cudaMemcpyHostToDevice, B->stream);
     if (e != cudaSuccess) { nm::set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
-    nm::k_batch1d<<<np, B1_THREADS, B->smem, B->stream>>>(B->d_probs, precision == NM_FP32 ? 1 : 0, B->d_order);
-    B->launches++;
-    e = cudaMemcpyAsync(g_dev, B->d_g, sizeof(double) * n, cudaMemcpyDeviceToDevice, B->stream);
+    e = nm::b1_launch(*B, precision == NM_FP32 ? 1 : 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(g_dev, B->d_g, sizeof(double) * n, cudaMemcpyDeviceToDevice, B->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(B->stream);
     for (int p = 0; p < np; p++) B->hp[p].eval_only = 0;
     if (e != cudaSuccess) { nm::set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
@@ -1130,6 +1231,34 @@ int nm_batch_times(nm_batch* b, double* seconds) {
     unsigned long long t0 = ~0ull;
     for (auto& h : B->hp) t0 = std::min(t0, h.t_begin);
     for (size_t p = 0; p < B->hp.size(); p++) seconds[p] = (double)(B->hp[p].t_end - t0) * 1e-9;
+    return NM_OK;
+}
+
+int nm_batch_timings(nm_batch* b, double* queued, double* solving) {
+    Batch* B = reinterpret_cast<Batch*>(b);
+    if (!B || (!queued && !solving)) { nm::set_error("nm_batch_timings: bad argument"); return NM_ERR_ARG; }
+    unsigned long long t0 = ~0ull;
+    for (auto& h : B->hp) t0 = std::min(t0, h.t_begin);
+    for (size_t p = 0; p < B->hp.size(); p++) {
+        if (queued) queued[p] = (double)(B->hp[p].t_begin - t0) * 1e-9;
+        if (solving) solving[p] = (double)(B->hp[p].t_end - B->hp[p].t_begin) * 1e-9;
+    }
+    return NM_OK;
+}
+
+int nm_batch_slots(nm_batch* b) {
+    Batch* B = reinterpret_cast<Batch*>(b);
+    return B ? B->slots : 0;
+}
+
+int nm_batch_set_slots(nm_batch* b, int slots) {
+    Batch* B = reinterpret_cast<Batch*>(b);
+    if (!B || slots < 1) { nm::set_error("nm_batch_set_slots: bad argument"); return NM_ERR_ARG; }
+    if (slots > B->slots_cap) {
+        nm::set_error("nm_batch_set_slots: more slots than resident CTAs fit (" + std::to_string(B->slots_cap) + ")");
+        return NM_ERR_ARG;
+    }
+    B->slots = slots;  // the scratch was sized for slots_cap
     return NM_OK;
 }
 
