@@ -283,6 +283,43 @@ int nm_propagate_dev(nm_ctx* ctx, double* G_in_dev, const double* G1_dev,
                      double* G_out_dev);
 int nm_side_dev(nm_ctx* ctx, const double* X_dev, double* X_side_dev);
 
+/* Lattice and molecule pieces for a caller that keeps the reference's own
+ * Molecule::ComputePhi loop (molecule.h:185-197) and moves its arithmetic
+ * to the device.  Device arrays of length M (n_molmon·M for rho), the
+ * reference's padded layout; all M entries, halo layers included, as the
+ * reference's flat-array loops.  Markov-1 chains.
+ * nm_add_phi_dev:      phi += Gf·Gb           Lattice::AddPhiS(phi,Gf,Gb,Markov,M)
+ * nm_add_phi_deg_dev:  phi += d·Gf·Gb         AddPhiS(phi,Gf,Gb,degeneracy,Markov,M)
+ * nm_add_phi_norm_dev: phi += norm·Gf·Gb/G1 where G1 > 0
+ *                      AddPhiS(phi,Gf,Gb,G1,norm,Markov,M) (LGrad1.cpp:924-941);
+ *                      2 and 3 gradients: NM_ERR_INPUT, phi unchanged (the
+ *                      reference prints "not implemented" there)
+ * nm_initiate_dev:     G = Gz                 Lattice::Initiate (LGrad1.cpp:943-949)
+ * nm_terminate_dev:    Gz = G on 2 and 3 gradients; on 1 gradient Gz is left
+ *                      as it is, as LGrad1::Terminate does for Markov 1
+ * nm_weighted_sum_dev, nm_compute_gn_dev: zero X's halo in place
+ *                      (remove_bounds), then Σ X (planar, 3-D) or Σ X·L
+ *                      (curved): Lattice::WeightedSum, ComputeGN
+ *                      (LGrad1.cpp:213-220, 863-874; LGrad2.cpp:147-157;
+ *                      LGrad3.cpp:40-46)
+ * nm_compose_dev:      Molecule::ComputePhi of molecule `mol` at the field
+ *                      x (mol_linear.cpp:12-135, mol_branched.cpp:170-418,
+ *                      mol_dendrimer.cpp:113-184): G1 from x, forward
+ *                      sweep, G(N), backward sweep with the composition;
+ *                      rho_dev [n_molmon·M] = Σ d·Gf·Gb per segment type of
+ *                      the molecule (before the division by G1 and the
+ *                      normalisation of System::ComputePhis), GN = G(N). */
+int nm_add_phi_dev(nm_ctx* ctx, double* phi_dev, const double* Gf_dev, const double* Gb_dev);
+int nm_add_phi_deg_dev(nm_ctx* ctx, double* phi_dev, const double* Gf_dev, const double* Gb_dev,
+                       double degeneracy);
+int nm_add_phi_norm_dev(nm_ctx* ctx, double* phi_dev, const double* Gf_dev, const double* Gb_dev,
+                        const double* G1_dev, double norm);
+int nm_initiate_dev(nm_ctx* ctx, double* G_dev, const double* Gz_dev);
+int nm_terminate_dev(nm_ctx* ctx, double* Gz_dev, const double* G_dev);
+int nm_weighted_sum_dev(nm_ctx* ctx, double* X_dev, double* sum);
+int nm_compute_gn_dev(nm_ctx* ctx, double* G_dev, double* GN);
+int nm_compose_dev(nm_ctx* ctx, int mol, const double* x_dev, double* rho_dev, double* GN);
+
 /* Device launches issued by this context since creation (diagnostics). */
 long long nm_ctx_launch_count(nm_ctx* ctx);
 

@@ -230,6 +230,39 @@ class Context:
     def side_dev(self, x_ptr: int, out_ptr: int) -> None:
         _check(_abi.load().nm_side_dev(self._h, C.c_void_p(x_ptr), C.c_void_p(out_ptr)))
 
+    # Lattice / Molecule pieces on device arrays (pointers), see the header
+    def add_phi_dev(self, phi_ptr: int, gf_ptr: int, gb_ptr: int, degeneracy: float | None = None,
+                    g1_ptr: int | None = None, norm: float | None = None) -> None:
+        lib, V = _abi.load(), C.c_void_p
+        if g1_ptr is not None:
+            _check(lib.nm_add_phi_norm_dev(self._h, V(phi_ptr), V(gf_ptr), V(gb_ptr), V(g1_ptr), float(norm)))
+        elif degeneracy is not None:
+            _check(lib.nm_add_phi_deg_dev(self._h, V(phi_ptr), V(gf_ptr), V(gb_ptr), float(degeneracy)))
+        else:
+            _check(lib.nm_add_phi_dev(self._h, V(phi_ptr), V(gf_ptr), V(gb_ptr)))
+
+    def initiate_dev(self, g_ptr: int, gz_ptr: int) -> None:
+        _check(_abi.load().nm_initiate_dev(self._h, C.c_void_p(g_ptr), C.c_void_p(gz_ptr)))
+
+    def terminate_dev(self, gz_ptr: int, g_ptr: int) -> None:
+        _check(_abi.load().nm_terminate_dev(self._h, C.c_void_p(gz_ptr), C.c_void_p(g_ptr)))
+
+    def weighted_sum_dev(self, x_ptr: int) -> float:
+        out = C.c_double()
+        _check(_abi.load().nm_weighted_sum_dev(self._h, C.c_void_p(x_ptr), C.byref(out)))
+        return out.value
+
+    def compute_gn_dev(self, g_ptr: int) -> float:
+        out = C.c_double()
+        _check(_abi.load().nm_compute_gn_dev(self._h, C.c_void_p(g_ptr), C.byref(out)))
+        return out.value
+
+    def compose_dev(self, mol: int, x_ptr: int, rho_ptr: int) -> float:
+        """Molecule::ComputePhi of molecule `mol` at the field x; returns G(N)."""
+        out = C.c_double()
+        _check(_abi.load().nm_compose_dev(self._h, mol, C.c_void_p(x_ptr), C.c_void_p(rho_ptr), C.byref(out)))
+        return out.value
+
     def launch_count(self) -> int:
         return int(_abi.load().nm_ctx_launch_count(self._h))
 

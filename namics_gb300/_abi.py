@@ -107,6 +107,14 @@ SIGNATURES = [
                                C.POINTER(nm_solve_result), C.c_int]),
     ("nm_propagate_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("nm_side_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("nm_add_phi_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("nm_add_phi_deg_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]),
+    ("nm_add_phi_norm_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]),
+    ("nm_initiate_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("nm_terminate_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("nm_weighted_sum_dev", C.c_int, [C.c_void_p, C.c_void_p, dp]),
+    ("nm_compute_gn_dev", C.c_int, [C.c_void_p, C.c_void_p, dp]),
+    ("nm_compose_dev", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, dp]),
     ("nm_ctx_launch_count", C.c_longlong, [C.c_void_p]),
     ("nm_batch_create", C.c_int, [C.POINTER(P_plan), C.c_int, C.POINTER(nm_ctx_options), C.POINTER(C.c_void_p)]),
     ("nm_batch_destroy", C.c_int, [C.c_void_p]),

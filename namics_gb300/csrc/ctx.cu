@@ -633,12 +633,17 @@ int Ctx::molecule_pass(int m) {
 
 // All launches of one residual evaluation, on `stream` (captured into a graph
 // by residual() on the 3-D path).
+int Ctx::launch_g1(const double* x, bool with32) {
+    k_g1<<<grid_for(plan->M), 256, 0, stream>>>(lat, plan->n_seg, x, d_seg_it, d_gmask, d_G1,
+                                                with32 ? d_G1f : nullptr, chg, d_EE, d_psi);
+    launches++;
+    return NM_OK;
+}
+
 int Ctx::residual_launches(const double* x, double* g) {
     int M = plan->M;
     if (charged) elec_field(x);
-    k_g1<<<grid_for(M), 256, 0, stream>>>(lat, plan->n_seg, x, d_seg_it, d_gmask, d_G1, phase32 ? d_G1f : nullptr,
-                                          chg, d_EE, d_psi);
-    launches++;
+    launch_g1(x, phase32);
     for (int m = 0; m < plan->n_mol; m++) {
         int rc;
         if (use3d) rc = ctx3d_molecule_pass(*this, m, phase32);

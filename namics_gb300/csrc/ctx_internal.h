@@ -217,6 +217,7 @@ struct Ctx {
     int init(const nm_plan* p, const nm_ctx_options* opt);
     ~Ctx();
     int launch_prop(const double* in, const double* G1, double* out);
+    int launch_g1(const double* x, bool with32);  // G1 (and its FP32 copy) from the field x
     int wsum(const double* X, double* out_dev);
     int molecule_pass(int m);
     int residual(const double* x, double* g);

@@ -32,6 +32,7 @@ def load() -> C.CDLL:
         lib.orc_get_molecule.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp]
         lib.orc_free_energy.argtypes = [C.c_void_p, dp, dp, dp]
         lib.orc_propagate.argtypes = [C.c_void_p, dp, dp, dp]
+        lib.orc_compose.argtypes = [C.c_void_p, dp, C.c_int, dp, dp]
         lib.orc_side.argtypes = [C.c_void_p, dp, dp]
         lib.orc_set_amount.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double]
         lib.orc_search.argtypes = [C.c_void_p, dp, dp, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
@@ -109,6 +110,16 @@ class Oracle:
         if rc:
             raise RuntimeError(f"orc_free_energy rc={rc}")
         return F.value, O.value, mu
+
+    def compose(self, x: np.ndarray, mol: int, n_molmon: int):
+        """Molecule::ComputePhi of one molecule at x: (rho [n_molmon*M], GN)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        rho = np.zeros(n_molmon * self.plan.M)
+        gn = C.c_double()
+        rc = load().orc_compose(self._h, _p(x), mol, _p(rho), C.byref(gn))
+        if rc:
+            raise RuntimeError(f"orc_compose rc={rc}")
+        return rho, gn.value
 
     def propagate(self, g_in: np.ndarray, g1: np.ndarray | None) -> np.ndarray:
         g_in = np.ascontiguousarray(g_in, dtype=np.float64).copy()

@@ -582,7 +582,7 @@ static void update_psi(orc_state* st, double* g, const double* psi, const double
 }
 
 /* ---- residual ------------------------------------------------------------ */
-static int compute_phis(orc_state* st, const double* x) {
+static void prepare_G1(orc_state* st, const double* x) {
     const nm_plan* P = st->P;
     int M = st->M, ns = P->n_seg;
     /* PutU (system.cpp:1987-2085) + Segment::PrepareForCalculations
@@ -610,26 +610,48 @@ static int compute_phis(orc_state* st, const double* x) {
         Cp(st->phi + (size_t)i * M, P->seg_phi_frozen + (size_t)i * M, M);
         st->seg_phibulk[i] = 0;
     }
+}
+
+/* Molecule::ComputePhi of molecule m: rho[m] = Σ d·Gf·Gb per segment type of
+ * the molecule, GN[m] = G(N) (mol_linear.cpp:12-135, mol_branched.cpp,
+ * mol_dendrimer.cpp; a monomer as molecule.cpp:2669-2683). */
+static void compose_mol(orc_state* st, int m) {
+    const nm_plan* P = st->P;
+    int M = st->M;
+    const nm_molecule* mol = &P->mols[m];
+    Zero(st->rho[m], mol->n_molmon * M);
+    Zero(st->mol_phitot + (size_t)m * M, M);
+    if (mol->n_store == 1 && mol->n_blocks == 1) {
+        const double* G1 = st->G1 + (size_t)mol->blocks[0].seg * M;
+        double* phi = st->rho[m];
+        Cp(phi, G1, M);
+        st->GN[m] = weighted_sum(st, phi);
+        Times(phi, phi, G1, M);
+    } else {
+        mol_forward(st, m);
+        mol_backward_block(st, m, mol->n_blocks - 1, NULL);
+    }
+}
+
+int orc_compose(orc_state* st, const double* x, int m, double* rho, double* GN) {
+    if (m < 0 || m >= st->P->n_mol) return NM_ERR_ARG;
+    prepare_G1(st, x);
+    compose_mol(st, m);
+    Cp(rho, st->rho[m], st->P->mols[m].n_molmon * st->M);
+    if (GN) *GN = st->GN[m];
+    st->have_state = 0;
+    return NM_OK;
+}
+
+static int compute_phis(orc_state* st, const double* x) {
+    const nm_plan* P = st->P;
+    int M = st->M, ns = P->n_seg;
+    prepare_G1(st, x);
     /* System::ComputePhis (system.cpp:2324-2640) */
     Zero(st->phitot, M);
     for (int i = 0; i < ns; i++)
         if (P->seg_freedom[i] == NM_SEG_FROZEN) Add(st->phitot, st->phi + (size_t)i * M, M);
-    for (int m = 0; m < P->n_mol; m++) {
-        const nm_molecule* mol = &P->mols[m];
-        Zero(st->rho[m], mol->n_molmon * M);
-        Zero(st->mol_phitot + (size_t)m * M, M);
-        if (mol->n_store == 1 && mol->n_blocks == 1) {
-            /* monomer: Molecule::ComputePhi (molecule.cpp:2669-2683) */
-            const double* G1 = st->G1 + (size_t)mol->blocks[0].seg * M;
-            double* phi = st->rho[m];
-            Cp(phi, G1, M);
-            st->GN[m] = weighted_sum(st, phi);
-            Times(phi, phi, G1, M);
-        } else {
-            mol_forward(st, m);
-            mol_backward_block(st, m, mol->n_blocks - 1, NULL);
-        }
-    }
+    for (int m = 0; m < P->n_mol; m++) compose_mol(st, m);
     double A = 0, B = 0;
     for (int m = 0; m < P->n_mol; m++) {
         const nm_molecule* mol = &P->mols[m];

@@ -36,6 +36,10 @@ int orc_free_energy(orc_state* st, double* F, double* Omega, double* mu);
  * and the plan's search from x (updated in place) */
 int orc_set_amount(orc_state* st, int mol, int what, double value);
 int orc_search(orc_state* st, double* x, double* value, double* error, int* iterations, int* solves);
+/* Molecule::ComputePhi of molecule m at the field x: rho [n_molmon*M] =
+ * Σ d·Gf·Gb per segment type (before System::ComputePhis divides by G1 and
+ * normalises), GN = G(N) */
+int orc_compose(orc_state* st, const double* x, int m, double* rho, double* GN);
 /* Lattice::propagate and Lattice::Side on one array of length M */
 void orc_propagate(orc_state* st, double* G_in, const double* G1, double* G_out);
 void orc_side(orc_state* st, double* X, double* X_side);
