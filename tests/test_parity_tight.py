@@ -44,7 +44,7 @@ FLOORED = {
     "charged2d": (2e-7, 2e-2, 2e-5),       # oracle spread φ 6.5e-4, F 4.6e-8; device φ 5.2e-3 (Cl), F 5.0e-6
     "charged2d_cyl": (1e-6, 1e-2, 1e-4),   # oracle spread φ 1.0e-3, F 3.6e-6; device Ω 3.4e-5
     "charged2d_hex": (1e-12, 2e-8, 1e-10),  # oracle spread φ 2.8e-9, F 4.2e-12
-    "charged3d": (1e-12, 1e-9, 1e-10),     # oracle spread φ 9.0e-11, F 2.6e-12
+    "charged3d": (1e-11, 1e-9, 1e-10),     # oracle spread φ 9.0e-11, F 2.6e-12; device floor ‖g‖ 3.7e-12
 }
 CASES = golden_names()
 TIGHT = [n for n in CASES if n not in FLOORED]
