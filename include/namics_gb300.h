@@ -155,6 +155,12 @@ typedef struct nm_plan {
      * values from nm_plan_scan_value */
     int    scan_mol, scan_what, scan_n, scan_exponential;
     double scan_start, scan_end, scan_step;
+    /* `mol : <name> : save_memory : true` on any molecule (the reference's
+     * checkpointed propagator storage, molecule.cpp:174-186): a context
+     * created with checkpoint_stride 0 then stores every k-th forward
+     * propagator with the reference's slot count, round(√(2·N_block)) per
+     * block.  Results are the same either way. */
+    int    save_memory;
 } nm_plan;
 
 /* Parse Namics input text (the `lat/mon/mol/sys/newton` key subset of the
@@ -171,7 +177,13 @@ typedef struct nm_ctx nm_ctx;
 
 typedef struct nm_ctx_options {
     int precision;           /* enum nm_precision for propagators           */
-    int checkpoint_stride;   /* store every k-th forward propagator (0=all) */
+    int checkpoint_stride;   /* k > 1: store every k-th forward propagator of
+                                each block (and its last), recompute the rest
+                                in the backward sweep from the checkpoint
+                                before them; 0: every propagator, unless the
+                                plan asks for save_memory; 3-gradient
+                                simple-cubic linear chains (other problems
+                                store every propagator); same results     */
     int device;              /* CUDA device ordinal                          */
     void* stream;            /* cudaStream_t, NULL = a private stream       */
 } nm_ctx_options;

@@ -153,10 +153,11 @@ class SearchResult:
 class Context:
     """Device state for one problem (nm_ctx)."""
 
-    def __init__(self, plan: Plan, precision: int = NM_FP64, device: int = 0, stream: int | None = None):
+    def __init__(self, plan: Plan, precision: int = NM_FP64, device: int = 0, stream: int | None = None,
+                 checkpoint_stride: int = 0):
         lib = _abi.load()
         self.plan = plan
-        opt = _abi.nm_ctx_options(precision, 0, device, C.c_void_p(stream) if stream else None)
+        opt = _abi.nm_ctx_options(precision, checkpoint_stride, device, C.c_void_p(stream) if stream else None)
         h = C.c_void_p()
         _check(lib.nm_ctx_create(plan.ptr, C.byref(opt), C.byref(h)))
         self._h = h

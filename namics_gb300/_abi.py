@@ -60,7 +60,8 @@ class nm_plan(C.Structure):
                 ("super_iterationlimit", C.c_int),
                 ("scan_mol", C.c_int), ("scan_what", C.c_int), ("scan_n", C.c_int),
                 ("scan_exponential", C.c_int), ("scan_start", C.c_double), ("scan_end", C.c_double),
-                ("scan_step", C.c_double)]
+                ("scan_step", C.c_double),
+                ("save_memory", C.c_int)]
 
 
 class nm_ctx_options(C.Structure):

@@ -960,18 +960,46 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
         TRY(dalloc(&d_maxbits, 2 * 32 * (size_t)max_store, stream));  // 32 slots per stored vector
         TRY(dalloc(&d_E, 2 * (size_t)max_store, stream));
     }
+    // checkpointed propagator storage (3-D path): the caller's stride, else
+    // for save_memory inputs the reference's slot count per block,
+    // n = round(√(2·N_block)) (molecule.cpp:174-186), as a stride
+    std::vector<size_t> n_vec(p->n_mol);
+    if (use3d) {
+        ck_stride = opt && opt->checkpoint_stride > 1 ? opt->checkpoint_stride : 0;
+        if (!ck_stride && p->save_memory)
+            for (int m = 0; m < p->n_mol; m++)
+                for (int b = 0; b < p->mols[m].n_blocks; b++) {
+                    const int L = p->mols[m].blocks[b].length;
+                    int n = std::min(L, (int)(std::sqrt(2.0 * L) + 0.5));
+                    if (n > 0) ck_stride = std::max(ck_stride, (L + n - 1) / n);
+                }
+        if (ck_stride < 2) ck_stride = 0;
+    }
+    for (int m = 0; m < p->n_mol; m++) {
+        const nm_molecule& mol = p->mols[m];
+        n_vec[m] = mol.n_store;
+        if (!ck_stride) continue;
+        MolDev& D = mols[m];
+        D.slot.assign(mol.n_store, -1);
+        for (int b = 0; b < mol.n_blocks; b++) {
+            const nm_block& B = mol.blocks[b];
+            for (int j = 0; j < B.length; j++)
+                if (j % ck_stride == 0 || j == B.length - 1) D.slot[B.s0 + j] = D.n_slots++;
+        }
+        n_vec[m] = (size_t)D.n_slots + (ck_stride - 1) + 2;
+    }
     if (fp32 && use3d) {
         TRY(dalloc(&d_G1f, (size_t)ns * M, stream));
         TRY(dalloc(&d_gb32, 2 * (size_t)M, stream));
         for (int m = 0; m < p->n_mol; m++) {
             const nm_molecule& mol = p->mols[m];
-            TRY(dalloc(&mols[m].Gf32, (size_t)mol.n_store * M, stream));
+            TRY(dalloc(&mols[m].Gf32, n_vec[m] * M, stream));
             TRY(dalloc(&mols[m].rho32, 2 * (size_t)mol.n_molmon * M, stream));
         }
     }
     for (int m = 0; m < p->n_mol; m++) {
         const nm_molecule& mol = p->mols[m];
-        TRY(dalloc(&mols[m].Gf, (size_t)mol.n_store * M, stream));
+        TRY(dalloc(&mols[m].Gf, n_vec[m] * M, stream));
         TRY(dalloc(&mols[m].rho, (size_t)mol.n_molmon * M, stream));
         TRY(dalloc(&mols[m].Pc, (size_t)mol.n_blocks * M, stream));
         TRY(dalloc(&mols[m].Q, (size_t)mol.n_blocks * M, stream));

@@ -24,6 +24,7 @@
 // converted once per residual to the FP64 ρ the normalisation reads.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -206,8 +207,15 @@ static void k3(Ctx& C, const T* in, const T* G1, T* out, int sin, int sout, cons
     C.launches++;
 }
 
-// One molecule: forward sweep storing every Gf(s), G(N), backward sweep fused
-// with the composition.  Slots: forward s -> s, backward s -> n_store + s.
+// One molecule: forward sweep, G(N), backward sweep fused with the
+// composition.  Exponent slots (FP32): forward s -> s, backward s ->
+// n_store + s.  Storage: every Gf(s) (ck_stride 0), or with stride k > 1
+// (the reference's save_memory, molecule.cpp:2300-2446, as a fixed stride)
+// only Gf(s0 + j·k) and each block's last segment; the backward sweep then
+// recomputes each group of k segments from the checkpoint that starts it
+// into a buffer of k-1 vectors (small enough to stay in L2 on a 128³ box
+// at k ≈ 10) with the same step kernel and inputs as the forward sweep, so
+// every recomputed vector is bit-identical to the one a full store keeps.
 template <typename T>
 static int pass3d(Ctx& C, int m) {
     const nm_plan* p = C.plan;
@@ -217,6 +225,15 @@ static int pass3d(Ctx& C, int m) {
     const int ns = mol.n_store;
     const bool f32 = sizeof(T) == 4;
     T* Gf = f32 ? (T*)D.Gf32 : (T*)D.Gf;
+    const int k = C.ck_stride;
+    auto vec = [&](size_t j) { return Gf + j * M; };
+    // where the forward sweep leaves Gf(s)
+    auto fwd = [&](int s) -> T* {
+        if (k < 2) return vec(s);
+        const int sl = D.slot[s];
+        return sl >= 0 ? vec(sl) : vec((size_t)D.n_slots + (k - 1) + (s & 1));
+    };
+    auto kbuf = [&](int i) { return vec((size_t)D.n_slots + i - 1); };  // i = 1 .. k-1
     const T* G1 = f32 ? (const T*)C.d_G1f : (const T*)C.d_G1;
     T* gb = f32 ? (T*)C.d_gb32 : (T*)C.d_gb;
     T* rhi = f32 ? (T*)D.rho32 : (T*)D.rho;
@@ -231,26 +248,26 @@ static int pass3d(Ctx& C, int m) {
         const nm_block& B = mol.blocks[b];
         const T* g1 = G1 + (size_t)B.seg * M;
         if (B.n_child == 0) {
-            k3<T, 1>(C, nullptr, g1, Gf + (size_t)B.s0 * M, 0, B.s0, nullptr, 0, 0, nullptr, nullptr, 1.0);
+            k3<T, 1>(C, nullptr, g1, fwd(B.s0), 0, B.s0, nullptr, 0, 0, nullptr, nullptr, 1.0);
         } else {
             const nm_block& C0 = mol.blocks[mol.child_index[B.child0]];
             const int sl = C0.s0 + C0.length - 1;
-            k3<T, 0>(C, Gf + (size_t)sl * M, g1, Gf + (size_t)B.s0 * M, sl, B.s0, nullptr, 0, 0, nullptr, nullptr, 1.0);
+            k3<T, 0>(C, fwd(sl), g1, fwd(B.s0), sl, B.s0, nullptr, 0, 0, nullptr, nullptr, 1.0);
         }
-        for (int k = 1; k < B.length; k++) {
-            const int s = B.s0 + k;
-            k3<T, 0>(C, Gf + (size_t)(s - 1) * M, g1, Gf + (size_t)s * M, s - 1, s, nullptr, 0, 0, nullptr, nullptr, 1.0);
+        for (int j = 1; j < B.length; j++) {
+            const int s = B.s0 + j;
+            k3<T, 0>(C, fwd(s - 1), g1, fwd(s), s - 1, s, nullptr, 0, 0, nullptr, nullptr, 1.0);
         }
     }
     const nm_block& R = mol.blocks[mol.n_blocks - 1];
     const int sroot = R.s0 + R.length - 1;
     if (f32) {
         int nb = C.red_blocks;
-        k3_wsum32<<<nb, 256, 0, C.stream>>>(C.l3, (const float*)Gf + (size_t)sroot * M, C.d_partial);
+        k3_wsum32<<<nb, 256, 0, C.stream>>>(C.l3, (const float*)fwd(sroot), C.d_partial);
         k3_gn32<<<1, 32, 0, C.stream>>>(C.d_partial, nb, C.d_E, sroot, C.d_sc + 5 * m);
         C.launches += 2;
     } else {
-        C.wsum((const double*)Gf + (size_t)sroot * M, C.d_sc + 5 * m);
+        C.wsum((const double*)fwd(sroot), C.d_sc + 5 * m);
     }
     // backward: a linear chain walks its blocks from the root down, the
     // first segment of each block continuing the previous block's sweep
@@ -261,15 +278,25 @@ static int pass3d(Ctx& C, int m) {
         T* rh = rhi + (size_t)B.molmon * M;
         T* rl = rlo ? rlo + (size_t)B.molmon * M : nullptr;
         const int top = B.s0 + B.length - 1;
-        for (int s = top; s >= B.s0; s--) {
-            T* o = gb + (size_t)(s & 1) * M;
-            const int so = ns + s;
-            if (sprev < 0)
-                k3<T, 2>(C, nullptr, g1, o, 0, so, Gf + (size_t)s * M, s, sroot, rh, rl, B.degeneracy);
-            else
-                k3<T, 3>(C, gb + (size_t)(sprev & 1) * M, g1, o, ns + sprev, so, Gf + (size_t)s * M, s, sroot, rh, rl,
-                         B.degeneracy);
-            sprev = s;
+        const int kk = k < 2 ? B.length : k;  // group length: the whole block without checkpoints
+        for (int c = B.s0 + ((B.length - 1) / kk) * kk; c >= B.s0; c -= kk) {
+            const int e = std::min(c + kk - 1, top);
+            // the group's forward propagators: stored (k < 2) or recomputed
+            // from the checkpoint Gf(c)
+            auto gf = [&](int s) -> const T* { return k < 2 || s == c ? fwd(s) : kbuf(s - c); };
+            if (k >= 2)
+                for (int s = c + 1; s <= e; s++)
+                    k3<T, 0>(C, gf(s - 1), g1, kbuf(s - c), s - 1, s, nullptr, 0, 0, nullptr, nullptr, 1.0);
+            for (int s = e; s >= c; s--) {
+                T* o = gb + (size_t)(s & 1) * M;
+                const int so = ns + s;
+                if (sprev < 0)
+                    k3<T, 2>(C, nullptr, g1, o, 0, so, gf(s), s, sroot, rh, rl, B.degeneracy);
+                else
+                    k3<T, 3>(C, gb + (size_t)(sprev & 1) * M, g1, o, ns + sprev, so, gf(s), s, sroot, rh, rl,
+                             B.degeneracy);
+                sprev = s;
+            }
         }
     }
     if (f32) {

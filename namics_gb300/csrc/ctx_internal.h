@@ -116,6 +116,12 @@ struct MolDev {
     double* rho = nullptr;  // Σ d·Gf·Gb per molecule segment type [n_molmon*M]
     double* Pc = nullptr;   // P(G_end)·KSAM of each child block [n_blocks*M]
     double* Q = nullptr;    // backward start of each child block [n_blocks*M]
+    // checkpointed storage (3-D path, Ctx::ck_stride > 1): slot[s] = the
+    // stored vector of segment s or -1; n_slots stored vectors, then k-1
+    // vectors of the backward sweep's recompute buffer, then 2 vectors of
+    // the forward sweep's running propagator
+    std::vector<int> slot;
+    int n_slots = 0;
 };
 
 nmdev::Lat make_lat(const nm_plan* p);
@@ -178,6 +184,7 @@ struct Ctx {
     std::vector<MolDev> mols;
     // 3-D simple-cubic path (ctx3d.cu) and its FP32 propagators
     bool use3d = false;       // dedicated 3-D kernels for every molecule
+    int ck_stride = 0;        // > 1: every k-th forward propagator stored (3-D path)
     bool fp32 = false;        // context created with NM_FP32 propagators
     bool phase32 = false;     // the current residual uses FP32 propagators
     double sw_floor = 0;      // FP32 accuracy floor of ‖g‖ (switch to FP64 near it)

@@ -745,6 +745,10 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
         else if (fr == "solvent") { mb.mol.freedom = NM_MOL_SOLVENT; P.solvent = m; }
         else if (fr == "neutralizer") { mb.mol.freedom = NM_MOL_NEUTRALIZER; P.neutralizer = m; }
         else { err = "mol " + mn + " freedom '" + fr + "' is not supported"; delete H; return nullptr; }
+        {   // Molecule::CheckInput, molecule.cpp:369-372 (Input::Get_bool, input.cpp:270-277)
+            const std::string sm = in.get("mol", mn, "save_memory", "false");
+            if (sm == "true" || sm == "True" || sm == "TRUE") P.save_memory = 1;
+        }
         if (mb.mol.freedom == NM_MOL_FREE) {
             if (!in.has("mol", mn, "phibulk")) { err = "free mol " + mn + " needs phibulk"; delete H; return nullptr; }
             to_real(in.get("mol", mn, "phibulk"), mb.mol.phibulk);

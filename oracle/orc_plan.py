@@ -72,7 +72,7 @@ class PlanRecord(C.Structure):
                 ("super_tolerance", C.c_double), ("super_deltamax", C.c_double),
                 ("super_iterationlimit", C.c_int), ("scan_mol", C.c_int), ("scan_what", C.c_int),
                 ("scan_n", C.c_int), ("scan_exponential", C.c_int), ("scan_start", C.c_double),
-                ("scan_end", C.c_double), ("scan_step", C.c_double)]
+                ("scan_end", C.c_double), ("scan_step", C.c_double), ("save_memory", C.c_int)]
 
 
 def _entries(text: str):

@@ -447,3 +447,41 @@ def test_work_loop_results_independent_of_slots():
             its_i, _, _ = Batch([plans[i]], prec).solve_host(xi)
             assert its_i[0] == its_a[i]
             assert np.array_equal(xi, x_all[b.offsets[i]:b.offsets[i + 1]])
+
+
+@pytest.mark.parametrize("prec", [NM_FP64, NM_FP32])
+def test_checkpointed_storage_is_bit_identical(prec):
+    """3-D melt: every forward propagator stored, against every k-th stored
+    and the rest recomputed in the backward sweep (k = 3, 7, 10, and the
+    reference's own slot count for `save_memory : true`, round(√(2·50)) = 10
+    slots, a stride of 5): the same residual bit for bit, and the same solve."""
+    import bench
+    run = load_golden("melt3d")["runs"]["it0"]
+    plan = Plan(run["input"])
+    x0 = np.array(run["x"])
+    big = Plan(bench.melt3d_text(24, 30))
+    u = np.random.default_rng(5).uniform(-0.1, 0.1, big.M)
+    for p, x in ((plan, x0), (big, np.concatenate([u, -u]))):
+        ref = Context(p, prec)
+        xd = dev(x)
+        g0 = torch.zeros_like(xd)
+        ref.residual_dev(xd.data_ptr(), g0.data_ptr())
+        g0 = host(g0)
+        variants = [Context(p, prec, checkpoint_stride=k) for k in (3, 7, 10)]
+        text = run["input"] if p is plan else bench.melt3d_text(24, 30)
+        sm = Plan(text.replace("mol : AB : freedom : solvent", "mol : AB : freedom : solvent\nmol : AB : save_memory : true")
+                  if "mol : AB" in text else text)
+        assert sm.c.save_memory == ("mol : AB" in text)
+        variants.append(Context(sm, prec))
+        for c in variants:
+            g = torch.zeros_like(xd)
+            c.residual_dev(xd.data_ptr(), g.data_ptr())
+            assert np.array_equal(host(g), g0)
+        if p is big:  # 30 DIIS iterations
+            x1 = x.copy()
+            r0, _ = ref.solve_host(x1)
+            for c in variants:
+                xc = x.copy()
+                r, _ = c.solve_host(xc)
+                assert (r.iterations, r.residual) == (r0.iterations, r0.residual)
+                assert np.array_equal(xc, x1)
