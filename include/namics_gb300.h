@@ -380,6 +380,49 @@ int nm_batch_set_slots(nm_batch* b, int slots);
 int nm_batch_free_energy(nm_batch* b, double* F, double* Omega);
 long long nm_batch_launch_count(nm_batch* b);
 
+/* ---- streaming work loop (continuous batching of 1-gradient solves) -------
+ * No single counterpart in the reference (it runs one Solve at a time): a
+ * persistent launch whose resident CTAs ("slots") take 1-gradient solves
+ * from a ring the host appends to while the loop runs.  A request is
+ * admitted the moment a slot is free, its field, stored propagators and
+ * DIIS history stay in the slot's device memory until it has converged, and
+ * its result is handed back through pinned host memory; nothing waits for
+ * other requests.  The ring, the fields and the results live in pinned host
+ * memory mapped into the device.  A CTA without work for idle_seconds
+ * leaves the loop; the next request (or a waiter) launches it again.
+ * Requests must fit the envelope given at creation (it sizes the slots and
+ * the ring's per-request space); a request outside it is NM_ERR_INPUT. */
+typedef struct nm_stream nm_stream;
+typedef struct nm_stream_options {
+    int    device;
+    int    capacity;       /* ring entries: requests submitted and not yet waited for */
+    int    max_layers;     /* largest MX admitted (<= 512)                      */
+    int    max_segments;   /* segment types (<= 16)                             */
+    int    max_pairs;      /* (molecule, segment type) pairs (<= 32)            */
+    int    max_molecules;  /* molecules (<= 16)                                 */
+    int    max_store;      /* stored propagators, summed over the molecules     */
+    int    max_blocks;     /* blocks, summed over the molecules                 */
+    int    max_diis;       /* DIIS history m (<= 12)                            */
+    int    slots;          /* resident CTAs; 0: as many as fit on the device    */
+    double idle_seconds;   /* a CTA without work this long leaves; 0: 0.2 s     */
+} nm_stream_options;
+int nm_stream_create(const nm_stream_options* opt, nm_stream** out);
+/* Queue one solve of `plan` (a 1-gradient, uncharged problem; the plan may
+ * be destroyed after the call) from the field x_host (plan->iv values,
+ * copied), with FP32-first (NM_FP32) or FP64 (NM_FP64) propagators.
+ * NM_ERR_NOMEM when the ring is full of requests not yet waited for. */
+int nm_stream_submit(nm_stream* s, const nm_plan* plan, const double* x_host, int precision,
+                     long long* ticket);
+/* Block until the request is solved: the field (may be NULL), the result,
+ * and the seconds from submit to the solve's end (host clock).  Returns
+ * NM_OK for a converged or iteration-limited solve (see res->status). */
+int nm_stream_wait(nm_stream* s, long long ticket, double* x_host, nm_solve_result* res,
+                   double* seconds);
+int nm_stream_slots(nm_stream* s);
+long long nm_stream_launch_count(nm_stream* s);
+/* Stops the loop (requests not yet claimed are dropped) and frees it. */
+int nm_stream_destroy(nm_stream* s);
+
 /* ---- request server (continuous batching on one GPU) ----------------------
  * No single counterpart in the reference (it runs one Solve at a time): a
  * stream of independent solves of any gradient count, served while others

@@ -16,7 +16,7 @@ import numpy as np
 from . import _abi
 from ._abi import NM_FP32, NM_FP64  # noqa: F401
 
-__all__ = ["Plan", "Context", "Batch", "Server", "NamicsError", "load_library", "NM_FP32", "NM_FP64"]
+__all__ = ["Plan", "Context", "Batch", "Stream", "Server", "NamicsError", "load_library", "NM_FP32", "NM_FP64"]
 
 
 class NamicsError(RuntimeError):
@@ -386,6 +386,54 @@ class Batch:
 
     def launch_count(self) -> int:
         return int(_abi.load().nm_batch_launch_count(self._h))
+
+
+class Stream:
+    """Streaming work loop for 1-gradient solves (nm_stream_*): requests are
+    admitted into resident CTAs as slots free up, while the loop runs."""
+
+    def __init__(self, device: int = 0, capacity: int = 1024, max_layers: int = 512, max_segments: int = 6,
+                 max_pairs: int = 6, max_molecules: int = 3, max_store: int = 520, max_blocks: int = 8,
+                 max_diis: int = 10, slots: int = 0, idle_seconds: float = 0.2):
+        opt = _abi.nm_stream_options(device, capacity, max_layers, max_segments, max_pairs, max_molecules,
+                                     max_store, max_blocks, max_diis, slots, idle_seconds)
+        h = C.c_void_p()
+        _check(_abi.load().nm_stream_create(C.byref(opt), C.byref(h)))
+        self._h = h
+
+    def submit(self, plan: Plan, x: np.ndarray, precision: int = NM_FP32) -> int:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        _check_len(x, plan.iv, "Stream.submit")
+        t = C.c_longlong()
+        _check(_abi.load().nm_stream_submit(self._h, plan.ptr, _dptr(x), precision, C.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, iv: int | None = None):
+        """(SolveResult, field or None, seconds from submit to the solve's end)."""
+        r = _abi.nm_solve_result()
+        sec = C.c_double()
+        x = np.zeros(iv) if iv else None
+        _check(_abi.load().nm_stream_wait(self._h, ticket, _dptr(x) if x is not None else None, C.byref(r),
+                                          C.byref(sec)))
+        return SolveResult(r.iterations, r.residual, r.status), x, sec.value
+
+    @property
+    def slots(self) -> int:
+        return int(_abi.load().nm_stream_slots(self._h))
+
+    def launch_count(self) -> int:
+        return int(_abi.load().nm_stream_launch_count(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _abi.load().nm_stream_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Server:

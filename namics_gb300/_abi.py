@@ -81,6 +81,12 @@ class nm_search_result(C.Structure):
 P_plan = C.POINTER(nm_plan)
 
 
+class nm_stream_options(C.Structure):
+    _fields_ = [("device", C.c_int), ("capacity", C.c_int), ("max_layers", C.c_int), ("max_segments", C.c_int),
+                ("max_pairs", C.c_int), ("max_molecules", C.c_int), ("max_store", C.c_int),
+                ("max_blocks", C.c_int), ("max_diis", C.c_int), ("slots", C.c_int), ("idle_seconds", C.c_double)]
+
+
 class nm_server_options(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("workers", C.c_int),
                 ("max_batch", C.c_int), ("memory_budget", C.c_size_t)]
@@ -130,6 +136,12 @@ SIGNATURES = [
     ("nm_batch_set_slots", C.c_int, [C.c_void_p, C.c_int]),
     ("nm_batch_free_energy", C.c_int, [C.c_void_p, dp, dp]),
     ("nm_batch_launch_count", C.c_longlong, [C.c_void_p]),
+    ("nm_stream_create", C.c_int, [C.POINTER(nm_stream_options), C.POINTER(C.c_void_p)]),
+    ("nm_stream_submit", C.c_int, [C.c_void_p, P_plan, dp, C.c_int, C.POINTER(C.c_longlong)]),
+    ("nm_stream_wait", C.c_int, [C.c_void_p, C.c_longlong, dp, C.POINTER(nm_solve_result), C.POINTER(C.c_double)]),
+    ("nm_stream_slots", C.c_int, [C.c_void_p]),
+    ("nm_stream_launch_count", C.c_longlong, [C.c_void_p]),
+    ("nm_stream_destroy", C.c_int, [C.c_void_p]),
     ("nm_server_create", C.c_int, [C.POINTER(nm_server_options), C.POINTER(C.c_void_p)]),
     ("nm_server_submit", C.c_int, [C.c_void_p, P_plan, dp, C.POINTER(C.c_longlong)]),
     ("nm_server_wait", C.c_int, [C.c_void_p, C.c_longlong, dp, C.POINTER(nm_solve_result), C.POINTER(C.c_double)]),

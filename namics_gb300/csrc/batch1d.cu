@@ -923,8 +923,15 @@ struct Batch {
 
 #define TRYB(x) do { int r_ = (x); if (r_) return r_; } while (0)
 
-// Raise the dynamic shared-memory limit of k_batch1d and k_batch1d_queue on
-// device `dev` (current) to at least `bytes`.  The limit only ever rises, and every path that launches
+struct StreamEntry;
+struct StreamCtl;
+__global__ void k_stream1d(StreamEntry* ring, double* xring, int cap, int iv_max, StreamCtl* ctl,
+                           unsigned long long* head, unsigned char* slots, unsigned long long slot_bytes,
+                           B1Prob* priv, double* xpriv, double* gpriv, unsigned long long idle_ns,
+                           const unsigned char* blobs, unsigned char* cpriv, unsigned long long blob_max);
+
+// Raise the dynamic shared-memory limit of k_batch1d, k_batch1d_queue and
+// k_stream1d on device `dev` (current) to at least `bytes`.  The limit only ever rises, and every path that launches
 // k_batch1d (batches, the server's workers, the allocation-free solve) goes
 // through this one lock, so no caller can lower it under another's launch.
 static cudaError_t b1_raise_smem(int dev, size_t bytes) {
@@ -936,6 +943,8 @@ static cudaError_t b1_raise_smem(int dev, size_t bytes) {
     cudaError_t e = cudaFuncSetAttribute(k_batch1d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_batch1d_queue, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_stream1d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e == cudaSuccess) set[dev] = bytes;
     return e;
 }
@@ -956,6 +965,109 @@ static int batch_check(const nm_plan* P) {
     return NM_OK;
 }
 
+// Device copies of one plan's constant arrays (curved-lattice weights, KSAM,
+// G1 masks, frozen profiles, block trees), shared by every problem that
+// uses the plan.
+struct B1PlanDev {
+    const double *lm1 = nullptr, *l0 = nullptr, *l1 = nullptr, *L = nullptr, *ksam = nullptr, *gmask = nullptr,
+                 *phi_frozen = nullptr;
+    const nm_block* blocks[NM_MAX_MOL] = {};
+    const int* child_index[NM_MAX_MOL] = {};
+};
+
+// upload(dst, src, bytes): device copy of a host array (an allocation the
+// caller owns)
+template <typename Up>
+static int b1_plan_upload(const nm_plan* P, B1PlanDev& D, Up&& upload) {
+    const int M = P->M;
+    auto up = [&](const void** dst, const void* src, size_t bytes) {
+        void* d = nullptr;
+        int rc = upload(&d, src, bytes);
+        *dst = d;
+        return rc;
+    };
+    if (P->geometry != NM_PLANAR) {
+        TRYB(up((const void**)&D.lm1, P->lambda_1, sizeof(double) * M));
+        TRYB(up((const void**)&D.l0, P->lambda0, sizeof(double) * M));
+        TRYB(up((const void**)&D.l1, P->lambda1, sizeof(double) * M));
+        TRYB(up((const void**)&D.L, P->L, sizeof(double) * M));
+    }
+    std::vector<double> ks(M);
+    for (int s = 0; s < M; s++) ks[s] = P->ksam[s];
+    TRYB(up((const void**)&D.ksam, ks.data(), sizeof(double) * M));
+    TRYB(up((const void**)&D.gmask, P->seg_gmask, sizeof(double) * P->n_seg * M));
+    TRYB(up((const void**)&D.phi_frozen, P->seg_phi_frozen, sizeof(double) * P->n_seg * M));
+    for (int m = 0; m < P->n_mol; m++) {
+        const nm_molecule& mol = P->mols[m];
+        if (mol.n_blocks > B1_MAXB) { set_error("molecule has too many blocks for the batched solver"); return NM_ERR_INPUT; }
+        std::vector<int> ci(mol.child_index, mol.child_index + (mol.n_blocks > 1 ? mol.n_blocks - 1 : 0));
+        if (ci.empty()) ci.push_back(0);
+        TRYB(up((const void**)&D.blocks[m], mol.blocks, sizeof(nm_block) * mol.n_blocks));
+        TRYB(up((const void**)&D.child_index[m], ci.data(), sizeof(int) * ci.size()));
+    }
+    return NM_OK;
+}
+
+// The descriptor of one problem of plan P over its plan's device constants.
+// Its stored propagators and DIIS history get byte offsets inside a slot of
+// the work loop's scratch (256-byte aligned pieces): `scratch` returns the
+// bytes one slot needs for it, `smem` the kernel's dynamic shared memory.
+static int b1_describe(const nm_plan* P, const B1PlanDev& PD, B1Prob& H, size_t& scratch, size_t& smem) {
+    std::memset(&H, 0, sizeof(H));
+    const int M = P->M;
+    // one stored vector: M doubles (FP64 phase) or 128·SP floats (FP32 phase)
+    const size_t tsz = std::max((size_t)8 * M, (size_t)4 * BC_NT * b1_sp(P->MX));
+    H.MX = P->MX; H.M = M; H.geom = P->geometry; H.ns = P->n_seg; H.nit = P->n_it;
+    H.nmol = P->n_mol; H.solvent = P->solvent; H.m = P->diis_m; H.itlim = P->iterationlimit;
+    H.max_norm = P->max_norm; H.iv = P->iv; H.lam = P->lambda; H.tol = P->tolerance; H.dmax = P->deltamax;
+    H.b1 = P->bc[0] == NM_BC_MIRROR ? 1 : P->bc[0] == NM_BC_PERIODIC ? P->MX : 0;
+    H.bm = P->bc[3] == NM_BC_MIRROR ? P->MX : P->bc[3] == NM_BC_PERIODIC ? 1 : P->MX + 1;
+    H.lm1 = PD.lm1; H.l0 = PD.l0; H.l1 = PD.l1; H.L = PD.L;
+    H.ksam = PD.ksam; H.gmask = PD.gmask; H.phi_frozen = PD.phi_frozen;
+    size_t used = 0;
+    auto take = [&used](size_t bytes) {
+        size_t o = (used + 255) & ~(size_t)255;
+        used = o + std::max<size_t>(bytes, 1);
+        return (unsigned long long)o;
+    };
+    for (int i = 0; i < P->n_seg; i++) {
+        H.seg_it[i] = P->seg_it[i];
+        H.seg_frozen[i] = P->seg_freedom[i] == NM_SEG_FROZEN;
+        H.seg_inmol[i] = P->seg_it[i] >= 0;
+    }
+    for (int i = 0; i < P->n_it; i++) H.it_seg[i] = P->it_seg[i];
+    for (int i = 0; i < P->n_seg * P->n_seg; i++) H.chi[i] = P->chi[i];
+    int kk = 0;
+    for (int m = 0; m < P->n_mol; m++) {
+        const nm_molecule& mol = P->mols[m];
+        B1Mol& D = H.mol[m];
+        D.freedom = mol.freedom; D.pinned = mol.pinned; D.n_blocks = mol.n_blocks; D.n_store = mol.n_store;
+        D.n_molmon = mol.n_molmon; D.mm0 = kk;
+        D.n_in = mol.n; D.theta_in = mol.theta; D.phibulk_in = mol.phibulk; D.N = mol.chainlength;
+        D.blocks = PD.blocks[m]; D.child_index = PD.child_index[m];
+        H.so[m].gf = take(tsz * (size_t)mol.n_store);
+        H.so[m].pc = take(tsz * (size_t)mol.n_blocks);
+        H.so[m].q = take(tsz * (size_t)mol.n_blocks);
+        // power-of-two exponents: one per thread (128) per stored vector
+        H.so[m].ef = take(sizeof(int) * BC_NT * (size_t)mol.n_store);
+        H.so[m].epc = take(sizeof(int) * BC_NT * (size_t)mol.n_blocks);
+        H.so[m].eq = take(sizeof(int) * BC_NT * (size_t)mol.n_blocks);
+        for (int j = 0; j < mol.n_molmon; j++) {
+            if (kk >= NM_MAX_MM) { set_error("too many (molecule, segment) pairs"); return NM_ERR_INPUT; }
+            H.mm_mol[kk] = m; H.mm_seg[kk] = mol.molmon_seg[j]; H.mm_frac[kk] = mol.molmon_fraction[j];
+            kk++;
+        }
+    }
+    H.n_mm = kk;
+    H.so_xR = take(sizeof(double) * (size_t)P->diis_m * P->iv);
+    H.so_xx0 = take(sizeof(double) * (size_t)P->diis_m * P->iv);
+    scratch = (used + 255) & ~(size_t)255;
+    H.sw_tol = 2e-6;
+    H.sw_floor = b1_fp32_floor(P);
+    smem = sizeof(double) * b1_smem_doubles(P->n_seg, kk, M, P->MX);
+    return NM_OK;
+}
+
 static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx_options* opt) {
     for (int p = 0; p < n; p++) {
         if (!plans[p]) { set_error("nm_batch_create: null plan"); return NM_ERR_ARG; }
@@ -972,105 +1084,28 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
     size_t maxsmem = 0;
     B.hp.resize(n);
     B.offsets.resize(n + 1);
-    // device copies of a plan's constant arrays, shared by every problem of
-    // the batch that uses the same plan
-    struct PlanDev {
-        const double *lm1 = nullptr, *l0 = nullptr, *l1 = nullptr, *L = nullptr, *ksam = nullptr, *gmask = nullptr,
-                     *phi_frozen = nullptr;
-        const nm_block* blocks[NM_MAX_MOL] = {};
-        const int* child_index[NM_MAX_MOL] = {};
+    std::map<const nm_plan*, B1PlanDev> pdev;
+    auto upload = [&B](void** dst, const void* src, size_t bytes) -> int {
+        char* d = nullptr;
+        int rc = B.upload(&d, (const char*)src, bytes);
+        *dst = d;
+        return rc;
     };
-    std::map<const nm_plan*, PlanDev> pdev;
     for (int p = 0; p < n; p++) {
         const nm_plan* P = plans[p];
         B.plans.push_back(P);
-        B1Prob& H = B.hp[p];
-        std::memset(&H, 0, sizeof(H));
-        int M = P->M;
-        // one stored vector: M doubles (FP64 phase) or 128·SP floats (FP32 phase)
-        size_t tsz = std::max((size_t)8 * M, (size_t)4 * BC_NT * b1_sp(P->MX));
-        H.MX = P->MX; H.M = M; H.geom = P->geometry; H.ns = P->n_seg; H.nit = P->n_it;
-        H.nmol = P->n_mol; H.solvent = P->solvent; H.m = P->diis_m; H.itlim = P->iterationlimit;
-        H.max_norm = P->max_norm; H.iv = P->iv; H.lam = P->lambda; H.tol = P->tolerance; H.dmax = P->deltamax;
-        H.b1 = P->bc[0] == NM_BC_MIRROR ? 1 : P->bc[0] == NM_BC_PERIODIC ? P->MX : 0;
-        H.bm = P->bc[3] == NM_BC_MIRROR ? P->MX : P->bc[3] == NM_BC_PERIODIC ? 1 : P->MX + 1;
         auto found = pdev.find(P);
         if (found == pdev.end()) {
-            PlanDev D;
-            if (P->geometry != NM_PLANAR) {
-                double *a, *b, *c, *dL;
-                TRYB(B.upload(&a, P->lambda_1, M)); TRYB(B.upload(&b, P->lambda0, M)); TRYB(B.upload(&c, P->lambda1, M));
-                TRYB(B.upload(&dL, P->L, M));
-                D.lm1 = a; D.l0 = b; D.l1 = c; D.L = dL;
-            }
-            double *dk, *dg, *dpf;
-            std::vector<double> ks(M);
-            for (int s = 0; s < M; s++) ks[s] = P->ksam[s];
-            TRYB(B.upload(&dk, ks.data(), M));
-            TRYB(B.upload(&dg, P->seg_gmask, (size_t)P->n_seg * M));
-            TRYB(B.upload(&dpf, P->seg_phi_frozen, (size_t)P->n_seg * M));
-            D.ksam = dk; D.gmask = dg; D.phi_frozen = dpf;
-            for (int m = 0; m < P->n_mol; m++) {
-                const nm_molecule& mol = P->mols[m];
-                if (mol.n_blocks > B1_MAXB) { set_error("molecule has too many blocks for the batched solver"); return NM_ERR_INPUT; }
-                nm_block* db; int* dci;
-                TRYB(B.upload(&db, mol.blocks, mol.n_blocks));
-                std::vector<int> ci(mol.child_index, mol.child_index + (mol.n_blocks > 1 ? mol.n_blocks - 1 : 0));
-                if (ci.empty()) ci.push_back(0);
-                TRYB(B.upload(&dci, ci.data(), ci.size()));
-                D.blocks[m] = db; D.child_index[m] = dci;
-            }
+            B1PlanDev D;
+            TRYB(b1_plan_upload(P, D, upload));
             found = pdev.emplace(P, D).first;
         }
-        const PlanDev& PD = found->second;
-        H.lm1 = PD.lm1; H.l0 = PD.l0; H.l1 = PD.l1; H.L = PD.L;
-        H.ksam = PD.ksam; H.gmask = PD.gmask; H.phi_frozen = PD.phi_frozen;
-        // this problem's scratch inside one slot of the work loop (256-byte
-        // aligned pieces); the slot is sized for the batch's largest layout
-        size_t used = 0;
-        auto take = [&used](size_t bytes) {
-            size_t o = (used + 255) & ~(size_t)255;
-            used = o + std::max<size_t>(bytes, 1);
-            return (unsigned long long)o;
-        };
-        for (int i = 0; i < P->n_seg; i++) {
-            H.seg_it[i] = P->seg_it[i];
-            H.seg_frozen[i] = P->seg_freedom[i] == NM_SEG_FROZEN;
-            H.seg_inmol[i] = P->seg_it[i] >= 0;
-        }
-        for (int i = 0; i < P->n_it; i++) H.it_seg[i] = P->it_seg[i];
-        for (int i = 0; i < P->n_seg * P->n_seg; i++) H.chi[i] = P->chi[i];
-        int kk = 0;
-        for (int m = 0; m < P->n_mol; m++) {
-            const nm_molecule& mol = P->mols[m];
-            B1Mol& D = H.mol[m];
-            D.freedom = mol.freedom; D.pinned = mol.pinned; D.n_blocks = mol.n_blocks; D.n_store = mol.n_store;
-            D.n_molmon = mol.n_molmon; D.mm0 = kk;
-            D.n_in = mol.n; D.theta_in = mol.theta; D.phibulk_in = mol.phibulk; D.N = mol.chainlength;
-            D.blocks = PD.blocks[m]; D.child_index = PD.child_index[m];
-            H.so[m].gf = take(tsz * (size_t)mol.n_store);
-            H.so[m].pc = take(tsz * (size_t)mol.n_blocks);
-            H.so[m].q = take(tsz * (size_t)mol.n_blocks);
-            // power-of-two exponents: one per thread (128) per stored vector
-            H.so[m].ef = take(sizeof(int) * BC_NT * (size_t)mol.n_store);
-            H.so[m].epc = take(sizeof(int) * BC_NT * (size_t)mol.n_blocks);
-            H.so[m].eq = take(sizeof(int) * BC_NT * (size_t)mol.n_blocks);
-            for (int j = 0; j < mol.n_molmon; j++) {
-                if (kk >= NM_MAX_MM) { set_error("too many (molecule, segment) pairs"); return NM_ERR_INPUT; }
-                H.mm_mol[kk] = m; H.mm_seg[kk] = mol.molmon_seg[j]; H.mm_frac[kk] = mol.molmon_fraction[j];
-                kk++;
-            }
-        }
-        H.n_mm = kk;
-        H.so_xR = take(sizeof(double) * (size_t)P->diis_m * P->iv);
-        H.so_xx0 = take(sizeof(double) * (size_t)P->diis_m * P->iv);
-        B.slot_bytes = std::max(B.slot_bytes, (used + 255) & ~(size_t)255);
+        size_t scratch = 0, smem = 0;
+        TRYB(b1_describe(P, found->second, B.hp[p], scratch, smem));
+        B.slot_bytes = std::max(B.slot_bytes, scratch);
+        maxsmem = std::max(maxsmem, smem);
         B.offsets[p] = off;
         off += P->iv;
-        H.sw_tol = 2e-6;
-        H.sw_floor = b1_fp32_floor(P);
-        size_t smem = sizeof(double) * b1_smem_doubles(P->n_seg, kk, M, P->MX);
-        maxsmem = std::max(maxsmem, smem);
     }
     B.offsets[n] = off;
     TRYB(B.alloc(&B.d_x, (size_t)off));
@@ -1472,3 +1507,436 @@ extern "C" int nm_solve1d_noalloc(const nm_plan* plan, double* x_dev, int precis
     res->status = H.status;
     return H.status == NM_OK ? NM_OK : H.status;
 }
+
+// ======================================================================
+// Streaming work loop (continuous batching of 1-gradient solves).
+//
+// The host appends requests to a ring while the loop runs; each resident
+// CTA (slot) claims the next published request as soon as its last one has
+// converged.  Ring entries, their fields x and their results live in pinned
+// host memory mapped into the device's address space: the host publishes an
+// entry with a release store of `tail` (system scope), a CTA claims it by a
+// compare-and-swap on `head` in device memory, copies descriptor and field
+// into its slot-private device memory with uncached loads, solves there
+// (b1_solve, the batch kernel's body), writes the field and results back and
+// marks the entry done with a release store (system scope).  A CTA that
+// finds no work for `idle_ns` leaves the loop; the host relaunches the loop
+// when a request arrives, or is waited for, and the loop is gone.  Every
+// device-side wait is bounded by that idle limit.
+// ======================================================================
+namespace nm {
+
+struct StreamEntry {
+    B1Prob desc;                   // host-written; its constant-array pointers are rebased on the device
+    // the problem's constant arrays, packed by the host into the entry's blob
+    // (byte offsets; ~0 = absent): L, λ-1, λ0, λ+1, KSAM, G1 masks, frozen φ,
+    // and per molecule the blocks and the children lists
+    unsigned long long co_L, co_lm1, co_l0, co_l1, co_ksam, co_gmask, co_pf;
+    unsigned long long co_blocks[NM_MAX_MOL], co_ci[NM_MAX_MOL];
+    unsigned long long blob_bytes;
+    int mode;                      // 0: FP64 propagators, 1: FP32 first
+    int iv;
+    // device-written results
+    int iterations, fp32_iterations, status, pad;
+    double residual;
+    unsigned long long t_begin, t_end;  // device global timer, ns
+    unsigned long long done;       // ticket + 1 once solved (release, system scope)
+};
+
+struct StreamCtl {
+    unsigned long long tail;       // requests published (host, release)
+    unsigned int stop;             // host: 1 ends the loop
+    unsigned int pad;
+};
+
+__device__ __forceinline__ unsigned long long ld_acquire_sys(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.sys.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_sys(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.release.sys.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__global__ void __launch_bounds__(B1_THREADS, 3) k_stream1d(StreamEntry* ring, double* xring, int cap, int iv_max,
+                                                           StreamCtl* ctl, unsigned long long* head,
+                                                           unsigned char* slots, unsigned long long slot_bytes,
+                                                           B1Prob* priv, double* xpriv, double* gpriv,
+                                                           unsigned long long idle_ns, const unsigned char* blobs,
+                                                           unsigned char* cpriv, unsigned long long blob_max) {
+    __shared__ unsigned long long s_tk, s_blob;
+    __shared__ int s_go, s_mode, s_iv;
+    B1Prob& P = priv[blockIdx.x];
+    unsigned char* base = slots + (size_t)blockIdx.x * slot_bytes;
+    unsigned char* cbase = cpriv + (size_t)blockIdx.x * blob_max;
+    double* xs = xpriv + (size_t)blockIdx.x * iv_max;
+    double* gs = gpriv + (size_t)blockIdx.x * iv_max;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_go = 0;
+            const unsigned long long t0 = b1_clock();
+            for (;;) {  // ends on a claim, on stop, or after idle_ns without work
+                const unsigned long long tail = ld_acquire_sys(&ctl->tail);
+                if (*(volatile unsigned int*)&ctl->stop) break;
+                const unsigned long long h = *(volatile unsigned long long*)head;
+                if (h < tail) {
+                    if (atomicCAS(head, h, h + 1) == h) { s_tk = h; s_go = 1; break; }
+                    continue;
+                }
+                if (b1_clock() - t0 > idle_ns) break;
+                __nanosleep(2000);
+            }
+            if (s_go) {
+                const StreamEntry* E = ring + (s_tk % (unsigned long long)cap);
+                s_mode = *(const volatile int*)&E->mode;
+                s_iv = *(const volatile int*)&E->iv;
+                s_blob = *(const volatile unsigned long long*)&E->blob_bytes;
+            }
+        }
+        __syncthreads();
+        if (!s_go) break;
+        const unsigned long long tk = s_tk;
+        const int slot = (int)(tk % (unsigned long long)cap);
+        StreamEntry* E = ring + slot;
+        {   // private copies: uncached loads of the host-written entry
+            const unsigned long long* src = reinterpret_cast<const unsigned long long*>(&E->desc);
+            unsigned long long* dst = reinterpret_cast<unsigned long long*>(&P);
+            for (int i = threadIdx.x; i < (int)(sizeof(B1Prob) / 8); i += blockDim.x) dst[i] = __ldcv(src + i);
+            const double* xsrc = xring + (size_t)slot * iv_max;
+            for (int i = threadIdx.x; i < s_iv; i += blockDim.x) xs[i] = __ldcv(xsrc + i);
+            const unsigned int* bsrc = reinterpret_cast<const unsigned int*>(blobs + (size_t)slot * blob_max);
+            unsigned int* bdst = reinterpret_cast<unsigned int*>(cbase);
+            for (int i = threadIdx.x; i < (int)(s_blob / 4); i += blockDim.x) bdst[i] = __ldcv(bsrc + i);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const volatile StreamEntry* V = E;
+            auto at = [&](unsigned long long o) -> const double* {
+                return o == ~0ull ? nullptr : reinterpret_cast<const double*>(cbase + o);
+            };
+            P.L = at(V->co_L); P.lm1 = at(V->co_lm1); P.l0 = at(V->co_l0); P.l1 = at(V->co_l1);
+            P.ksam = at(V->co_ksam); P.gmask = at(V->co_gmask); P.phi_frozen = at(V->co_pf);
+            for (int m = 0; m < P.nmol; m++) {
+                P.mol[m].blocks = reinterpret_cast<const nm_block*>(cbase + V->co_blocks[m]);
+                P.mol[m].child_index = reinterpret_cast<const int*>(cbase + V->co_ci[m]);
+            }
+            P.x = xs;
+            P.g = gs;
+            P.eval_only = 0;
+            b1_rebase(P, base);
+        }
+        __syncthreads();
+        b1_solve(P, s_mode);
+        __syncthreads();
+        {
+            double* xdst = xring + (size_t)slot * iv_max;
+            for (int i = threadIdx.x; i < s_iv; i += blockDim.x) ((volatile double*)xdst)[i] = xs[i];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            volatile StreamEntry* V = E;
+            V->iterations = P.iterations;
+            V->fp32_iterations = P.fp32_iterations;
+            V->status = P.status;
+            V->residual = P.residual;
+            V->t_begin = P.t_begin;
+            V->t_end = P.t_end;
+            __threadfence_system();
+            st_release_sys(&E->done, tk + 1);
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace nm
+
+#include <atomic>
+#include <chrono>
+#include <thread>
+
+namespace nm {
+
+static double stream_now() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct Stream1D {
+    int dev = 0, cap = 0, iv_max = 0, slots = 0;
+    nm_stream_options env{};
+    size_t slot_bytes = 0, smem = 0, blob_max = 0;
+    unsigned long long idle_ns = 0;
+    // pinned host memory mapped into the device's address space
+    StreamEntry* ring = nullptr;  StreamEntry* ring_d = nullptr;
+    double* xring = nullptr;      double* xring_d = nullptr;
+    unsigned char* blobs = nullptr; unsigned char* blobs_d = nullptr;
+    StreamCtl* ctl = nullptr;     StreamCtl* ctl_d = nullptr;
+    // device memory
+    unsigned long long* head = nullptr;
+    unsigned char* d_slots = nullptr;
+    unsigned char* d_cpriv = nullptr;
+    B1Prob* d_priv = nullptr;
+    double *d_xpriv = nullptr, *d_gpriv = nullptr;
+    cudaStream_t loop_stream = nullptr;
+    cudaEvent_t loop_done = nullptr;
+    bool launched = false;
+    long long launches = 0;
+    std::mutex mu;
+    unsigned long long tail = 0;      // next ticket
+    unsigned long long reaped = 0;    // tickets below this are done (times recorded)
+    std::vector<char> busy;           // per ring entry: submitted and not yet waited for
+    std::vector<unsigned long long> owner;
+    std::vector<double> t_submit, t_done;
+    std::thread reaper;
+    std::atomic<bool> quit{false};
+
+    bool loop_alive() { return launched && cudaEventQuery(loop_done) == cudaErrorNotReady; }
+    int launch_locked() {
+        cudaSetDevice(dev);
+        k_stream1d<<<slots, B1_THREADS, smem, loop_stream>>>(ring_d, xring_d, cap, iv_max, ctl_d, head, d_slots,
+                                                            (unsigned long long)slot_bytes, d_priv, d_xpriv, d_gpriv,
+                                                            idle_ns, blobs_d, d_cpriv,
+                                                            (unsigned long long)blob_max);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaEventRecord(loop_done, loop_stream);
+        if (e != cudaSuccess) { set_error(std::string("stream loop launch: ") + cudaGetErrorString(e)); return NM_ERR_CUDA; }
+        launched = true;
+        launches++;
+        return NM_OK;
+    }
+    // completion times of finished requests, and a new loop if requests wait
+    // while the loop is gone (its CTAs leave after idle_ns without work)
+    void reap() {
+        while (!quit.load()) {
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                while (reaped < tail) {
+                    const int s = (int)(reaped % (unsigned long long)cap);
+                    if (__atomic_load_n(&ring[s].done, __ATOMIC_ACQUIRE) != reaped + 1) break;
+                    t_done[s] = stream_now();
+                    reaped++;
+                }
+                if (reaped < tail && !loop_alive()) launch_locked();
+            }
+            std::this_thread::sleep_for(std::chrono::microseconds(20));
+        }
+    }
+    ~Stream1D() {
+        if (ctl) __atomic_store_n(&ctl->stop, 1u, __ATOMIC_RELEASE);
+        quit.store(true);
+        if (reaper.joinable()) reaper.join();
+        if (launched) cudaEventSynchronize(loop_done);
+        if (loop_done) cudaEventDestroy(loop_done);
+        void* dev_ptrs[] = {head, d_slots, d_cpriv, d_priv, d_xpriv, d_gpriv};
+        for (void* q : dev_ptrs) if (q) cudaFree(q);
+        void* host_ptrs[] = {ring, xring, blobs, ctl};
+        for (void* q : host_ptrs) if (q) cudaFreeHost(q);
+        if (loop_stream) cudaStreamDestroy(loop_stream);
+    }
+};
+
+// The problem's constant arrays into its entry's blob (16-byte aligned pieces)
+static int stream_pack(const nm_plan* P, StreamEntry& E, unsigned char* blob, size_t blob_max) {
+    const int M = P->M;
+    size_t used = 0;
+    bool ok = true;
+    auto put = [&](const void* src, size_t bytes) -> unsigned long long {
+        const size_t o = (used + 15) & ~(size_t)15;
+        if (o + bytes > blob_max) { ok = false; return ~0ull; }
+        std::memcpy(blob + o, src, bytes);
+        used = o + bytes;
+        return o;
+    };
+    const bool curved = P->geometry != NM_PLANAR;
+    E.co_L = curved ? put(P->L, sizeof(double) * M) : ~0ull;
+    E.co_lm1 = curved ? put(P->lambda_1, sizeof(double) * M) : ~0ull;
+    E.co_l0 = curved ? put(P->lambda0, sizeof(double) * M) : ~0ull;
+    E.co_l1 = curved ? put(P->lambda1, sizeof(double) * M) : ~0ull;
+    std::vector<double> ks(M);
+    for (int s = 0; s < M; s++) ks[s] = P->ksam[s];
+    E.co_ksam = put(ks.data(), sizeof(double) * M);
+    E.co_gmask = put(P->seg_gmask, sizeof(double) * P->n_seg * M);
+    E.co_pf = put(P->seg_phi_frozen, sizeof(double) * P->n_seg * M);
+    for (int m = 0; m < P->n_mol; m++) {
+        const nm_molecule& mol = P->mols[m];
+        E.co_blocks[m] = put(mol.blocks, sizeof(nm_block) * mol.n_blocks);
+        const int nci = mol.n_blocks > 1 ? mol.n_blocks - 1 : 0;
+        const int zero = 0;
+        E.co_ci[m] = nci ? put(mol.child_index, sizeof(int) * nci) : put(&zero, sizeof(int));
+    }
+    E.blob_bytes = (used + 15) & ~(size_t)15;
+    if (!ok) { set_error("request exceeds the stream's constant-array space"); return NM_ERR_INPUT; }
+    return NM_OK;
+}
+
+}  // namespace nm
+
+using nm::Stream1D;
+
+extern "C" {
+
+int nm_stream_create(const nm_stream_options* opt, nm_stream** out) {
+    using namespace nm;
+    if (!opt || !out) { set_error("nm_stream_create: bad argument"); return NM_ERR_ARG; }
+    *out = nullptr;
+    const nm_stream_options& o = *opt;
+    if (o.capacity < 1 || o.max_layers < 1 || o.max_layers > B1_KS * B1_THREADS || o.max_segments < 1 ||
+        o.max_segments > NM_MAX_SEG || o.max_pairs < 1 || o.max_pairs > NM_MAX_MM || o.max_molecules < 1 ||
+        o.max_molecules > NM_MAX_MOL || o.max_store < 1 || o.max_blocks < 1 || o.max_diis < 1 || o.max_diis > B1_MAXM) {
+        set_error("nm_stream_create: envelope out of range (layers <= 512, segments <= 16, pairs <= 32, "
+                  "molecules <= 16, DIIS m <= 12)");
+        return NM_ERR_ARG;
+    }
+    Stream1D* S = new Stream1D();
+    S->env = o;
+    S->dev = o.device;
+    S->cap = o.capacity;
+    cudaError_t e = cudaSetDevice(S->dev);
+    if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); delete S; return NM_ERR_CUDA; }
+    const int Mmax = o.max_layers + 2;
+    S->iv_max = o.max_segments * Mmax;
+    const size_t tsz = std::max((size_t)8 * Mmax, (size_t)4 * BC_NT * b1_sp(o.max_layers));
+    const size_t nvec = (size_t)o.max_store + 2 * (size_t)o.max_blocks;
+    S->slot_bytes = tsz * nvec + sizeof(int) * BC_NT * nvec + 2 * sizeof(double) * o.max_diis * (size_t)S->iv_max +
+                    256 * (6 * (size_t)o.max_molecules + 4);
+    S->slot_bytes = (S->slot_bytes + 255) & ~(size_t)255;
+    S->blob_max = sizeof(double) * Mmax * (5 + 2 * (size_t)o.max_segments) +
+                  (size_t)o.max_molecules * (sizeof(nm_block) + sizeof(int)) * o.max_blocks + 16 * (8 + 2 * o.max_molecules);
+    S->blob_max = (S->blob_max + 255) & ~(size_t)255;
+    S->smem = sizeof(double) * b1_smem_doubles(o.max_segments, o.max_pairs, Mmax, o.max_layers);
+    S->idle_ns = (unsigned long long)((o.idle_seconds > 0 ? o.idle_seconds : 0.2) * 1e9);
+    if (S->smem > 220 * 1024) { set_error("nm_stream_create: envelope too large for shared memory"); delete S; return NM_ERR_ARG; }
+    auto fail = [&](cudaError_t err) {
+        set_error(std::string("nm_stream_create: ") + cudaGetErrorString(err));
+        delete S;
+        return NM_ERR_CUDA;
+    };
+    if ((e = b1_raise_smem(S->dev, S->smem))) return fail(e);
+    int per_sm = 0, sms = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stream1d, B1_THREADS, S->smem))) return fail(e);
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, S->dev))) return fail(e);
+    S->slots = std::max(1, per_sm * sms);
+    if (o.slots > 0) S->slots = std::min(S->slots, o.slots);
+    const unsigned fl = cudaHostAllocMapped | cudaHostAllocPortable;
+    if ((e = cudaHostAlloc((void**)&S->ring, sizeof(StreamEntry) * S->cap, fl))) return fail(e);
+    if ((e = cudaHostAlloc((void**)&S->xring, sizeof(double) * S->cap * (size_t)S->iv_max, fl))) return fail(e);
+    if ((e = cudaHostAlloc((void**)&S->blobs, S->blob_max * S->cap, fl))) return fail(e);
+    if ((e = cudaHostAlloc((void**)&S->ctl, sizeof(StreamCtl), fl))) return fail(e);
+    std::memset((void*)S->ring, 0, sizeof(StreamEntry) * S->cap);
+    std::memset(S->ctl, 0, sizeof(StreamCtl));
+    if ((e = cudaHostGetDevicePointer((void**)&S->ring_d, S->ring, 0))) return fail(e);
+    if ((e = cudaHostGetDevicePointer((void**)&S->xring_d, S->xring, 0))) return fail(e);
+    if ((e = cudaHostGetDevicePointer((void**)&S->blobs_d, S->blobs, 0))) return fail(e);
+    if ((e = cudaHostGetDevicePointer((void**)&S->ctl_d, S->ctl, 0))) return fail(e);
+    if ((e = cudaMalloc((void**)&S->head, sizeof(unsigned long long)))) return fail(e);
+    if ((e = cudaMemset(S->head, 0, sizeof(unsigned long long)))) return fail(e);
+    if ((e = cudaMalloc((void**)&S->d_slots, S->slot_bytes * S->slots))) return fail(e);
+    if ((e = cudaMemset(S->d_slots, 0, S->slot_bytes * S->slots))) return fail(e);
+    if ((e = cudaMalloc((void**)&S->d_cpriv, S->blob_max * S->slots))) return fail(e);
+    if ((e = cudaMalloc((void**)&S->d_priv, sizeof(B1Prob) * S->slots))) return fail(e);
+    if ((e = cudaMalloc((void**)&S->d_xpriv, sizeof(double) * S->iv_max * (size_t)S->slots))) return fail(e);
+    if ((e = cudaMalloc((void**)&S->d_gpriv, sizeof(double) * S->iv_max * (size_t)S->slots))) return fail(e);
+    if ((e = cudaStreamCreateWithFlags(&S->loop_stream, cudaStreamNonBlocking))) return fail(e);
+    if ((e = cudaEventCreateWithFlags(&S->loop_done, cudaEventDisableTiming))) return fail(e);
+    if ((e = cudaDeviceSynchronize())) return fail(e);
+    S->busy.assign(S->cap, 0);
+    S->owner.assign(S->cap, 0);
+    S->t_submit.assign(S->cap, 0.0);
+    S->t_done.assign(S->cap, 0.0);
+    S->reaper = std::thread([S] { S->reap(); });
+    *out = reinterpret_cast<nm_stream*>(S);
+    return NM_OK;
+}
+
+int nm_stream_submit(nm_stream* st, const nm_plan* P, const double* x_host, int precision, long long* ticket) {
+    using namespace nm;
+    Stream1D* S = reinterpret_cast<Stream1D*>(st);
+    if (!S || !P || !x_host || !ticket) { set_error("nm_stream_submit: bad argument"); return NM_ERR_ARG; }
+    if (precision != NM_FP32 && precision != NM_FP64) { set_error("nm_stream_submit: bad precision"); return NM_ERR_ARG; }
+    if (int rc = batch_check(P)) return rc;
+    const nm_stream_options& o = S->env;
+    int store = 0, blocks = 0, pairs = 0;
+    for (int m = 0; m < P->n_mol; m++) {
+        store += P->mols[m].n_store; blocks += P->mols[m].n_blocks; pairs += P->mols[m].n_molmon;
+    }
+    if (P->MX > o.max_layers || P->n_seg > o.max_segments || pairs > o.max_pairs || P->n_mol > o.max_molecules ||
+        store > o.max_store || blocks > o.max_blocks || P->diis_m > o.max_diis) {
+        set_error("nm_stream_submit: the problem exceeds the stream's envelope");
+        return NM_ERR_INPUT;
+    }
+    B1PlanDev none;
+    size_t scratch = 0, smem = 0;
+    B1Prob H;
+    if (int rc = b1_describe(P, none, H, scratch, smem)) return rc;
+    if (scratch > S->slot_bytes || smem > S->smem || P->iv > S->iv_max) {
+        set_error("nm_stream_submit: the problem exceeds the stream's slot");
+        return NM_ERR_INPUT;
+    }
+    std::lock_guard<std::mutex> lk(S->mu);
+    const unsigned long long t = S->tail;
+    const int s = (int)(t % (unsigned long long)S->cap);
+    if (S->busy[s]) { set_error("nm_stream_submit: ring full (wait for earlier requests first)"); return NM_ERR_NOMEM; }
+    StreamEntry& E = S->ring[s];
+    E.desc = H;
+    if (int rc = stream_pack(P, E, S->blobs + (size_t)s * S->blob_max, S->blob_max)) return rc;
+    E.mode = precision == NM_FP32 ? 1 : 0;
+    E.iv = P->iv;
+    __atomic_store_n(&E.done, 0ull, __ATOMIC_RELAXED);
+    std::memcpy(S->xring + (size_t)s * S->iv_max, x_host, sizeof(double) * P->iv);
+    S->busy[s] = 1;
+    S->owner[s] = t;
+    S->t_submit[s] = stream_now();
+    __atomic_store_n(&S->ctl->tail, t + 1, __ATOMIC_RELEASE);
+    S->tail = t + 1;
+    *ticket = (long long)t;
+    if (!S->loop_alive()) return S->launch_locked();
+    return NM_OK;
+}
+
+int nm_stream_wait(nm_stream* st, long long ticket, double* x_host, nm_solve_result* res, double* seconds) {
+    using namespace nm;
+    Stream1D* S = reinterpret_cast<Stream1D*>(st);
+    if (!S || ticket < 0) { set_error("nm_stream_wait: bad argument"); return NM_ERR_ARG; }
+    const int s = (int)((unsigned long long)ticket % (unsigned long long)S->cap);
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        if (!S->busy[s] || S->owner[s] != (unsigned long long)ticket) {
+            set_error("nm_stream_wait: unknown or already collected ticket");
+            return NM_ERR_ARG;
+        }
+    }
+    const double t0 = stream_now();
+    for (;;) {
+        {
+            std::lock_guard<std::mutex> lk(S->mu);
+            if ((unsigned long long)ticket < S->reaped) break;  // done, time recorded
+        }
+        if (stream_now() - t0 > 3600.0) { set_error("nm_stream_wait: no result within an hour"); return NM_ERR_TIMEOUT; }
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+    std::lock_guard<std::mutex> lk(S->mu);
+    const StreamEntry& E = S->ring[s];
+    if (x_host) std::memcpy(x_host, S->xring + (size_t)s * S->iv_max, sizeof(double) * E.iv);
+    if (res) { res->iterations = E.iterations; res->residual = E.residual; res->status = E.status; }
+    if (seconds) *seconds = S->t_done[s] - S->t_submit[s];
+    S->busy[s] = 0;
+    return E.status == NM_OK || E.status == NM_ERR_NOT_CONVERGED ? NM_OK : E.status;
+}
+
+int nm_stream_slots(nm_stream* st) {
+    Stream1D* S = reinterpret_cast<Stream1D*>(st);
+    return S ? S->slots : 0;
+}
+
+long long nm_stream_launch_count(nm_stream* st) {
+    Stream1D* S = reinterpret_cast<Stream1D*>(st);
+    if (!S) return 0;
+    std::lock_guard<std::mutex> lk(S->mu);
+    return S->launches;
+}
+
+int nm_stream_destroy(nm_stream* st) {
+    delete reinterpret_cast<Stream1D*>(st);
+    return NM_OK;
+}
+
+}  // extern "C"
