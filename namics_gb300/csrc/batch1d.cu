@@ -1689,7 +1689,16 @@ struct Stream1D {
     std::thread reaper;
     std::atomic<bool> quit{false};
 
-    bool loop_alive() { return launched && cudaEventQuery(loop_done) == cudaErrorNotReady; }
+    int broken = 0;                   // a CUDA error seen by the loop: every wait fails with it
+    bool loop_alive() {
+        if (!launched) return false;
+        const cudaError_t e = cudaEventQuery(loop_done);
+        if (e != cudaSuccess && e != cudaErrorNotReady && !broken) {
+            broken = NM_ERR_CUDA;
+            set_error(std::string("stream loop: ") + cudaGetErrorString(e));
+        }
+        return e == cudaErrorNotReady;
+    }
     int launch_locked() {
         cudaSetDevice(dev);
         k_stream1d<<<slots, B1_THREADS, smem, loop_stream>>>(ring_d, xring_d, cap, iv_max, ctl_d, head, d_slots,
@@ -1715,7 +1724,7 @@ struct Stream1D {
                     t_done[s] = stream_now();
                     reaped++;
                 }
-                if (reaped < tail && !loop_alive()) launch_locked();
+                if (reaped < tail && !loop_alive() && !broken && launch_locked()) broken = NM_ERR_CUDA;
             }
             std::this_thread::sleep_for(std::chrono::microseconds(20));
         }
@@ -1888,6 +1897,7 @@ int nm_stream_submit(nm_stream* st, const nm_plan* P, const double* x_host, int 
     __atomic_store_n(&S->ctl->tail, t + 1, __ATOMIC_RELEASE);
     S->tail = t + 1;
     *ticket = (long long)t;
+    if (S->broken) { set_error("nm_stream_submit: the loop failed with a CUDA error"); return S->broken; }
     if (!S->loop_alive()) return S->launch_locked();
     return NM_OK;
 }
@@ -1909,6 +1919,7 @@ int nm_stream_wait(nm_stream* st, long long ticket, double* x_host, nm_solve_res
         {
             std::lock_guard<std::mutex> lk(S->mu);
             if ((unsigned long long)ticket < S->reaped) break;  // done, time recorded
+            if (S->broken) { set_error("nm_stream_wait: the loop failed with a CUDA error"); return S->broken; }
         }
         if (stream_now() - t0 > 3600.0) { set_error("nm_stream_wait: no result within an hour"); return NM_ERR_TIMEOUT; }
         std::this_thread::sleep_for(std::chrono::microseconds(20));
