@@ -271,7 +271,7 @@ def melt3d_text(n: int = 128, itlim: int = 20) -> str:
     ]) + "\n"
 
 
-def run_melt3d(args) -> None:
+def run_melt3d(args) -> dict:
     """On one GPU: DIIS iterations of the 128³ A50B50 melt with FP32
     propagators (per-vector power-of-two exponents, FP64 DIIS) and with plain
     FP64 propagators, from the same seeded field u_A = -u_B ~ U(-0.1, 0.1).
@@ -341,7 +341,7 @@ def run_melt3d(args) -> None:
         "fp32": f32, "fp32_full_storage": out["fp32_full_storage"],
         "fp64_gpu": dict(f64, value=1000.0 / f64["ms_per_residual_and_update"], unit="iterations/s"),
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def ads2d_text(n: int = 100, N: int = 200) -> str:
@@ -403,7 +403,7 @@ def cyl2d_plan(nx: int, ny: int, N: int, sigma: float, chi: float, itlim: int, t
     return Plan(cyl2d_text(nx, ny, N, sigma * first, chi, itlim, tol))
 
 
-def run_cyl2d(args) -> None:
+def run_cyl2d(args) -> dict:
     """On one GPU: the 200×200 cylindrical charged brush (A_500, sigma
     0.02, A valence -0.1, Na neutraliser, Cl phi_b 0.01) at both chi_AS values
     of the configuration, 0 and 0.5, solved side by side: one device context
@@ -525,14 +525,15 @@ def run_cyl2d(args) -> None:
         "fp64_gpu": dict({k: v for k, v in f64.items() if k != "phi"},
                          value=f64["iterations_per_s"], unit="iterations/s"),
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
-def run_served(args) -> None:
+def run_served(args) -> dict:
     """A Poisson request stream served on one GPU by nm_server
-    (continuous batching: 1-gradient requests waiting together share one
-    batched launch, others get a device context each; W workers with one
-    stream each; admission by device footprint).  Mix: 70% 1-D brushes/stars drawn like the batched workload,
+    (continuous batching: 1-gradient requests go into the streaming work
+    loop, admitted into resident CTAs as slots free up; the others get a
+    device context each on W worker streams, admitted by device footprint).
+    Mix: 70% 1-D brushes/stars drawn like the batched workload,
     25% 2-D 100×100 (A)200 adsorption, 5% 3-D 64³ (A)20(B)20 melts at
     chi 0.4, all from seeded fields.  Reported: converged solves/s over the
     span from the first submit to the last completion, p50/p99 of the
@@ -584,6 +585,10 @@ def run_served(args) -> None:
                      "span_s": span, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                      "p50_ms_by_kind": {kn: (float(np.percentile(np.array(v) * 1e3, 50)) if v else None)
                                         for kn, v in zip(("brush1d", "ads2d", "melt3d"), by_kind.values())},
+                     "p99_ms_by_kind": {kn: (float(np.percentile(np.array(v) * 1e3, 99)) if v else None)
+                                        for kn, v in zip(("brush1d", "ads2d", "melt3d"), by_kind.values())},
+                     "requests_by_kind": {kn: len(v) for kn, v in zip(("brush1d", "ads2d", "melt3d"),
+                                                                     by_kind.values())},
                      "gpu_launches": launches}
     f32 = out["fp32"]
     line = {
@@ -596,7 +601,7 @@ def run_served(args) -> None:
         "latency": {"p50_ms": f32["p50_ms"], "p99_ms": f32["p99_ms"], "what": "submit to completion"},
         "fp32": f32, "fp64_gpu": out["fp64"],
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def main():
@@ -621,18 +626,20 @@ def main():
     ap.add_argument("--n3d", type=int, default=128, help="melt3d: box edge")
     ap.add_argument("--ckpt", type=int, default=10, help="melt3d: checkpoint stride of the FP32 arm (0: store all)")
     ap.add_argument("--instances", type=int, default=N_INSTANCES)
+    ap.add_argument("--no-others", action="store_true",
+                    help="brush1d: skip the short runs of the melt, cylinder and served workloads")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
         return
     if args.workload == "melt3d":
-        run_melt3d(args)
+        print(json.dumps(run_melt3d(args)), flush=True)
         return
     if args.workload == "served":
-        run_served(args)
+        print(json.dumps(run_served(args)), flush=True)
         return
     if args.workload == "cyl2d":
-        run_cyl2d(args)
+        print(json.dumps(run_cyl2d(args)), flush=True)
         return
     run_brush1d(args)
 
@@ -672,6 +679,33 @@ def plain_fp64_sample(plans, xs, budget_s: float = 6.0, stream=None):
     return {"value": ok / t_gpu if t_gpu > 0 else None, "unit": UNIT, "converged": ok, "solves": done,
             "seconds": t_gpu, "what": "one solve at a time, device context, FP64 propagators, DIIS with a host "
                                       "sync per iteration (nm_solve_dev); first instances of the workload"}
+
+
+def other_workloads(args) -> dict:
+    """Short runs of the other workloads, measured in the same process: the
+    128³ melt (DIIS iterations/s, FP32 propagators checkpointed every 10
+    segments vs plain FP64), the 200×200 charged cylindrical brushes at both
+    χ (iterations/s, FP32 vs FP64, |Δφ| of one residual against the oracle)
+    and the served Poisson mix of 1-D, 2-D and 3-D requests (converged
+    solves/s, p50/p99, FP32 server vs plain-FP64 server).  Each reports its
+    own line's fields without the per-line contract keys."""
+    import copy
+    out = {}
+    keep = ("metric", "value", "unit", "ms_per_step", "config", "roofline", "updates_per_s", "latency",
+            "fp32", "fp32_full_storage", "fp64_gpu")
+    runs = (("melt128", run_melt3d, dict(n3d=128, iters=5, steps=2, warmup=1, ckpt=10)),
+            ("cylinder200", run_cyl2d, dict(n2d=200, iters=5, steps=2, warmup=1, no_solve=True)),
+            ("served_mix", run_served, dict(rate=40.0, requests=160, workers=8)))
+    for name, fn, over in runs:
+        a = copy.copy(args)
+        for k, v in over.items():
+            setattr(a, k, v)
+        try:
+            d = fn(a)
+            out[name] = {k: d[k] for k in keep if k in d}
+        except Exception as e:  # a failure of one short run must not lose the headline line
+            out[name] = {"error": f"{type(e).__name__}: {e}"[:300]}
+    return out
 
 
 def run_brush1d(args) -> None:
@@ -818,6 +852,8 @@ def run_brush1d(args) -> None:
     }
     if rank == 0 and not args.no_cpu and ws == 1:
         line["cpu_baseline"] = cpu_baseline(texts, xs[:len(plans)], budget_s=15.0)
+    if rank == 0 and ws == 1 and not args.no_others:
+        line["other_workloads"] = other_workloads(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

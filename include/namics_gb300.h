@@ -426,10 +426,13 @@ int nm_stream_destroy(nm_stream* s);
 /* ---- request server (continuous batching on one GPU) ----------------------
  * No single counterpart in the reference (it runs one Solve at a time): a
  * stream of independent solves of any gradient count, served while others
- * run.  `workers` threads, one CUDA stream each, take requests from one
- * FIFO queue; 1-gradient requests waiting together are solved in one
- * batched launch (up to max_batch), others one per device context.  Work is
- * admitted by estimated device footprint against memory_budget bytes.
+ * run.  1-gradient requests go to a streaming work loop (below) unless
+ * stream_slots is -1 or the request falls outside its envelope.  `workers`
+ * threads, one CUDA stream each, take the other requests from one FIFO
+ * queue; 1-gradient requests waiting there together are solved in one
+ * batched launch (up to max_batch), others one per device context.  Work of
+ * the workers is admitted by estimated device footprint against
+ * memory_budget bytes.
  * precision: NM_FP32 or NM_FP64 propagators (FP32 where the solver for the
  * request supports it, FP64 otherwise). */
 typedef struct nm_server nm_server;
@@ -439,6 +442,11 @@ typedef struct nm_server_options {
     int    workers;          /* concurrent solves (streams)                  */
     int    max_batch;        /* most 1-gradient requests per batched launch  */
     size_t memory_budget;    /* device bytes admitted requests may hold      */
+    int    stream_slots;     /* 1-gradient requests go to a streaming work
+                                loop (nm_stream_*) with this many resident
+                                CTAs; 0: two per SM; -1: no loop, batched
+                                launches only.  The loop's memory is fixed
+                                at creation and outside memory_budget. */
 } nm_server_options;
 int nm_server_create(const nm_server_options* opt, nm_server** out);
 /* Queue one solve from the field x_host (plan->iv values, copied).  The plan

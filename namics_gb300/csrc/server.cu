@@ -1,13 +1,18 @@
 // Request server: continuous batching of SCF solves on one GPU.
 //
 // Requests of any gradient count arrive one at a time (nm_server_submit) and
-// are solved on the device while others are running.  W worker threads each
-// own a CUDA stream.  A free worker takes work from the queue:
-//   - when the oldest waiting request is a batched-solver problem
-//     (1 gradient), the worker takes it and every other waiting 1-gradient
-//     request, up to max_batch, and solves them in one k_batch1d launch;
-//   - otherwise it takes that request alone into a device context (2-D,
-//     3-D; FP32 propagators for 3-D simple-cubic linear chains).
+// are solved on the device while others are running.
+//   - 1-gradient requests go straight into the streaming work loop
+//     (nm_stream_*): a persistent launch whose resident CTAs take each
+//     request the moment one of them is free, with the field, stored
+//     propagators and DIIS history in that slot's device memory until it
+//     converged.  A request outside the loop's envelope, or one that finds
+//     the ring full, takes the path below as a batched problem.
+//   - W worker threads each own a CUDA stream.  A free worker takes work
+//     from the queue: a waiting 1-gradient request together with every
+//     other waiting one, up to max_batch, in one batched launch; any other
+//     request alone in a device context (2-D, 3-D; FP32 propagators for 3-D
+//     simple-cubic linear chains).
 // Work is admitted by device footprint: a request (or group) starts only when
 // its estimated memory fits beside what is already running, so memory never
 // oversubscribes; a request larger than the whole budget is rejected at
@@ -42,6 +47,7 @@ struct Request {
     std::vector<double> x;
     size_t bytes = 0;
     bool batched = false;
+    long long ticket = -1;  // >= 0: solved by the streaming work loop
     clk::time_point t_submit, t_done;
     nm_solve_result res{};
     int rc = 0;
@@ -77,6 +83,7 @@ struct Server {
     bool stop = false;
     std::vector<std::thread> workers;
     std::atomic<long long> launches{0};
+    nm_stream* loop = nullptr;  // the 1-gradient streaming work loop (may be null)
 
     void worker(int wi);
     void run_batch(std::vector<Request*>& group, cudaStream_t st);
@@ -203,6 +210,17 @@ int nm_server_create(const nm_server_options* opt, nm_server** out) {
     Server* s = new Server();
     s->opt = *opt;
     if (s->opt.max_batch < 1) s->opt.max_batch = 1;
+    if (opt->stream_slots >= 0) {
+        // envelope of the loop: brushes, stars and other 1-gradient problems
+        // of up to 512 layers, six segment types and 1024 stored propagators;
+        // two CTAs per SM by default leave room for the context kernels of
+        // 2-D and 3-D requests beside it
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, opt->device);
+        nm_stream_options so{opt->device, 1024, 512, 6, 6, 4, 1024, 32, 12,
+                             opt->stream_slots > 0 ? opt->stream_slots : 2 * sms, 0.2};
+        if (int rc = nm_stream_create(&so, &s->loop)) { delete s; return rc; }
+    }
     for (int i = 0; i < opt->workers; i++) s->workers.emplace_back(&Server::worker, s, i);
     *out = reinterpret_cast<nm_server*>(s);
     return NM_OK;
@@ -229,12 +247,18 @@ int nm_server_submit(nm_server* srv, const nm_plan* plan, const double* x_host, 
     {
         std::lock_guard<std::mutex> lk(s->mu);
         if (s->stop) { delete r; nm::set_error("nm_server_submit: server is shutting down"); return NM_ERR_ARG; }
+        if (r->batched && s->loop) {
+            long long t = -1;
+            const int rc = nm_stream_submit(s->loop, plan, x_host, s->opt.precision, &t);
+            if (rc == NM_OK) r->ticket = t;
+            else if (rc != NM_ERR_INPUT && rc != NM_ERR_NOMEM) { delete r; return rc; }
+        }
         r->id = s->next_id++;
         s->all[r->id] = r;
-        s->queue.push_back(r);
+        if (r->ticket < 0) s->queue.push_back(r);
         *request_id = r->id;
     }
-    s->cv_work.notify_one();
+    if (r->ticket < 0) s->cv_work.notify_one();
     return NM_OK;
 }
 
@@ -247,8 +271,13 @@ int nm_server_wait(nm_server* srv, long long request_id, double* x_host, nm_solv
         auto it = s->all.find(request_id);
         if (it == s->all.end()) { nm::set_error("nm_server_wait: unknown request"); return NM_ERR_ARG; }
         r = it->second;
-        s->cv_done.wait(lk, [&] { return r->done; });
         s->all.erase(it);
+        if (r->ticket < 0) s->cv_done.wait(lk, [&] { return r->done; });
+    }
+    if (r->ticket >= 0) {  // the streaming loop: its own wait and clock
+        const int rc = nm_stream_wait(s->loop, r->ticket, x_host, res, seconds);
+        delete r;
+        return rc;
     }
     if (x_host) std::memcpy(x_host, r->x.data(), sizeof(double) * r->x.size());
     if (res) *res = r->res;
@@ -261,7 +290,8 @@ int nm_server_wait(nm_server* srv, long long request_id, double* x_host, nm_solv
 
 long long nm_server_launch_count(nm_server* srv) {
     Server* s = reinterpret_cast<Server*>(srv);
-    return s ? s->launches.load() : 0;
+    if (!s) return 0;
+    return s->launches.load() + (s->loop ? nm_stream_launch_count(s->loop) : 0);
 }
 
 int nm_server_destroy(nm_server* srv) {
@@ -274,6 +304,7 @@ int nm_server_destroy(nm_server* srv) {
     s->cv_work.notify_all();
     for (auto& t : s->workers) t.join();
     for (auto& kv : s->all) delete kv.second;
+    if (s->loop) nm_stream_destroy(s->loop);
     delete s;
     return NM_OK;
 }

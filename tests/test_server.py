@@ -1,11 +1,11 @@
 """Request server (nm_server_*): continuous batching of mixed solves.
 
 Each request's result must be the same when it is solved in the mix
-(batched with other 1-gradient requests, overlapping on other streams,
-admitted under a memory budget) as when it is solved alone through the
-existing entry points: bit-identical here, because every reduction on the
-device has a fixed order and a batched problem's CTA does not depend on its
-neighbours.
+(1-gradient requests in the streaming work loop or batched with each other,
+overlapping on other streams, admitted under a memory budget) as when it is
+solved alone through the existing entry points: bit-identical here, because
+every reduction on the device has a fixed order and a problem's CTA does not
+depend on its neighbours.
 """
 import numpy as np
 import pytest
@@ -49,13 +49,16 @@ def _alone(plan, x, precision):
     return r.iterations, r.residual, r.status, xx
 
 
+@pytest.mark.parametrize("stream_slots", [0, -1])
 @pytest.mark.parametrize("precision", [NM_FP32, NM_FP64])
-def test_server_results_equal_alone_and_in_the_mix(precision):
+def test_server_results_equal_alone_and_in_the_mix(precision, stream_slots):
+    """1-gradient requests through the streaming work loop (stream_slots 0)
+    or in batched launches (-1), the others in device contexts."""
     cases = _cases()
     kinds = {c[1].c.gradients for c in cases}
     assert kinds == {1, 2, 3}, kinds
     # a budget that holds only part of the mix at once, so requests queue
-    srv = Server(precision=precision, workers=4, max_batch=8, memory_budget=256 << 20)
+    srv = Server(precision=precision, workers=4, max_batch=8, memory_budget=256 << 20, stream_slots=stream_slots)
     ids = [(n, plan, x, srv.submit(plan, x)) for n, plan, x in cases for _ in range(2)]
     results = [(n, plan, x) + srv.wait(rid) for n, plan, x, rid in ids]
     assert srv.launch_count() > 0
