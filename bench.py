@@ -39,6 +39,10 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
+# more hardware work queues than streams: a stream that shares a queue with
+# the persistent work loop's stream would wait behind the loop (read when
+# the CUDA context is created, so set before torch or the library touch it)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 N_INSTANCES = 512
 SEED = 20251203
@@ -695,7 +699,7 @@ def other_workloads(args) -> dict:
             "fp32", "fp32_full_storage", "fp64_gpu")
     runs = (("melt128", run_melt3d, dict(n3d=128, iters=5, steps=2, warmup=1, ckpt=10)),
             ("cylinder200", run_cyl2d, dict(n2d=200, iters=5, steps=2, warmup=1, no_solve=True)),
-            ("served_mix", run_served, dict(rate=40.0, requests=160, workers=8)))
+            ("served_mix", run_served, dict(rate=400.0, requests=200, workers=8)))
     for name, fn, over in runs:
         a = copy.copy(args)
         for k, v in over.items():

@@ -1652,9 +1652,19 @@ __global__ void __launch_bounds__(B1_THREADS, 3) k_stream1d(StreamEntry* ring, d
 
 #include <atomic>
 #include <chrono>
+#include <cstdlib>
 #include <thread>
 
 namespace nm {
+
+// A persistent work loop occupies its stream's hardware work queue while it
+// runs, so any stream mapped to the same queue waits behind it.  CUDA maps
+// streams onto CUDA_DEVICE_MAX_CONNECTIONS queues (8 unless set) when the
+// context is created; the library asks for 32 at load time, without
+// overriding a value the process set, for contexts created after it loads.
+__attribute__((constructor)) static void stream_connections_default() {
+    setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
+}
 
 static double stream_now() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -1844,7 +1854,11 @@ int nm_stream_create(const nm_stream_options* opt, nm_stream** out) {
     if ((e = cudaMalloc((void**)&S->d_priv, sizeof(B1Prob) * S->slots))) return fail(e);
     if ((e = cudaMalloc((void**)&S->d_xpriv, sizeof(double) * S->iv_max * (size_t)S->slots))) return fail(e);
     if ((e = cudaMalloc((void**)&S->d_gpriv, sizeof(double) * S->iv_max * (size_t)S->slots))) return fail(e);
-    if ((e = cudaStreamCreateWithFlags(&S->loop_stream, cudaStreamNonBlocking))) return fail(e);
+    // the loop's CTAs are placed before pending blocks of other streams as
+    // SMs free up (a relaunch while context kernels fill the device)
+    int prio_low = 0, prio_high = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+    if ((e = cudaStreamCreateWithPriority(&S->loop_stream, cudaStreamNonBlocking, prio_high))) return fail(e);
     if ((e = cudaEventCreateWithFlags(&S->loop_done, cudaEventDisableTiming))) return fail(e);
     if ((e = cudaDeviceSynchronize())) return fail(e);
     S->busy.assign(S->cap, 0);

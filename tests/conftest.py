@@ -1,6 +1,11 @@
 import json
+import os
 import sys
 from pathlib import Path
+
+# more hardware work queues than streams, so no stream waits behind the
+# persistent work loop's queue (read when the CUDA context is created)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 import pytest
 
