@@ -297,9 +297,11 @@ def run_melt3d(args) -> dict:
     flush = torch.empty(int(256e6) // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.Stream()
     out = {}
-    arms = ((NM_FP32, "fp32", args.ckpt), (NM_FP32, "fp32_full_storage", 0), (NM_FP64, "fp64", 0))
+    arms = ((NM_FP32, "fp32", args.ckpt), (NM_FP32, "fp32_full_storage", 0), (NM_FP32, "fp32_autotuned", -1),
+            (NM_FP64, "fp64", 0))
     for prec, name, ck in arms:
-        ctx = Context(plan, prec, stream=stream.cuda_stream, checkpoint_stride=ck)
+        ctx = Context(plan, prec, stream=stream.cuda_stream, checkpoint_stride=max(ck, 0))
+        tuned = ctx.autotune(x0.data_ptr()) if ck < 0 else None
         xw = torch.empty_like(x0)
         times = []
         for k in range(args.warmup + args.steps):
@@ -318,6 +320,8 @@ def run_melt3d(args) -> dict:
         its = r.iterations + 1  # residual evaluations: the first plus one per iteration
         out[name] = {"ms_per_step": ms, "residuals_per_step": its, "ms_per_residual_and_update": ms / its,
                      "launches": ctx.launch_count(), "checkpoint_stride": ck}
+        if tuned:
+            out[name].update(autotuned=tuned, checkpoint_stride=tuned["checkpoint_stride"])
         ctx.close()
     updates = 2.0 * 100 * n ** 3  # segment-site updates per residual
     f32, f64 = out["fp32"], out["fp64"]
@@ -342,7 +346,7 @@ def run_melt3d(args) -> dict:
                      "note": "22 B per segment-site update x updates / (residual + DIIS update) time; peak of "
                              "measured (MEASURED_PEAKS.json hbm_gbs)"},
         "updates_per_s": updates / (f32["ms_per_residual_and_update"] / 1000.0),
-        "fp32": f32, "fp32_full_storage": out["fp32_full_storage"],
+        "fp32": f32, "fp32_full_storage": out["fp32_full_storage"], "fp32_autotuned": out["fp32_autotuned"],
         "fp64_gpu": dict(f64, value=1000.0 / f64["ms_per_residual_and_update"], unit="iterations/s"),
     }
     return line
@@ -696,7 +700,7 @@ def other_workloads(args) -> dict:
     import copy
     out = {}
     keep = ("metric", "value", "unit", "ms_per_step", "config", "roofline", "updates_per_s", "latency",
-            "fp32", "fp32_full_storage", "fp64_gpu")
+            "fp32", "fp32_full_storage", "fp32_autotuned", "fp64_gpu")
     runs = (("melt128", run_melt3d, dict(n3d=128, iters=5, steps=2, warmup=1, ckpt=10)),
             ("cylinder200", run_cyl2d, dict(n2d=200, iters=5, steps=2, warmup=1, no_solve=True)),
             ("served_mix", run_served, dict(rate=400.0, requests=200, workers=8)))
@@ -746,12 +750,18 @@ def run_brush1d(args) -> None:
     x0 = torch.from_numpy(np.concatenate(xs)).cuda()
     xw = torch.empty_like(x0)
     job = Batch(plans * K, prec, device=local, stream=stream.cuda_stream)
-    # untimed warm-up: W steps of the same stream (their own seeds)
+    # untimed warm-up: W steps of the same stream (their own seeds); the
+    # autotuner picks the work loop's resident CTAs per SM on them
+    tuning = None
     if W > 0:
         xwu = np.concatenate(stream_fields(plans, W, SEED + 1001))
         warm = Batch(plans * W, prec, device=local, stream=stream.cuda_stream)
+        xwd = torch.from_numpy(xwu).cuda()
+        tuning = warm.autotune(xwd.data_ptr())
         warm.solve_host(xwu)
         warm.close()
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        job.slots = min(job.slots, tuning["ctas_per_sm"] * sms)
     # timed: the K steps in one work loop, inputs resident in HBM, L2 flushed
     xw.copy_(x0)
     flush.zero_()
@@ -836,6 +846,7 @@ def run_brush1d(args) -> None:
                                "work loop",
                    "instances_per_step": args.instances, "solves": len(its_all) * ws, "converged": n_all,
                    "precision": args.precision, "slots": job.slots,
+                   "autotuned": tuning,
                    "iterations_mean": float(np.mean(its_all)), "iterations_max": int(np.max(its_all)),
                    "segment_site_updates": updates,
                    "l2": "flushed once before the timed region (256 MB write); the K steps' inputs "

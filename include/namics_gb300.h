@@ -200,7 +200,30 @@ int nm_ctx_destroy(nm_ctx* ctx);
  * instead of one launch per segment step.  Same arithmetic, same results;
  * on GB300 the per-step launches are the faster of the two. */
 #define NM_OPT_SWEEP2D 1
+/* NM_OPT_ROWS3D (default 4): rows along y per block of the 3-D step kernels,
+ * 2, 4 or 8.  NM_OPT_CHECKPOINT: the checkpoint stride of the 3-D path, 0
+ * (every propagator) or k >= 2, within the propagator storage the context
+ * was created with (NM_ERR_ARG when it does not fit).  Same results. */
+#define NM_OPT_ROWS3D 2
+#define NM_OPT_CHECKPOINT 3
 int nm_ctx_set_option(nm_ctx* ctx, int option, int value);
+
+/* The autotuner: times one residual evaluation of this context at the field
+ * x_dev (device, length iv) for each candidate of its tunable kernel
+ * choices, keeps the fastest and caches it for contexts of the same shape
+ * (a later call with the same shape applies the cached choice untimed).
+ * 3-D path: rows per block {2, 4, 8} × checkpoint stride {0, 5, 10} (the
+ * strides that fit the storage); 2-D linear chains: one launch per step or
+ * one persistent launch per sweep (NM_OPT_SWEEP2D); other contexts have no
+ * choice to make.  Results are the same for every candidate. */
+typedef struct nm_ctx_tuning {
+    int    rows;               /* rows per block (3-D), -1 where it does not apply */
+    int    checkpoint_stride;  /* 3-D checkpoint stride, -1 where it does not apply */
+    int    sweep2d;            /* 2-D persistent sweeps, -1 where it does not apply */
+    int    candidates;         /* configurations timed (0: taken from the cache) */
+    double ms_per_residual;    /* the chosen configuration's time (0 if cached) */
+} nm_ctx_tuning;
+int nm_ctx_autotune(nm_ctx* ctx, const double* x_dev, nm_ctx_tuning* out);
 
 /* The value of step k (0 .. plan->scan_n) of the plan's scan
  * (Molecule::UpdateVarInfo, molecule.cpp:884-930): start + k·step, or on the
@@ -376,6 +399,18 @@ int nm_batch_timings(nm_batch* b, double* queued, double* solving);
  * as fit on the device, at most one per problem) with identical results */
 int nm_batch_slots(nm_batch* b);
 int nm_batch_set_slots(nm_batch* b, int slots);
+/* The work loop's autotuner: solves the batch from x_dev (not changed) once
+ * per candidate number of resident CTAs per SM (1 up to what fits), keeps
+ * the fastest for later solves and remembers it for batches of the same
+ * shape (a later call applies the remembered choice without solving).
+ * Results are the same for every candidate. */
+typedef struct nm_batch_tuning {
+    int    ctas_per_sm;        /* the choice                                   */
+    int    slots;              /* resident CTAs it gives                        */
+    int    candidates;         /* solves timed (0: taken from the cache)        */
+    double ms_per_solve;       /* the chosen configuration's time (0 if cached) */
+} nm_batch_tuning;
+int nm_batch_autotune(nm_batch* b, const double* x_dev, nm_batch_tuning* out);
 /* per-problem free energy / grand potential of the final state */
 int nm_batch_free_energy(nm_batch* b, double* F, double* Omega);
 long long nm_batch_launch_count(nm_batch* b);

@@ -264,6 +264,13 @@ class Context:
         _check(_abi.load().nm_compose_dev(self._h, mol, C.c_void_p(x_ptr), C.c_void_p(rho_ptr), C.byref(out)))
         return out.value
 
+    def autotune(self, x_ptr: int) -> dict:
+        """nm_ctx_autotune at the device field x: the kernel choices kept."""
+        t = _abi.nm_ctx_tuning()
+        _check(_abi.load().nm_ctx_autotune(self._h, C.c_void_p(x_ptr), C.byref(t)))
+        return {"rows": t.rows, "checkpoint_stride": t.checkpoint_stride, "sweep2d": t.sweep2d,
+                "candidates": t.candidates, "ms_per_residual": t.ms_per_residual}
+
     def launch_count(self) -> int:
         return int(_abi.load().nm_ctx_launch_count(self._h))
 
@@ -367,6 +374,13 @@ class Batch:
         s = np.zeros(len(self.plans))
         _check(_abi.load().nm_batch_timings(self._h, _dptr(q), _dptr(s)))
         return q, s
+
+    def autotune(self, x_ptr: int) -> dict:
+        """nm_batch_autotune from the device fields x (not changed)."""
+        t = _abi.nm_batch_tuning()
+        _check(_abi.load().nm_batch_autotune(self._h, C.c_void_p(x_ptr), C.byref(t)))
+        return {"ctas_per_sm": t.ctas_per_sm, "slots": t.slots, "candidates": t.candidates,
+                "ms_per_solve": t.ms_per_solve}
 
     @property
     def slots(self) -> int:

@@ -81,6 +81,15 @@ class nm_search_result(C.Structure):
 P_plan = C.POINTER(nm_plan)
 
 
+class nm_ctx_tuning(C.Structure):
+    _fields_ = [("rows", C.c_int), ("checkpoint_stride", C.c_int), ("sweep2d", C.c_int), ("candidates", C.c_int),
+                ("ms_per_residual", C.c_double)]
+
+
+class nm_batch_tuning(C.Structure):
+    _fields_ = [("ctas_per_sm", C.c_int), ("slots", C.c_int), ("candidates", C.c_int), ("ms_per_solve", C.c_double)]
+
+
 class nm_stream_options(C.Structure):
     _fields_ = [("device", C.c_int), ("capacity", C.c_int), ("max_layers", C.c_int), ("max_segments", C.c_int),
                 ("max_pairs", C.c_int), ("max_molecules", C.c_int), ("max_store", C.c_int),
@@ -133,6 +142,8 @@ SIGNATURES = [
     ("nm_batch_times", C.c_int, [C.c_void_p, dp]),
     ("nm_batch_timings", C.c_int, [C.c_void_p, dp, dp]),
     ("nm_batch_slots", C.c_int, [C.c_void_p]),
+    ("nm_batch_autotune", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(nm_batch_tuning)]),
+    ("nm_ctx_autotune", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(nm_ctx_tuning)]),
     ("nm_batch_set_slots", C.c_int, [C.c_void_p, C.c_int]),
     ("nm_batch_free_energy", C.c_int, [C.c_void_p, dp, dp]),
     ("nm_batch_launch_count", C.c_longlong, [C.c_void_p]),

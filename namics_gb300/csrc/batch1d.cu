@@ -1297,6 +1297,75 @@ int nm_batch_set_slots(nm_batch* b, int slots) {
     return NM_OK;
 }
 
+// The work loop's autotuner: one solve of the batch (from x_dev, which is not
+// changed) per candidate number of resident CTAs per SM, 1 up to what fits;
+// the fastest is kept and remembered for batches of the same shape.
+int nm_batch_autotune(nm_batch* b, const double* x_dev, nm_batch_tuning* out) {
+    using namespace nm;
+    Batch* B = reinterpret_cast<Batch*>(b);
+    if (!B || !x_dev || !out) { set_error("nm_batch_autotune: bad argument"); return NM_ERR_ARG; }
+    static std::mutex mu;
+    static std::map<std::string, int> tuned;  // shape -> CTAs per SM
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int n = (int)B->hp.size();
+    int mx = 0;
+    long long steps = 0;
+    for (const nm_plan* P : B->plans) {
+        mx = std::max(mx, P->MX);
+        for (int m = 0; m < P->n_mol; m++) steps += P->mols[m].n_store;
+    }
+    const std::string key = std::to_string(n) + ":" + std::to_string(mx) + ":" + std::to_string(steps) + ":" +
+                            std::to_string(B->precision) + ":" + std::to_string(B->slots_cap);
+    out->candidates = 0;
+    out->ms_per_solve = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = tuned.find(key);
+        if (it != tuned.end()) {
+            B->slots = std::min(B->slots_cap, it->second * sms);
+            out->slots = B->slots;
+            out->ctas_per_sm = it->second;
+            return NM_OK;
+        }
+    }
+    const int per_sm_max = std::max(1, (B->slots_cap + sms - 1) / sms);
+    double best = 1e300;
+    int pick = 1;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int rc = NM_OK;
+    for (int k = 1; k <= per_sm_max && !rc; k++) {
+        B->slots = std::min(B->slots_cap, k * sms);
+        cudaError_t e = cudaMemcpyAsync(B->d_x, x_dev, sizeof(double) * B->offsets.back(), cudaMemcpyDeviceToDevice,
+                                        B->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(e0, B->stream);
+        if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); rc = NM_ERR_CUDA; break; }
+        rc = batch_run(*B);
+        if (rc) break;
+        cudaEventRecord(e1, B->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        out->candidates++;
+        if (ms < best) { best = ms; pick = k; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    B->slots = std::min(B->slots_cap, pick * sms);
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        tuned[key] = pick;
+    }
+    out->slots = B->slots;
+    out->ctas_per_sm = pick;
+    out->ms_per_solve = best;
+    return NM_OK;
+}
+
 int nm_batch_free_energy(nm_batch* b, double* F, double* Omega) {
     Batch* B = reinterpret_cast<Batch*>(b);
     if (!B) { nm::set_error("nm_batch_free_energy: bad argument"); return NM_ERR_ARG; }

@@ -687,6 +687,39 @@ int Ctx::residual(const double* x, double* g) {
     return NM_OK;
 }
 
+// Storage of every k-th forward propagator (k >= 2; 0: every one) on the 3-D
+// path: the slot table of each molecule (block starts, every k-th segment
+// and each block's last) within the vectors allocated for it.
+int Ctx::set_ck_stride(int k) {
+    if (k != 0 && (k < 2 || !use3d)) { set_error("checkpoint stride: 0, or >= 2 on the 3-D path"); return NM_ERR_ARG; }
+    std::vector<std::vector<int>> slots(plan->n_mol);
+    std::vector<int> n_slots(plan->n_mol, 0);
+    for (int m = 0; m < plan->n_mol && !k; m++)
+        if (gf_vectors.size() == (size_t)plan->n_mol && gf_vectors[m] < (size_t)plan->mols[m].n_store) {
+            set_error("every propagator stored needs the storage the context was not created with");
+            return NM_ERR_ARG;
+        }
+    for (int m = 0; m < plan->n_mol && k; m++) {
+        const nm_molecule& mol = plan->mols[m];
+        slots[m].assign(mol.n_store, -1);
+        for (int b = 0; b < mol.n_blocks; b++) {
+            const nm_block& B = mol.blocks[b];
+            for (int j = 0; j < B.length; j++)
+                if (j % k == 0 || j == B.length - 1) slots[m][B.s0 + j] = n_slots[m]++;
+        }
+        if ((size_t)n_slots[m] + (k - 1) + 2 > gf_vectors[m]) {
+            set_error("checkpoint stride does not fit the propagator storage of this context");
+            return NM_ERR_ARG;
+        }
+    }
+    for (int m = 0; m < plan->n_mol; m++) {
+        mols[m].slot = slots[m];
+        mols[m].n_slots = n_slots[m];
+    }
+    ck_stride = k;
+    return NM_OK;
+}
+
 int Ctx::check_status() {
     int st = 0;
     CK(cudaMemcpyAsync(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost, stream));
@@ -975,19 +1008,15 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
                 }
         if (ck_stride < 2) ck_stride = 0;
     }
-    for (int m = 0; m < p->n_mol; m++) {
-        const nm_molecule& mol = p->mols[m];
-        n_vec[m] = mol.n_store;
-        if (!ck_stride) continue;
-        MolDev& D = mols[m];
-        D.slot.assign(mol.n_store, -1);
-        for (int b = 0; b < mol.n_blocks; b++) {
-            const nm_block& B = mol.blocks[b];
-            for (int j = 0; j < B.length; j++)
-                if (j % ck_stride == 0 || j == B.length - 1) D.slot[B.s0 + j] = D.n_slots++;
-        }
-        n_vec[m] = (size_t)D.n_slots + (ck_stride - 1) + 2;
+    if (ck_stride) {
+        gf_vectors.assign(p->n_mol, ~(size_t)0);
+        int k = ck_stride;
+        ck_stride = 0;
+        TRY(set_ck_stride(k));  // the slot tables of the stride
     }
+    for (int m = 0; m < p->n_mol; m++)
+        n_vec[m] = ck_stride ? (size_t)mols[m].n_slots + (ck_stride - 1) + 2 : (size_t)p->mols[m].n_store;
+    gf_vectors = n_vec;
     if (fp32 && use3d) {
         TRY(dalloc(&d_G1f, (size_t)ns * M, stream));
         TRY(dalloc(&d_gb32, 2 * (size_t)M, stream));
@@ -1178,8 +1207,17 @@ int nm_ctx_set_values(nm_ctx* ctx, const char* const* items, const double* value
 int nm_ctx_set_option(nm_ctx* ctx, int option, int value) {
     Ctx* c = reinterpret_cast<Ctx*>(ctx);
     if (!c) { nm::set_error("nm_ctx_set_option: null context"); return NM_ERR_ARG; }
-    if (option != NM_OPT_SWEEP2D) { nm::set_error("nm_ctx_set_option: unknown option"); return NM_ERR_ARG; }
-    c->sweep2d = value != 0;
+    if (option == NM_OPT_SWEEP2D) {
+        c->sweep2d = value != 0;
+    } else if (option == NM_OPT_ROWS3D) {
+        if (value != 2 && value != 4 && value != 8) { nm::set_error("nm_ctx_set_option: rows per block 2, 4 or 8"); return NM_ERR_ARG; }
+        c->c3_rows = value;
+    } else if (option == NM_OPT_CHECKPOINT) {
+        if (int rc = c->set_ck_stride(value)) return rc;
+    } else {
+        nm::set_error("nm_ctx_set_option: unknown option");
+        return NM_ERR_ARG;
+    }
     if (c->graph) {  // the captured residual used the other kernels
         cudaGraphExecDestroy(c->graph);
         c->graph = nullptr;

@@ -5,7 +5,7 @@
 // (LGrad3::propagate, LGrad3.cpp:673-744, simple-cubic stencil), with the
 // halo coordinates mapped to the layers set_bounds copies (mirror, periodic)
 // or to the wall slot that holds 0 ('surface').  The grid is (z-chunk,
-// y-chunk, x): a block runs 128 consecutive z of C3_RY consecutive y rows,
+// y-chunk, x): a block runs 128 consecutive z of RY consecutive y rows,
 // so no site index is ever divided, every warp load is 32 consecutive z,
 // and the y±1 rows of a block's later rows come from L1.
 //
@@ -35,7 +35,8 @@
 namespace nm {
 
 #define C3_SLOTS 32  // maximum slots per stored vector
-#define C3_RY 4      // rows along y per block (measured: 4 > 8 > 16 on a 128³ melt)
+// rows along y per block: 2, 4 or 8, the context's c3_rows (4 unless the
+// autotuner picks another; measured 4 > 8 > 16 on a 128³ melt)
 
 // exact 2^e for e <= 127 (0 below 2^-149), selects only
 __device__ __forceinline__ float c3_p2f(int e) {
@@ -53,7 +54,7 @@ __device__ __forceinline__ int c3_map(int c, int n, int b1, int bm) {
 
 // Step modes: 0 forward step, 1 forward start (copy G1), 2 backward start
 // (copy G1 + composition), 3 backward step (+ composition).
-template <typename T, int MODE>
+template <typename T, int MODE, int RY>
 __global__ void __launch_bounds__(128) k3_prop(L3 L, const T* __restrict__ in, const T* __restrict__ G1,
                                                T* __restrict__ out, unsigned* __restrict__ maxbits,
                                                int* __restrict__ E, int sin, int sout,
@@ -74,8 +75,8 @@ __global__ void __launch_bounds__(128) k3_prop(L3 L, const T* __restrict__ in, c
     const int Eout = FP32 ? ((MODE == 1 || MODE == 2) ? 0 : E[sin] + e) : 0;
     float vmax = 0.f;
 #pragma unroll
-    for (int yy = 0; yy < C3_RY; yy++) {
-        const int y = blockIdx.y * C3_RY + yy + 1;
+    for (int yy = 0; yy < RY; yy++) {
+        const int y = blockIdx.y * RY + yy + 1;
         T v = 0;
         if (z <= L.MZ && y <= L.MY) {
             const int s = x * L.JX + y * L.JY + z;
@@ -201,9 +202,17 @@ template <typename T, int MODE>
 static void k3(Ctx& C, const T* in, const T* G1, T* out, int sin, int sout, const T* Gf, int sgf, int sroot, T* rhi,
                T* rlo, double d) {
     const nm_plan* p = C.plan;
-    dim3 grid((p->MZ + 127) / 128, (p->MY + C3_RY - 1) / C3_RY, p->MX);
-    launch_pdl(k3_prop<T, MODE>, grid, 128, C.stream, C.l3, in, G1, out, C.d_maxbits, C.d_E, sin, sout, Gf, sgf, sroot,
-               rhi, rlo, (T)d);
+    const int ry = C.c3_rows;
+    dim3 grid((p->MZ + 127) / 128, (p->MY + ry - 1) / ry, p->MX);
+    if (ry == 2)
+        launch_pdl(k3_prop<T, MODE, 2>, grid, 128, C.stream, C.l3, in, G1, out, C.d_maxbits, C.d_E, sin, sout, Gf, sgf,
+                   sroot, rhi, rlo, (T)d);
+    else if (ry == 8)
+        launch_pdl(k3_prop<T, MODE, 8>, grid, 128, C.stream, C.l3, in, G1, out, C.d_maxbits, C.d_E, sin, sout, Gf, sgf,
+                   sroot, rhi, rlo, (T)d);
+    else
+        launch_pdl(k3_prop<T, MODE, 4>, grid, 128, C.stream, C.l3, in, G1, out, C.d_maxbits, C.d_E, sin, sout, Gf, sgf,
+                   sroot, rhi, rlo, (T)d);
     C.launches++;
 }
 

@@ -185,6 +185,9 @@ struct Ctx {
     // 3-D simple-cubic path (ctx3d.cu) and its FP32 propagators
     bool use3d = false;       // dedicated 3-D kernels for every molecule
     int ck_stride = 0;        // > 1: every k-th forward propagator stored (3-D path)
+    int c3_rows = 4;          // rows along y per block of the 3-D step kernels (2, 4, 8)
+    std::vector<size_t> gf_vectors;  // per molecule: propagator vectors allocated (3-D path)
+    int set_ck_stride(int k); // a stride that fits the allocation (NM_ERR_ARG otherwise)
     bool fp32 = false;        // context created with NM_FP32 propagators
     bool phase32 = false;     // the current residual uses FP32 propagators
     double sw_floor = 0;      // FP32 accuracy floor of ‖g‖ (switch to FP64 near it)

@@ -485,3 +485,41 @@ def test_checkpointed_storage_is_bit_identical(prec):
                 r, _ = c.solve_host(xc)
                 assert (r.iterations, r.residual) == (r0.iterations, r0.residual)
                 assert np.array_equal(xc, x1)
+
+
+def test_autotuners_keep_results_and_cache_their_choice():
+    """nm_ctx_autotune on a 3-D melt and nm_batch_autotune on a batch of the
+    1-D workload: a choice among the candidates, the same residual and solve
+    as the untuned defaults bit for bit, and the cached choice on a second
+    call of the same shape (no candidates timed)."""
+    import bench
+    plan = Plan(bench.melt3d_text(24, 10))
+    u = np.random.default_rng(9).uniform(-0.1, 0.1, plan.M)
+    x = np.concatenate([u, -u])
+    for prec in (NM_FP64, NM_FP32):
+        ref = Context(plan, prec)
+        xd = dev(x)
+        g0 = torch.zeros_like(xd)
+        ref.residual_dev(xd.data_ptr(), g0.data_ptr())
+        c = Context(plan, prec)
+        t = c.autotune(xd.data_ptr())
+        assert t["rows"] in (2, 4, 8) and t["checkpoint_stride"] in (0, 5, 10) and t["candidates"] == 9, t
+        g = torch.zeros_like(xd)
+        c.residual_dev(xd.data_ptr(), g.data_ptr())
+        assert np.array_equal(host(g), host(g0))
+        t2 = Context(plan, prec).autotune(xd.data_ptr())
+        assert t2["candidates"] == 0 and (t2["rows"], t2["checkpoint_stride"]) == (t["rows"], t["checkpoint_stride"])
+    texts = bench.workload(48)
+    plans = [Plan(t) for t in texts]
+    xb = np.concatenate(bench.fields(plans))
+    b = Batch(plans, NM_FP32)
+    x0 = xb.copy()
+    its0, _, _ = b.solve_host(x0)
+    xbd = dev(xb)
+    t = b.autotune(xbd.data_ptr())
+    assert 1 <= t["ctas_per_sm"] <= 3 and t["candidates"] >= 1, t
+    assert np.array_equal(host(xbd), xb)  # the tuner leaves the fields alone
+    x1 = xb.copy()
+    its1, _, _ = b.solve_host(x1)
+    assert np.array_equal(its0, its1) and np.array_equal(x0, x1)
+    assert Batch(plans, NM_FP32).autotune(xbd.data_ptr())["candidates"] == 0
