@@ -330,8 +330,8 @@ int nm_side_dev(nm_ctx* ctx, const double* X_dev, double* X_side_dev);
  *                      2 and 3 gradients: NM_ERR_INPUT, phi unchanged (the
  *                      reference prints "not implemented" there)
  * nm_initiate_dev:     G = Gz                 Lattice::Initiate (LGrad1.cpp:943-949)
- * nm_terminate_dev:    Gz = G on 2 and 3 gradients; on 1 gradient Gz is left
- *                      as it is, as LGrad1::Terminate does for Markov 1
+ * nm_terminate_dev:    Gz = G                 Lattice::Terminate (LGrad1.cpp:951-969,
+ *                      LGrad2.cpp:1934-1960, LGrad3.cpp:1937-1950)
  * nm_weighted_sum_dev, nm_compute_gn_dev: zero X's halo in place
  *                      (remove_bounds), then Σ X (planar, 3-D) or Σ X·L
  *                      (curved): Lattice::WeightedSum, ComputeGN

@@ -12,11 +12,10 @@
 //                                     (Composition; 1 gradient only, as in the
 //                                     reference)
 //   Initiate(G, Gz)                   G = Gz
-//   Terminate(Gz, G)                  Gz = G (2 and 3 gradients; the 1-gradient
-//                                     reference leaves Gz as it is)
+//   Terminate(Gz, G)                  Gz = G
 //   WeightedSum(X), ComputeGN(G)      halos zeroed in place (remove_bounds), then
 //                                     Σ X (planar, 3-D) or Σ X·L (curved)
-// LGrad1.cpp:213-220, 863-960; LGrad2.cpp:147-157, 1814-1960;
+// LGrad1.cpp:213-220, 863-969; LGrad2.cpp:147-157, 1814-1960;
 // LGrad3.cpp:40-46, 1883-1945; tools_host.h:349-356, 400-402.
 #include <cuda_runtime.h>
 
@@ -114,7 +113,6 @@ int nm_initiate_dev(nm_ctx* ctx, double* G_dev, const double* Gz_dev) {
 int nm_terminate_dev(nm_ctx* ctx, double* Gz_dev, const double* G_dev) {
     Ctx* C = reinterpret_cast<Ctx*>(ctx);
     if (!C || !Gz_dev || !G_dev) { nm::set_error("nm_terminate_dev: null argument"); return NM_ERR_ARG; }
-    if (C->plan->gradients == 1) return NM_OK;  // LGrad1::Terminate copies nothing for Markov 1
     nm::k_copy_all<<<nm::grid_m(C->plan->M), 256, 0, C->stream>>>(C->plan->M, Gz_dev, G_dev);
     C->launches++;
     return nm::sync_ctx(C, "nm_terminate_dev");
