@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <sstream>
 #include <string>
@@ -326,60 +327,110 @@ static bool build_blocks_from_tree(std::vector<SegNode>& nodes, int root, PlanHo
     return true;
 }
 
-// Symmetric dendrimer `@dend(A,(B)2,3; A,(B)2,3)`: generations separated by
-// ';', each `bp,(arm),n_arm` (molecule.cpp:1437-1560, mol_dendrimer.cpp).
-static bool build_dendrimer(const std::string& body, const std::map<std::string, int>& segidx,
-                            MolBuild& mb, std::string& err) {
-    std::vector<std::string> gens = split(body, ';');
-    struct Gen { int bp; std::vector<std::pair<int, int>> arm; int n_arm; };
+// Dendrimer `@dend(bp,(arm),f; ...)`: generations separated by ';'; in each,
+// a branch-point segment followed by one or more pairs `(arm runs),f`, f
+// copies of that arm (molecule.cpp:1437-1560; mol_dendrimer.cpp:113-184 for
+// one arm type per generation, mol_asym_dendrimer.cpp:128-240 for several).
+// Every arm, whatever its type, ends at a branch point of the next
+// generation.  The backward propagator that reaches a next-generation branch
+// point depends on the arm it came through, so the block tree holds one copy
+// of the next generation under each arm type (the reference recurses into
+// the next generation once per arm type, mol_asym_dendrimer.cpp:221): the
+// arm type's first run carries mult = f (the join raises its end
+// propagator to the f-th power), and every block of a copy the degeneracy
+// of that copy, so the copies' degeneracies add up to the reference's d_mon.
+// `written`: segment types in written order (generation by generation, the
+// branch point, then the arms' runs), for the molecule's monomer list.
+static bool build_dendrimer(const std::string& body, const std::map<std::string, int>& segidx, MolBuild& mb,
+                            std::vector<int>& written, std::string& err) {
+    struct Arm { std::vector<std::pair<int, int>> runs; int f = 1; };
+    struct Gen { int bp = -1; std::vector<Arm> arms; };
     std::vector<Gen> G;
-    for (auto& g : gens) {
+    for (auto& g : split(body, ';')) {
         std::vector<std::string> a = split(trim(g), ',');
-        if (a.size() != 3) { err = "only symmetric dendrimers '@dend(bp,(arm)n,f;...)' are supported"; return false; }
+        if (a.size() < 3 || (a.size() - 1) % 2 != 0) {
+            err = "dendrimer generation '" + trim(g) + "': a branch point, then pairs (arm),count";
+            return false;
+        }
         Gen gg;
         auto it = segidx.find(trim(a[0]));
         if (it == segidx.end()) { err = "dendrimer branch point '" + a[0] + "' is not a mon"; return false; }
         gg.bp = it->second;
-        CompParser cp(trim(a[1]), segidx);
-        std::vector<CompParser::Item> items;
-        if (!cp.parse_chain(items, false)) { err = cp.err; return false; }
-        for (auto& itm : items) {
-            if (itm.is_side) { err = "side chains inside dendrimer arms are not supported"; return false; }
-            gg.arm.push_back({itm.seg, itm.count});
+        written.push_back(gg.bp);
+        for (size_t k = 1; k + 1 < a.size(); k += 2) {
+            Arm arm;
+            CompParser cp(trim(a[k]), segidx);
+            std::vector<CompParser::Item> items;
+            if (!cp.parse_chain(items, false)) { err = cp.err; return false; }
+            for (auto& itm : items) {
+                if (itm.is_side) { err = "side chains inside dendrimer arms are not supported"; return false; }
+                arm.runs.push_back({itm.seg, itm.count});
+                written.push_back(itm.seg);
+            }
+            if (arm.runs.empty()) { err = "empty dendrimer arm"; return false; }
+            if (!to_int(trim(a[k + 1]), arm.f) || arm.f < 1) {
+                err = "dendrimer arm count must be a positive integer"; return false;
+            }
+            gg.arms.push_back(arm);
         }
-        if (!to_int(trim(a[2]), gg.n_arm) || gg.n_arm < 1) { err = "dendrimer functionality must be a positive integer"; return false; }
         G.push_back(gg);
     }
-    // Tree (root = core bp of generation 0).  Per generation g: bp_g, then
-    // the arm runs written from bp outward; the next generation's bp is
-    // bonded to the arm's last run.  Blocks in post-order: outermost first.
-    // Build top-down list first, then number in post-order (reverse of the
-    // top-down chain since every level has a single child group).
-    struct TB { int seg, len, mult; double d; };
-    std::vector<TB> chain;  // root-first
-    double d = 1.0;
-    for (size_t g = 0; g < G.size(); g++) {
-        chain.push_back({G[g].bp, 1, 1, d});
-        d *= G[g].n_arm;
-        for (size_t r = 0; r < G[g].arm.size(); r++)
-            chain.push_back({G[g].arm[r].first, G[g].arm[r].second, r == 0 ? G[g].n_arm : 1, d});
+    // the tree, root (the core's branch point) first; children in written order
+    struct Node { int seg, len, mult; double d; std::vector<int> ch; };
+    std::vector<Node> nodes;
+    bool too_big = false;
+    std::function<int(size_t, double)> grow = [&](size_t g, double d) -> int {
+        const int id = (int)nodes.size();
+        nodes.push_back({G[g].bp, 1, 1, d, {}});
+        for (const Arm& arm : G[g].arms) {
+            const double da = d * arm.f;
+            int prev = id;
+            for (size_t r = 0; r < arm.runs.size(); r++) {
+                const int rid = (int)nodes.size();
+                nodes.push_back({arm.runs[r].first, arm.runs[r].second, r == 0 ? arm.f : 1, da, {}});
+                nodes[prev].ch.push_back(rid);
+                prev = rid;
+            }
+            if (nodes.size() > 4096) { too_big = true; return id; }
+            if (g + 1 < G.size()) {
+                const int nb = grow(g + 1, da);
+                nodes[prev].ch.push_back(nb);
+            }
+        }
+        return id;
+    };
+    grow(0, 1.0);
+    if (too_big) { err = "dendrimer expands to more than 4096 blocks"; return false; }
+    // post-order: children before their parent, the root last
+    std::vector<int> post, newid(nodes.size());
+    std::vector<std::pair<int, size_t>> stack{{0, 0}};
+    while (!stack.empty()) {
+        auto& top = stack.back();
+        if (top.second < nodes[top.first].ch.size()) {
+            const int c = nodes[top.first].ch[top.second++];
+            stack.push_back({c, 0});
+        } else {
+            post.push_back(top.first);
+            stack.pop_back();
+        }
     }
-    // chain[0] is root; chain[i+1] is the child of chain[i].  Merge nothing
-    // (runs of equal type across a bp are kept separate: the bp is a join).
-    int nb = (int)chain.size();
+    for (size_t i = 0; i < post.size(); i++) newid[post[i]] = (int)i;
+    std::vector<int> parent(nodes.size(), -1);
+    for (size_t n = 0; n < nodes.size(); n++)
+        for (int c : nodes[n].ch) parent[c] = (int)n;
+    const int nb = (int)post.size();
     mb.blocks.resize(nb);
     int s = 0;
     for (int i = 0; i < nb; i++) {
-        // post-order index i corresponds to chain[nb-1-i]
-        const TB& t = chain[nb - 1 - i];
+        const Node& t = nodes[post[i]];
         nm_block& B = mb.blocks[i];
         B.seg = t.seg; B.length = t.len; B.s0 = s; s += t.len;
-        B.parent = (i == nb - 1) ? -1 : i + 1;
+        B.parent = parent[post[i]] < 0 ? -1 : newid[parent[post[i]]];
         B.mult = t.mult;
         B.degeneracy = t.d;
-        B.n_child = (i == 0) ? 0 : 1;
+        B.n_child = (int)t.ch.size();
         B.child0 = (int)mb.child_index.size();
-        if (i > 0) mb.child_index.push_back(i - 1);
+        for (int c : t.ch) mb.child_index.push_back(newid[c]);
         B.molmon = -1;
     }
     mb.n_store = s;
@@ -755,9 +806,12 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
         }
         // parse composition
         std::vector<std::string> order_seen;
+        std::vector<int> dend_written;
         if (comp.rfind("@dend(", 0) == 0) {
             if (comp.back() != ')') { err = "dendrimer composition must end with ')'"; delete H; return nullptr; }
-            if (!build_dendrimer(comp.substr(6, comp.size() - 7), segidx, mb, err)) { delete H; return nullptr; }
+            if (!build_dendrimer(comp.substr(6, comp.size() - 7), segidx, mb, dend_written, err)) {
+                delete H; return nullptr;
+            }
             mb.is_dendrimer = true;
         } else if (comp[0] == '@') {
             err = "composition keyword not supported (only @dend)"; delete H; return nullptr;
@@ -783,7 +837,7 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
             std::vector<int> segs_in_order;
             if (mb.is_dendrimer) {
                 // written order: generation by generation, bp then arm runs
-                for (int i = (int)mb.blocks.size() - 1; i >= 0; i--) segs_in_order.push_back(mb.blocks[i].seg);
+                segs_in_order = dend_written;
             } else {
                 // recover written order from the composition text
                 CompParser cp(comp, segidx);

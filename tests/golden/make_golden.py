@@ -112,6 +112,21 @@ def cases() -> list[dict]:
                          "mol : pol : freedom : restricted", "mol : pol : theta : 4",
                          "mol : water : composition : (W)1", "mol : water : freedom : solvent"]
     C.append(dict(name="dend1d", lines=lines, field=(-0.05, 0.05), seed=6, modes=["it0", "conv"]))
+    # asymmetric dendrimers (several arm types per generation): near the wall,
+    # in a 2-gradient box, and a 5-arm star grafted through its one odd arm
+    asym = [ln.replace("@dend(A,(B)3,3; A,(A)2(B)2,2)", "@dend(A,(B)3,2,(A)2(B)4,1; A,(A)2(B)2,2,(B)3,1)")
+            for ln in lines]
+    C.append(dict(name="asym_dend1d", lines=asym, field=(-0.05, 0.05), seed=12, modes=["it0", "conv"]))
+    lines2 = lat2d(20, 14, ["surface", "mirror", "mirror", "mirror"]) + [
+        "mon : S : freedom : frozen", "mon : S : frozen_range : lowerbound",
+        "mon : A : freedom : free", "mon : B : freedom : free", "mon : W : freedom : free",
+        "mon : A : chi_S : -1", "mon : B : chi_W : 0.4",
+        "mol : pol : composition : @dend(A,(B)4,2,(A)1(B)2,1; A,(B)3,2)",
+        "mol : pol : freedom : free", "mol : pol : phibulk : 0.002",
+        "mol : water : composition : (W)1", "mol : water : freedom : solvent"]
+    C.append(dict(name="asym_dend2d", lines=lines2, field=(-0.05, 0.05), seed=13, modes=["it0", "conv"]))
+    C.append(dict(name="asym_star1d", lines=lat1d(60) + brush_lines("@dend(A,(A)15,4,(A)14(X)1,1)", n=0.02, chi=0.4),
+                  field=(-0.01, 0.01), seed=14, modes=["it0", "conv"]))
     # 2-gradient planar adsorption (the 2-D requests of the request stream, reduced size)
     lines = lat2d(24, 16, ["surface", "mirror", "mirror", "mirror"]) + [
         "mon : S : freedom : frozen", "mon : S : frozen_range : lowerbound",
