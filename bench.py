@@ -703,7 +703,7 @@ def other_workloads(args) -> dict:
             "fp32", "fp32_full_storage", "fp32_autotuned", "fp64_gpu")
     runs = (("melt128", run_melt3d, dict(n3d=128, iters=5, steps=2, warmup=1, ckpt=10)),
             ("cylinder200", run_cyl2d, dict(n2d=200, iters=5, steps=2, warmup=1, no_solve=True)),
-            ("served_mix", run_served, dict(rate=400.0, requests=200, workers=8)))
+            ("served_mix", run_served, dict(rate=400.0, requests=200, workers=24)))
     for name, fn, over in runs:
         a = copy.copy(args)
         for k, v in over.items():

@@ -206,18 +206,24 @@ int nm_ctx_destroy(nm_ctx* ctx);
  * was created with (NM_ERR_ARG when it does not fit).  Same results. */
 #define NM_OPT_ROWS3D 2
 #define NM_OPT_CHECKPOINT 3
+/* NM_OPT_TILE3D (default 0): the 3-D steps as 2.5-D shared-memory tiles, a
+ * block of R rows × 128 z marching along P planes, value R·100 + P (204,
+ * 208, 404, 408); 0 keeps the gather kernel.  Same results. */
+#define NM_OPT_TILE3D 4
 int nm_ctx_set_option(nm_ctx* ctx, int option, int value);
 
 /* The autotuner: times one residual evaluation of this context at the field
  * x_dev (device, length iv) for each candidate of its tunable kernel
  * choices, keeps the fastest and caches it for contexts of the same shape
  * (a later call with the same shape applies the cached choice untimed).
- * 3-D path: rows per block {2, 4, 8} × checkpoint stride {0, 5, 10} (the
- * strides that fit the storage); 2-D linear chains: one launch per step or
+ * 3-D path: the step kernel (the gather kernel with 2, 4 or 8 rows per
+ * block, or a 2.5-D tile 204, 208, 404, 408) × checkpoint stride {0, 5, 10}
+ * (the strides that fit the storage); 2-D linear chains: one launch per step or
  * one persistent launch per sweep (NM_OPT_SWEEP2D); other contexts have no
  * choice to make.  Results are the same for every candidate. */
 typedef struct nm_ctx_tuning {
-    int    rows;               /* rows per block (3-D), -1 where it does not apply */
+    int    rows;               /* rows per block of the gather kernel (3-D), -1 where it does not apply */
+    int    tile;               /* 3-D tile (R·100 + P), 0 for the gather kernel, -1 where it does not apply */
     int    checkpoint_stride;  /* 3-D checkpoint stride, -1 where it does not apply */
     int    sweep2d;            /* 2-D persistent sweeps, -1 where it does not apply */
     int    candidates;         /* configurations timed (0: taken from the cache) */
@@ -401,14 +407,16 @@ int nm_batch_slots(nm_batch* b);
 int nm_batch_set_slots(nm_batch* b, int slots);
 /* The work loop's autotuner: solves the batch from x_dev (not changed) once
  * per candidate number of resident CTAs per SM (1 up to what fits), keeps
- * the fastest for later solves and remembers it for batches of the same
- * shape (a later call applies the remembered choice without solving).
+ * the one with the highest steady throughput (slots × problems / the sum of
+ * the problems' solve times: the rate of a long stream, not one batch's
+ * wall time, which its longest solves set) for later solves and remembers
+ * it for batches of the same shape (a later call applies it untimed).
  * Results are the same for every candidate. */
 typedef struct nm_batch_tuning {
     int    ctas_per_sm;        /* the choice                                   */
     int    slots;              /* resident CTAs it gives                        */
     int    candidates;         /* solves timed (0: taken from the cache)        */
-    double ms_per_solve;       /* the chosen configuration's time (0 if cached) */
+    double ms_per_solve;       /* the chosen configuration's batch time (0 if cached) */
 } nm_batch_tuning;
 int nm_batch_autotune(nm_batch* b, const double* x_dev, nm_batch_tuning* out);
 /* per-problem free energy / grand potential of the final state */

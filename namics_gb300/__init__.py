@@ -268,7 +268,7 @@ class Context:
         """nm_ctx_autotune at the device field x: the kernel choices kept."""
         t = _abi.nm_ctx_tuning()
         _check(_abi.load().nm_ctx_autotune(self._h, C.c_void_p(x_ptr), C.byref(t)))
-        return {"rows": t.rows, "checkpoint_stride": t.checkpoint_stride, "sweep2d": t.sweep2d,
+        return {"rows": t.rows, "tile": t.tile, "checkpoint_stride": t.checkpoint_stride, "sweep2d": t.sweep2d,
                 "candidates": t.candidates, "ms_per_residual": t.ms_per_residual}
 
     def launch_count(self) -> int:

@@ -19,6 +19,9 @@ NM_ERR_NOMEM = -13
 NM_ERR_NOT_CONVERGED = -14
 NM_ERR_TIMEOUT = -15
 NM_OPT_SWEEP2D = 1
+NM_OPT_ROWS3D = 2
+NM_OPT_CHECKPOINT = 3
+NM_OPT_TILE3D = 4
 
 NM_FP64, NM_FP32 = 0, 1
 
@@ -82,8 +85,8 @@ P_plan = C.POINTER(nm_plan)
 
 
 class nm_ctx_tuning(C.Structure):
-    _fields_ = [("rows", C.c_int), ("checkpoint_stride", C.c_int), ("sweep2d", C.c_int), ("candidates", C.c_int),
-                ("ms_per_residual", C.c_double)]
+    _fields_ = [("rows", C.c_int), ("tile", C.c_int), ("checkpoint_stride", C.c_int), ("sweep2d", C.c_int),
+                ("candidates", C.c_int), ("ms_per_residual", C.c_double)]
 
 
 class nm_batch_tuning(C.Structure):

@@ -1298,8 +1298,12 @@ int nm_batch_set_slots(nm_batch* b, int slots) {
 }
 
 // The work loop's autotuner: one solve of the batch (from x_dev, which is not
-// changed) per candidate number of resident CTAs per SM, 1 up to what fits;
-// the fastest is kept and remembered for batches of the same shape.
+// changed) per candidate number of resident CTAs per SM, 1 up to what fits.
+// The objective is the loop's steady throughput, slots × problems / Σ of
+// the problems' solve times (device timer): a batch's wall time is set by its
+// longest solves, which fewer CTAs per SM speed up, while a long stream is
+// served at the rate all slots together finish problems.  The best is kept
+// and remembered for batches of the same shape.
 int nm_batch_autotune(nm_batch* b, const double* x_dev, nm_batch_tuning* out) {
     using namespace nm;
     Batch* B = reinterpret_cast<Batch*>(b);
@@ -1349,8 +1353,11 @@ int nm_batch_autotune(nm_batch* b, const double* x_dev, nm_batch_tuning* out) {
         cudaEventSynchronize(e1);
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
+        double busy = 0;  // slot-seconds spent solving
+        for (const B1Prob& h : B->hp) busy += (double)(h.t_end - h.t_begin) * 1e-9;
+        const double cost = busy > 0 ? busy / B->slots : 1e300;  // seconds per batch at full occupancy
         out->candidates++;
-        if (ms < best) { best = ms; pick = k; }
+        if (cost < best) { best = cost; pick = k; out->ms_per_solve = ms; }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1362,7 +1369,6 @@ int nm_batch_autotune(nm_batch* b, const double* x_dev, nm_batch_tuning* out) {
     }
     out->slots = B->slots;
     out->ctas_per_sm = pick;
-    out->ms_per_solve = best;
     return NM_OK;
 }
 

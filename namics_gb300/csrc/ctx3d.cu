@@ -127,6 +127,102 @@ __global__ void __launch_bounds__(128) k3_prop(L3 L, const T* __restrict__ in, c
     nmdev::pdl_end();
 }
 
+// The same steps (modes 0 and 3) as a 2.5-D tile: a block owns 128
+// consecutive z (plus the two z halo slots) of RY consecutive rows (plus the
+// y halo rows) and marches along x over XC planes, holding the rows of planes
+// x-1, x and x+1 in a ring of three shared-memory planes.  Each element of
+// `in` is loaded once per block instead of up to seven times by the gather
+// kernel, and the six neighbours are summed in the same order, so every
+// output is bit-identical to k3_prop's.  Halo rows, slots and planes are
+// staged from the layers set_bounds copies (c3_map).
+template <typename T, int MODE, int RY, int XC>
+__global__ void __launch_bounds__(128) k3_tile(L3 L, const T* __restrict__ in, const T* __restrict__ G1,
+                                               T* __restrict__ out, unsigned* __restrict__ maxbits,
+                                               int* __restrict__ E, int sin, int sout,
+                                               const T* __restrict__ Gf, int sgf, int sroot,
+                                               T* __restrict__ rhi, T* __restrict__ rlo, T d) {
+    static_assert(MODE == 0 || MODE == 3, "tile steps: forward and backward steps");
+    constexpr bool FP32 = sizeof(T) == 4;
+    constexpr int W = 130;                // z slots of a staged row: 128 sites and 2 halo slots
+    __shared__ T ring[3][RY + 2][W];
+    nmdev::pdl_begin();
+    const int zc = blockIdx.x * 128;      // z of slot 0 is zc (site z = zc + 1 + threadIdx.x)
+    const int y0 = blockIdx.y * RY + 1;
+    const int x0 = blockIdx.z * XC + 1;
+    const int x1 = min(x0 + XC - 1, L.MX);
+    int e = 0;
+    T f = (T)(1.0 / 6.0);
+    if (FP32) {
+        unsigned mb = maxbits[sin * C3_SLOTS + (threadIdx.x & 31)];
+        for (int o = 16; o > 0; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+        e = c3_expo(__uint_as_float(mb));
+        f = (T)c3_p2f(-e) * (T)(1.0 / 6.0);
+    }
+    const int Eout = FP32 ? E[sin] + e : 0;
+    // stage plane x (0 .. MX+1) into ring slot k: rows y0-1 .. y0+RY, slots z = zc .. zc+129
+    auto stage = [&](int k, int x) {
+        const int px = c3_map(x, L.MX, L.b1x, L.bmx);
+        for (int i = threadIdx.x; i < (RY + 2) * W; i += blockDim.x) {
+            const int r = i / W, zz = i - r * W;
+            const int y = y0 - 1 + r, z = zc + zz;
+            T v = 0;
+            if (y <= L.MY + 1 && z <= L.MZ + 1)
+                v = in[px * L.JX + c3_map(y, L.MY, L.b1y, L.bmy) * L.JY + c3_map(z, L.MZ, L.b1z, L.bmz)];
+            ring[k][r][zz] = v;
+        }
+    };
+    stage(0, x0 - 1);
+    stage(1, x0);
+    int km = 0, kc = 1, kp = 2;
+    const int c = threadIdx.x + 1;        // this thread's slot
+    const int z = zc + c;
+    float vmax = 0.f;
+    for (int x = x0; x <= x1; x++) {
+        stage(kp, x + 1);
+        __syncthreads();
+#pragma unroll
+        for (int r = 1; r <= RY; r++) {
+            const int y = y0 + r - 1;
+            if (z <= L.MZ && y <= L.MY) {
+                const int s = x * L.JX + y * L.JY + z;
+                const T s6 = ((ring[km][r][c] + ring[kp][r][c]) + (ring[kc][r - 1][c] + ring[kc][r + 1][c])) +
+                             (ring[kc][r][c - 1] + ring[kc][r][c + 1]);
+                const T v = FP32 ? s6 * f * G1[s] : s6 * (T)(1.0 / 6.0) * G1[s];
+                out[s] = v;
+                if (MODE == 3) {
+                    if (FP32) {
+                        const int Es = E[sgf] + Eout - E[sroot], h = Es >> 1;
+                        const float sa = c3_p2f(min(h, 127)), sb = c3_p2f(min(Es - h, 127));
+                        const float yv = ((float)Gf[s] * sa) * ((float)v * sb * (float)d) - (float)rlo[s];
+                        const float t2 = (float)rhi[s] + yv;
+                        rlo[s] = (T)((t2 - (float)rhi[s]) - yv);
+                        rhi[s] = (T)t2;
+                    } else {
+                        rhi[s] += d == (T)1 ? Gf[s] * v : d * Gf[s] * v;
+                    }
+                }
+                vmax = fmaxf(vmax, (float)v);
+            }
+        }
+        __syncthreads();  // the ring slot of plane x-1 is restaged next
+        const int t = km; km = kc; kc = kp; kp = t;
+    }
+    if (FP32) {
+        float m = vmax;
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        __shared__ float wm[4];
+        if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int i = 1; i < (int)(blockDim.x >> 5); i++) m = fmaxf(m, wm[i]);
+            const int b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+            if (m > 0.f) atomicMax(&maxbits[sout * C3_SLOTS + (b & (C3_SLOTS - 1))], __float_as_uint(m));
+            if (b == 0) E[sout] = Eout;
+        }
+    }
+    nmdev::pdl_end();
+}
+
 // Σ_interior of an FP32 vector (FP64 partial sums), G(N) = Σ·2^E(root), and
 // the true-scale FP64 ρ
 __global__ void k3_wsum32(L3 L, const float* __restrict__ X, double* __restrict__ partial) {
@@ -198,10 +294,30 @@ bool ctx3d_eligible(const nm_plan* p, std::string* why) {
     return true;
 }
 
+template <typename T, int MODE, int RY, int XC>
+static void k3t(Ctx& C, const T* in, const T* G1, T* out, int sin, int sout, const T* Gf, int sgf, int sroot, T* rhi,
+                T* rlo, double d) {
+    const nm_plan* p = C.plan;
+    dim3 grid((p->MZ + 127) / 128, (p->MY + RY - 1) / RY, (p->MX + XC - 1) / XC);
+    launch_pdl(k3_tile<T, MODE, RY, XC>, grid, 128, C.stream, C.l3, in, G1, out, C.d_maxbits, C.d_E, sin, sout, Gf,
+               sgf, sroot, rhi, rlo, (T)d);
+    C.launches++;
+}
+
 template <typename T, int MODE>
 static void k3(Ctx& C, const T* in, const T* G1, T* out, int sin, int sout, const T* Gf, int sgf, int sroot, T* rhi,
                T* rlo, double d) {
     const nm_plan* p = C.plan;
+    if constexpr (MODE == 0 || MODE == 3) {
+        // the 2.5-D tile kernel: c3_tile = rows per block × 100 + planes per block
+        switch (C.c3_tile) {
+            case 204: k3t<T, MODE, 2, 4>(C, in, G1, out, sin, sout, Gf, sgf, sroot, rhi, rlo, d); return;
+            case 208: k3t<T, MODE, 2, 8>(C, in, G1, out, sin, sout, Gf, sgf, sroot, rhi, rlo, d); return;
+            case 404: k3t<T, MODE, 4, 4>(C, in, G1, out, sin, sout, Gf, sgf, sroot, rhi, rlo, d); return;
+            case 408: k3t<T, MODE, 4, 8>(C, in, G1, out, sin, sout, Gf, sgf, sroot, rhi, rlo, d); return;
+            default: break;  // 0: the gather kernel
+        }
+    }
     const int ry = C.c3_rows;
     dim3 grid((p->MZ + 127) / 128, (p->MY + ry - 1) / ry, p->MX);
     if (ry == 2)

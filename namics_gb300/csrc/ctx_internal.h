@@ -185,7 +185,8 @@ struct Ctx {
     // 3-D simple-cubic path (ctx3d.cu) and its FP32 propagators
     bool use3d = false;       // dedicated 3-D kernels for every molecule
     int ck_stride = 0;        // > 1: every k-th forward propagator stored (3-D path)
-    int c3_rows = 4;          // rows along y per block of the 3-D step kernels (2, 4, 8)
+    int c3_rows = 4;          // rows along y per block of the 3-D gather step kernels (2, 4, 8)
+    int c3_tile = 0;          // 3-D 2.5-D tile steps: rows × 100 + planes (204, 208, 404, 408); 0: gather
     std::vector<size_t> gf_vectors;  // per molecule: propagator vectors allocated (3-D path)
     int set_ck_stride(int k); // a stride that fits the allocation (NM_ERR_ARG otherwise)
     bool fp32 = false;        // context created with NM_FP32 propagators

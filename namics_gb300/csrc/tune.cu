@@ -1,8 +1,9 @@
 // The autotuner of the device contexts: for the problem at hand it times one
 // residual evaluation per candidate of the kernel choices that leave the
 // arithmetic unchanged, keeps the fastest and remembers it per shape.
-//   3-D path: rows along y per block of the step kernels (the tile's height,
-//     2, 4 or 8) × the checkpoint stride of the stored propagators (0, 5,
+//   3-D path: the step kernel (the gather kernel with 2, 4 or 8 rows along
+//     y per block, or a 2.5-D shared-memory tile of 2 or 4 rows marching 4
+//     or 8 planes) × the checkpoint stride of the stored propagators (0, 5,
 //     10; recomputing a group of segments from L2 against reading every
 //     forward propagator back from HBM);
 //   2-D linear chains: one launch per segment step or one persistent
@@ -21,7 +22,7 @@ namespace nm {
 
 namespace {
 
-struct Choice { int rows, ck, sweep; };
+struct Choice { int rows, ck, sweep, tile; };
 
 std::mutex g_tune_mu;
 std::map<std::string, Choice> g_tuned;  // shape -> choice
@@ -43,6 +44,7 @@ void drop_graph(Ctx& C) {
 
 int apply(Ctx& C, const Choice& c) {
     if (c.rows > 0) C.c3_rows = c.rows;
+    if (c.tile >= 0) C.c3_tile = c.tile;
     if (c.ck >= 0) {
         if (int rc = C.set_ck_stride(c.ck)) return rc;
     }
@@ -83,13 +85,16 @@ extern "C" int nm_ctx_autotune(nm_ctx* ctx, const double* x_dev, nm_ctx_tuning* 
     if (!C || !x_dev || !out) { set_error("nm_ctx_autotune: null argument"); return NM_ERR_ARG; }
     std::vector<Choice> cands;
     if (C->use3d) {
-        for (int rows : {2, 4, 8})
-            for (int ck : {0, 5, 10}) cands.push_back({rows, ck, -1});
+        for (int ck : {0, 5, 10}) {
+            for (int rows : {2, 4, 8}) cands.push_back({rows, ck, -1, 0});
+            for (int tile : {204, 208, 404, 408}) cands.push_back({-1, ck, -1, tile});
+        }
     } else if (C->use2d) {
-        cands.push_back({-1, -1, 0});
-        cands.push_back({-1, -1, 1});
+        cands.push_back({-1, -1, 0, -1});
+        cands.push_back({-1, -1, 1, -1});
     }
     out->rows = C->use3d ? C->c3_rows : -1;
+    out->tile = C->use3d ? C->c3_tile : -1;
     out->checkpoint_stride = C->use3d ? C->ck_stride : -1;
     out->sweep2d = C->use2d ? (C->sweep2d ? 1 : 0) : -1;
     out->candidates = 0;
@@ -101,13 +106,14 @@ extern "C" int nm_ctx_autotune(nm_ctx* ctx, const double* x_dev, nm_ctx_tuning* 
         auto it = g_tuned.find(key);
         if (it != g_tuned.end() && apply(*C, it->second) == NM_OK) {
             out->rows = C->use3d ? C->c3_rows : -1;
+            out->tile = C->use3d ? C->c3_tile : -1;
             out->checkpoint_stride = C->use3d ? C->ck_stride : -1;
             out->sweep2d = C->use2d ? (C->sweep2d ? 1 : 0) : -1;
             return NM_OK;
         }
     }
     const Choice before{C->use3d ? C->c3_rows : -1, C->use3d ? C->ck_stride : -1,
-                        C->use2d ? (C->sweep2d ? 1 : 0) : -1};
+                        C->use2d ? (C->sweep2d ? 1 : 0) : -1, C->use3d ? C->c3_tile : -1};
     double best = 1e300;
     Choice pick = before;
     for (const Choice& c : cands) {
@@ -123,6 +129,7 @@ extern "C" int nm_ctx_autotune(nm_ctx* ctx, const double* x_dev, nm_ctx_tuning* 
         g_tuned[key] = pick;
     }
     out->rows = C->use3d ? C->c3_rows : -1;
+    out->tile = C->use3d ? C->c3_tile : -1;
     out->checkpoint_stride = C->use3d ? C->ck_stride : -1;
     out->sweep2d = C->use2d ? (C->sweep2d ? 1 : 0) : -1;
     out->ms_per_residual = best;

@@ -503,12 +503,14 @@ def test_autotuners_keep_results_and_cache_their_choice():
         ref.residual_dev(xd.data_ptr(), g0.data_ptr())
         c = Context(plan, prec)
         t = c.autotune(xd.data_ptr())
-        assert t["rows"] in (2, 4, 8) and t["checkpoint_stride"] in (0, 5, 10) and t["candidates"] == 9, t
+        assert t["checkpoint_stride"] in (0, 5, 10) and t["candidates"] == 21, t
+        assert t["tile"] in (204, 208, 404, 408) or (t["tile"] == 0 and t["rows"] in (2, 4, 8)), t
         g = torch.zeros_like(xd)
         c.residual_dev(xd.data_ptr(), g.data_ptr())
         assert np.array_equal(host(g), host(g0))
         t2 = Context(plan, prec).autotune(xd.data_ptr())
-        assert t2["candidates"] == 0 and (t2["rows"], t2["checkpoint_stride"]) == (t["rows"], t["checkpoint_stride"])
+        assert t2["candidates"] == 0
+        assert (t2["rows"], t2["tile"], t2["checkpoint_stride"]) == (t["rows"], t["tile"], t["checkpoint_stride"])
     texts = bench.workload(48)
     plans = [Plan(t) for t in texts]
     xb = np.concatenate(bench.fields(plans))
@@ -523,3 +525,37 @@ def test_autotuners_keep_results_and_cache_their_choice():
     its1, _, _ = b.solve_host(x1)
     assert np.array_equal(its0, its1) and np.array_equal(x0, x1)
     assert Batch(plans, NM_FP32).autotune(xbd.data_ptr())["candidates"] == 0
+
+
+@pytest.mark.parametrize("prec", [NM_FP64, NM_FP32])
+def test_tiled_3d_steps_are_bit_identical(prec):
+    """The 2.5-D shared-memory tile steps (every rows × planes variant)
+    against the gather steps: the same residual bit for bit, on a periodic
+    melt, on a mirror-bounded box whose edges are not multiples of the tile
+    (partial row and plane blocks), and on a box wider than one 128-slot z
+    chunk; and the same 12-iteration solve."""
+    import bench
+    from namics_gb300 import _abi
+    texts = [bench.melt3d_text(24, 12),
+             bench.melt3d_text(21, 12).replace("periodic", "mirror"),
+             bench.melt3d_text(9, 12).replace("n_layers_z : 9", "n_layers_z : 150")]
+    for text in texts:
+        plan = Plan(text)
+        u = np.random.default_rng(3).uniform(-0.1, 0.1, plan.M)
+        x = np.concatenate([u, -u])
+        xd = dev(x)
+        ref = Context(plan, prec)
+        g0 = torch.zeros_like(xd)
+        ref.residual_dev(xd.data_ptr(), g0.data_ptr())
+        g0 = host(g0)
+        x1 = x.copy()
+        r0, _ = ref.solve_host(x1)
+        for tile in (204, 208, 404, 408):
+            c = Context(plan, prec)
+            c.set_option(_abi.NM_OPT_TILE3D, tile)
+            g = torch.zeros_like(xd)
+            c.residual_dev(xd.data_ptr(), g.data_ptr())
+            assert np.array_equal(host(g), g0), (text.splitlines()[1], tile)
+            xt = x.copy()
+            r, _ = c.solve_host(xt)
+            assert (r.iterations, r.residual) == (r0.iterations, r0.residual) and np.array_equal(xt, x1)
