@@ -1215,11 +1215,7 @@ int nm_ctx_set_option(nm_ctx* ctx, int option, int value) {
     } else if (option == NM_OPT_CHECKPOINT) {
         if (int rc = c->set_ck_stride(value)) return rc;
     } else if (option == NM_OPT_TILE3D) {
-        if (value != 0 && value != 204 && value != 208 && value != 404 && value != 408) {
-            nm::set_error("nm_ctx_set_option: 3-D tile 0, 204, 208, 404 or 408");
-            return NM_ERR_ARG;
-        }
-        c->c3_tile = value;
+        if (int rc = nm::ctx3d_set_tile(*c, value)) return rc;
     } else {
         nm::set_error("nm_ctx_set_option: unknown option");
         return NM_ERR_ARG;

@@ -129,12 +129,21 @@ __global__ void __launch_bounds__(128) k3_prop(L3 L, const T* __restrict__ in, c
 
 // The same steps (modes 0 and 3) as a 2.5-D tile: a block owns 128
 // consecutive z (plus the two z halo slots) of RY consecutive rows (plus the
-// y halo rows) and marches along x over XC planes, holding the rows of planes
-// x-1, x and x+1 in a ring of three shared-memory planes.  Each element of
-// `in` is loaded once per block instead of up to seven times by the gather
-// kernel, and the six neighbours are summed in the same order, so every
-// output is bit-identical to k3_prop's.  Halo rows, slots and planes are
-// staged from the layers set_bounds copies (c3_map).
+// y halo rows) over XC consecutive planes (plus the x halo planes).  It first
+// copies that whole slab of `in` into shared memory with asynchronous copies
+// (cp.async, every load of the slab in flight at once), then computes its
+// RY × XC rows from shared memory.  Each element of `in` is loaded once per
+// block instead of up to seven times by the gather kernel, and the six
+// neighbours are summed in the same order, so every output is bit-identical
+// to k3_prop's.  Halo rows, slots and planes are staged from the layers
+// set_bounds copies (c3_map).  Dynamic shared memory: (XC+2)(RY+2)·130
+// elements.
+__device__ __forceinline__ void c3_cp_async(void* dst, const void* src, int bytes) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if (bytes == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+
 template <typename T, int MODE, int RY, int XC>
 __global__ void __launch_bounds__(128) k3_tile(L3 L, const T* __restrict__ in, const T* __restrict__ G1,
                                                T* __restrict__ out, unsigned* __restrict__ maxbits,
@@ -143,13 +152,28 @@ __global__ void __launch_bounds__(128) k3_tile(L3 L, const T* __restrict__ in, c
                                                T* __restrict__ rhi, T* __restrict__ rlo, T d) {
     static_assert(MODE == 0 || MODE == 3, "tile steps: forward and backward steps");
     constexpr bool FP32 = sizeof(T) == 4;
-    constexpr int W = 130;                // z slots of a staged row: 128 sites and 2 halo slots
-    __shared__ T ring[3][RY + 2][W];
+    constexpr int W = 130;                 // z slots of a staged row: 128 sites and 2 halo slots
+    constexpr int PL = (RY + 2) * W;       // elements of one staged plane
+    extern __shared__ __align__(16) unsigned char c3_smem[];
+    T* tile = reinterpret_cast<T*>(c3_smem);  // [XC+2][RY+2][W]
     nmdev::pdl_begin();
-    const int zc = blockIdx.x * 128;      // z of slot 0 is zc (site z = zc + 1 + threadIdx.x)
+    const int zc = blockIdx.x * 128;       // z of slot 0 (site z = zc + 1 + threadIdx.x)
     const int y0 = blockIdx.y * RY + 1;
     const int x0 = blockIdx.z * XC + 1;
     const int x1 = min(x0 + XC - 1, L.MX);
+    const int np = x1 - x0 + 3;            // planes x0-1 .. x1+1
+    for (int i = threadIdx.x; i < np * PL; i += blockDim.x) {
+        const int pl = i / PL, rem = i - pl * PL, r = rem / W, zz = rem - r * W;
+        const int x = x0 - 1 + pl, y = y0 - 1 + r, z = zc + zz;
+        if (y <= L.MY + 1 && z <= L.MZ + 1) {
+            const int g = c3_map(x, L.MX, L.b1x, L.bmx) * L.JX + c3_map(y, L.MY, L.b1y, L.bmy) * L.JY +
+                          c3_map(z, L.MZ, L.b1z, L.bmz);
+            c3_cp_async(tile + i, in + g, (int)sizeof(T));
+        } else {
+            tile[i] = (T)0;
+        }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
     int e = 0;
     T f = (T)(1.0 / 6.0);
     if (FP32) {
@@ -159,34 +183,23 @@ __global__ void __launch_bounds__(128) k3_tile(L3 L, const T* __restrict__ in, c
         f = (T)c3_p2f(-e) * (T)(1.0 / 6.0);
     }
     const int Eout = FP32 ? E[sin] + e : 0;
-    // stage plane x (0 .. MX+1) into ring slot k: rows y0-1 .. y0+RY, slots z = zc .. zc+129
-    auto stage = [&](int k, int x) {
-        const int px = c3_map(x, L.MX, L.b1x, L.bmx);
-        for (int i = threadIdx.x; i < (RY + 2) * W; i += blockDim.x) {
-            const int r = i / W, zz = i - r * W;
-            const int y = y0 - 1 + r, z = zc + zz;
-            T v = 0;
-            if (y <= L.MY + 1 && z <= L.MZ + 1)
-                v = in[px * L.JX + c3_map(y, L.MY, L.b1y, L.bmy) * L.JY + c3_map(z, L.MZ, L.b1z, L.bmz)];
-            ring[k][r][zz] = v;
-        }
-    };
-    stage(0, x0 - 1);
-    stage(1, x0);
-    int km = 0, kc = 1, kp = 2;
-    const int c = threadIdx.x + 1;        // this thread's slot
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();
+    const int c = threadIdx.x + 1;         // this thread's slot
     const int z = zc + c;
     float vmax = 0.f;
-    for (int x = x0; x <= x1; x++) {
-        stage(kp, x + 1);
-        __syncthreads();
+    if (z <= L.MZ) {
+        for (int x = x0; x <= x1; x++) {
+            const T* pm = tile + (x - x0) * PL;  // plane x-1
+            const T* pc = pm + PL;               // plane x
+            const T* pp = pc + PL;               // plane x+1
 #pragma unroll
-        for (int r = 1; r <= RY; r++) {
-            const int y = y0 + r - 1;
-            if (z <= L.MZ && y <= L.MY) {
+            for (int r = 1; r <= RY; r++) {
+                const int y = y0 + r - 1;
+                if (y > L.MY) break;
                 const int s = x * L.JX + y * L.JY + z;
-                const T s6 = ((ring[km][r][c] + ring[kp][r][c]) + (ring[kc][r - 1][c] + ring[kc][r + 1][c])) +
-                             (ring[kc][r][c - 1] + ring[kc][r][c + 1]);
+                const T s6 = ((pm[r * W + c] + pp[r * W + c]) + (pc[(r - 1) * W + c] + pc[(r + 1) * W + c])) +
+                             (pc[r * W + c - 1] + pc[r * W + c + 1]);
                 const T v = FP32 ? s6 * f * G1[s] : s6 * (T)(1.0 / 6.0) * G1[s];
                 out[s] = v;
                 if (MODE == 3) {
@@ -204,8 +217,6 @@ __global__ void __launch_bounds__(128) k3_tile(L3 L, const T* __restrict__ in, c
                 vmax = fmaxf(vmax, (float)v);
             }
         }
-        __syncthreads();  // the ring slot of plane x-1 is restaged next
-        const int t = km; km = kc; kc = kp; kp = t;
     }
     if (FP32) {
         float m = vmax;
@@ -298,9 +309,20 @@ template <typename T, int MODE, int RY, int XC>
 static void k3t(Ctx& C, const T* in, const T* G1, T* out, int sin, int sout, const T* Gf, int sgf, int sroot, T* rhi,
                 T* rlo, double d) {
     const nm_plan* p = C.plan;
+    const size_t smem = sizeof(T) * (size_t)(XC + 2) * (RY + 2) * 130;
     dim3 grid((p->MZ + 127) / 128, (p->MY + RY - 1) / RY, (p->MX + XC - 1) / XC);
-    launch_pdl(k3_tile<T, MODE, RY, XC>, grid, 128, C.stream, C.l3, in, G1, out, C.d_maxbits, C.d_E, sin, sout, Gf,
-               sgf, sroot, rhi, rlo, (T)d);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(128);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = C.stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k3_tile<T, MODE, RY, XC>, C.l3, in, G1, out, C.d_maxbits, C.d_E, sin, sout, Gf, sgf,
+                       sroot, rhi, rlo, (T)d);
     C.launches++;
 }
 
@@ -433,6 +455,37 @@ static int pass3d(Ctx& C, int m) {
             C.launches++;
         }
     }
+    return NM_OK;
+}
+
+// The tile kernels' dynamic shared-memory limit (above 48 KB it needs the
+// opt-in), on the current device, before any launch or stream capture uses
+// the tile.
+template <int RY, int XC>
+static cudaError_t tile_limits() {
+    cudaError_t e = cudaSuccess;
+    auto one = [&](auto k, size_t bytes) {
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    };
+    one(k3_tile<float, 0, RY, XC>, 4 * (size_t)(XC + 2) * (RY + 2) * 130);
+    one(k3_tile<float, 3, RY, XC>, 4 * (size_t)(XC + 2) * (RY + 2) * 130);
+    one(k3_tile<double, 0, RY, XC>, 8 * (size_t)(XC + 2) * (RY + 2) * 130);
+    one(k3_tile<double, 3, RY, XC>, 8 * (size_t)(XC + 2) * (RY + 2) * 130);
+    return e;
+}
+
+int ctx3d_set_tile(Ctx& C, int tile) {
+    cudaError_t e = cudaSuccess;
+    switch (tile) {
+        case 0: break;
+        case 204: e = tile_limits<2, 4>(); break;
+        case 208: e = tile_limits<2, 8>(); break;
+        case 404: e = tile_limits<4, 4>(); break;
+        case 408: e = tile_limits<4, 8>(); break;
+        default: set_error("3-D tile 0, 204, 208, 404 or 408"); return NM_ERR_ARG;
+    }
+    if (e != cudaSuccess) { set_error(std::string("3-D tile: ") + cudaGetErrorString(e)); return NM_ERR_CUDA; }
+    C.c3_tile = tile;
     return NM_OK;
 }
 

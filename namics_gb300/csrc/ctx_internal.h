@@ -153,6 +153,7 @@ void nm_pool_setup(int dev);  // keep freed stream-ordered memory in the device'
 L3 make_l3(const nm_plan* p);
 bool ctx3d_eligible(const nm_plan* p, std::string* why);
 int ctx3d_molecule_pass(Ctx& C, int m, bool fp32);
+int ctx3d_set_tile(Ctx& C, int tile);  // choose the 3-D step kernel (0: gather; R·100+P: a tile)
 // persistent 2-D sweeps (ctx2d.cu)
 bool ctx2d_eligible(const nm_plan* p);
 int ctx2d_init(Ctx& C);

@@ -44,7 +44,9 @@ void drop_graph(Ctx& C) {
 
 int apply(Ctx& C, const Choice& c) {
     if (c.rows > 0) C.c3_rows = c.rows;
-    if (c.tile >= 0) C.c3_tile = c.tile;
+    if (c.tile >= 0) {
+        if (int rc = ctx3d_set_tile(C, c.tile)) return rc;
+    }
     if (c.ck >= 0) {
         if (int rc = C.set_ck_stride(c.ck)) return rc;
     }
