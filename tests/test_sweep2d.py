@@ -20,12 +20,23 @@ from namics_gb300 import NM_FP64, Context, Plan  # noqa: E402
 from namics_gb300._abi import NM_OPT_SWEEP2D  # noqa: E402
 
 
+def _linear_chains(plan) -> bool:
+    """The persistent sweep takes linear chains (no joins)."""
+    for m in range(plan.n_mol):
+        mol = plan.c.mols[m]
+        for b in range(mol.n_blocks):
+            B = mol.blocks[b]
+            if B.n_child > 1 or B.mult != 1:
+                return False
+    return True
+
+
 def _two_d():
     out = []
     for n in golden_names():
         run = next(iter(load_golden(n)["runs"].values()))
         plan = Plan(run["input"])  # keep alive while reading it
-        if plan.c.gradients == 2:
+        if plan.c.gradients == 2 and _linear_chains(plan):
             out.append(n)
     return out
 
