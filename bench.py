@@ -782,6 +782,7 @@ def run_brush1d(args) -> None:
     total_ms = e0.elapsed_time(e1)
     launches = job.launch_count() - launches0
     queued, solving = job.timings()
+    fp32_its = job.fp32_iterations() if prec == NM_FP32 else None
     ok = st == 0
     n_ok = int(ok.sum())
     latency = {"p50_ms": float(np.percentile(solving[ok] * 1e3, 50)) if ok.any() else None,
@@ -848,6 +849,7 @@ def run_brush1d(args) -> None:
                    "precision": args.precision, "slots": job.slots,
                    "autotuned": tuning,
                    "iterations_mean": float(np.mean(its_all)), "iterations_max": int(np.max(its_all)),
+                   "fp32_residuals_mean": float(np.mean(fp32_its)) if fp32_its is not None else None,
                    "segment_site_updates": updates,
                    "l2": "flushed once before the timed region (256 MB write); the K steps' inputs "
                          f"({nbytes / 1e6:.0f} MB of fields) are written to HBM before it",
