@@ -100,6 +100,12 @@ typedef struct nm_molecule {
     const int* child_index;  /* children lists                               */
     int    n_store;          /* forward propagators stored per site          */
     double charge;           /* Σ valence·fraction (Mol::Charge)             */
+    int    markov;           /* 1; or 2: semiflexible chain, every propagator
+                                resolved into FJC = 3 bond directions
+                                (molecule.cpp:627-674, 1-gradient simple-cubic
+                                lattices)                                    */
+    double bend[3];          /* Markov 2: bond-angle weights P[k] of angles
+                                k·π/2 (molecule.cpp:135-152); P[2] = 0       */
 } nm_molecule;
 
 typedef struct nm_plan {
@@ -210,6 +216,21 @@ int nm_ctx_destroy(nm_ctx* ctx);
  * block of R rows × 128 z marching along P planes, value R·100 + P (204,
  * 208, 404, 408); 0 keeps the gather kernel.  Same results. */
 #define NM_OPT_TILE3D 4
+/* NM_OPT_CLUSTER3D (default 0; the autotuner may pick it): the FP32 sweeps of a small
+ * 3-D box (linear chains, every propagator stored, two propagator buffers
+ * within the shared memory of a thread-block cluster of up to 16 CTAs) run
+ * as one cluster launch per sweep, the propagators held in distributed
+ * shared memory; 0 keeps one launch per step.  Same results, bit for bit;
+ * NM_ERR_ARG asks for it where it does not apply. */
+#define NM_OPT_CLUSTER3D 5
+/* NM_OPT_DEVICE_LOOP (default 0): 1 runs nm_solve_dev (and the solves of a
+ * search) as one CUDA graph with a conditional WHILE node: residual, field
+ * update, DIIS and the stopping test all on the device, one host
+ * synchronisation per solve instead of one per iteration.  The small DIIS
+ * solve is then Gaussian elimination with floored pivots (as in the batched
+ * solver) instead of the pseudo-inverse: the same fixed point, reached along
+ * a slightly different path near convergence. */
+#define NM_OPT_DEVICE_LOOP 6
 int nm_ctx_set_option(nm_ctx* ctx, int option, int value);
 
 /* The autotuner: times one residual evaluation of this context at the field
@@ -218,7 +239,8 @@ int nm_ctx_set_option(nm_ctx* ctx, int option, int value);
  * (a later call with the same shape applies the cached choice untimed).
  * 3-D path: the step kernel (the gather kernel with 2, 4 or 8 rows per
  * block, or a 2.5-D tile 204, 208, 404, 408) × checkpoint stride {0, 5, 10}
- * (the strides that fit the storage); 2-D linear chains: one launch per step or
+ * (the strides that fit the storage), and on small FP32 boxes the cluster
+ * sweeps (NM_OPT_CLUSTER3D); 2-D linear chains: one launch per step or
  * one persistent launch per sweep (NM_OPT_SWEEP2D); other contexts have no
  * choice to make.  Results are the same for every candidate. */
 typedef struct nm_ctx_tuning {
@@ -226,6 +248,7 @@ typedef struct nm_ctx_tuning {
     int    tile;               /* 3-D tile (R·100 + P), 0 for the gather kernel, -1 where it does not apply */
     int    checkpoint_stride;  /* 3-D checkpoint stride, -1 where it does not apply */
     int    sweep2d;            /* 2-D persistent sweeps, -1 where it does not apply */
+    int    cluster3d;          /* 3-D FP32 cluster sweeps (NM_OPT_CLUSTER3D), -1 where they do not apply */
     int    candidates;         /* configurations timed (0: taken from the cache) */
     double ms_per_residual;    /* the chosen configuration's time (0 if cached) */
 } nm_ctx_tuning;

@@ -269,7 +269,7 @@ class Context:
         t = _abi.nm_ctx_tuning()
         _check(_abi.load().nm_ctx_autotune(self._h, C.c_void_p(x_ptr), C.byref(t)))
         return {"rows": t.rows, "tile": t.tile, "checkpoint_stride": t.checkpoint_stride, "sweep2d": t.sweep2d,
-                "candidates": t.candidates, "ms_per_residual": t.ms_per_residual}
+                "cluster3d": t.cluster3d, "candidates": t.candidates, "ms_per_residual": t.ms_per_residual}
 
     def launch_count(self) -> int:
         return int(_abi.load().nm_ctx_launch_count(self._h))

@@ -22,6 +22,8 @@ NM_OPT_SWEEP2D = 1
 NM_OPT_ROWS3D = 2
 NM_OPT_CHECKPOINT = 3
 NM_OPT_TILE3D = 4
+NM_OPT_CLUSTER3D = 5
+NM_OPT_DEVICE_LOOP = 6
 
 NM_FP64, NM_FP32 = 0, 1
 
@@ -40,7 +42,7 @@ class nm_molecule(C.Structure):
                 ("phibulk", C.c_double), ("chainlength", C.c_double), ("n_molmon", C.c_int),
                 ("molmon_seg", ip), ("molmon_fraction", dp), ("n_blocks", C.c_int),
                 ("blocks", C.POINTER(nm_block)), ("child_index", ip), ("n_store", C.c_int),
-                ("charge", C.c_double)]
+                ("charge", C.c_double), ("markov", C.c_int), ("bend", C.c_double * 3)]
 
 
 class nm_plan(C.Structure):
@@ -86,7 +88,7 @@ P_plan = C.POINTER(nm_plan)
 
 class nm_ctx_tuning(C.Structure):
     _fields_ = [("rows", C.c_int), ("tile", C.c_int), ("checkpoint_stride", C.c_int), ("sweep2d", C.c_int),
-                ("candidates", C.c_int), ("ms_per_residual", C.c_double)]
+                ("cluster3d", C.c_int), ("candidates", C.c_int), ("ms_per_residual", C.c_double)]
 
 
 class nm_batch_tuning(C.Structure):

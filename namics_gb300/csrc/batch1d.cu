@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "ctx_internal.h"
+#include "warp_solve.cuh"
 
 namespace nm {
 
@@ -126,60 +127,6 @@ __device__ __forceinline__ float pow2f(int e) {
 __device__ __forceinline__ int expo(float v) {  // frexp exponent of v > 0
     int e = ((__float_as_int(v) >> 23) & 0xff) - 126;
     return v > 0.f ? e : 0;
-}
-
-// Solve A c = 1 (A: kd×kd in shared memory, row-major with stride kd+1 and
-// the right-hand side in column kd) by Gaussian elimination with partial
-// pivoting, FP64, one warp.  Same system as SFNewton::Ax (sfnewton.cpp:793).
-__device__ void warp_solve(double* A, double* c, int kd) {
-    const int lane = threadIdx.x & 31;
-    const int ld = kd + 1;
-    // pivots that rounding made (almost) zero are floored at 1e-30·max|A|
-    // (near convergence A ≈ 1e-9·(all ones) is numerically singular; the
-    // reference's SVD pseudo-inverse still returns finite coefficients)
-    double amax = 0;
-    for (int e = lane; e < kd * ld; e += 32)
-        if (e % ld < kd) amax = fmax(amax, fabs(A[e]));
-    for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-    const double tiny = 1e-30 * amax;
-    for (int k = 0; k < kd; k++) {
-        // pivot: max |A[i][k]| for i >= k
-        double best = -1;
-        int bi = k;
-        for (int i = k + lane; i < kd; i += 32) {
-            double v = fabs(A[i * ld + k]);
-            if (v > best) { best = v; bi = i; }
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            double ob = __shfl_down_sync(0xffffffffu, best, o);
-            int oi = __shfl_down_sync(0xffffffffu, bi, o);
-            if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-        }
-        bi = __shfl_sync(0xffffffffu, bi, 0);
-        if (bi != k)
-            for (int j = k + lane; j <= kd; j += 32) {
-                double t = A[k * ld + j]; A[k * ld + j] = A[bi * ld + j]; A[bi * ld + j] = t;
-            }
-        __syncwarp();
-        double piv = A[k * ld + k];
-        if (!(fabs(piv) > tiny)) piv = piv < 0 ? -tiny : tiny;
-        __syncwarp();
-        if (lane == 0) A[k * ld + k] = piv;
-        __syncwarp();
-        int rows = kd - k - 1, cols = kd - k;  // columns k+1..kd
-        for (int e = lane; e < rows * cols; e += 32) {
-            int i = k + 1 + e / cols, j = k + 1 + e % cols;
-            A[i * ld + j] -= (A[i * ld + k] / piv) * A[k * ld + j];
-        }
-        __syncwarp();
-    }
-    if (lane == 0)
-        for (int i = kd - 1; i >= 0; i--) {
-            double v = A[i * ld + kd];
-            for (int j = i + 1; j < kd; j++) v -= A[i * ld + j] * c[j];
-            c[i] = v / A[i * ld + i];
-        }
-    __syncwarp();
 }
 
 }  // namespace nm
@@ -342,11 +289,12 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<double> C, B1S& 
             const T* w = G1 + B.seg * M;
             T* rr = rho + (D.mm0 + B.molmon) * M;
             const T d = (T)B.degeneracy;
-            T wr[B1_KS], acc[B1_KS], cmp[B1_KS], gfn[B1_KS];
+            const bool d1 = B.degeneracy == 1.0;
+            T wr[B1_KS], acc[B1_KS], gfn[B1_KS];
 #pragma unroll
             for (int q = 0; q < B1_KS; q++) {
                 wr[q] = q < nk ? w[tid + 1 + q * nth] : (T)0;
-                acc[q] = (T)0; cmp[q] = (T)0;
+                acc[q] = (T)0;
             }
             int s = B.s0 + B.length - 1;
             if (B.parent < 0) {
@@ -399,21 +347,18 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<double> C, B1S& 
                         nxt[xk] = v;
                         if (lor[q]) nxt[0] = v;
                         if (hir[q]) nxt[MX + 1] = v;
-                        gf[q] *= v;
+                        // ρ += d·Gf·Gb in plain FP64, the reference's sum
+                        // (GB300 issues ~2 FP64 operations per clock per SM:
+                        // this loop is bound by them)
+                        if (d1) acc[q] = fma(gf[q], v, acc[q]);
+                        else acc[q] = fma(gf[q] * v, d, acc[q]);
                     }
                 __syncthreads();
                 T* t = cur; cur = nxt; nxt = t;
-#pragma unroll
-                for (int q = 0; q < B1_KS; q++) {  // compensated sum (Kahan)
-                    T y = gf[q] * d - cmp[q];
-                    T t2 = acc[q] + y;
-                    cmp[q] = (t2 - acc[q]) - y;
-                    acc[q] = t2;
-                }
             }
 #pragma unroll
             for (int q = 0; q < B1_KS; q++)
-                if (q < nk) rr[tid + 1 + q * nth] += acc[q] - cmp[q];
+                if (q < nk) rr[tid + 1 + q * nth] += acc[q];
             __syncthreads();
             if (B.n_child == 0) continue;
             // backward starts of the children: Q = Gb(join)·Π other P(Gf)
@@ -845,11 +790,14 @@ __device__ __forceinline__ void b1_rebase(B1Prob& P, unsigned char* base) {
     P.xx0 = (double*)(base + P.so_xx0);
 }
 
-__global__ void __launch_bounds__(B1_THREADS, 3) k_batch1d_queue(B1Prob* __restrict__ probs, int n, int mode,
-                                                                const int* __restrict__ order,
-                                                                unsigned char* __restrict__ slots,
-                                                                unsigned long long slot_bytes,
-                                                                unsigned int* __restrict__ head) {
+// MINB resident CTAs per SM: 3 (168 registers a thread) or 4 (128); the
+// autotuner picks the slot count, and with it the variant.
+template <int MINB>
+__global__ void __launch_bounds__(B1_THREADS, MINB) k_batch1d_queue(B1Prob* __restrict__ probs, int n, int mode,
+                                                                   const int* __restrict__ order,
+                                                                   unsigned char* __restrict__ slots,
+                                                                   unsigned long long slot_bytes,
+                                                                   unsigned int* __restrict__ head) {
     __shared__ unsigned int s_idx;
     unsigned char* base = slots + (size_t)blockIdx.x * slot_bytes;
     for (;;) {
@@ -890,6 +838,7 @@ struct Batch {
     std::vector<long long> offsets;
     int precision = NM_FP64;
     int slots_cap = 0;  // slots the scratch holds: as many CTAs as fit, at most one per problem
+    int per_sm3 = 0;    // CTAs per SM of the 168-register variant
     size_t smem = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -942,7 +891,9 @@ static cudaError_t b1_raise_smem(int dev, size_t bytes) {
     if (bytes <= set[dev]) return cudaSuccess;
     cudaError_t e = cudaFuncSetAttribute(k_batch1d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_batch1d_queue, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        e = cudaFuncSetAttribute(k_batch1d_queue<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_batch1d_queue<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_stream1d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e == cudaSuccess) set[dev] = bytes;
@@ -958,6 +909,11 @@ static int batch_check(const nm_plan* P) {
     }
     if (P->MX > B1_KS * B1_THREADS) { set_error("batched solver takes at most 512 layers"); return NM_ERR_INPUT; }
     if (P->charged) { set_error("charged systems are not supported by the batched solver"); return NM_ERR_INPUT; }
+    for (int m = 0; m < P->n_mol; m++)
+        if (P->mols[m].markov == 2) {
+            set_error("Markov 2 chains run on a device context, not in a batch");
+            return NM_ERR_INPUT;
+        }
     if (P->n_seg > NM_MAX_SEG || P->n_mol > NM_MAX_MOL || P->diis_m > B1_MAXM) {
         set_error("problem exceeds the batched solver's limits (segments, molecules, DIIS m <= 12)");
         return NM_ERR_INPUT;
@@ -1134,14 +1090,20 @@ static int batch_init(Batch& B, const nm_plan* const* plans, int n, const nm_ctx
     }
     // the work loop: as many slots as CTAs of k_batch1d_queue fit on the
     // device at once with this shared memory, at most one per problem
-    int per_sm = 0, sms = 0;
-    cudaError_t e2 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch1d_queue, B1_THREADS, maxsmem);
+    int per_sm = 0, per_sm4 = 0, sms = 0;
+    cudaError_t e2 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch1d_queue<3>, B1_THREADS, maxsmem);
+    if (e2 == cudaSuccess)
+        e2 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm4, k_batch1d_queue<4>, B1_THREADS, maxsmem);
     if (e2 == cudaSuccess) e2 = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e2 != cudaSuccess || per_sm < 1) {
         set_error(std::string("batched solver occupancy: ") + cudaGetErrorString(e2));
         return NM_ERR_CUDA;
     }
-    B.slots = B.slots_cap = std::min(n, per_sm * sms);
+    // the default: the 168-register variant, as many CTAs as fit; the
+    // scratch also holds the 128-register variant's larger count, for the tuner
+    B.per_sm3 = per_sm;
+    B.slots = std::min(n, per_sm * sms);
+    B.slots_cap = std::min(n, std::max(per_sm, per_sm4) * sms);
     TRYB(B.alloc(&B.d_slots, B.slot_bytes * (size_t)B.slots_cap));
     TRYB(B.alloc(&B.d_head, 1));
     return NM_OK;
@@ -1153,8 +1115,15 @@ static cudaError_t b1_launch(Batch& B, int mode) {
     int n = (int)B.hp.size();
     cudaError_t e = cudaMemsetAsync(B.d_head, 0, sizeof(unsigned int), B.stream);
     if (e != cudaSuccess) return e;
-    k_batch1d_queue<<<B.slots, B1_THREADS, B.smem, B.stream>>>(B.d_probs, n, mode, B.d_order, B.d_slots,
-                                                              (unsigned long long)B.slot_bytes, B.d_head);
+    int sms = 1, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (B.slots > B.per_sm3 * sms)  // more slots than the 168-register variant keeps resident
+        k_batch1d_queue<4><<<B.slots, B1_THREADS, B.smem, B.stream>>>(B.d_probs, n, mode, B.d_order, B.d_slots,
+                                                                      (unsigned long long)B.slot_bytes, B.d_head);
+    else
+        k_batch1d_queue<3><<<B.slots, B1_THREADS, B.smem, B.stream>>>(B.d_probs, n, mode, B.d_order, B.d_slots,
+                                                                      (unsigned long long)B.slot_bytes, B.d_head);
     B.launches++;
     return cudaGetLastError();
 }
@@ -1448,6 +1417,8 @@ static int noalloc_layout(const nm_plan* P, StaticArena& A, double* x_dev, B1Pro
     }
     if (P->MX > B1_KS * B1_THREADS) { set_error("nm_solve1d_noalloc: at most 512 layers"); return NM_ERR_INPUT; }
     if (P->charged) { set_error("nm_solve1d_noalloc: charged systems are not supported"); return NM_ERR_INPUT; }
+    for (int m = 0; m < P->n_mol; m++)
+        if (P->mols[m].markov == 2) { set_error("nm_solve1d_noalloc: Markov 2 chains are not supported"); return NM_ERR_INPUT; }
     if (P->n_seg > NM_MAX_SEG || P->n_mol > NM_MAX_MOL || P->diis_m > B1_MAXM) {
         set_error("nm_solve1d_noalloc: problem exceeds the limits (segments, molecules, DIIS m <= 12)");
         return NM_ERR_INPUT;

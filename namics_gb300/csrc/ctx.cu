@@ -44,6 +44,7 @@ namespace nm {
     } while (0)
 
 static const int RED_THREADS = 256;
+thread_local bool g_plain_launch = false;
 
 // ---------------------------------------------------------------- kernels --
 
@@ -546,6 +547,7 @@ int Ctx::wsum(const double* X, double* out_dev) {
 }
 
 int Ctx::molecule_pass(int m) {
+    if (plan->mols[m].markov == 2) return ctx_m2_molecule_pass(*this, m);
     const nm_molecule& mol = plan->mols[m];
     MolDev& D = mols[m];
     size_t M = plan->M;
@@ -732,6 +734,7 @@ int Ctx::check_status() {
 }
 
 int Ctx::solve(double* x, nm_solve_result* res, int max_iter) {
+    if (device_loop) return ctx_loop_solve(*this, x, res, max_iter);
     int nvar = plan->iv, m = plan->diis_m;
     double dmax = plan->deltamax, tol = tol_override > 0 ? tol_override : plan->tolerance;
     int nb = red_blocks;
@@ -1025,10 +1028,11 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
             TRY(dalloc(&mols[m].Gf32, n_vec[m] * M, stream));
             TRY(dalloc(&mols[m].rho32, 2 * (size_t)mol.n_molmon * M, stream));
         }
+        TRY(ctx3dc_init(*this));  // small boxes: sweeps in one thread-block cluster
     }
     for (int m = 0; m < p->n_mol; m++) {
         const nm_molecule& mol = p->mols[m];
-        TRY(dalloc(&mols[m].Gf, n_vec[m] * M, stream));
+        TRY(dalloc(&mols[m].Gf, n_vec[m] * M * (mol.markov == 2 ? 3 : 1), stream));  // Markov 2: 3 directions
         TRY(dalloc(&mols[m].rho, (size_t)mol.n_molmon * M, stream));
         TRY(dalloc(&mols[m].Pc, (size_t)mol.n_blocks * M, stream));
         TRY(dalloc(&mols[m].Q, (size_t)mol.n_blocks * M, stream));
@@ -1042,6 +1046,7 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
     TRY(dalloc(&d_Ci, (size_t)mm, stream));
     TRY(dalloc(&d_gram_partial, (size_t)mm * red_blocks, stream));
     if (want2d32) TRY(ctx2d32_init(*this));  // after the molecules' state exists
+    TRY(ctx_m2_init(*this));
     // kernel argument blocks
     std::memset(&norm_args, 0, sizeof(norm_args));
     std::memset(&phi_args, 0, sizeof(phi_args));
@@ -1090,6 +1095,8 @@ Ctx::~Ctx() {
     if (d_gb32) cudaFreeAsync(d_gb32, stream);
     if (d_maxbits) cudaFreeAsync(d_maxbits, stream);
     if (d_E) cudaFreeAsync(d_E, stream);
+    ctx3dc_free(*this);
+    ctx_m2_free(*this);
     for (auto& T : sw_tabs) {
         if (T.seg) cudaFreeAsync(T.seg, stream);
         if (T.mm) cudaFreeAsync(T.mm, stream);
@@ -1100,6 +1107,8 @@ Ctx::~Ctx() {
     if (d_E2b) cudaFreeAsync(d_E2b, stream);
     if (d_rowpart) cudaFreeAsync(d_rowpart, stream);
     if (graph) cudaGraphExecDestroy(graph);
+    ctx_loop_drop(*this);
+    if (d_loop) cudaFreeAsync(d_loop, stream);
     if (own_stream && stream) cudaStreamDestroy(stream);
 }
 
@@ -1201,6 +1210,7 @@ int nm_ctx_set_values(nm_ctx* ctx, const char* const* items, const double* value
     for (int k = 0; k < ns * ns; k++) c->res_args.chi[k] = chi[k];
     c->norm_args = na;
     if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+    nm::ctx_loop_drop(*c);
     return NM_OK;
 }
 
@@ -1216,6 +1226,15 @@ int nm_ctx_set_option(nm_ctx* ctx, int option, int value) {
         if (int rc = c->set_ck_stride(value)) return rc;
     } else if (option == NM_OPT_TILE3D) {
         if (int rc = nm::ctx3d_set_tile(*c, value)) return rc;
+    } else if (option == NM_OPT_CLUSTER3D) {
+        if (value && !c->c3c_ctas) {
+            nm::set_error("nm_ctx_set_option: no cluster sweep for this context (FP32 3-D linear chains on a box "
+                          "whose two propagator buffers fit a cluster's shared memory)");
+            return NM_ERR_ARG;
+        }
+        c->c3c_on = value != 0;
+    } else if (option == NM_OPT_DEVICE_LOOP) {
+        c->device_loop = value != 0;
     } else {
         nm::set_error("nm_ctx_set_option: unknown option");
         return NM_ERR_ARG;
@@ -1224,6 +1243,7 @@ int nm_ctx_set_option(nm_ctx* ctx, int option, int value) {
         cudaGraphExecDestroy(c->graph);
         c->graph = nullptr;
     }
+    nm::ctx_loop_drop(*c);
     return NM_OK;
 }
 

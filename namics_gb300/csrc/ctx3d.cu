@@ -30,6 +30,7 @@
 #include <string>
 #include <vector>
 
+#include "ctx3d_common.cuh"
 #include "ctx_internal.h"
 
 namespace nm {
@@ -37,20 +38,6 @@ namespace nm {
 #define C3_SLOTS 32  // maximum slots per stored vector
 // rows along y per block: 2, 4 or 8, the context's c3_rows (4 unless the
 // autotuner picks another; measured 4 > 8 > 16 on a 128³ melt)
-
-// exact 2^e for e <= 127 (0 below 2^-149), selects only
-__device__ __forceinline__ float c3_p2f(int e) {
-    const int bits = e >= -126 ? (e + 127) << 23 : (e >= -149 ? 1 << max(e + 149, 0) : 0);
-    return __int_as_float(bits);
-}
-__device__ __forceinline__ int c3_expo(float v) {  // frexp exponent of v > 0, 0 for v <= 0
-    const int e = ((__float_as_int(v) >> 23) & 0xff) - 126;
-    return v > 0.f ? e : 0;
-}
-
-__device__ __forceinline__ int c3_map(int c, int n, int b1, int bm) {
-    return c == 0 ? b1 : (c == n + 1 ? bm : c);
-}
 
 // Step modes: 0 forward step, 1 forward start (copy G1), 2 backward start
 // (copy G1 + composition), 3 backward step (+ composition).
@@ -69,8 +56,7 @@ __global__ void __launch_bounds__(128) k3_prop(L3 L, const T* __restrict__ in, c
     if (FP32 && (MODE == 0 || MODE == 3)) {
         unsigned mb = maxbits[sin * C3_SLOTS + (threadIdx.x & 31)];
         for (int o = 16; o > 0; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
-        e = c3_expo(__uint_as_float(mb));
-        f = (T)c3_p2f(-e) * (T)(1.0 / 6.0);
+        f = (T)c3_scale(__uint_as_float(mb), e);
     }
     const int Eout = FP32 ? ((MODE == 1 || MODE == 2) ? 0 : E[sin] + e) : 0;
     float vmax = 0.f;
@@ -94,15 +80,9 @@ __global__ void __launch_bounds__(128) k3_prop(L3 L, const T* __restrict__ in, c
             }
             out[s] = v;
             if (MODE >= 2) {
-                if (FP32) {
-                    // ρ relative to 2^E(root): Gf·Gb·d·2^(Ef + Eout - Eroot), the
-                    // scale applied half to each factor
-                    const int Es = E[sgf] + Eout - E[sroot], h = Es >> 1;
-                    const float sa = c3_p2f(min(h, 127)), sb = c3_p2f(min(Es - h, 127));
-                    const float yv = ((float)Gf[s] * sa) * ((float)v * sb * (float)d) - (float)rlo[s];
-                    const float t2 = (float)rhi[s] + yv;
-                    rlo[s] = (T)((t2 - (float)rhi[s]) - yv);
-                    rhi[s] = (T)t2;
+                if constexpr (FP32) {
+                    // ρ relative to 2^E(root): Gf·Gb·d·2^(Ef + Eout - Eroot)
+                    c3_comp(Gf[s], v, E[sgf] + Eout - E[sroot], d, rhi + s, rlo + s);
                 } else {
                     rhi[s] += d == (T)1 ? Gf[s] * v : d * Gf[s] * v;
                 }
@@ -179,8 +159,7 @@ __global__ void __launch_bounds__(128) k3_tile(L3 L, const T* __restrict__ in, c
     if (FP32) {
         unsigned mb = maxbits[sin * C3_SLOTS + (threadIdx.x & 31)];
         for (int o = 16; o > 0; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
-        e = c3_expo(__uint_as_float(mb));
-        f = (T)c3_p2f(-e) * (T)(1.0 / 6.0);
+        f = (T)c3_scale(__uint_as_float(mb), e);
     }
     const int Eout = FP32 ? E[sin] + e : 0;
     asm volatile("cp.async.wait_group 0;" ::: "memory");
@@ -203,13 +182,8 @@ __global__ void __launch_bounds__(128) k3_tile(L3 L, const T* __restrict__ in, c
                 const T v = FP32 ? s6 * f * G1[s] : s6 * (T)(1.0 / 6.0) * G1[s];
                 out[s] = v;
                 if (MODE == 3) {
-                    if (FP32) {
-                        const int Es = E[sgf] + Eout - E[sroot], h = Es >> 1;
-                        const float sa = c3_p2f(min(h, 127)), sb = c3_p2f(min(Es - h, 127));
-                        const float yv = ((float)Gf[s] * sa) * ((float)v * sb * (float)d) - (float)rlo[s];
-                        const float t2 = (float)rhi[s] + yv;
-                        rlo[s] = (T)((t2 - (float)rhi[s]) - yv);
-                        rhi[s] = (T)t2;
+                    if constexpr (FP32) {
+                        c3_comp(Gf[s], v, E[sgf] + Eout - E[sroot], d, rhi + s, rlo + s);
                     } else {
                         rhi[s] += d == (T)1 ? Gf[s] * v : d * Gf[s] * v;
                     }
@@ -320,7 +294,7 @@ static void k3t(Ctx& C, const T* in, const T* G1, T* out, int sin, int sout, con
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = g_plain_launch ? 0 : 1;
     cudaLaunchKernelEx(&cfg, k3_tile<T, MODE, RY, XC>, C.l3, in, G1, out, C.d_maxbits, C.d_E, sin, sout, Gf, sgf,
                        sroot, rhi, rlo, (T)d);
     C.launches++;
@@ -391,6 +365,26 @@ static int pass3d(Ctx& C, int m) {
     } else {
         cudaMemsetAsync(D.rho, 0, sizeof(double) * M * mol.n_molmon, C.stream);
     }
+    const nm_block& R = mol.blocks[mol.n_blocks - 1];
+    const int sroot = R.s0 + R.length - 1;
+    if constexpr (sizeof(T) == 4) {
+        if (C.c3c_on && k < 2) {  // both sweeps in one thread-block cluster each (ctx3dc.cu)
+            if (int rc = ctx3dc_sweep(C, m, false, sroot)) return rc;
+            const int nb = C.red_blocks;
+            k3_wsum32<<<nb, 256, 0, C.stream>>>(C.l3, (const float*)fwd(sroot), C.d_partial);
+            k3_gn32<<<1, 32, 0, C.stream>>>(C.d_partial, nb, C.d_E, sroot, C.d_sc + 5 * m);
+            C.launches += 2;
+            if (int rc = ctx3dc_sweep(C, m, true, sroot)) return rc;
+            cudaMemsetAsync(D.rho, 0, sizeof(double) * M * mol.n_molmon, C.stream);
+            for (int j = 0; j < mol.n_molmon; j++) {
+                k3_rho64<<<4 * 152, 256, 0, C.stream>>>(C.l3, (const float*)rhi + (size_t)j * M,
+                                                        (const float*)rlo + (size_t)j * M, C.d_E, sroot,
+                                                        D.rho + (size_t)j * M);
+                C.launches++;
+            }
+            return NM_OK;
+        }
+    }
     for (int b = 0; b < mol.n_blocks; b++) {
         const nm_block& B = mol.blocks[b];
         const T* g1 = G1 + (size_t)B.seg * M;
@@ -406,8 +400,6 @@ static int pass3d(Ctx& C, int m) {
             k3<T, 0>(C, fwd(s - 1), g1, fwd(s), s - 1, s, nullptr, 0, 0, nullptr, nullptr, 1.0);
         }
     }
-    const nm_block& R = mol.blocks[mol.n_blocks - 1];
-    const int sroot = R.s0 + R.length - 1;
     if (f32) {
         int nb = C.red_blocks;
         k3_wsum32<<<nb, 256, 0, C.stream>>>(C.l3, (const float*)fwd(sroot), C.d_partial);

@@ -126,6 +126,12 @@ struct MolDev {
 
 nmdev::Lat make_lat(const nm_plan* p);
 
+// Set while the bodies of the device-resident solve loop are captured: the
+// kernel edges inside a conditional node's body are plain stream-order
+// edges, so launches there drop the programmatic-serialisation attribute
+// (pdl_begin is then a no-op).
+extern thread_local bool g_plain_launch;
+
 // launch with programmatic stream serialisation (the kernel calls pdl_begin
 // before it touches memory); also recorded that way in a captured graph
 template <typename... KArgs, typename... Args>
@@ -139,7 +145,7 @@ inline cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, cudaSt
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = g_plain_launch ? 0 : 1;
     return cudaLaunchKernelEx(&cfg, k, args...);
 }
 
@@ -154,6 +160,18 @@ L3 make_l3(const nm_plan* p);
 bool ctx3d_eligible(const nm_plan* p, std::string* why);
 int ctx3d_molecule_pass(Ctx& C, int m, bool fp32);
 int ctx3d_set_tile(Ctx& C, int tile);  // choose the 3-D step kernel (0: gather; R·100+P: a tile)
+// cluster-resident FP32 sweeps for small 3-D boxes (ctx3dc.cu)
+struct C3cTab { int* seg = nullptr; int* mm = nullptr; float* deg = nullptr; };
+int ctx3dc_init(Ctx& C);                            // pick a cluster size, or none
+void ctx3dc_free(Ctx& C);
+int ctx3dc_sweep(Ctx& C, int m, bool bwd, int sroot);  // one sweep of molecule m
+// Markov 2 chains, 1-gradient simple cubic (ctx_markov2.cu)
+int ctx_m2_init(Ctx& C);
+void ctx_m2_free(Ctx& C);
+int ctx_m2_molecule_pass(Ctx& C, int m);
+// the device-resident solve loop (ctxloop.cu)
+int ctx_loop_solve(Ctx& C, double* x, nm_solve_result* res, int max_iter);
+void ctx_loop_drop(Ctx& C);  // the captured loop used kernels or values that changed
 // persistent 2-D sweeps (ctx2d.cu)
 bool ctx2d_eligible(const nm_plan* p);
 int ctx2d_init(Ctx& C);
@@ -189,6 +207,13 @@ struct Ctx {
     int c3_rows = 4;          // rows along y per block of the 3-D gather step kernels (2, 4, 8)
     int c3_tile = 0;          // 3-D 2.5-D tile steps: rows × 100 + planes (204, 208, 404, 408); 0: gather
     std::vector<size_t> gf_vectors;  // per molecule: propagator vectors allocated (3-D path)
+    // FP32 sweeps of small boxes in one thread-block cluster (ctx3dc.cu):
+    // c3c_ctas CTAs of c3c_planes x-planes each, when eligible; c3c_on
+    // selects them (NM_OPT_CLUSTER3D) while every propagator is stored
+    int c3c_ctas = 0, c3c_planes = 0;
+    size_t c3c_smem = 0;
+    bool c3c_on = false;
+    std::vector<C3cTab> c3c_tabs;
     int set_ck_stride(int k); // a stride that fits the allocation (NM_ERR_ARG otherwise)
     bool fp32 = false;        // context created with NM_FP32 propagators
     bool phase32 = false;     // the current residual uses FP32 propagators
@@ -203,6 +228,17 @@ struct Ctx {
     double* graph_g = nullptr;
     bool graph_32 = false;
     long long graph_launches = 0;
+    // Markov 2 chains (ctx_markov2.cu): the backward pair (3 directions
+    // each), three partial sums for G(N), curved-lattice weights l1, l11,
+    // l_1, l_11
+    double *d_m2gb = nullptr, *d_m2w = nullptr, *d_m2l = nullptr;
+    // the device-resident solve loop (NM_OPT_DEVICE_LOOP): one graph per
+    // field pointer, its state in d_loop, launches per pass of each branch
+    bool device_loop = false;
+    void* d_loop = nullptr;
+    cudaGraphExec_t loop_graph = nullptr;
+    const double* loop_x = nullptr;
+    long long loop_l32 = 0, loop_l64 = 0, loop_lrest = 0;
     NormArgs norm_args;
     PhiArgs phi_args;
     ResArgs res_args;

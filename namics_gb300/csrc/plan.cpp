@@ -883,6 +883,51 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
         mb.mol.n_molmon = (int)mb.molmon.size();
         mb.mol.n_blocks = (int)mb.blocks.size();
         mb.mol.n_store = mb.n_store;
+        // Markov 2: semiflexible chains (molecule.cpp:627-674), the bond-angle
+        // weights of Molecule::AllocateMemory (molecule.cpp:135-152): FJC = 3
+        // directions on a simple-cubic lattice, P[k] = exp(-k_stiff/2·(kπ/2)²)
+        // for k = 0, 1 over Q = P[0] + 4·P[1], P[2] = 0
+        mb.mol.markov = 1;
+        if (in.has("mol", mn, "Markov")) {
+            int mk = 0;
+            if (!to_int(in.get("mol", mn, "Markov"), mk) || mk < 1 || mk > 2) {
+                err = "mol " + mn + ": Markov is 1 or 2"; delete H; return nullptr;
+            }
+            mb.mol.markov = mk;
+        }
+        if (mb.mol.markov == 2) {
+            std::string why;
+            if (P.gradients != 1) why = "1-gradient lattices";
+            else if (P.lattice_type != NM_SIMPLE_CUBIC) why = "simple-cubic lattices";
+            else if (mb.is_dendrimer || comp.find('[') != std::string::npos) why = "linear chains";
+            if (!why.empty()) {
+                err = "mol " + mn + ": Markov 2 is built for " + why + " only"; delete H; return nullptr;
+            }
+            // the reference's default is the lattice's k_stiff, which it never sets
+            if (!in.has("mol", mn, "k_stiff")) {
+                err = "mol " + mn + ": Markov 2 needs k_stiff"; delete H; return nullptr;
+            }
+            double ks = 0;
+            if (!to_real(in.get("mol", mn, "k_stiff"), ks) || ks < 0 || ks > 10) {
+                err = "mol " + mn + ": k_stiff in [0, 10]"; delete H; return nullptr;
+            }
+            const int FJC = 3;
+            double Pk[FJC], Q = 0;
+            for (int k = 0; k < FJC - 1; k++) {
+                const double a = k * PIE / (FJC - 1);
+                Pk[k] = std::exp(-0.5 * ks * a * a);
+                if (k > 0) Q += 4 * Pk[k];
+                else Q = Pk[k];
+            }
+            Pk[FJC - 1] = 0;
+            for (int k = 0; k < FJC; k++) mb.mol.bend[k] = Pk[k] / Q;
+        } else if (in.has("mol", mn, "k_stiff")) {
+            // read, range-checked and unused with Markov 1 (molecule.cpp:634-641)
+            double ks = 0;
+            if (!to_real(in.get("mol", mn, "k_stiff"), ks) || ks < 0 || ks > 10) {
+                err = "mol " + mn + ": k_stiff in [0, 10]"; delete H; return nullptr;
+            }
+        }
     }
     // solvent rules (system.cpp CheckInput)
     if (P.solvent < 0) {
@@ -908,6 +953,11 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
     P.n_it = (int)H->it_seg.size();
     P.charged = 0;
     for (int i = 0; i < ns; i++) if (H->seg_valence[i] != 0) P.charged = 1;
+    if (P.charged)
+        for (int m = 0; m < nmol; m++)
+            if (H->mb[m].mol.markov == 2) {
+                err = "Markov 2 chains in a charged system are not built"; delete H; return nullptr;
+            }
     P.iv = P.n_it * M + (P.charged ? M : 0);
     // ---- newton ----
     auto newt = in.order("newton");

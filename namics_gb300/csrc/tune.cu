@@ -6,6 +6,8 @@
 //     or 8 planes) × the checkpoint stride of the stored propagators (0, 5,
 //     10; recomputing a group of segments from L2 against reading every
 //     forward propagator back from HBM);
+//     On small FP32 boxes, also the cluster-resident sweeps (one
+//     thread-block cluster per sweep, every propagator stored);
 //   2-D linear chains: one launch per segment step or one persistent
 //     cooperative launch per sweep.
 // Every candidate gives bit-identical residuals, so the choice is speed only.
@@ -22,7 +24,7 @@ namespace nm {
 
 namespace {
 
-struct Choice { int rows, ck, sweep, tile; };
+struct Choice { int rows, ck, sweep, tile, cluster; };
 
 std::mutex g_tune_mu;
 std::map<std::string, Choice> g_tuned;  // shape -> choice
@@ -40,6 +42,7 @@ void drop_graph(Ctx& C) {
         cudaGraphExecDestroy(C.graph);
         C.graph = nullptr;
     }
+    ctx_loop_drop(C);
 }
 
 int apply(Ctx& C, const Choice& c) {
@@ -51,6 +54,7 @@ int apply(Ctx& C, const Choice& c) {
         if (int rc = C.set_ck_stride(c.ck)) return rc;
     }
     if (c.sweep >= 0) C.sweep2d = c.sweep != 0;
+    if (c.cluster >= 0) C.c3c_on = c.cluster != 0 && C.c3c_ctas > 0;
     drop_graph(C);
     return NM_OK;
 }
@@ -86,19 +90,22 @@ extern "C" int nm_ctx_autotune(nm_ctx* ctx, const double* x_dev, nm_ctx_tuning* 
     Ctx* C = reinterpret_cast<Ctx*>(ctx);
     if (!C || !x_dev || !out) { set_error("nm_ctx_autotune: null argument"); return NM_ERR_ARG; }
     std::vector<Choice> cands;
+    const int cl = C->c3c_ctas > 0 ? 0 : -1;  // per-step candidates leave the cluster sweeps off
     if (C->use3d) {
         for (int ck : {0, 5, 10}) {
-            for (int rows : {2, 4, 8}) cands.push_back({rows, ck, -1, 0});
-            for (int tile : {204, 208, 404, 408}) cands.push_back({-1, ck, -1, tile});
+            for (int rows : {2, 4, 8}) cands.push_back({rows, ck, -1, 0, cl});
+            for (int tile : {204, 208, 404, 408}) cands.push_back({-1, ck, -1, tile, cl});
         }
+        if (C->c3c_ctas > 0) cands.push_back({-1, 0, -1, 0, 1});
     } else if (C->use2d) {
-        cands.push_back({-1, -1, 0, -1});
-        cands.push_back({-1, -1, 1, -1});
+        cands.push_back({-1, -1, 0, -1, -1});
+        cands.push_back({-1, -1, 1, -1, -1});
     }
     out->rows = C->use3d ? C->c3_rows : -1;
     out->tile = C->use3d ? C->c3_tile : -1;
     out->checkpoint_stride = C->use3d ? C->ck_stride : -1;
     out->sweep2d = C->use2d ? (C->sweep2d ? 1 : 0) : -1;
+    out->cluster3d = C->c3c_ctas > 0 ? (C->c3c_on ? 1 : 0) : -1;
     out->candidates = 0;
     out->ms_per_residual = 0;
     if (cands.empty()) return time_residual(*C, x_dev, 3, out->ms_per_residual);  // nothing to choose
@@ -111,11 +118,13 @@ extern "C" int nm_ctx_autotune(nm_ctx* ctx, const double* x_dev, nm_ctx_tuning* 
             out->tile = C->use3d ? C->c3_tile : -1;
             out->checkpoint_stride = C->use3d ? C->ck_stride : -1;
             out->sweep2d = C->use2d ? (C->sweep2d ? 1 : 0) : -1;
+            out->cluster3d = C->c3c_ctas > 0 ? (C->c3c_on ? 1 : 0) : -1;
             return NM_OK;
         }
     }
     const Choice before{C->use3d ? C->c3_rows : -1, C->use3d ? C->ck_stride : -1,
-                        C->use2d ? (C->sweep2d ? 1 : 0) : -1, C->use3d ? C->c3_tile : -1};
+                        C->use2d ? (C->sweep2d ? 1 : 0) : -1, C->use3d ? C->c3_tile : -1,
+                        C->c3c_ctas > 0 ? (C->c3c_on ? 1 : 0) : -1};
     double best = 1e300;
     Choice pick = before;
     for (const Choice& c : cands) {
@@ -134,6 +143,7 @@ extern "C" int nm_ctx_autotune(nm_ctx* ctx, const double* x_dev, nm_ctx_tuning* 
     out->tile = C->use3d ? C->c3_tile : -1;
     out->checkpoint_stride = C->use3d ? C->ck_stride : -1;
     out->sweep2d = C->use2d ? (C->sweep2d ? 1 : 0) : -1;
+    out->cluster3d = C->c3c_ctas > 0 ? (C->c3c_on ? 1 : 0) : -1;
     out->ms_per_residual = best;
     return NM_OK;
 }

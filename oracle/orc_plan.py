@@ -51,7 +51,7 @@ class Molecule(C.Structure):
                 ("phibulk", C.c_double), ("chainlength", C.c_double), ("n_molmon", C.c_int),
                 ("molmon_seg", ip), ("molmon_fraction", dp), ("n_blocks", C.c_int),
                 ("blocks", C.POINTER(Block)), ("child_index", ip), ("n_store", C.c_int),
-                ("charge", C.c_double)]
+                ("charge", C.c_double), ("markov", C.c_int), ("bend", C.c_double * 3)]
 
 
 class PlanRecord(C.Structure):
@@ -319,6 +319,8 @@ class OraclePlan:
         molmons = []
         for m, mn in enumerate(mols):
             R = recs[m]
+            if get("mol", mn, "Markov", "1") != "1":
+                raise ValueError("Markov 2 chains are outside this builder's scope")
             comp = get("mol", mn, "composition")
             if comp.startswith("@"):
                 raise ValueError("keyword compositions are outside the oracle's own builder")
@@ -355,6 +357,7 @@ class OraclePlan:
             R.blocks = bl
             R.child_index = arr(child_index or [0], C.c_int)
             R.n_store = n_store
+            R.markov = 1  # Markov 2 chains are outside this builder's scope (the key is refused)
             if R.freedom == MOL_RESTRICTED:
                 if get("mol", mn, "n") is not None:
                     R.n = float(get("mol", mn, "n"))

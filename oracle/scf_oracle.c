@@ -21,6 +21,8 @@ struct orc_state {
     double *mol_phitot;
     double **Gf, **rho, **jGb, **Pc, **Qb;
     double *gb;
+    double *gb3;                        /* Markov 2: the backward pair, 3 directions each */
+    double *m2l1, *m2l11, *m2l_1, *m2l_11; /* Markov 2, curved lattices: LGrad1.cpp:63-68 */
     double *GN, *norm, *mol_n, *mol_theta, *mol_phibulk, *seg_phibulk;
     double *psi, *EE, *q, *eps, *X;  /* electrostatics (charged systems) */
     int have_state;
@@ -353,6 +355,142 @@ static void mol_backward_block(orc_state* st, int m, int b, double* Q) {
     }
 }
 
+/* ---- Markov 2 (semiflexible) chains, 1-gradient simple-cubic lattices ----
+ * Every propagator of such a molecule holds FJC = 3 direction components
+ * d = 0, 1, 2 of the bond that arrives at a site (down, lateral, up; the
+ * lateral one stands for 4 of the 6 simple-cubic directions).  The bond-angle
+ * weights P[k] (angles k·π/2) are the plan's `bend`.  LG1Planar.cpp:57-135
+ * (planar) and LGrad1.cpp:285-429 (curved) for the steps; LGrad1.cpp:863-960
+ * for G(N), AddPhiS and Initiate; molecule.cpp:2448-2615 and
+ * mol_linear.cpp:115-129 for the sweeps of a linear chain (every propagator
+ * stored, no ring). */
+#define M2_FJC 3
+
+/* set_bounds of a direction pair (LGrad1.cpp:787-804, fjc = 1): the halo of
+ * one direction takes the other's boundary value, a reflected bond */
+static void m2_bounds_pair(orc_state* st, double* X, double* Y) {
+    int MX = st->P->MX;
+    X[0] = Y[st->BX1];
+    X[MX + 1] = Y[st->BXM];
+    Y[0] = X[st->BX1];
+    Y[MX + 1] = X[st->BXM];
+}
+
+/* One step gs <- gs_1: forward (LG1Planar::propagateF, LGrad1::propagateF)
+ * or backward (propagateB), simple cubic, fjc = 1. */
+static void m2_propagate(orc_state* st, double* gs, double* gs_1, const double* G1, const double* P, int fwd) {
+    int M = st->M;
+    Zero(gs, M2_FJC * M);
+    m2_bounds_pair(st, gs_1, gs_1 + 2 * M);
+    set_bounds(st, gs_1 + M);
+    double *gz0 = gs_1, *gz1 = gs_1 + M, *gz2 = gs_1 + 2 * M;
+    double *gx0 = gs, *gx1 = gs + M, *gx2 = gs + 2 * M;
+    if (st->P->geometry == NM_PLANAR) {
+        if (fwd) {
+            YplusisCtimesX(gx0 + 1, gz0, P[0], M - 1);
+            YplusisCtimesX(gx0 + 1, gz1, 4 * P[1], M - 1);
+            YplusisCtimesX(gx1, gz0, P[1], M);
+            YplusisCtimesX(gx1, gz1, 2 * P[1] + P[0], M);
+            YplusisCtimesX(gx1, gz2, P[1], M);
+            YplusisCtimesX(gx2, gz1 + 1, 4 * P[1], M - 1);
+            YplusisCtimesX(gx2, gz2 + 1, P[0], M - 1);
+        } else {
+            YplusisCtimesX(gx0, gz0 + 1, P[0], M - 1);
+            YplusisCtimesX(gx0, gz1, 4 * P[1], M);
+            YplusisCtimesX(gx1, gz0 + 1, P[1], M - 1);
+            YplusisCtimesX(gx1, gz1, 2 * P[1] + P[0], M);
+            YplusisCtimesX(gx1 + 1, gz2, P[1], M - 1);
+            YplusisCtimesX(gx2, gz1, 4 * P[1], M);
+            YplusisCtimesX(gx2 + 1, gz2, P[0], M - 1);
+        }
+    } else {
+        const double *l1 = st->m2l1, *l11 = st->m2l11, *l_1 = st->m2l_1, *l_11 = st->m2l_11;
+        double* H = st->tmp;
+        if (fwd) {
+            Times(H, l_1 + 1, gz0, M - 1);
+            AddTimes(H, l_11 + 1, gz2 + 1, M - 1);
+            YplusisCtimesX(gx0 + 1, H, P[0], M - 1);
+            Times(H, l_1 + 1, gz1, M - 1);
+            AddTimes(H, l_11 + 1, gz1 + 1, M - 1);
+            YplusisCtimesX(gx0 + 1, H, 4 * P[1], M - 1);
+            YplusisCtimesX(gx1, gz0, P[1], M);
+            YplusisCtimesX(gx1, gz1, 2 * P[1] + P[0], M);
+            YplusisCtimesX(gx1, gz2, P[1], M);
+            Times(H + 1, l1, gz1 + 1, M - 1);
+            AddTimes(H + 1, l11, gz1, M - 1);
+            YplusisCtimesX(gx2, H + 1, 4 * P[1], M - 1);
+            Times(H + 1, l1, gz2 + 1, M - 1);
+            AddTimes(H + 1, l11, gz0, M - 1);
+            YplusisCtimesX(gx2, H + 1, P[0], M - 1);
+        } else {
+            Times(H, l_1 + 1, gz2, M - 1);
+            AddTimes(H, l_11 + 1, gz0 + 1, M - 1);
+            YplusisCtimesX(gx1 + 1, H, P[1], M - 1);
+            YplusisCtimesX(gx2 + 1, H, P[0], M - 1);
+            YplusisCtimesX(gx0, gz1, 4 * P[1], M);
+            YplusisCtimesX(gx1, gz1, 2 * P[1] + P[0], M);
+            YplusisCtimesX(gx2, gz1, 4 * P[1], M);
+            Times(H + 1, l1, gz0 + 1, M - 1);
+            AddTimes(H + 1, l11, gz2, M - 1);
+            YplusisCtimesX(gx0, H + 1, P[0], M - 1);
+            YplusisCtimesX(gx1, H + 1, P[1], M - 1);
+        }
+    }
+    for (int k = 0; k < M2_FJC; k++) Times(gs + k * M, gs + k * M, G1, M);
+}
+
+/* Initiate (LGrad1.cpp:943-949): every direction starts from Gz */
+static void m2_initiate(double* G, const double* Gz, int M) {
+    for (int k = 0; k < M2_FJC; k++) Cp(G + k * M, Gz, M);
+}
+
+/* AddPhiS (LGrad1.cpp:876-905, simple cubic): rho += Σ_d C_d·Gf_d·Gb_d */
+static void m2_add_phi(double* rho, const double* Gf, const double* Gb, int M) {
+    const double C1 = 1.0 / 6.0, C2 = 4.0 / 6.0;
+    for (int i = 0; i < M; i++) rho[i] += C1 * Gf[i] * Gb[i];
+    for (int i = 0; i < M; i++) rho[i] += C2 * Gf[M + i] * Gb[M + i];
+    for (int i = 0; i < M; i++) rho[i] += C1 * Gf[2 * M + i] * Gb[2 * M + i];
+}
+
+/* Both sweeps of a Markov 2 linear chain (mol_linear.cpp:115-129 without a
+ * ring, molecule.cpp:2448-2615 without save_memory): the forward sweep
+ * stores every Gf(s); G(N) = Σ_d w_d·WeightedSum(Gf(N-1)_d)/6 with w = 1, 4,
+ * 1 (LGrad1.cpp:863-874); the backward sweep from Initiate(G1) at the last
+ * segment, AddPhiS at every s. */
+static void m2_compose(orc_state* st, int m) {
+    const nm_molecule* mol = &st->P->mols[m];
+    int M = st->M, N = mol->n_store;
+    double* Gf = st->Gf[m];
+    const double* P = mol->bend;
+    int s = 0;
+    for (int b = 0; b < mol->n_blocks; b++) {
+        const nm_block* B = &mol->blocks[b];
+        const double* G1 = st->G1 + (size_t)B->seg * M;
+        for (int k = 0; k < B->length; k++, s++) {
+            if (s > 0) m2_propagate(st, Gf + (size_t)s * M2_FJC * M, Gf + (size_t)(s - 1) * M2_FJC * M, G1, P, 1);
+            else m2_initiate(Gf, G1, M);
+        }
+    }
+    double* last = Gf + (size_t)(N - 1) * M2_FJC * M;
+    double GN = weighted_sum(st, last);
+    GN += 4.0 * weighted_sum(st, last + M);
+    GN += weighted_sum(st, last + 2 * M);
+    st->GN[m] = GN / 6.0;
+    s = N - 1;
+    double* gb = st->gb3;
+    for (int b = mol->n_blocks - 1; b >= 0; b--) {
+        const nm_block* B = &mol->blocks[b];
+        const double* G1 = st->G1 + (size_t)B->seg * M;
+        double* rho = st->rho[m] + (size_t)B->molmon * M;
+        for (int k = 0; k < B->length; k++, s--) {
+            double* cur = gb + (size_t)(s % 2) * M2_FJC * M;
+            if (s < N - 1) m2_propagate(st, cur, gb + (size_t)((s + 1) % 2) * M2_FJC * M, G1, P, 0);
+            else m2_initiate(cur, G1, M);
+            m2_add_phi(rho, Gf + (size_t)s * M2_FJC * M, cur, M);
+        }
+    }
+}
+
 /* ---- electrostatics (charged systems) ------------------------------------
  * Constants of namics.cpp:44-49; the lattice routines of LG1Planar.cpp:162-200,
  * LGrad1.cpp:593-680 and 820-833, LG2Planar.cpp:1130-1175, LGrad2.cpp:
@@ -627,6 +765,8 @@ static void compose_mol(orc_state* st, int m) {
         Cp(phi, G1, M);
         st->GN[m] = weighted_sum(st, phi);
         Times(phi, phi, G1, M);
+    } else if (mol->markov == 2) {
+        m2_compose(st, m);
     } else {
         mol_forward(st, m);
         mol_backward_block(st, m, mol->n_blocks - 1, NULL);
@@ -1098,12 +1238,27 @@ orc_state* orc_create(const nm_plan* P) {
     st->Qb = calloc((size_t)nm, sizeof(double*));
     for (int m = 0; m < nm; m++) {
         const nm_molecule* mol = &P->mols[m];
-        st->Gf[m] = calloc((size_t)mol->n_store * M, sizeof(double));
+        st->Gf[m] = calloc((size_t)mol->n_store * M * (mol->markov == 2 ? M2_FJC : 1), sizeof(double));
         st->rho[m] = calloc((size_t)mol->n_molmon * M, sizeof(double));
         st->jGb[m] = calloc((size_t)mol->n_blocks * M, sizeof(double));
         st->Pc[m] = calloc((size_t)mol->n_blocks * M, sizeof(double));
         st->Qb[m] = calloc((size_t)mol->n_blocks * M, sizeof(double));
     }
+    for (int m = 0; m < nm; m++)
+        if (P->mols[m].markov == 2 && !st->gb3) {
+            st->gb3 = calloc((size_t)2 * M2_FJC * M, sizeof(double));
+            st->m2l1 = calloc((size_t)M, sizeof(double));
+            st->m2l11 = calloc((size_t)M, sizeof(double));
+            st->m2l_1 = calloc((size_t)M, sizeof(double));
+            st->m2l_11 = calloc((size_t)M, sizeof(double));
+            if (P->geometry != NM_PLANAR)  /* interior only; the halo weights stay 0 */
+                for (int i = 1; i < P->MX + 1; i++) {
+                    st->m2l1[i] = P->lambda1[i] / P->lambda;
+                    st->m2l11[i] = 1.0 - st->m2l1[i];
+                    st->m2l_1[i] = P->lambda_1[i] / P->lambda;
+                    st->m2l_11[i] = 1.0 - st->m2l_1[i];
+                }
+        }
     st->GN = calloc((size_t)nm, sizeof(double));
     st->norm = calloc((size_t)nm, sizeof(double));
     st->mol_n = calloc((size_t)nm, sizeof(double));
@@ -1231,5 +1386,6 @@ void orc_destroy(orc_state* st) {
     free(st->GN); free(st->norm); free(st->mol_n); free(st->mol_theta); free(st->mol_phibulk);
     free(st->seg_phibulk);
     free(st->psi); free(st->EE); free(st->q); free(st->eps); free(st->X);
+    free(st->gb3); free(st->m2l1); free(st->m2l11); free(st->m2l_1); free(st->m2l_11);
     free(st);
 }

@@ -206,6 +206,23 @@ def cases() -> list[dict]:
             .replace("pinned_range : firstlayer", "pinned_range : 2,1,1;2,6,6") for ln in charged_lines("(X)1(A)15", 1.8)]
     C.append(dict(name="charged3d", lines=lat + wall, field=(-0.01, 0.01), seed=27,
                   modes=["it0", "it5", "conv"], conv_itlim=5000, split_tol=2e-4))
+    # Markov 2 (semiflexible) chains, 1-gradient simple cubic: a planar brush
+    # (LG1Planar's steps), a spherical brush (LGrad1's curved steps) and a
+    # free two-block chain adsorbing from solution (a segment-type change
+    # inside the chain)
+    m2 = lambda mol, k: [f"mol : {mol} : Markov : 2", f"mol : {mol} : k_stiff : {k}"]
+    C.append(dict(name="markov2_brush1d", lines=lat1d(60) + brush_lines("(X)1(A)39", n=0.05, chi=0.5) +
+                  m2("pol", 1), field=(-0.01, 0.01), seed=31, modes=["it0", "conv"]))
+    C.append(dict(name="markov2_sph", lines=lat1d(40, geom="spherical", offset=5) +
+                  brush_lines("(X)1(A)29", theta=400, chi=0.3) + m2("pol", 2),
+                  field=(-0.02, 0.02), seed=32, modes=["it0", "conv"]))
+    lines = lat1d(50) + [
+        "mon : S : freedom : frozen", "mon : S : frozen_range : lowerbound",
+        "mon : A : freedom : free", "mon : B : freedom : free", "mon : W : freedom : free",
+        "mon : A : chi_S : -1.2", "mon : B : chi_W : 0.6",
+        "mol : pol : composition : (A)10(B)20", "mol : pol : freedom : free", "mol : pol : phibulk : 0.005",
+        "mol : water : composition : (W)1", "mol : water : freedom : solvent"] + m2("pol", 0.5)
+    C.append(dict(name="markov2_ads1d", lines=lines, field=(-0.01, 0.01), seed=33, modes=["it0", "conv"]))
     # a sample of the batched workload: random 1-gradient brushes (seeded), 10% stars
     rng = np.random.default_rng(2024)
     for i in range(6):

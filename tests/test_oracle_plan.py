@@ -1,6 +1,6 @@
 """The oracle's own plan builder (oracle/orc_plan.py) against the product's
 plan compiler: on every 1-gradient neutral golden fixture without a keyword
-composition, and on instances of the batch workload (linear brushes and
+composition or a Markov 2 chain, and on instances of the batch workload (linear brushes and
 3-arm stars), the oracle gives bit-identical residuals and solves from
 either record.  The CPU legs of the bench build their problems with
 orc_plan only, so this is what ties them to the inputs the device solves."""
@@ -19,7 +19,7 @@ def _cases():
     for n in golden_names():
         run = next(iter(load_golden(n)["runs"].values()))
         t = run["input"]
-        if "gradients : 1" in t and "valence" not in t and "@" not in t:
+        if "gradients : 1" in t and "valence" not in t and "@" not in t and "Markov : 2" not in t:
             out.append((n, t, np.array(run["x"])))
     return out
 

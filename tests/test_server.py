@@ -36,7 +36,8 @@ def _cases():
 
 
 def _alone(plan, x, precision):
-    if plan.c.gradients == 1 and not plan.c.charged:  # the server batches these
+    markov2 = any(plan.c.mols[m].markov == 2 for m in range(plan.c.n_mol))
+    if plan.c.gradients == 1 and not plan.c.charged and not markov2:  # the server batches these
         xx = x.copy()
         its, res, st = Batch([plan], precision).solve_host(xx)
         return int(its[0]), float(res[0]), int(st[0]), xx

@@ -29,7 +29,8 @@ def _one_gradient_cases():
         runs = load_golden(n)["runs"]
         if "conv" in runs:
             plan = Plan(runs["conv"]["input"])  # keep alive while reading it
-            if plan.c.gradients == 1 and not plan.c.charged:
+            markov2 = any(plan.c.mols[m].markov == 2 for m in range(plan.c.n_mol))
+            if plan.c.gradients == 1 and not plan.c.charged and not markov2:
                 out.append((plan.M, runs["conv"]))
     return out
 
