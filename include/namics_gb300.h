@@ -227,9 +227,8 @@ int nm_ctx_destroy(nm_ctx* ctx);
  * search) as one CUDA graph with a conditional WHILE node: residual, field
  * update, DIIS and the stopping test all on the device, one host
  * synchronisation per solve instead of one per iteration.  The small DIIS
- * solve is then Gaussian elimination with floored pivots (as in the batched
- * solver) instead of the pseudo-inverse: the same fixed point, reached along
- * a slightly different path near convergence. */
+ * solve is the same pseudo-inverse, run by one warp: the same path up to
+ * rounding.  Measured slower than the host-driven loop on GB300. */
 #define NM_OPT_DEVICE_LOOP 6
 int nm_ctx_set_option(nm_ctx* ctx, int option, int value);
 

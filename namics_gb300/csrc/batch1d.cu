@@ -104,6 +104,14 @@ __device__ __forceinline__ T stb(const T* __restrict__ g, int x, T lam, T lmid, 
     return lam * g[x - 1] + lmid * g[x] + lam * g[x + 1];
 }
 
+// One FP64 step at x with the site's weights already multiplied by G1
+// (aL = λ_-1·G1, aC = λ_0·G1, aR = λ_1·G1): one multiply and two FMAs where
+// the neighbour sum followed by the G1 product takes four operations, and
+// GB300 issues ~2 FP64 operations per clock per SM.
+__device__ __forceinline__ double st3(const double* __restrict__ g, int x, double aL, double aC, double aR) {
+    return fma(aR, g[x + 1], fma(aC, g[x], aL * g[x - 1]));
+}
+
 __device__ __forceinline__ double b1_block_sum(double v, double* red) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -198,9 +206,14 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<double> C, B1S& 
         for (int b = 0; b < D.n_blocks; b++) {
             const nm_block B = D.blocks[b];
             const T* w = G1 + B.seg * M;
-            T wr[B1_KS];
+            T wr[B1_KS], aL[B1_KS], aC[B1_KS], aR[B1_KS];
 #pragma unroll
-            for (int q = 0; q < B1_KS; q++) wr[q] = q < nk ? w[tid + 1 + q * nth] : (T)0;
+            for (int q = 0; q < B1_KS; q++) {
+                wr[q] = q < nk ? w[tid + 1 + q * nth] : (T)0;
+                aL[q] = (CURV ? cmr[q] : lam) * wr[q];
+                aC[q] = (CURV ? c0r[q] : lmid) * wr[q];
+                aR[q] = (CURV ? cpr[q] : lam) * wr[q];
+            }
             int s = B.s0;
             if (B.n_child == 0) {
 #pragma unroll
@@ -256,7 +269,7 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<double> C, B1S& 
                 for (int q = 0; q < B1_KS; q++)
                     if (q < nk) {
                         int xk = tid + 1 + q * nth;
-                        T v = stb<T, CURV>(cur, xk, lam, lmid, cmr[q], c0r[q], cpr[q]) * wr[q];
+                        T v = st3(cur, xk, aL[q], aC[q], aR[q]);
                         nxt[xk] = v;
                         if (lor[q]) nxt[0] = v;
                         if (hir[q]) nxt[MX + 1] = v;
@@ -290,10 +303,13 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<double> C, B1S& 
             T* rr = rho + (D.mm0 + B.molmon) * M;
             const T d = (T)B.degeneracy;
             const bool d1 = B.degeneracy == 1.0;
-            T wr[B1_KS], acc[B1_KS], gfn[B1_KS];
+            T wr[B1_KS], acc[B1_KS], gfn[B1_KS], aL[B1_KS], aC[B1_KS], aR[B1_KS];
 #pragma unroll
             for (int q = 0; q < B1_KS; q++) {
                 wr[q] = q < nk ? w[tid + 1 + q * nth] : (T)0;
+                aL[q] = (CURV ? cmr[q] : lam) * wr[q];
+                aC[q] = (CURV ? c0r[q] : lmid) * wr[q];
+                aR[q] = (CURV ? cpr[q] : lam) * wr[q];
                 acc[q] = (T)0;
             }
             int s = B.s0 + B.length - 1;
@@ -343,7 +359,7 @@ __device__ void b1_residual(B1Prob& P, const Lat1 L, const Coef<double> C, B1S& 
                 for (int q = 0; q < B1_KS; q++)
                     if (q < nk) {
                         int xk = tid + 1 + q * nth;
-                        T v = stb<T, CURV>(cur, xk, lam, lmid, cmr[q], c0r[q], cpr[q]) * wr[q];
+                        T v = st3(cur, xk, aL[q], aC[q], aR[q]);
                         nxt[xk] = v;
                         if (lor[q]) nxt[0] = v;
                         if (hir[q]) nxt[MX + 1] = v;

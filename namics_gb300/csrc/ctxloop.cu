@@ -17,20 +17,16 @@
 //                        switch, the stopping test, it++ and the WHILE handle
 //           mix        : x ← Σ c_i·xR_i }
 // The control logic is the host loop's, statement for statement (the first
-// pass is the initial residual and plain mixing step into slot 0).  The one
-// difference is the small solve: one warp solves A c = 1 by Gaussian
-// elimination with partial pivoting and pivots floored at 1e-30·max|A|
-// (the batched solver's warp_solve), where the host loop takes the
-// pseudo-inverse of a Jacobi eigen-decomposition: a single warp needs ~60
-// dependent FP64 divisions and square roots per Jacobi sweep, tens of µs.
-// Both solve the reference's system; near convergence, where A ≈ 1e-9·(all
-// ones) is numerically singular, they pick different (equally valid)
-// coefficients, so the two loops reach the same fixed point along slightly
-// different paths.  The WHILE loop ends: every pass increments `it` and
-// stops at the iteration limit.
+// pass is the initial residual and plain mixing step into slot 0), and so is
+// the small solve: the pseudo-inverse of a cyclic Jacobi eigen-decomposition
+// with the host's rotation order, one warp (warp_pinv_solve), so the two
+// loops take the same DIIS path up to rounding.  (Gaussian elimination, the
+// batched 1-D solver's warp_solve, was tried here first: on a 3-D melt whose
+// early Gram matrices are ill-conditioned its coefficients ran the fields away
+// within five iterations where the pseudo-inverse's stay finite.)  The WHILE
+// loop ends: every pass increments `it` and stops at the iteration limit.
 #include <cuda_runtime.h>
 
-#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -168,7 +164,8 @@ __global__ void kl_gram(LoopState* S, int n, int m, const double* __restrict__ x
 // The host loop's control statements (Ctx::solve), one warp.
 __global__ void kl_control(LoopState* S, const double* __restrict__ gpart, int nb, int m, int nvar, double sw_floor,
                            int* status, cudaGraphConditionalHandle hl) {
-    __shared__ double As[NM_MAX_DIIS * (NM_MAX_DIIS + 1)], Ci[NM_MAX_DIIS];
+    __shared__ double As[NM_MAX_DIIS * NM_MAX_DIIS], Ci[NM_MAX_DIIS];
+    __shared__ double Ja[NM_MAX_DIIS * NM_MAX_DIIS], Jq[NM_MAX_DIIS * NM_MAX_DIIS];
     const int lane = threadIdx.x & 31;
     // the state as the pass left it, in every lane before lane 0 changes it
     double resid = S->resid_new;
@@ -218,17 +215,14 @@ __global__ void kl_control(LoopState* S, const double* __restrict__ gpart, int n
                 const int i = e / kd, j = e % kd;
                 const double v = S->Aij[j + m * i];
                 if (v != v) nan = true;
-                As[i * (kd + 1) + j] = v;
+                As[i * kd + j] = v;
             }
-            for (int i = lane; i < kd; i += 32) As[i * (kd + 1) + kd] = 1.0;
             nan = __any_sync(0xffffffffu, nan);
             __syncwarp();
             if (nan) {
                 rc = NM_ERR_NAN_DIIS;
             } else {
-                if (kd == 1) { if (lane == 0) Ci[0] = 1.0; }
-                else warp_solve(As, Ci, kd);
-                __syncwarp();
+                warp_pinv_solve(As, Ci, kd, Ja, Jq);
                 if (lane == 0) {
                     double nC = 0;
                     for (int i = 0; i < kd; i++) nC += Ci[i];
@@ -414,22 +408,8 @@ int ctx_loop_solve(Ctx& C, double* x, nm_solve_result* res, int max_iter) {
     const nm_plan* p = C.plan;
     if (!C.d_loop) LK(cudaMallocAsync(&C.d_loop, sizeof(LoopState), C.stream));
     if (!C.loop_graph || C.loop_x != x) {
-        // the residual's launches keep their programmatic (PDL) edges inside
-        // the conditional bodies where the driver instantiates them; plain
-        // stream-order edges otherwise
-        static std::atomic<int> pdl_ok{1};
-        int rc = NM_ERR_CUDA;
-        const long long l0 = C.launches;
-        if (pdl_ok.load()) {
-            rc = build_loop(C, x, false);
-            if (rc == NM_ERR_CUDA) {
-                pdl_ok.store(0);
-                cudaGetLastError();
-                C.launches = l0;
-            }
-        }
-        if (rc) rc = build_loop(C, x, true);
-        if (rc) return rc;
+        // plain stream-order edges inside the conditional bodies
+        if (int rc = build_loop(C, x, true)) return rc;
     }
     LoopState h;
     std::memset(&h, 0, sizeof(h));

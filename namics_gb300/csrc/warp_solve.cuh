@@ -61,3 +61,80 @@ __device__ inline void warp_solve(double* A, double* c, int kd) {
 }
 
 }  // namespace nm
+
+namespace nm {
+
+// Solve A c = 1 (A symmetric n×n, row-major in Ain, n ≤ 32) by the
+// pseudo-inverse of a cyclic Jacobi eigen-decomposition, c = Q·diag(1/λ)·Qᵀ·1,
+// one warp: the host's nm_pinv_solve with the same sweep and rotation order,
+// lane k carrying index k of every row, column and eigenvector update, so
+// each element sees the same operations in the same order.  a and q are n×n
+// shared-memory scratch.  Near convergence, where A ≈ 1e-9·(all ones) is
+// numerically singular, the rounding-noise eigenvectors are nearly
+// orthogonal to the ones vector and c stays finite (an elimination there can
+// divide by a noise pivot).
+__device__ inline void warp_pinv_solve(const double* Ain, double* c, int n, double* a, double* q) {
+    const int lane = threadIdx.x & 31;
+    if (n == 1) {
+        if (lane == 0) c[0] = 1.0;
+        __syncwarp();
+        return;
+    }
+    for (int e = lane; e < n * n; e += 32) {
+        a[e] = Ain[e];
+        q[e] = (e / n == e % n) ? 1.0 : 0.0;
+    }
+    __syncwarp();
+    for (int sweep = 0; sweep < 60; sweep++) {
+        int stop = 0;
+        if (lane == 0) {
+            double off = 0, dg = 0;
+            for (int i = 0; i < n; i++)
+                for (int j = 0; j < n; j++) {
+                    const double v = a[i * n + j] * a[i * n + j];
+                    if (i == j) dg += v; else off += v;
+                }
+            stop = (off == 0 || off <= 1e-30 * dg);
+        }
+        if (__shfl_sync(0xffffffffu, stop, 0)) break;
+        for (int p = 0; p < n - 1; p++)
+            for (int r = p + 1; r < n; r++) {
+                const double apr = a[p * n + r];
+                if (apr == 0) continue;  // the same value in every lane
+                const double th = (a[r * n + r] - a[p * n + p]) / (2 * apr);
+                const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1));
+                const double cs = 1 / sqrt(t * t + 1), sn = t * cs;
+                __syncwarp();
+                if (lane < n) {  // columns p, r
+                    const double u = a[lane * n + p], v = a[lane * n + r];
+                    a[lane * n + p] = cs * u - sn * v;
+                    a[lane * n + r] = sn * u + cs * v;
+                }
+                __syncwarp();
+                if (lane < n) {  // rows p, r
+                    const double u = a[p * n + lane], v = a[r * n + lane];
+                    a[p * n + lane] = cs * u - sn * v;
+                    a[r * n + lane] = sn * u + cs * v;
+                }
+                if (lane < n) {  // eigenvectors
+                    const double u = q[lane * n + p], v = q[lane * n + r];
+                    q[lane * n + p] = cs * u - sn * v;
+                    q[lane * n + r] = sn * u + cs * v;
+                }
+                __syncwarp();
+            }
+    }
+    if (lane < n) {
+        double ci = 0;
+        for (int j = 0; j < n; j++) {
+            double proj = 0;  // (Qᵀ·1)_j, in the host's order
+            for (int k = 0; k < n; k++) proj += q[k * n + j];
+            const double w = proj / a[j * n + j];
+            ci += q[lane * n + j] * w;
+        }
+        c[lane] = ci;
+    }
+    __syncwarp();
+}
+
+}  // namespace nm
