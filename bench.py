@@ -731,6 +731,11 @@ def other_workloads(args) -> dict:
     return out
 
 
+# DRAM bytes (read + write) per problem of the work loop on this workload,
+# from an ncu capture of a 1024-problem launch: 42.31 + 57.11 GB
+TRAFFIC_PER_PROBLEM = (42.31e9 + 57.11e9) / 1024
+
+
 def run_brush1d(args) -> None:
     """The headline: a sustained stream of batched 1-D brush/star solves.
 
@@ -870,10 +875,12 @@ def run_brush1d(args) -> None:
                          f"({nbytes / 1e6:.0f} MB of fields) are written to HBM before it",
                    "parallelism": f"replicas x{ws}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak, "traffic": TRAFFIC_PER_PROBLEM * len(its_all),
                      "note": f"{bpu:.0f} B per segment-site update x updates / work-loop time; peak of measured "
-                             "(MEASURED_PEAKS.json hbm_gbs, burst copy); traffic: not measured in this run "
-                             "(the ncu capture of the work loop is summarised beside the kernel's profile)"},
+                             "(MEASURED_PEAKS.json hbm_gbs, burst copy); traffic: a constant from one ncu capture "
+                             f"of this work loop ({TRAFFIC_PER_PROBLEM / 1e6:.1f} MB of DRAM reads + writes per "
+                             "problem, the same at 512 and 1024 problems a launch) times the launch's problems, "
+                             "not measured in this run"},
         "e2e": {"value": n_all / e2e_s, "unit": UNIT, "h2d_bytes_per_step": nbytes * ws // K,
                 "d2h_bytes_per_step": nbytes * ws // K},
         "gpu_launches": launches,
