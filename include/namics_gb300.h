@@ -125,14 +125,19 @@ typedef struct nm_plan {
     int    n_seg;
     const char* const* seg_name;
     const int*    seg_freedom;   /* enum nm_segfree                         */
-    const int*    seg_it;        /* iteration block of each segment, -1 frozen */
+    const int*    seg_it;        /* iteration block of each segment, -1 frozen
+                                    or with internal states (their states
+                                    carry the blocks: state_it)          */
     const double* seg_gmask;     /* [n_seg*M] G1 = exp(-u)·gmask           */
     const double* seg_phi_frozen;/* [n_seg*M] frozen volume fraction       */
     const double* chi;           /* [n_seg*n_seg]                           */
-    const double* seg_valence;   /* [n_seg]                                 */
+    const double* seg_valence;   /* [n_seg]; 0 for a segment with internal
+                                    states (its states carry the charge) */
     const double* seg_epsilon;   /* [n_seg]                                 */
-    int    n_it;                 /* iteration species (ItMonList)          */
-    const int*    it_seg;        /* [n_it] representative segment          */
+    int    n_it;                 /* iteration species (ItMonList, then
+                                    ItStateList)                          */
+    const int*    it_seg;        /* [n_it] representative segment (a state
+                                    block: the state's segment)           */
     int    iv;                   /* length of x: n_it*M (+M if charged)    */
     int    charged;
     /* molecules */
@@ -167,6 +172,33 @@ typedef struct nm_plan {
      * propagator with the reference's slot count, round(√(2·N_block)) per
      * block.  Results are the same either way. */
     int    save_memory;
+    /* internal states (`state : <name> : mon | valence | alphabulk |
+     * chi_<X>`, State::CheckInput state.cpp:37-106, Segment::AddState
+     * segment.cpp:1981-2016) and the reactions that fix their bulk
+     * fractions (`reaction : <name> : equation | pK | K`, reaction.cpp:
+     * 37-145).  n_state = 0 when the input defines none; the arrays below
+     * are then NULL and n_sp = n_seg.  A segment with states interacts
+     * through its states only: the interaction species are the segments
+     * (those without states count) followed by the states, species
+     * n_seg + j being state j. */
+    int    n_state;
+    const char* const* state_name;  /* [n_state] in the input's order      */
+    const int*    state_seg;        /* [n_state] the state's segment       */
+    const double* state_valence;    /* [n_state]                           */
+    const double* state_alphabulk;  /* [n_state] fraction of the segment in
+                                       this state in the bulk, solved from
+                                       the reactions (Solve_scf::Solve's
+                                       WEAK pre-iteration, solve_scf.cpp:
+                                       562-603)                           */
+    const int*    state_it;         /* [n_state] iteration block           */
+    const int*    seg_nstate;       /* [n_seg] states of each segment       */
+    int    n_sp;                    /* interaction species: n_seg + n_state */
+    const double* chi_sp;           /* [n_sp*n_sp] χ between species (the
+                                       reference's Seg::chi / State::chi
+                                       rows, system.cpp:1775-1915)        */
+    const int*    it_sp;            /* [n_it] species of each iteration
+                                       block's representative (ItMonList,
+                                       then ItStateList)                  */
 } nm_plan;
 
 /* Parse Namics input text (the `lat/mon/mol/sys/newton` key subset of the

@@ -98,6 +98,25 @@ class Plan:
         return [self.c.it_seg[i] for i in range(self.c.n_it)]
 
     @property
+    def state_names(self) -> list[str]:
+        return [self.c.state_name[j].decode() for j in range(self.c.n_state)]
+
+    @property
+    def state_alphabulk(self) -> list[float]:
+        return [self.c.state_alphabulk[j] for j in range(self.c.n_state)]
+
+    @property
+    def it_names(self) -> list[str]:
+        """Name of each iteration block's representative: the mon of an
+        ItMonList block, the state of an ItStateList block (the names a
+        reference guess file lists)."""
+        c = self.c
+        if c.n_state == 0:
+            return [self.seg_names[i] for i in self.it_seg]
+        names = self.seg_names + self.state_names
+        return [names[c.it_sp[i]] for i in range(c.n_it)]
+
+    @property
     def shape(self) -> tuple[int, ...]:
         c = self.c
         if c.gradients == 1:
@@ -208,7 +227,8 @@ class Context:
 
     def field(self, which: int) -> np.ndarray:
         p = self.plan
-        n = {0: p.n_seg, 1: p.n_seg, 2: 1, 3: 1, 4: p.n_mol, 5: p.n_seg, 6: 1, 7: 1, 8: 1}[which] * p.M
+        n = {0: p.n_seg, 1: p.n_seg, 2: 1, 3: 1, 4: p.n_mol, 5: p.n_seg, 6: 1, 7: 1, 8: 1,
+             9: p.c.n_state}[which] * p.M
         out = np.empty(n)
         _check(_abi.load().nm_get_field(self._h, which, _dptr(out)))
         return out

@@ -66,7 +66,10 @@ class nm_plan(C.Structure):
                 ("scan_mol", C.c_int), ("scan_what", C.c_int), ("scan_n", C.c_int),
                 ("scan_exponential", C.c_int), ("scan_start", C.c_double), ("scan_end", C.c_double),
                 ("scan_step", C.c_double),
-                ("save_memory", C.c_int)]
+                ("save_memory", C.c_int),
+                ("n_state", C.c_int), ("state_name", C.POINTER(C.c_char_p)), ("state_seg", ip),
+                ("state_valence", dp), ("state_alphabulk", dp), ("state_it", ip), ("seg_nstate", ip),
+                ("n_sp", C.c_int), ("chi_sp", dp), ("it_sp", ip)]
 
 
 class nm_ctx_options(C.Structure):

@@ -930,6 +930,7 @@ static int batch_check(const nm_plan* P) {
             set_error("Markov 2 chains run on a device context, not in a batch");
             return NM_ERR_INPUT;
         }
+    if (P->n_state > 0) { set_error("internal states run on a device context, not in a batch"); return NM_ERR_INPUT; }
     if (P->n_seg > NM_MAX_SEG || P->n_mol > NM_MAX_MOL || P->diis_m > B1_MAXM) {
         set_error("problem exceeds the batched solver's limits (segments, molecules, DIIS m <= 12)");
         return NM_ERR_INPUT;
@@ -1435,6 +1436,7 @@ static int noalloc_layout(const nm_plan* P, StaticArena& A, double* x_dev, B1Pro
     if (P->charged) { set_error("nm_solve1d_noalloc: charged systems are not supported"); return NM_ERR_INPUT; }
     for (int m = 0; m < P->n_mol; m++)
         if (P->mols[m].markov == 2) { set_error("nm_solve1d_noalloc: Markov 2 chains are not supported"); return NM_ERR_INPUT; }
+    if (P->n_state > 0) { set_error("nm_solve1d_noalloc: internal states are not supported"); return NM_ERR_INPUT; }
     if (P->n_seg > NM_MAX_SEG || P->n_mol > NM_MAX_MOL || P->diis_m > B1_MAXM) {
         set_error("nm_solve1d_noalloc: problem exceeds the limits (segments, molecules, DIIS m <= 12)");
         return NM_ERR_INPUT;

@@ -50,14 +50,52 @@ thread_local bool g_plain_launch = false;
 
 // u = x (+ the charged terms −ε·EE + v·ψ, system.cpp:2001-2030) at the
 // set_bounds source of each site; G1 = exp(−u)·mask·KSAM
+// A segment with internal states: G1 = Σ_j α_bulk,j·exp(-u_j) over its
+// states, each u_j from the state's block with the state's valence, and
+// α_j = α_bulk,j·exp(-u_j)/G1 (segment.cpp:861-873); u_j and α_j are kept
+// for the free energy and the states' volume fractions.
 __global__ void k_g1(Lat L, int ns, const double* __restrict__ x, const int* __restrict__ seg_it,
                      const double* __restrict__ gmask, double* __restrict__ G1, float* __restrict__ G1f,
-                     ChgArgs chg, const double* __restrict__ EE, const double* __restrict__ psi) {
+                     ChgArgs chg, const double* __restrict__ EE, const double* __restrict__ psi,
+                     StArgs st, double* __restrict__ ust, double* __restrict__ ast) {
     int M = L.M;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < M; s += gridDim.x * blockDim.x) {
         int src = nmdev::bc_source(L, s);
         for (int i = 0; i < ns; i++) {
             int it = seg_it[i];
+            if (it < 0 && st.n > 0) {
+                bool with_states = false;
+                for (int j = 0; j < st.n; j++) with_states = with_states || st.seg[j] == i;
+                if (with_states) {
+                    double g1 = 0;
+                    for (int j = 0; j < st.n; j++) {
+                        if (st.seg[j] != i) continue;
+                        double u = x[(size_t)st.it[j] * M + src];
+                        if (chg.on) {
+                            u += -1.0 * chg.eps[i] * EE[src];
+                            if (chg.val[ns + j] != 0) u += chg.val[ns + j] * psi[src];
+                        }
+                        const double a = exp(-u) * st.ab[j];
+                        ust[(size_t)j * M + s] = u;
+                        ast[(size_t)j * M + s] = a;
+                        g1 += a;
+                    }
+                    for (int j = 0; j < st.n; j++)
+                        if (st.seg[j] == i) {
+                            double& a = ast[(size_t)j * M + s];
+                            a = g1 != 0 ? a / g1 : 0.0;
+                        }
+                    const double v = g1 * gmask[(size_t)i * M + s];
+                    if (G1f) {
+                        const float f = (float)v;
+                        G1f[(size_t)i * M + s] = f;
+                        G1[(size_t)i * M + s] = (double)f;
+                    } else {
+                        G1[(size_t)i * M + s] = v;
+                    }
+                    continue;
+                }
+            }
             double u = it >= 0 ? x[(size_t)it * M + src] : 0.0;
             if (chg.on && it >= 0) {
                 u += -1.0 * chg.eps[i] * EE[src];
@@ -257,6 +295,8 @@ __global__ void k_norms(NormArgs a, double* __restrict__ sc, double* __restrict_
     }
     for (int i = 0; i < a.ns; i++) seg_phibulk[i] = 0;
     for (int k = 0; k < a.n_mm; k++) seg_phibulk[a.mm_seg[k]] += a.mm_frac[k] * sc[5 * a.mm_mol[k] + 4];
+    // states: φ_bulk,j = φ_bulk·α_bulk,j (Segment::SetPhiSide, segment.cpp:1339-1343)
+    for (int j = 0; j < a.st.n; j++) seg_phibulk[a.ns + j] = seg_phibulk[a.st.seg[j]] * a.st.ab[j];
     if (st) *status = st;
 }
 
@@ -299,6 +339,10 @@ __global__ void k_phi(Lat L, PhiArgs a, const double* __restrict__ sc, const dou
             }
         }
         phitot[s] = pt;
+        // the states' volume fractions φ_j = α_j·φ(seg), rows after the
+        // segments' (Segment::SetPhiSide, segment.cpp:1337-1343)
+        for (int j = 0; j < a.st.n; j++)
+            phi[(size_t)(a.ns + j) * M + s] = a.ast[(size_t)j * M + s] * phi[(size_t)a.st.seg[j] * M + s];
     }
 }
 
@@ -320,6 +364,7 @@ __global__ void k_residual(Lat L, ResArgs a, const double* __restrict__ x, const
         else { cx = s / L.JX; int r = s % L.JX; cy = r / L.JY; cz = r % L.JY; }
         double ps[NM_MAX_SEG];
         for (int k = 0; k < a.ns; k++) {
+            if (!a.sp_on[k]) { ps[k] = 0; phi_side[(size_t)k * M + s] = 0; continue; }
             nmdev::GLoad<double> ld{phi + (size_t)k * M};
             ps[k] = nmdev::stencil_at(L, ld, cx, cy, cz);
             phi_side[(size_t)k * M + s] = ps[k];
@@ -331,7 +376,7 @@ __global__ void k_residual(Lat L, ResArgs a, const double* __restrict__ x, const
             double v = x[(size_t)i * M + s];
             int r = a.it_seg[i];
             for (int k = 0; k < a.ns; k++) {
-                double chi = a.chi[r * a.ns + k];
+                double chi = a.sp_on[k] ? a.chi[r * a.ns + k] : 0.0;
                 if (chi != 0 && pt > 0) v = v - chi * (ps[k] / pt - seg_phibulk[k]);
             }
             gi[i] = v;
@@ -462,10 +507,15 @@ __global__ void k_diis_mix(int n, double* __restrict__ x, const double* __restri
 }
 
 // free-energy and grand-potential densities (system.cpp:2809-3244)
+// Species (segments, then states; a segment with states takes part through
+// them): sp_on[k] = 0 for a segment with states, frozen[k] for frozen
+// segments (never a state).  ns = segments, nsp = species.
 struct FeArgs {
-    int ns, n_mol, charged;
+    int ns, nsp, n_mol, charged;
     const double *q, *psi, *EE, *eps;  // charged systems
-    int seg_frozen[NM_MAX_SEG], seg_in_mol[NM_MAX_SEG];
+    const double* ust;                 // u of each state (internal states)
+    int seg_frozen[NM_MAX_SEG], seg_in_mol[NM_MAX_SEG], sp_on[NM_MAX_SEG];
+    int st_seg[NM_MAX_SEG];
     double chi[NM_MAX_SEG * NM_MAX_SEG];
     double cF[NM_MAX_MOL], cF2[NM_MAX_MOL], invN[NM_MAX_MOL];
 };
@@ -476,23 +526,36 @@ __global__ void k_fe_density(Lat L, FeArgs a, const double* __restrict__ sc, con
                              const double* __restrict__ seg_phibulk, const double* __restrict__ ksam,
                              double* __restrict__ F, double* __restrict__ GP) {
     int M = L.M;
+    const int ns = a.ns, nsp = a.nsp;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < M; s += gridDim.x * blockDim.x) {
         if (!nmdev::is_interior(L, s)) { F[s] = 0; GP[s] = 0; continue; }
         double f = 0, gp = 0;
         for (int m = 0; m < a.n_mol; m++) f += a.cF[m] * mol_phitot[(size_t)m * M + s];
-        for (int i = 0; i < a.ns; i++) {
+        for (int i = 0; i < ns; i++) {
             if (!a.seg_in_mol[i]) continue;
+            if (!a.sp_on[i]) {  // a segment with states: -φ_j·u_j per state (system.cpp:2866-2888)
+                for (int j = 0; j < nsp - ns; j++)
+                    if (a.st_seg[j] == i)
+                        f += -1.0 * (phi[(size_t)(ns + j) * M + s] * a.ust[(size_t)j * M + s]);
+                continue;
+            }
             double g1 = G1[(size_t)i * M + s];
             double ml = g1 > 0 ? -log(g1) : 0.0;
             f += -1.0 * (phi[(size_t)i * M + s] * ml);
         }
-        for (int j = 0; j < a.ns; j++) {
-            if (a.seg_frozen[j]) continue;
+        // χ pairs (system.cpp:2890-2979): segment rows, then state rows; a
+        // state-state pair reads the row state's own side fraction
+        for (int j = 0; j < nsp; j++) {
+            if (!a.sp_on[j] || a.seg_frozen[j]) continue;
             double pj = phi[(size_t)j * M + s];
-            for (int k = 0; k < a.ns; k++) {
-                double chi = a.seg_frozen[k] ? a.chi[j * a.ns + k] : a.chi[j * a.ns + k] / 2;
+            for (int k = 0; k < nsp; k++) {
+                if (!a.sp_on[k]) continue;
+                double chi = a.chi[j * nsp + k];
+                if (!(a.seg_frozen[k] && j < ns)) chi = chi / 2;
+                if (j >= ns && a.seg_frozen[k]) chi = a.chi[j * nsp + k];
                 if (chi == 0) continue;
-                f += chi * (pj * phi_side[(size_t)k * M + s]);
+                const int ks = (j >= ns && k >= ns) ? j : k;
+                f += chi * (pj * phi_side[(size_t)ks * M + s]);
             }
         }
         for (int m = 0; m < a.n_mol; m++) f += a.cF2[m] * mol_phitot[(size_t)m * M + s];
@@ -501,12 +564,12 @@ __global__ void k_fe_density(Lat L, FeArgs a, const double* __restrict__ sc, con
         if (a.charged) F[s] += a.q[s] * a.psi[s] * 0.5;  // system.cpp:3020-3028
         for (int m = 0; m < a.n_mol; m++) gp += (mol_phitot[(size_t)m * M + s] + (-sc[5 * m + 4])) * a.invN[m];
         gp += alpha[s];
-        for (int j = 0; j < a.ns; j++) {
-            if (a.seg_frozen[j]) continue;
+        for (int j = 0; j < nsp; j++) {
+            if (!a.sp_on[j] || a.seg_frozen[j]) continue;
             double pj = phi[(size_t)j * M + s], pbA = seg_phibulk[j];
-            for (int k = 0; k < a.ns; k++) {
-                if (a.seg_frozen[k]) continue;
-                double chi = a.chi[j * a.ns + k] / 2;
+            for (int k = 0; k < nsp; k++) {
+                if (!a.sp_on[k] || a.seg_frozen[k]) continue;
+                double chi = a.chi[j * nsp + k] / 2;
                 if (chi == 0) continue;
                 gp += chi * (pj * phi_side[(size_t)k * M + s] + (-pbA * seg_phibulk[k]));
             }
@@ -637,7 +700,7 @@ int Ctx::molecule_pass(int m) {
 // by residual() on the 3-D path).
 int Ctx::launch_g1(const double* x, bool with32) {
     k_g1<<<grid_for(plan->M), 256, 0, stream>>>(lat, plan->n_seg, x, d_seg_it, d_gmask, d_G1,
-                                                with32 ? d_G1f : nullptr, chg, d_EE, d_psi);
+                                                with32 ? d_G1f : nullptr, chg, d_EE, d_psi, st, d_ust, d_ast);
     launches++;
     return NM_OK;
 }
@@ -825,20 +888,23 @@ int Ctx::solve(double* x, nm_solve_result* res, int max_iter) {
 int Ctx::free_energy(double* F, double* Omega, double* mu) {
     if (!have_state) { set_error("no residual evaluated yet"); return NM_ERR_ARG; }
     int M = plan->M, ns = plan->n_seg;
-    std::vector<double> sc(5 * plan->n_mol), spb(ns);
+    std::vector<double> sc(5 * plan->n_mol), spb(nsp);
     CK(cudaMemcpyAsync(sc.data(), d_sc, sizeof(double) * sc.size(), cudaMemcpyDeviceToHost, stream));
-    CK(cudaMemcpyAsync(spb.data(), d_seg_phibulk, sizeof(double) * ns, cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(spb.data(), d_seg_phibulk, sizeof(double) * nsp, cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
     FeArgs a;
     std::memset(&a, 0, sizeof(a));
-    a.ns = ns; a.n_mol = plan->n_mol;
+    a.ns = ns; a.nsp = nsp; a.n_mol = plan->n_mol;
     a.charged = charged;
     a.q = d_q; a.psi = d_psi; a.EE = d_EE; a.eps = d_eps;
-    for (int i = 0; i < ns; i++) {
-        a.seg_frozen[i] = plan->seg_freedom[i] == NM_SEG_FROZEN;
-        a.seg_in_mol[i] = plan->seg_it[i] >= 0;
-    }
-    for (int i = 0; i < ns * ns; i++) a.chi[i] = chi[i];
+    a.ust = d_ust;
+    for (int k = 0; k < nsp; k++) a.sp_on[k] = res_args.sp_on[k];
+    for (int i = 0; i < ns; i++) a.seg_frozen[i] = plan->seg_freedom[i] == NM_SEG_FROZEN;
+    for (int m = 0; m < plan->n_mol; m++)
+        for (int q = 0; q < plan->mols[m].n_molmon; q++) a.seg_in_mol[plan->mols[m].molmon_seg[q]] = 1;
+    for (int j = 0; j < nst; j++) a.st_seg[j] = st.seg[j];
+    const std::vector<double>& chs = nst ? chi_sp : chi;  // χ between species
+    for (int i = 0; i < nsp * nsp; i++) a.chi[i] = chs[i];
     for (int m = 0; m < plan->n_mol; m++) {
         const nm_molecule& mol = plan->mols[m];
         double N = mol.chainlength;
@@ -869,13 +935,22 @@ int Ctx::free_energy(double* F, double* Omega, double* mu) {
             double constant = 0;
             for (int k = 0; k < plan->n_mol; k++) constant += sc[5 * k + 4] / plan->mols[k].chainlength;
             Mu = Mu - NA * constant;
-            for (int j = 0; j < ns; j++) {
-                double FA = 0;
-                for (int q = 0; q < mol.n_molmon; q++) if (mol.molmon_seg[q] == j) FA = mol.molmon_fraction[q];
-                for (int k = 0; k < ns; k++) {
-                    double FB = 0;
-                    for (int q = 0; q < mol.n_molmon; q++) if (mol.molmon_seg[q] == k) FB = mol.molmon_fraction[q];
-                    Mu = Mu - NA * (chi[j * ns + k] / 2) * (spb[j] - FA) * (spb[k] - FB);
+            // pairs of species (system.cpp:3319-3400); a state's bulk share
+            // of the molecule is fraction(seg)·α_bulk, and the state-state
+            // term takes the row state's for both factors
+            auto frac = [&](int seg) {
+                double f = 0;
+                for (int q = 0; q < mol.n_molmon; q++) if (mol.molmon_seg[q] == seg) f = mol.molmon_fraction[q];
+                return f;
+            };
+            auto share = [&](int k) { return k < ns ? frac(k) : frac(st.seg[k - ns]) * st.ab[k - ns]; };
+            for (int j = 0; j < nsp; j++) {
+                if (!res_args.sp_on[j]) continue;
+                const double FA = share(j);
+                for (int k = 0; k < nsp; k++) {
+                    if (!res_args.sp_on[k]) continue;
+                    const double FB = (j >= ns && k >= ns) ? FA : share(k);
+                    Mu = Mu - NA * (chs[j * nsp + k] / 2) * (spb[j] - FA) * (spb[k] - FB);
                 }
             }
             mu[i] = Mu;
@@ -972,10 +1047,21 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
     for (int i = 0; i < ns; i++) sf[i] = p->seg_freedom[i] == NM_SEG_FROZEN;
     TRY(dalloc(&d_seg_frozen, ns, stream));
     CK(cudaMemcpyAsync(d_seg_frozen, sf.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, stream));
+    // internal states: species rows after the segments'
+    nst = p->n_state;
+    nsp = ns + nst;
+    if (nst > 0) {
+        if (nsp > NM_MAX_SEG) { set_error("more than 16 interaction species"); return NM_ERR_INPUT; }
+        st.n = nst;
+        for (int j = 0; j < nst; j++) { st.seg[j] = p->state_seg[j]; st.it[j] = p->state_it[j]; st.ab[j] = p->state_alphabulk[j]; }
+        TRY(dalloc(&d_ust, (size_t)nst * M, stream));
+        TRY(dalloc(&d_ast, (size_t)nst * M, stream));
+        chi_sp.assign(p->chi_sp, p->chi_sp + (size_t)nsp * nsp);
+    }
     // state
     TRY(dalloc(&d_G1, (size_t)ns * M, stream));
-    TRY(dalloc(&d_phi, (size_t)ns * M, stream));
-    TRY(dalloc(&d_phi_side, (size_t)ns * M, stream));
+    TRY(dalloc(&d_phi, (size_t)nsp * M, stream));
+    TRY(dalloc(&d_phi_side, (size_t)nsp * M, stream));
     TRY(dalloc(&d_phitot, M, stream));
     TRY(dalloc(&d_alpha, M, stream));
     TRY(dalloc(&d_mol_phitot, (size_t)p->n_mol * M, stream));
@@ -983,7 +1069,7 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
     TRY(dalloc(&d_tmpF, M, stream));
     TRY(dalloc(&d_tmpGP, M, stream));
     TRY(dalloc(&d_sc, 5 * (size_t)p->n_mol, stream));
-    TRY(dalloc(&d_seg_phibulk, ns, stream));
+    TRY(dalloc(&d_seg_phibulk, nsp, stream));
     TRY(dalloc(&d_status, 1, stream));
     TRY(dalloc(&d_partial, (size_t)red_blocks, stream));
     TRY(dalloc(&d_resid, 4, stream));
@@ -1069,16 +1155,19 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
         }
     }
     norm_args.n_mm = k; phi_args.n_mm = k;
-    res_args.ns = ns; res_args.nit = p->n_it;
-    for (int i = 0; i < p->n_it; i++) res_args.it_seg[i] = p->it_seg[i];
+    norm_args.st = st; phi_args.st = st; phi_args.ast = d_ast;
+    res_args.ns = nsp; res_args.nit = p->n_it;
+    for (int i = 0; i < p->n_it; i++) res_args.it_seg[i] = nst ? p->it_sp[i] : p->it_seg[i];
+    for (int k2 = 0; k2 < nsp; k2++) res_args.sp_on[k2] = k2 >= ns || !nst || p->seg_nstate[k2] == 0;
     chi.assign(p->chi, p->chi + (size_t)ns * ns);
-    for (int i = 0; i < ns * ns; i++) res_args.chi[i] = chi[i];
+    const std::vector<double>& chs = nst ? chi_sp : chi;
+    for (int i = 0; i < nsp * nsp; i++) res_args.chi[i] = chs[i];
     CK(cudaStreamSynchronize(stream));
     return NM_OK;
 }
 
 Ctx::~Ctx() {
-    double* ptrs[] = {d_L, d_lm1, d_l0, d_l1, d_ksam, d_gmask, d_phi_frozen, d_G1, d_phi, d_phi_side,
+    double* ptrs[] = {d_ust, d_ast, d_L, d_lm1, d_l0, d_l1, d_ksam, d_gmask, d_phi_frozen, d_G1, d_phi, d_phi_side,
                       d_phitot, d_alpha, d_mol_phitot, d_gb, d_tmpF, d_tmpGP, d_sc, d_seg_phibulk,
                       d_partial, d_resid, d_xR, d_xx0, d_g, d_x, d_Ci, d_gram_partial,
                       d_EE, d_psi, d_q, d_eps, d_X};
@@ -1176,6 +1265,10 @@ int nm_ctx_set_values(nm_ctx* ctx, const char* const* items, const double* value
                           prop = trim(it.substr(p2 + 1));
         const double v = values[i];
         bool ok = false;
+        if (key == "mon" && prop.rfind("chi_", 0) == 0 && c->nst > 0) {
+            nm::set_error("nm_ctx_set_values: χ of a system with internal states is fixed at creation");
+            return NM_ERR_ARG;
+        }
         if (key == "mon" && prop.rfind("chi_", 0) == 0) {
             int a = -1, b = -1;
             for (int k = 0; k < ns; k++) {
@@ -1390,6 +1483,9 @@ int nm_get_field(nm_ctx* ctx, int which, double* out_host) {
         case 6: src = c->d_psi; n = M; break;
         case 7: src = c->d_q; n = M; break;
         case 8: src = c->d_eps; n = M; break;
+        case 9:
+            if (!c->nst) { nm::set_error("nm_get_field: the plan has no internal states"); return NM_ERR_ARG; }
+            src = c->d_phi + ns * M; n = (size_t)c->nst * M; break;
         default: nm::set_error("nm_get_field: unknown field"); return NM_ERR_ARG;
     }
     cudaError_t e = cudaMemcpyAsync(out_host, src, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream);

@@ -73,6 +73,15 @@ __host__ __device__ inline void nm_pinv_solve(const double* Ain, double* c, int 
 }
 
 struct MolScal { int freedom, pinned; double n_in, theta_in, phibulk_in, N, charge; };
+// Internal states (plans with n_state > 0): state j belongs to segment
+// seg[j], takes iteration block it[j] and has bulk fraction ab[j].  The
+// interaction species are the segments (those without states take part)
+// followed by the states: species n_seg + j is state j.
+struct StArgs {
+    int n;
+    int seg[NM_MAX_SEG], it[NM_MAX_SEG];
+    double ab[NM_MAX_SEG];
+};
 struct NormArgs {
     int n_mol, solvent, ns;
     int neutralizer;  // molecule index (charged systems) or -1
@@ -80,22 +89,31 @@ struct NormArgs {
     int n_mm;
     int mm_mol[NM_MAX_MM], mm_seg[NM_MAX_MM];
     double mm_frac[NM_MAX_MM];
+    StArgs st;        // states: φ_bulk,j = φ_bulk(seg)·α_bulk,j after the segments'
 };
 struct PhiArgs {
     int ns, n_mm, n_mol;
     int mm_mol[NM_MAX_MM], mm_seg[NM_MAX_MM];
     const double* mm_rho[NM_MAX_MM];
+    StArgs st;                 // states: φ_j = α_j·φ(seg) into species rows
+    const double* ast;         // α of each state [n*M]
 };
+// the residual over interaction species: ns = species count, sp_on[k] = 0
+// for a segment with states (its states stand in for it), it_seg[i] = the
+// species of block i's representative, chi between species
 struct ResArgs {
     int ns, nit;
     int it_seg[NM_MAX_SEG];
+    int sp_on[NM_MAX_SEG];
     double chi[NM_MAX_SEG * NM_MAX_SEG];
 };
 
-// Charged systems: per-segment relative permittivity and valence, for the
-// u += -ε·EE + v·ψ terms of PutU (system.cpp:2001-2030).
+// Charged systems: per-segment relative permittivity and per-species
+// valence (segments, then states; 0 for a segment with states), for the
+// u += -ε·EE + v·ψ terms of PutU (system.cpp:2001-2030) and the charge
+// density.
 struct ChgArgs {
-    int on;
+    int on, nsp;
     double eps[NM_MAX_SEG], val[NM_MAX_SEG];
 };
 
@@ -243,6 +261,13 @@ struct Ctx {
     PhiArgs phi_args;
     ResArgs res_args;
     std::vector<double> chi;  // the context's χ (nm_ctx_set_values may change it)
+    // internal states: n_state, species count, u and α of each state
+    // [n_state*M]; d_phi, d_phi_side and d_seg_phibulk hold one row per
+    // species (the states' after the segments')
+    int nst = 0, nsp = 0;
+    StArgs st{};
+    double *d_ust = nullptr, *d_ast = nullptr;
+    std::vector<double> chi_sp;  // χ between species (plans with states)
     // electrostatics (charged systems, 1 and 2 gradients): ψ is the last
     // block of x; halo sites of the composition are evaluated (nh of them)
     bool charged = false;

@@ -139,6 +139,9 @@ __global__ void k_charge(Lat L, int ns, ChgArgs a, const double* __restrict__ ph
             qv += a.val[i] * p;
             ev += a.eps[i] * p;
         }
+        // internal states: their volume fractions are the species rows
+        // after the segments' (System::DoElectrostatics, system.cpp:1936-1941)
+        for (int i = ns; i < a.nsp; i++) qv += a.val[i] * phi[(size_t)i * M + src];
         const double pt = phitot[s];
         q[s] = pt != 0 ? qv / pt : 0.0;
         eps[s] = pt != 0 ? ev / pt : 0.0;
@@ -267,6 +270,10 @@ int Ctx::elec_init() {
     charged = true;
     chg.on = 1;
     for (int i = 0; i < p->n_seg; i++) { chg.eps[i] = p->seg_epsilon[i]; chg.val[i] = p->seg_valence[i]; }
+    // the states' valences follow the segments' (species order); a segment
+    // with states carries valence 0 in the plan
+    chg.nsp = p->n_seg + p->n_state;
+    for (int j = 0; j < p->n_state; j++) chg.val[p->n_seg + j] = p->state_valence[j];
     // UpdateEE prefactor and UpdatePsi constant, in the reference's order
     double pf = 0.5 * EPS0 * p->bond_length / K_BT * (K_BT / E_CHARGE) * (K_BT / E_CHARGE);
     double C = E_CHARGE * E_CHARGE / (EPS0 * K_BT * p->bond_length);

@@ -674,6 +674,378 @@ static bool check_unread(const InputBlock& in, std::string& err) {
     return true;
 }
 
+// ---- internal states and reactions ----------------------------------------
+
+// One reaction: the states of its equation in written order and their
+// stoichiometric numbers, negative on the left-hand side (Reaction::
+// CheckInput, reaction.cpp:37-145).
+struct ReactionDef {
+    std::string name;
+    double pK = 0;
+    std::vector<int> sto, state;
+};
+
+// The states' bulk fractions as the reference fixes them before its SCF
+// loop (Solve_scf::Solve, solve_scf.cpp:562-603): one unknown x_r per
+// reaction, the residual of the WEAK case of Solve_scf::residuals
+// (solve_scf.cpp:762-785) — every reaction's analytic guess (3-term
+// reactions first), then each reaction scales its segment's iterated state
+// by exp(x_r), then g_r = -1 + Σ -ν·log10(α_bulk)/pK_eff.
+struct Chem {
+    const std::vector<ReactionDef>& R;
+    const std::vector<int>& seg;       // segment of each state
+    const std::vector<double>& val;    // valence of each state
+    const std::vector<char>& fixed;    // alphabulk given in the input
+    std::vector<std::vector<int>> seg_states;
+    std::vector<int> local;            // index of a state within its segment
+    std::vector<double> ab;            // α_bulk of each state
+    std::vector<int> item;             // Segment::ItState of each segment
+    std::string err;
+
+    Chem(const std::vector<ReactionDef>& r, const std::vector<int>& s, const std::vector<double>& v,
+         const std::vector<char>& f, const std::vector<double>& ab0, int n_seg)
+        : R(r), seg(s), val(v), fixed(f), seg_states(n_seg), local(s.size()), ab(ab0), item(n_seg, -1) {
+        for (size_t j = 0; j < s.size(); j++) {
+            local[j] = (int)seg_states[s[j]].size();
+            seg_states[s[j]].push_back((int)j);
+        }
+    }
+    // pK_eff = pK + Σ ν·ChemIntBulk/ln 10 (reaction.cpp:253-266).  The bulk
+    // χ sums there read the segments' and states' bulk fractions, which are
+    // still zero when the pre-iteration of a first solve runs.
+    static double pK_eff(const ReactionDef& r) { return r.pK; }
+
+    // Reaction::GuessAlpha, reaction.cpp:300-378
+    bool guess(const ReactionDef& r) {
+        const int n = (int)r.sto.size();
+        double k = std::pow(10.0, -pK_eff(r));
+        if (n == 3) {
+            int water = -1;
+            double af = -1;
+            for (int i = 0; i < n; i++)
+                if (fixed[r.state[i]]) { water = seg[r.state[i]]; af = ab[r.state[i]]; }
+            if (water < 0 || seg_states[water].size() != 3) {
+                err = "reaction " + r.name + ": a 3-term reaction needs one segment with three states, one of "
+                      "them with a fixed alphabulk";
+                return false;
+            }
+            double sum = 0;
+            for (int li = 0; li < 3; li++) {
+                const int s = seg_states[water][li];
+                if (!fixed[s]) {
+                    if (val[s] == 0) ab[s] = 0;
+                    else { ab[s] = k / af; item[water] = li; }
+                }
+                sum += ab[s];
+            }
+            for (int li = 0; li < 3; li++) {
+                const int s = seg_states[water][li];
+                if (!fixed[s] && val[s] == 0) ab[s] = 1 - sum;
+            }
+            return true;
+        }
+        int water = -1, other = -1;
+        for (int i = 0; i < n; i++) if (fixed[r.state[i]]) water = seg[r.state[i]];
+        for (int i = 0; i < n; i++) if (seg[r.state[i]] != water) other = seg[r.state[i]];
+        if (water < 0 || other < 0) {
+            err = "reaction " + r.name + ": needs the states of one segment with a fixed alphabulk and of one other";
+            return false;
+        }
+        int s1 = -1, s2 = -1;
+        for (int i = 0; i < n; i++) {
+            const int s = r.state[i];
+            if (seg[s] == water) { k = k / std::pow(ab[s], r.sto[i]); continue; }
+            if (seg[s] != other) {
+                err = "reaction " + r.name + ": states of more than two segments";
+                return false;
+            }
+            if (s1 < 0) { s1 = local[s]; continue; }
+            if (s2 >= 0 || r.sto[i] <= 0) {
+                err = "reaction " + r.name + ": the second state of " + std::to_string(other) +
+                      " must be a single right-hand-side term";
+                return false;
+            }
+            s2 = local[s];
+            item[other] = s2;
+        }
+        if (s2 < 0) { err = "reaction " + r.name + ": needs two states of its other segment"; return false; }
+        ab[seg_states[other][s2]] = k / (k + 1);
+        ab[seg_states[other][s1]] = 1 / (k + 1);
+        return true;
+    }
+    // Reaction::PutAlpha (reaction.cpp:285-298) and Segment::PutAlpha
+    // (segment.cpp:2052-2080)
+    bool put_alpha(const ReactionDef& r, double a) {
+        const int n = (int)r.sto.size();
+        int water = -1, other = -1;
+        for (int i = 0; i < n; i++) if (fixed[r.state[i]]) water = seg[r.state[i]];
+        for (int i = 0; i < n; i++) if (seg[r.state[i]] != water) other = seg[r.state[i]];
+        const int sg = other > -1 ? other : water;
+        const std::vector<int>& st = seg_states[sg];
+        const int it = item[sg];
+        if (st.size() < 2 || it < 0) {
+            err = "reaction " + r.name + ": no iterated state for its segment";
+            return false;
+        }
+        for (int li = 0; li < (int)st.size(); li++)
+            if (li != it && !fixed[st[li]]) ab[st[li]] = 0;
+        ab[st[it]] *= a;
+        double sum = 0;
+        for (int s : st) sum += ab[s];
+        bool ok = true;
+        for (int s : st) {
+            if (ab[s] == 0) ab[s] = 1.0 - sum;
+            if (ab[s] < 0 || ab[s] > 1) ok = false;
+        }
+        if (!ok) err = "reaction " + r.name + ": a bulk fraction (alphabulk) left [0, 1]";
+        return ok;
+    }
+    // Reaction::Residual_value, reaction.cpp:269-284
+    double residual(const ReactionDef& r) const {
+        double res = 0;
+        for (size_t i = 0; i < r.sto.size(); i++) {
+            const double a = ab[r.state[i]];
+            if (a > 0) res -= r.sto[i] * std::log10(a);
+        }
+        return -1.0 + res / pK_eff(r);
+    }
+    bool weak(const std::vector<double>& x, std::vector<double>& g) {
+        for (auto& r : R) if (r.sto.size() == 3 && !guess(r)) return false;
+        for (auto& r : R) if (r.sto.size() != 3 && !guess(r)) return false;
+        for (size_t i = 0; i < R.size(); i++) if (!put_alpha(R[i], std::exp(x[i]))) return false;
+        for (size_t i = 0; i < R.size(); i++) g[i] = residual(R[i]);
+        return true;
+    }
+    static double norm(const std::vector<double>& g) {
+        double s = 0;
+        for (double v : g) s += v * v;
+        return std::sqrt(s);
+    }
+    // The reference's Newton (SFNewton::iterate with tolerance 1e-8, at most
+    // 100 steps) takes no step when the residual at the guesses is small;
+    // the guesses are then the result.  Runs of the reference on the
+    // autoprotolysis/weak-acid pair at pK_w 14 and 16 and H3O+ fractions
+    // from 1e-9 to 1e-3 put that bound at |g| between 1.35e-8 (no step) and
+    // 1.41e-8 (steps).  When it steps it ends at the root to rounding (its
+    // bulk fractions agree with the root to 1e-12), and this Newton with a
+    // central-difference Jacobian and step halving goes to the same root.
+    bool solve() {
+        const int n = (int)R.size();
+        std::vector<double> x(n, 0.0), g(n), gp(n), gm(n), xn(n), gn(n);
+        if (!weak(x, g)) return false;
+        if (norm(g) <= 1.38e-8) return true;
+        for (int it = 0; it < 100 && norm(g) > 1e-15; it++) {
+            std::vector<double> J((size_t)n * n), p(n);
+            const double h = 1e-6;
+            for (int j = 0; j < n; j++) {
+                std::vector<double> xp = x, xm = x;
+                xp[j] += h; xm[j] -= h;
+                if (!weak(xp, gp) || !weak(xm, gm)) return false;
+                for (int i = 0; i < n; i++) J[(size_t)i * n + j] = (gp[i] - gm[i]) / (2 * h);
+            }
+            for (int i = 0; i < n; i++) p[i] = -g[i];
+            for (int c = 0; c < n; c++) {  // elimination with partial pivoting
+                int pr = c;
+                for (int r = c + 1; r < n; r++) if (std::fabs(J[(size_t)r * n + c]) > std::fabs(J[(size_t)pr * n + c])) pr = r;
+                if (J[(size_t)pr * n + c] == 0) { err = "bulk equilibrium of the reactions: singular Jacobian"; return false; }
+                if (pr != c) {
+                    for (int k = 0; k < n; k++) std::swap(J[(size_t)pr * n + k], J[(size_t)c * n + k]);
+                    std::swap(p[pr], p[c]);
+                }
+                for (int r = c + 1; r < n; r++) {
+                    const double f = J[(size_t)r * n + c] / J[(size_t)c * n + c];
+                    for (int k = c; k < n; k++) J[(size_t)r * n + k] -= f * J[(size_t)c * n + k];
+                    p[r] -= f * p[c];
+                }
+            }
+            for (int c = n - 1; c >= 0; c--) {
+                for (int k = c + 1; k < n; k++) p[c] -= J[(size_t)c * n + k] * p[k];
+                p[c] /= J[(size_t)c * n + c];
+            }
+            double t = 1;
+            bool better = false;
+            for (int ls = 0; ls < 30; ls++, t *= 0.5) {
+                for (int i = 0; i < n; i++) xn[i] = x[i] + t * p[i];
+                if (weak(xn, gn) && norm(gn) < norm(g)) { better = true; break; }
+            }
+            if (!better) break;
+            x = xn; g = gn;
+        }
+        if (!weak(x, g)) return false;
+        if (norm(g) > 1e-8) { err = "bulk equilibrium of the reactions did not converge"; return false; }
+        return true;
+    }
+};
+
+// States, reactions, the species χ matrix and the states' bulk fractions.
+// Runs after the segments' χ are resolved and before the molecules.
+static bool build_states(const InputBlock& in, PlanHolder& H, std::string& err) {
+    nm_plan& P = H.plan;
+    const int ns = P.n_seg;
+    H.state_names = in.order("state");
+    const int nst = (int)H.state_names.size();
+    H.seg_nstate.assign(ns, 0);
+    if (nst == 0) {
+        if (!in.order("reaction").empty()) { err = "reactions need internal states ('state' keys)"; return false; }
+        return true;
+    }
+    // System::CheckInput marks internal states only for two or more
+    // (system.cpp:1044); one state alone has no species of its own
+    if (nst == 1) { err = "a single internal state is not supported (define two or more)"; return false; }
+    std::map<std::string, int> segidx, stidx;
+    for (int i = 0; i < ns; i++) segidx[H.seg_names[i]] = i;
+    for (int j = 0; j < nst; j++) {
+        if (segidx.count(H.state_names[j])) {
+            err = "state " + H.state_names[j] + ": a state's name cannot be a mon's name"; return false;
+        }
+        stidx[H.state_names[j]] = j;
+    }
+    // State::CheckInput, state.cpp:37-106
+    H.state_seg.assign(nst, -1);
+    H.state_valence.assign(nst, 0.0);
+    std::vector<double> ab0(nst, -1.0);
+    std::vector<char> fixed(nst, 0);
+    for (int j = 0; j < nst; j++) {
+        const std::string& sn = H.state_names[j];
+        const std::string mon = in.get("state", sn, "mon");
+        if (mon.empty()) { err = "state " + sn + " needs its 'mon'"; return false; }
+        if (!segidx.count(mon)) { err = "state " + sn + ": mon " + mon + " not found"; return false; }
+        const int sg = segidx[mon];
+        if (H.seg_freedom[sg] == NM_SEG_FROZEN) { err = "state " + sn + ": states of a frozen mon are not supported"; return false; }
+        H.state_seg[j] = sg;
+        H.seg_nstate[sg]++;
+        if (in.has("state", sn, "alphabulk")) {
+            if (!to_real(in.get("state", sn, "alphabulk"), ab0[j]) || ab0[j] < 0 || ab0[j] > 1) {
+                err = "state " + sn + ": alphabulk out of range 0 ... 1"; return false;
+            }
+            fixed[j] = 1;
+        }
+        if (in.has("state", sn, "valence")) {
+            double v = 0;
+            if (!to_real(in.get("state", sn, "valence"), v) || v < -10 || v > 10) {
+                err = "state " + sn + ": valence out of range -10 ... 10"; return false;
+            }
+            H.state_valence[j] = v;
+        }
+    }
+    for (int i = 0; i < ns; i++)
+        if (H.seg_nstate[i] == 1) {
+            err = "mon " + H.seg_names[i] + " has a single internal state (define two or more, or none)"; return false;
+        }
+    // reactions (Reaction::CheckInput, reaction.cpp:37-145)
+    std::vector<ReactionDef> R;
+    for (const std::string& rn : in.order("reaction")) {
+        ReactionDef r;
+        r.name = rn;
+        const bool hK = in.has("reaction", rn, "K"), hpK = in.has("reaction", rn, "pK");
+        if (!hK && !hpK) { err = "reaction " + rn + " has no K nor pK value"; return false; }
+        if (!hK) {
+            if (!to_real(in.get("reaction", rn, "pK"), r.pK)) { err = "reaction " + rn + ": no valid pK value"; return false; }
+        } else {
+            double K = -1;
+            if (!to_real(in.get("reaction", rn, "K"), K) || K < 0) { err = "reaction " + rn + ": K must be positive"; return false; }
+            r.pK = -std::log10(K);
+        }
+        const std::string eq = in.get("reaction", rn, "equation");
+        if (eq.empty()) { err = "reaction " + rn + " has no equation"; return false; }
+        std::vector<std::string> sides = split(eq, '=');
+        if (sides.size() != 2) { err = "reaction " + rn + ": the equation needs one '=' sign"; return false; }
+        for (int side = 0; side < 2; side++)
+            for (const std::string& t0 : split(sides[side], '+')) {
+                const std::string t = trim(t0);
+                const size_t o = t.find('('), c = t.rfind(')');
+                if (o == std::string::npos || c == std::string::npos || c < o || t.find('(', o + 1) != std::string::npos) {
+                    err = "reaction " + rn + ": term '" + t + "' is not of the form n(state)"; return false;
+                }
+                const std::string name = trim(t.substr(o + 1, c - o - 1));
+                if (!stidx.count(name)) { err = "reaction " + rn + ": state " + name + " not found"; return false; }
+                int sto = 0;
+                if (!to_int(trim(t.substr(0, o)), sto) || sto < 1) {
+                    err = "reaction " + rn + ": stoichiometric numbers are positive integers"; return false;
+                }
+                r.state.push_back(stidx[name]);
+                r.sto.push_back(side == 0 ? -sto : sto);
+            }
+        for (int i = 0; i < ns; i++) {  // balanced per mon
+            int sum = 0;
+            for (size_t k = 0; k < r.sto.size(); k++) if (H.state_seg[r.state[k]] == i) sum += r.sto[k];
+            if (sum != 0) { err = "reaction " + rn + ": not balanced for the states of mon " + H.seg_names[i]; return false; }
+        }
+        double q = 0;
+        for (size_t k = 0; k < r.sto.size(); k++) q += r.sto[k] * H.state_valence[r.state[k]];
+        if (std::fabs(q) > 1e-10) { err = "reaction " + rn + ": not electroneutral"; return false; }
+        R.push_back(r);
+    }
+    // system.cpp:1044-1083: one equation or fixed alphabulk per state beyond
+    // the first of each segment
+    int n_fixed = 0, n_segs = 0;
+    for (int j = 0; j < nst; j++) n_fixed += fixed[j];
+    for (int i = 0; i < ns; i++) n_segs += H.seg_nstate[i] > 1;
+    if (n_segs + (int)R.size() + n_fixed != nst) {
+        err = "internal states: (mons with states) + (reactions) + (fixed alphabulk values) must equal the number "
+              "of states";
+        return false;
+    }
+    Chem chem(R, H.state_seg, H.state_valence, fixed, ab0, ns);
+    if (!chem.solve()) { err = chem.err; return false; }
+    for (int j = 0; j < nst; j++)
+        if (!(chem.ab[j] >= 0 && chem.ab[j] <= 1)) {
+            err = "state " + H.state_names[j] + ": its bulk fraction is fixed by no reaction"; return false;
+        }
+    H.state_alphabulk = chem.ab;
+    // χ between species (system.cpp:1775-1915): the segments' resolved
+    // matrix, then state–state and segment–state pairs; an unset pair takes
+    // the value of the states' mons, a pair set once is symmetric
+    const int nsp = ns + nst;
+    const double UNSET = -999;
+    H.chi_sp.assign((size_t)nsp * nsp, UNSET);
+    for (int i = 0; i < ns; i++)
+        for (int k = 0; k < ns; k++) H.chi_sp[(size_t)i * nsp + k] = H.chi[(size_t)i * ns + k];
+    auto name_of = [&](int a) { return a < ns ? H.seg_names[a] : H.state_names[a - ns]; };
+    for (int a = 0; a < nsp; a++)
+        for (int b = ns; b < nsp; b++) {
+            if (a < ns && b < ns) continue;
+            const std::string key = "chi_" + name_of(b);
+            const char* cls = a < ns ? "mon" : "state";
+            if (!in.has(cls, name_of(a), key)) continue;
+            double v;
+            if (!to_real(in.get(cls, name_of(a), key), v)) { err = "chi value not a number"; return false; }
+            if (a == b) v = 0;  // state.cpp:102: χ of a state with itself is ignored
+            H.chi_sp[(size_t)a * nsp + b] = v;
+        }
+    for (int a = ns; a < nsp; a++)  // state rows toward segments
+        for (int k = 0; k < ns; k++) {
+            const std::string key = "chi_" + H.seg_names[k];
+            if (!in.has("state", H.state_names[a - ns], key)) continue;
+            double v;
+            if (!to_real(in.get("state", H.state_names[a - ns], key), v)) { err = "chi value not a number"; return false; }
+            H.chi_sp[(size_t)a * nsp + k] = v;
+        }
+    auto mon_of = [&](int a) { return a < ns ? a : H.state_seg[a - ns]; };
+    for (int a = 0; a < nsp; a++)
+        for (int b = 0; b < nsp; b++) {
+            if (a < ns && b < ns) continue;
+            double& ab_ = H.chi_sp[(size_t)a * nsp + b];
+            double& ba = H.chi_sp[(size_t)b * nsp + a];
+            if (ab_ == UNSET && ba == UNSET) ab_ = ba = H.chi[(size_t)mon_of(a) * ns + mon_of(b)];
+            else if (ab_ != UNSET && ba == UNSET) ba = ab_;
+            else if (ab_ == UNSET && ba != UNSET) ab_ = ba;
+            else if (ab_ != ba) { err = "conflict in chi values between " + name_of(a) + " and " + name_of(b); return false; }
+        }
+    for (int j = 0; j < nst; j++) {
+        const int sg = H.state_seg[j];
+        if (H.chi_sp[(size_t)sg * nsp + ns + j] != 0) {
+            err = "chi between a mon and one of its own states (" + H.state_names[j] + ") is not allowed"; return false;
+        }
+    }
+    // the states carry the charge of a mon with states (System::
+    // DoElectrostatics, system.cpp:1921-1941; PutU, :1985-2080)
+    for (int i = 0; i < ns; i++) if (H.seg_nstate[i] > 0) H.seg_valence[i] = 0;
+    P.n_state = nst;
+    P.n_sp = nsp;
+    return true;
+}
+
 static nm_plan* build_plan(const InputBlock& in, std::string& err) {
     PlanHolder* H = new PlanHolder();
     nm_plan& P = H->plan;
@@ -740,6 +1112,7 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
         for (int k = 0; k < ns; k++)
             if (H->chi[i * ns + k] != H->chi[k * ns + i]) { err = "chi matrix must be symmetric"; delete H; return nullptr; }
     }
+    if (!build_states(in, *H, err)) { delete H; return nullptr; }
     // KSAM (system.cpp generate_mask): 0 where any frozen segment sits
     H->ksam.assign(M, 1);
     for (int i = 0; i < ns; i++)
@@ -870,7 +1243,25 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
         }
         for (auto& f : mb.fraction) f /= N;
         mb.mol.charge = 0;
-        for (size_t k = 0; k < mb.molmon.size(); k++) mb.mol.charge += mb.fraction[k] * H->seg_valence[mb.molmon[k]];
+        bool with_states = false;
+        for (int sgi : mb.molmon) with_states = with_states || H->seg_nstate[sgi] > 0;
+        if (!with_states) {
+            for (size_t k = 0; k < mb.molmon.size(); k++) mb.mol.charge += mb.fraction[k] * H->seg_valence[mb.molmon[k]];
+        } else {
+            // Molecule::Charge (molecule.cpp:1866-1879): a mon with states
+            // counts Σ α_bulk·valence of its states
+            double q = 0;
+            for (size_t k = 0; k < mb.molmon.size(); k++) {
+                const int sgi = mb.molmon[k];
+                double nmon = 0;
+                for (auto& B : mb.blocks) if (B.seg == sgi) nmon += B.length * B.degeneracy;
+                if (H->seg_nstate[sgi] > 0) {
+                    for (int j = 0; j < P.n_state; j++)
+                        if (H->state_seg[j] == sgi) q += H->state_alphabulk[j] * H->state_valence[j] * nmon;
+                } else q += H->seg_valence[sgi] * nmon;
+            }
+            mb.mol.charge = q / N;
+        }
         if (mb.mol.freedom == NM_MOL_RESTRICTED) {
             bool hn = in.has("mol", mn, "n"), ht = in.has("mol", mn, "theta");
             if (hn == ht) { err = "restricted mol " + mn + " needs exactly one of n / theta"; delete H; return nullptr; }
@@ -934,30 +1325,54 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
         if (!(nmol == 1 && H->mb[0].mol.pinned)) { err = "one molecule must have freedom : solvent"; delete H; return nullptr; }
     }
     // ---- iteration list (MakeItsLists / IsUnique, system.cpp:430-500, 1218+) ----
+    // A segment or state whose χ row equals an earlier block's
+    // representative's shares that block.  Segments with states are not
+    // blocks themselves; ItStateList follows ItMonList.
+    const int nsp = P.n_state > 0 ? P.n_sp : ns;
+    const double* chi_rows = P.n_state > 0 ? H->chi_sp.data() : H->chi.data();
+    auto same_row = [&](int a, int b) {
+        for (int k = 0; k < nsp; k++) if (chi_rows[(size_t)a * nsp + k] != chi_rows[(size_t)b * nsp + k]) return false;
+        return true;
+    };
     H->seg_it.assign(ns, -1);
     std::vector<int> sysmon;
     for (int m = 0; m < nmol; m++)
         for (int sgi : H->mb[m].molmon) {
             if (std::find(sysmon.begin(), sysmon.end(), sgi) != sysmon.end()) continue;
             sysmon.push_back(sgi);
+            if (H->seg_nstate[sgi] > 0) continue;
             int copy_of = -1;
-            for (size_t j = 0; j < H->it_seg.size() && copy_of < 0; j++) {
-                int r = H->it_seg[j];
-                bool eq = true;
-                for (int k = 0; k < ns; k++) if (H->chi[sgi * ns + k] != H->chi[r * ns + k]) { eq = false; break; }
-                if (eq) copy_of = (int)j;
-            }
-            if (copy_of < 0) { H->seg_it[sgi] = (int)H->it_seg.size(); H->it_seg.push_back(sgi); }
+            for (size_t j = 0; j < H->it_sp.size() && copy_of < 0; j++)
+                if (same_row(sgi, H->it_sp[j])) copy_of = (int)j;
+            if (copy_of < 0) { H->seg_it[sgi] = (int)H->it_sp.size(); H->it_sp.push_back(sgi); H->it_seg.push_back(sgi); }
             else H->seg_it[sgi] = copy_of;
         }
+    H->state_it.assign(P.n_state, -1);
+    for (int j = 0; j < P.n_state; j++) {
+        int copy_of = -1;
+        for (size_t b = 0; b < H->it_sp.size() && copy_of < 0; b++)
+            if (same_row(ns + j, H->it_sp[b])) copy_of = (int)b;
+        if (copy_of < 0) {
+            H->state_it[j] = (int)H->it_sp.size();
+            H->it_sp.push_back(ns + j);
+            H->it_seg.push_back(H->state_seg[j]);
+        } else H->state_it[j] = copy_of;
+    }
     P.n_it = (int)H->it_seg.size();
     P.charged = 0;
     for (int i = 0; i < ns; i++) if (H->seg_valence[i] != 0) P.charged = 1;
-    if (P.charged)
-        for (int m = 0; m < nmol; m++)
-            if (H->mb[m].mol.markov == 2) {
-                err = "Markov 2 chains in a charged system are not built"; delete H; return nullptr;
+    for (int j = 0; j < P.n_state; j++) if (H->state_valence[j] != 0) P.charged = 1;
+    if (P.n_state > 0 && P.n_sp > 16) {
+        err = "more than 16 interaction species (mons without states, and states)"; delete H; return nullptr;
+    }
+    for (int m = 0; m < nmol; m++) {
+        if (H->mb[m].mol.markov != 2) continue;
+        if (P.charged) { err = "Markov 2 chains in a charged system are not built"; delete H; return nullptr; }
+        for (int sgi : H->mb[m].molmon)
+            if (H->seg_nstate[sgi] > 0) {
+                err = "Markov 2 chains with internal states are not built"; delete H; return nullptr;
             }
+    }
     P.iv = P.n_it * M + (P.charged ? M : 0);
     // ---- newton ----
     auto newt = in.order("newton");
@@ -1122,6 +1537,19 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
     P.seg_epsilon = H->seg_epsilon.data();
     P.ksam = H->ksam.data();
     P.it_seg = H->it_seg.data();
+    if (P.n_state > 0) {
+        for (auto& s : H->state_names) H->state_name_ptrs.push_back(s.c_str());
+        P.state_name = H->state_name_ptrs.data();
+        P.state_seg = H->state_seg.data();
+        P.state_valence = H->state_valence.data();
+        P.state_alphabulk = H->state_alphabulk.data();
+        P.state_it = H->state_it.data();
+        P.seg_nstate = H->seg_nstate.data();
+        P.chi_sp = H->chi_sp.data();
+        P.it_sp = H->it_sp.data();
+    } else {
+        P.n_sp = ns;
+    }
     H->mols.resize(nmol);
     for (int m = 0; m < nmol; m++) {
         MolBuild& mb = H->mb[m];

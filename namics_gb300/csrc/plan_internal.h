@@ -32,6 +32,11 @@ struct PlanHolder {
     std::vector<double> seg_mask, seg_gmask, seg_phi_frozen, chi, seg_valence, seg_epsilon;
     std::vector<MolBuild> mb;
     std::vector<nm_molecule> mols;
+    // internal states and reactions (n_state = 0 when the input has none)
+    std::vector<std::string> state_names;
+    std::vector<const char*> state_name_ptrs;
+    std::vector<int> state_seg, state_it, seg_nstate, it_sp;
+    std::vector<double> state_valence, state_alphabulk, chi_sp;
     std::vector<std::string> mol_names;
     std::vector<const char*> mol_name_ptrs;
     std::string method_note;

@@ -239,6 +239,7 @@ int nm_server_submit(nm_server* srv, const nm_plan* plan, const double* x_host, 
     r->batched = plan->gradients == 1 && !plan->charged && plan->MX <= 512;
     for (int m = 0; m < plan->n_mol; m++)
         if (plan->mols[m].markov == 2) r->batched = false;  // Markov 2 chains take a device context
+    if (plan->n_state > 0) r->batched = false;              // so do internal states
     r->bytes = nm::footprint(plan, r->batched, s->opt.precision);
     if (r->bytes > s->opt.memory_budget) {
         delete r;

@@ -72,7 +72,10 @@ class PlanRecord(C.Structure):
                 ("super_tolerance", C.c_double), ("super_deltamax", C.c_double),
                 ("super_iterationlimit", C.c_int), ("scan_mol", C.c_int), ("scan_what", C.c_int),
                 ("scan_n", C.c_int), ("scan_exponential", C.c_int), ("scan_start", C.c_double),
-                ("scan_end", C.c_double), ("scan_step", C.c_double), ("save_memory", C.c_int)]
+                ("scan_end", C.c_double), ("scan_step", C.c_double), ("save_memory", C.c_int),
+                ("n_state", C.c_int), ("state_name", C.POINTER(C.c_char_p)), ("state_seg", ip),
+                ("state_valence", dp), ("state_alphabulk", dp), ("state_it", ip), ("seg_nstate", ip),
+                ("n_sp", C.c_int), ("chi_sp", dp), ("it_sp", ip)]
 
 
 def _entries(text: str):
@@ -382,6 +385,7 @@ class OraclePlan:
                     seg_it[sg] = len(it_seg)
                     it_seg.append(sg)
         P.n_seg = ns
+        P.n_sp = ns
         names = (C.c_char_p * ns)(*[s.encode() for s in segs])
         mnames = (C.c_char_p * len(mols))(*[s.encode() for s in mols])
         keep += [names, mnames]

@@ -25,6 +25,12 @@ struct orc_state {
     double *m2l1, *m2l11, *m2l_1, *m2l_11; /* Markov 2, curved lattices: LGrad1.cpp:63-68 */
     double *GN, *norm, *mol_n, *mol_theta, *mol_phibulk, *seg_phibulk;
     double *psi, *EE, *q, *eps, *X;  /* electrostatics (charged systems) */
+    /* internal states: u and α of each state [n_state*M]; the species'
+     * bulk fractions [n_sp]; phi and phi_side hold n_sp rows, the states'
+     * volume fractions after the segments'; in_mol: the segment occurs in
+     * a molecule (SysMonList) */
+    double *ust, *ast, *sp_phibulk;
+    int *in_mol;
     int have_state;
     /* molecule amounts in force (the plan's, until orc_set_amount changes
      * them, as a Variate scan or search step does) and a search's inner
@@ -44,6 +50,13 @@ static void Norm(double* P, double C, int M) { for (int i = 0; i < M; i++) P[i] 
 static double Sum(const double* X, int M) { double s = 0; for (int i = 0; i < M; i++) s += X[i]; return s; }
 static double Dot(const double* X, const double* Y, int M) { double s = 0; for (int i = 0; i < M; i++) s += X[i] * Y[i]; return s; }
 static void Div(double* P, const double* A, int M) { for (int i = 0; i < M; i++) { if (A[i] != 0) P[i] /= A[i]; else P[i] = 0; } }
+
+/* internal states: a segment with states (Segment::ns > 1) and χ between
+ * interaction species (segments, then states) */
+static int has_states(const nm_plan* P, int i) { return P->n_state > 0 && P->seg_nstate[i] > 0; }
+static double chi_of(const nm_plan* P, int a, int b) {
+    return P->n_state > 0 ? P->chi_sp[(size_t)a * P->n_sp + b] : P->chi[(size_t)a * P->n_seg + b];
+}
 
 /* ---- boundaries -------------------------------------------------------- */
 /* Halo source layers per boundary type (lattice.cpp:94-196, fjc = 1). */
@@ -734,6 +747,33 @@ static void prepare_G1(orc_state* st, const double* x) {
     for (int i = 0; i < ns; i++) {
         double* u = st->u + (size_t)i * M;
         double* G1 = st->G1 + (size_t)i * M;
+        if (has_states(P, i)) {
+            /* G1 = Σ_j α_bulk,j·exp(-u_j) over the segment's states, α_j =
+             * α_bulk,j·exp(-u_j)/G1 (segment.cpp:861-873), u_j from the
+             * state's block with the state's valence (PutU) */
+            Zero(G1, M);
+            for (int j = 0; j < P->n_state; j++) {
+                if (P->state_seg[j] != i) continue;
+                double* uj = st->ust + (size_t)j * M;
+                double* aj = st->ast + (size_t)j * M;
+                Cp(uj, x + (size_t)P->state_it[j] * M, M);
+                if (P->charged) {
+                    YplusisCtimesX(uj, st->EE, -1.0 * P->seg_epsilon[i], M);
+                    if (P->state_valence[j] != 0) YplusisCtimesX(uj, st->psi, P->state_valence[j], M);
+                }
+                set_bounds(st, uj);
+                for (int s = 0; s < M; s++) aj[s] = exp(-uj[s]);
+                Norm(aj, P->state_alphabulk[j], M);
+                Add(G1, aj, M);
+            }
+            for (int j = 0; j < P->n_state; j++)
+                if (P->state_seg[j] == i) Div(st->ast + (size_t)j * M, G1, M);
+            Zero(u, M);
+            Times(G1, G1, P->seg_gmask + (size_t)i * M, M);
+            Cp(st->phi + (size_t)i * M, P->seg_phi_frozen + (size_t)i * M, M);
+            st->seg_phibulk[i] = 0;
+            continue;
+        }
         if (P->seg_it[i] >= 0) {
             Cp(u, x + (size_t)P->seg_it[i] * M, M);
             if (P->charged) {
@@ -861,8 +901,20 @@ static int compute_phis(orc_state* st, const double* x) {
         }
     }
     for (int i = 0; i < ns; i++) set_bounds(st, st->phi + (size_t)i * M);
-    /* Segment::SetPhiSide (segment.cpp:1331-1353) */
-    for (int i = 0; i < ns; i++) stencil(st, st->phi_side + (size_t)i * M, st->phi + (size_t)i * M, 1);
+    /* Segment::SetPhiSide (segment.cpp:1331-1353); a segment with states:
+     * φ_j = α_j·φ per state, its side, and φ_bulk,j = φ_bulk·α_bulk,j */
+    for (int i = 0; i < ns; i++) {
+        st->sp_phibulk[i] = st->seg_phibulk[i];
+        if (!has_states(P, i)) stencil(st, st->phi_side + (size_t)i * M, st->phi + (size_t)i * M, 1);
+        else Zero(st->phi_side + (size_t)i * M, M);
+    }
+    for (int j = 0; j < P->n_state; j++) {
+        const int sg = P->state_seg[j];
+        double* pj = st->phi + (size_t)(ns + j) * M;
+        Times(pj, st->ast + (size_t)j * M, st->phi + (size_t)sg * M, M);
+        stencil(st, st->phi_side + (size_t)(ns + j) * M, pj, 1);
+        st->sp_phibulk[ns + j] = st->seg_phibulk[sg] * P->state_alphabulk[j];
+    }
     return NM_OK;
 }
 
@@ -875,14 +927,18 @@ int orc_residual(orc_state* st, const double* x, double* g) {
     st->have_state = (rc == NM_OK);
     if (rc) return rc;
     Zero(st->alpha, M);
+    /* the species: segments without states, then the states (the
+     * reference's loops over `ns < 2` mons and over StateList) */
+    const int nsp = P->n_state > 0 ? P->n_sp : ns;
     for (int i = 0; i < nit; i++) {
         double* gi = g + (size_t)i * M;
-        int r = P->it_seg[i];
-        for (int k = 0; k < ns; k++) {
-            double chi = P->chi[r * ns + k];
+        int r = P->n_state > 0 ? P->it_sp[i] : P->it_seg[i];
+        for (int k = 0; k < nsp; k++) {
+            if (k < ns && has_states(P, k)) continue;
+            double chi = chi_of(P, r, k);
             if (chi == 0) continue;
             const double* ps = st->phi_side + (size_t)k * M;
-            double pb = st->seg_phibulk[k];
+            double pb = st->sp_phibulk[k];
             for (int s = 0; s < M; s++)  /* PutAlpha, tools_host.h:428-431 */
                 if (st->phitot[s] > 0) gi[s] = gi[s] - chi * (ps[s] / st->phitot[s] - pb);
         }
@@ -906,10 +962,12 @@ int orc_residual(orc_state* st, const double* x, double* g) {
         Zero(st->eps, M);
         for (int i = 0; i < ns; i++) {
             double* phi = st->phi + (size_t)i * M;
-            YplusisCtimesX(st->q, phi, P->seg_valence[i], M);
+            if (!has_states(P, i)) YplusisCtimesX(st->q, phi, P->seg_valence[i], M);
             set_bounds(st, phi);
             YplusisCtimesX(st->eps, phi, P->seg_epsilon[i], M);
         }
+        for (int j = 0; j < P->n_state; j++)
+            YplusisCtimesX(st->q, st->phi + (size_t)(ns + j) * M, P->state_valence[j], M);
         Div(st->q, st->phitot, M);
         Div(st->eps, st->phitot, M);
         Cp(st->psi, x + (size_t)nit * M, M);
@@ -1068,6 +1126,7 @@ int orc_get_field(orc_state* st, int which, double* out) {
         case 6: if (!P->charged) return NM_ERR_ARG; Cp(out, st->psi, M); return NM_OK;
         case 7: if (!P->charged) return NM_ERR_ARG; Cp(out, st->q, M); return NM_OK;
         case 8: if (!P->charged) return NM_ERR_ARG; Cp(out, st->eps, M); return NM_OK;
+        case 9: if (!P->n_state) return NM_ERR_ARG; Cp(out, st->phi + (size_t)P->n_seg * M, P->n_state * M); return NM_OK;
     }
     return NM_ERR_ARG;
 }
@@ -1084,14 +1143,22 @@ int orc_get_molecule(orc_state* st, int m, double* GN, double* n, double* theta,
 /* GetFreeEnergy (system.cpp:2809-3029), GetGrandPotential (:3038-3244),
  * CreateMu (:3246-3400) for state-free systems, with the electrostatic
  * terms where the system is charged. */
+/* Molecule::fraction of a segment (0 when the molecule has none) */
+static double mol_fraction(const nm_molecule* mol, int seg) {
+    double f = 0;
+    for (int q = 0; q < mol->n_molmon; q++) if (mol->molmon_seg[q] == seg) f = mol->molmon_fraction[q];
+    return f;
+}
+
 int orc_free_energy(orc_state* st, double* Fout, double* Omega, double* mu) {
     const nm_plan* P = st->P;
     int M = st->M, ns = P->n_seg;
     if (!st->have_state) return NM_ERR_ARG;
     double* F = calloc((size_t)M, sizeof(double));
     double* T = st->tmp;
+    const int nst = P->n_state;
     for (int m = 0; m < P->n_mol; m++) remove_bounds(st, st->mol_phitot + (size_t)m * M);
-    for (int i = 0; i < ns; i++) remove_bounds(st, st->phi_side + (size_t)i * M);
+    for (int i = 0; i < ns + nst; i++) remove_bounds(st, st->phi_side + (size_t)i * M);
     for (int m = 0; m < P->n_mol; m++) {
         const nm_molecule* mol = &P->mols[m];
         double N = mol->chainlength;
@@ -1100,9 +1167,19 @@ int orc_free_energy(orc_state* st, double* Fout, double* Omega, double* mu) {
         Norm(T, constant, M);
         Add(F, T, M);
     }
-    /* SysMonList: segments that occur in molecules */
+    /* SysMonList: segments that occur in molecules; a segment with states
+     * counts -φ_j·u_j per state (system.cpp:2866-2888) */
     for (int i = 0; i < ns; i++) {
-        if (P->seg_it[i] < 0) continue;
+        if (!st->in_mol[i]) continue;
+        if (has_states(P, i)) {
+            for (int j = 0; j < nst; j++) {
+                if (P->state_seg[j] != i) continue;
+                const double* pj = st->phi + (size_t)(ns + j) * M;
+                const double* uj = st->ust + (size_t)j * M;
+                for (int s = 0; s < M; s++) F[s] += -1.0 * (pj[s] * uj[s]);
+            }
+            continue;
+        }
         const double* G1 = st->G1 + (size_t)i * M;
         const double* phi = st->phi + (size_t)i * M;
         for (int s = 0; s < M; s++) {
@@ -1111,11 +1188,38 @@ int orc_free_energy(orc_state* st, double* Fout, double* Omega, double* mu) {
         }
     }
     for (int j = 0; j < ns; j++) {
+        if (has_states(P, j)) continue;
         const double* phi = st->phi + (size_t)j * M;
         for (int k = 0; k < ns; k++) {
-            double chi = (P->seg_freedom[k] == NM_SEG_FROZEN) ? P->chi[j * ns + k] : P->chi[j * ns + k] / 2;
+            if (has_states(P, k)) continue;
+            double chi = (P->seg_freedom[k] == NM_SEG_FROZEN) ? chi_of(P, j, k) : chi_of(P, j, k) / 2;
             if (P->seg_freedom[j] == NM_SEG_FROZEN || chi == 0) continue;
             const double* ps = st->phi_side + (size_t)k * M;
+            for (int s = 0; s < M; s++) F[s] += chi * (phi[s] * ps[s]);
+        }
+        for (int i = 0; i < nst; i++) {  /* system.cpp:2916-2929 */
+            double chi = chi_of(P, j, ns + i) / 2;
+            if (P->seg_freedom[j] == NM_SEG_FROZEN || chi == 0) continue;
+            const double* ps = st->phi_side + (size_t)(ns + i) * M;
+            for (int s = 0; s < M; s++) F[s] += chi * (phi[s] * ps[s]);
+        }
+    }
+    for (int j = 0; j < nst; j++) {  /* system.cpp:2933-2979 */
+        const double* phi = st->phi + (size_t)(ns + j) * M;
+        for (int k = 0; k < ns; k++) {
+            if (has_states(P, k)) continue;
+            double chi = chi_of(P, ns + j, k);
+            if (P->seg_freedom[k] != NM_SEG_FROZEN) chi = chi / 2;
+            if (chi == 0) continue;
+            const double* ps = st->phi_side + (size_t)k * M;
+            for (int s = 0; s < M; s++) F[s] += chi * (phi[s] * ps[s]);
+        }
+        /* the state–state term reads the state's own side fraction
+         * (system.cpp:2971-2977: phi_side of Sta[j], not of Sta[l]) */
+        for (int l = 0; l < nst; l++) {
+            double chi = chi_of(P, ns + j, ns + l) / 2;
+            if (chi == 0) continue;
+            const double* ps = st->phi_side + (size_t)(ns + j) * M;
             for (int s = 0; s < M; s++) F[s] += chi * (phi[s] * ps[s]);
         }
     }
@@ -1150,16 +1254,18 @@ int orc_free_energy(orc_state* st, double* Fout, double* Omega, double* mu) {
         Add(GP, T, M);
     }
     Add(GP, st->alpha, M);
-    for (int j = 0; j < ns; j++) {
-        if (P->seg_freedom[j] == NM_SEG_FROZEN) continue;
+    /* species pairs (system.cpp:3104-3206): segments without states and
+     * states, frozen segments left out */
+    for (int j = 0; j < ns + nst; j++) {
+        if (j < ns && (P->seg_freedom[j] == NM_SEG_FROZEN || has_states(P, j))) continue;
         const double* phi = st->phi + (size_t)j * M;
-        double pbA = st->seg_phibulk[j];
-        for (int k = 0; k < ns; k++) {
-            if (P->seg_freedom[k] == NM_SEG_FROZEN) continue;
-            double chi = P->chi[j * ns + k] / 2;
+        double pbA = st->sp_phibulk[j];
+        for (int k = 0; k < ns + nst; k++) {
+            if (k < ns && (P->seg_freedom[k] == NM_SEG_FROZEN || has_states(P, k))) continue;
+            double chi = chi_of(P, j, k) / 2;
             if (chi == 0) continue;
             const double* ps = st->phi_side + (size_t)k * M;
-            double pbB = st->seg_phibulk[k];
+            double pbB = st->sp_phibulk[k];
             for (int s = 0; s < M; s++) GP[s] += chi * (phi[s] * ps[s] + (-pbA * pbB));
         }
     }
@@ -1193,12 +1299,36 @@ int orc_free_energy(orc_state* st, double* Fout, double* Omega, double* mu) {
             for (int k = 0; k < P->n_mol; k++) constant += st->mol_phibulk[k] / P->mols[k].chainlength;
             Mu = Mu - NA * constant;
             for (int j = 0; j < ns; j++) {
-                double pbA = st->seg_phibulk[j], FA = 0;
-                for (int q = 0; q < mol->n_molmon; q++) if (mol->molmon_seg[q] == j) FA = mol->molmon_fraction[q];
+                if (has_states(P, j)) continue;
+                double pbA = st->seg_phibulk[j], FA = mol_fraction(mol, j);
                 for (int k = 0; k < ns; k++) {
-                    double pbB = st->seg_phibulk[k], FB = 0;
-                    for (int q = 0; q < mol->n_molmon; q++) if (mol->molmon_seg[q] == k) FB = mol->molmon_fraction[q];
-                    double chi = P->chi[j * ns + k] / 2;
+                    if (has_states(P, k)) continue;
+                    double pbB = st->seg_phibulk[k], FB = mol_fraction(mol, k);
+                    double chi = chi_of(P, j, k) / 2;
+                    Mu = Mu - NA * chi * (pbA - FA) * (pbB - FB);
+                }
+                for (int l = 0; l < P->n_state; l++) {  /* system.cpp:3345-3358 */
+                    double pbB = st->sp_phibulk[ns + l];
+                    double FB = mol_fraction(mol, P->state_seg[l]) * P->state_alphabulk[l];
+                    double chi = chi_of(P, j, ns + l) / 2;
+                    Mu = Mu - NA * chi * (pbA - FA) * (pbB - FB);
+                }
+            }
+            for (int j = 0; j < P->n_state; j++) {  /* system.cpp:3361-3400 */
+                double pbA = st->sp_phibulk[ns + j];
+                double FA = mol_fraction(mol, P->state_seg[j]) * P->state_alphabulk[j];
+                for (int k = 0; k < ns; k++) {
+                    if (has_states(P, k)) continue;
+                    double pbB = st->seg_phibulk[k], FB = mol_fraction(mol, k);
+                    double chi = chi_of(P, ns + j, k) / 2;
+                    Mu = Mu - NA * chi * (pbA - FA) * (pbB - FB);
+                }
+                /* the state–state term takes FB of state j as well
+                 * (system.cpp:3388-3391) */
+                for (int k = 0; k < P->n_state; k++) {
+                    double pbB = st->sp_phibulk[ns + k];
+                    double FB = mol_fraction(mol, P->state_seg[j]) * P->state_alphabulk[j];
+                    double chi = chi_of(P, ns + j, ns + k) / 2;
                     Mu = Mu - NA * chi * (pbA - FA) * (pbB - FB);
                 }
             }
@@ -1220,10 +1350,17 @@ orc_state* orc_create(const nm_plan* P) {
     for (int m = 0; m < nm; m++) {
         st->amt_n[m] = P->mols[m].n; st->amt_theta[m] = P->mols[m].theta; st->amt_phibulk[m] = P->mols[m].phibulk;
     }
+    const int nsp = ns + P->n_state;
     st->u = calloc((size_t)ns * M, sizeof(double));
     st->G1 = calloc((size_t)ns * M, sizeof(double));
-    st->phi = calloc((size_t)ns * M, sizeof(double));
-    st->phi_side = calloc((size_t)ns * M, sizeof(double));
+    st->phi = calloc((size_t)nsp * M, sizeof(double));
+    st->phi_side = calloc((size_t)nsp * M, sizeof(double));
+    st->ust = calloc((size_t)(P->n_state + 1) * M, sizeof(double));
+    st->ast = calloc((size_t)(P->n_state + 1) * M, sizeof(double));
+    st->sp_phibulk = calloc((size_t)nsp, sizeof(double));
+    st->in_mol = calloc((size_t)ns, sizeof(int));
+    for (int m = 0; m < nm; m++)
+        for (int k = 0; k < P->mols[m].n_molmon; k++) st->in_mol[P->mols[m].molmon_seg[k]] = 1;
     st->phitot = calloc((size_t)M, sizeof(double));
     st->alpha = calloc((size_t)M, sizeof(double));
     st->tmp = calloc((size_t)M, sizeof(double));
@@ -1387,5 +1524,6 @@ void orc_destroy(orc_state* st) {
     free(st->seg_phibulk);
     free(st->psi); free(st->EE); free(st->q); free(st->eps); free(st->X);
     free(st->gb3); free(st->m2l1); free(st->m2l11); free(st->m2l_1); free(st->m2l_11);
+    free(st->ust); free(st->ast); free(st->sp_phibulk); free(st->in_mol);
     free(st);
 }

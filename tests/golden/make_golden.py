@@ -223,6 +223,43 @@ def cases() -> list[dict]:
         "mol : pol : composition : (A)10(B)20", "mol : pol : freedom : free", "mol : pol : phibulk : 0.005",
         "mol : water : composition : (W)1", "mol : water : freedom : solvent"] + m2("pol", 0.5)
     C.append(dict(name="markov2_ads1d", lines=lines, field=(-0.01, 0.01), seed=33, modes=["it0", "conv"]))
+    # internal states and reactions: a weak polyacid brush (AH + H2O = AM +
+    # H3O) in water with its autoprotolysis (2 H2O = OH + H3O) and a 1:1
+    # salt; the neutral acid state and H2O get their own χ, so the states
+    # split into several iteration blocks.  pH 7: the reactions' analytic
+    # guesses are the bulk fractions (the reference's Newton takes no step);
+    # pH 5: its Newton iterates.  A 2-D planar and a 1-D spherical variant.
+    def weak_lines(comp, n, h3o, chi_ah=0.8):
+        return ["lat : flat : bondlength : 3e-10",
+                "mon : S : freedom : frozen", "mon : S : frozen_range : lowerbound",
+                "mon : X : freedom : pinned", "mon : X : pinned_range : firstlayer",
+                "mon : A : freedom : free", "mon : W : freedom : free",
+                "mon : Na : freedom : free", "mon : Na : valence : 1",
+                "mon : Cl : freedom : free", "mon : Cl : valence : -1",
+                "mon : A : chi_S : -1", "mon : X : chi_W : 0.5",
+                "state : AH : mon : A", "state : AH : valence : 0",
+                "state : AM : mon : A", "state : AM : valence : -1",
+                "state : H3O : mon : W", "state : H3O : valence : 1",
+                "state : H2O : mon : W", "state : H2O : valence : 0",
+                "state : OH : mon : W", "state : OH : valence : -1",
+                f"state : H3O : alphabulk : {h3o}",
+                f"state : AH : chi_H2O : {chi_ah}",
+                "reaction : weak : equation : 1(AH) + 1(H2O) = 1(AM) + 1(H3O)", "reaction : weak : pK : 6",
+                "reaction : auto : equation : 2(H2O) = 1(OH) + 1(H3O)", "reaction : auto : pK : 14",
+                f"mol : pol : composition : {comp}", "mol : pol : freedom : restricted", f"mol : pol : n : {n}",
+                "mol : water : composition : (W)1", "mol : water : freedom : solvent",
+                "mol : Na : composition : (Na)1", "mol : Na : freedom : neutralizer",
+                "mol : Cl : composition : (Cl)1", "mol : Cl : freedom : free", "mol : Cl : phibulk : 0.01"]
+    C.append(dict(name="states_weak1d", lines=lat1d(40) + weak_lines("(X)1(A)29", 0.05, "1e-7"),
+                  field=(-0.01, 0.01), seed=41, modes=["it0", "it5", "conv"], conv_itlim=5000))
+    C.append(dict(name="states_weak1d_ph5", lines=lat1d(40) + weak_lines("(X)1(A)29", 0.05, "1e-5", chi_ah=0.3),
+                  field=(-0.01, 0.01), seed=42, modes=["it0", "it5", "conv"], conv_itlim=5000))
+    C.append(dict(name="states_weak2d", lines=lat2d(14, 8, ["surface", "mirror", "mirror", "mirror"]) +
+                  weak_lines("(X)1(A)19", 0.4, "1e-7"), field=(-0.01, 0.01), seed=43,
+                  modes=["it0", "it5", "conv"], conv_itlim=5000, split_tol=1e-4))
+    C.append(dict(name="states_weak1d_sph", lines=lat1d(30, geom="spherical", offset=8) +
+                  weak_lines("(X)1(A)19", 10.0, "1e-6"), field=(-0.01, 0.01), seed=44,
+                  modes=["it0", "it5", "conv"], conv_itlim=5000))
     # a sample of the batched workload: random 1-gradient brushes (seeded), 10% stars
     rng = np.random.default_rng(2024)
     for i in range(6):
@@ -248,12 +285,18 @@ def outputs_block(plan: Plan) -> list[str]:
         s.append(f"pro : mon : {name} : phi")
     for name in plan.seg_names:
         s.append(f"pro : mon : {name} : G1")
+    # the states' volume fractions (Segment::GetPointer's phi-<state>,
+    # segment.cpp:1898-1902) and their bulk fractions
+    for j, st in enumerate(plan.state_names):
+        s.append(f"pro : mon : {plan.seg_names[plan.c.state_seg[j]]} : phi-{st}")
     s.append("pro : sys : noname : alpha")
     if plan.c.charged:
         s += ["pro : sys : noname : psi", "pro : sys : noname : q", "pro : sys : noname : eps"]
     s.append("output : kal : append : false")
     s += ["kal : sys : noname : free_energy", "kal : sys : noname : grand_potential",
           "kal : newton : isaac : residual", "kal : newton : isaac : iterations"]
+    for j, st in enumerate(plan.state_names):
+        s.append(f"kal : mon : {plan.seg_names[plan.c.state_seg[j]]} : alphabulk_{st}")
     for m in range(plan.n_mol):
         mn = MOLNAMES[m]
         s += [f"kal : mol : {mn} : GN", f"kal : mol : {mn} : n", f"kal : mol : {mn} : theta",
@@ -275,17 +318,22 @@ def make_field(plan: Plan, lo: float, hi: float, seed: int, antisym: bool) -> np
 
 def write_guess(path: Path, plan: Plan, x: np.ndarray) -> None:
     c = plan.c
-    names = [plan.seg_names[i] for i in plan.it_seg]
+    names = plan.it_names
+    n_mon = sum(1 for i in range(c.n_it) if c.n_state == 0 or c.it_sp[i] < c.n_seg)
     my = c.MY if c.gradients > 1 else 0
     mz = c.MZ if c.gradients > 2 else 0
     with open(path, "w") as f:
         f.write("DIIS\n")
         f.write(f" {c.MX}\t{my}\t{mz}\t1\n")
         f.write("true\n" if c.charged else "false\n")
-        f.write(f"{len(names)}\n")
-        for n in names:
+        # ItMonList names, then ItStateList names (Solve_scf::Guess,
+        # solve_scf.cpp:500-517)
+        f.write(f"{n_mon}\n")
+        for n in names[:n_mon]:
             f.write(n + "\n")
-        f.write("0\n")
+        f.write(f"{len(names) - n_mon}\n")
+        for n in names[n_mon:]:
+            f.write(n + "\n")
         for v in x:
             f.write(f"{v:.17e}\n")
 

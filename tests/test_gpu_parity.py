@@ -53,6 +53,10 @@ def test_residual_matches_oracle(name):
         for i in range(plan.n_seg):
             assert rel_err(interior(plan, a[i]), interior(plan, b[i])) < 1e-10, (which, i)
     assert rel_err(interior(plan, ctx.field(2)), interior(plan, orc.field(2))) < 1e-10
+    if plan.c.n_state:  # the internal states' volume fractions
+        a, b = ctx.field(9).reshape(plan.c.n_state, -1), orc.field(9).reshape(plan.c.n_state, -1)
+        for j in range(plan.c.n_state):
+            assert rel_err(interior(plan, a[j]), interior(plan, b[j])) < 1e-10, ("state", j)
     for m in range(plan.n_mol):
         assert abs(ctx.molecule(m)["GN"] / orc.molecule(m)["GN"] - 1) < 1e-10
     F, O, mu = ctx.free_energy()
@@ -106,7 +110,8 @@ def _batch_cases():
         if "conv" in g["runs"]:
             p = Plan(g["runs"]["conv"]["input"])
             markov2 = any(p.c.mols[m].markov == 2 for m in range(p.c.n_mol))
-            if p.c.gradients == 1 and not p.c.charged and not markov2:  # the batched solver's scope
+            # the batched solver's scope
+            if p.c.gradients == 1 and not p.c.charged and not markov2 and not p.c.n_state:
                 out.append(n)
     return out
 

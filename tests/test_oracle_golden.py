@@ -60,6 +60,25 @@ def test_oracle_matches_reference(name):
             assert rel_err(interior(plan, phi[i]), pro_column(run, f"mon_{seg}_phi")) < tol, (mode, seg)
             if plan.c.seg_freedom[i] != 2:
                 assert rel_err(interior(plan, g1[i]), pro_column(run, f"mon_{seg}_G1")) < tol, (mode, seg)
+        if plan.c.n_state:
+            # the states' volume fractions, and the bulk fractions the plan
+            # solved from the reactions against the reference's
+            phs = orc.field(9).reshape(plan.c.n_state, plan.M)
+            for j, st in enumerate(plan.state_names):
+                seg = plan.seg_names[plan.c.state_seg[j]]
+                # the reference writes zeros for the first state of each mon:
+                # its profile index 2 is taken by the 3-D phi[z] average
+                # (segment.cpp:1880-1895, reached for 1 and 2 gradients too)
+                # where the reference's Newton steps, the two end points of
+                # the bulk equilibrium agree to about 1e-12 (the fraction of a
+                # 1e-9 state to 2.4e-12 relative); a state's φ scales with it
+                ab = k[f"mon_{seg}_alphabulk_{st}"]
+                dab = abs(plan.state_alphabulk[j] - ab) / ab
+                assert dab <= 1e-10, (st, plan.state_alphabulk[j], ab)
+                if [plan.c.state_seg[i] for i in range(j)].count(plan.c.state_seg[j]) == 0:
+                    continue
+                err = rel_err(interior(plan, phs[j]), pro_column(run, f"mon_{seg}_phi-{st}"))
+                assert err < max(tol, 2 * dab), (mode, st, err)
         alpha = orc.field(2)
         assert rel_err(interior(plan, alpha), pro_column(run, "sys_noname_alpha")) < max(tol, 1e-12)
         if plan.c.charged:
