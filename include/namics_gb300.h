@@ -342,7 +342,8 @@ int nm_solve_host(nm_ctx* ctx, double* x_host, double* phi_host,
  * which: 0 segment φ [n_seg*M], 1 G1 [n_seg*M], 2 α [M], 3 φ_tot [M],
  * 4 molecule φ_tot [n_mol*M], 5 φ_side [n_seg*M]; charged systems also
  * 6 ψ with mirror bounds [M], 7 charge density q [M], 8 relative
- * permittivity ε [M] (every site, halo layers included). */
+ * permittivity ε [M] (every site, halo layers included); plans with
+ * internal states also 9 the states' φ [n_state*M] (Segment::phi_state). */
 int nm_get_field(nm_ctx* ctx, int which, double* out_host);
 
 /* Per-molecule scalars of the last residual: GN, n, θ, φ_bulk.  Restricted

@@ -257,6 +257,11 @@ def cases() -> list[dict]:
     C.append(dict(name="states_weak2d", lines=lat2d(14, 8, ["surface", "mirror", "mirror", "mirror"]) +
                   weak_lines("(X)1(A)19", 0.4, "1e-7"), field=(-0.01, 0.01), seed=43,
                   modes=["it0", "it5", "conv"], conv_itlim=5000, split_tol=1e-4))
+    wall3 = [ln.replace("frozen_range : lowerbound", "frozen_range : 1,1,1;1,6,6")
+             .replace("pinned_range : firstlayer", "pinned_range : 2,1,1;2,6,6")
+             for ln in weak_lines("(X)1(A)15", 1.5, "1e-7")]
+    C.append(dict(name="states_weak3d", lines=lat3d((9, 6, 6), bc="mirror") + wall3, field=(-0.01, 0.01),
+                  seed=45, modes=["it0", "it5", "conv"], conv_itlim=5000, split_tol=1e-4))
     C.append(dict(name="states_weak1d_sph", lines=lat1d(30, geom="spherical", offset=8) +
                   weak_lines("(X)1(A)19", 10.0, "1e-6"), field=(-0.01, 0.01), seed=44,
                   modes=["it0", "it5", "conv"], conv_itlim=5000))
