@@ -536,6 +536,125 @@ def run_cyl2d(args) -> dict:
     return line
 
 
+def weak2d_text(nx: int = 100, ny: int = 100, N: int = 200, n: float = 1.0, h3o: str = "1e-7",
+                itlim: int = 20, tol: float = 1e-7) -> str:
+    """A weak-polyacid brush with internal states on a 2-D planar nx × ny
+    lattice: (X)1(A)N-1 pinned at the first layer (n chains), a frozen wall
+    below; A has states AH (neutral, χ 0.8 with H2O) and AM (charge -1),
+    water states H3O+ (bulk fraction h3o), H2O and OH-; reactions AH + H2O =
+    AM + H3O+ (pK 6) and 2 H2O = OH- + H3O+ (pK 14); Na neutraliser, Cl at
+    φ_b 0.01; bondlength 3e-10."""
+    return "\n".join([
+        "lat : flat : gradients : 2", f"lat : flat : n_layers_x : {nx}", f"lat : flat : n_layers_y : {ny}",
+        "lat : flat : geometry : planar", "lat : flat : lattice_type : simple_cubic",
+        "lat : flat : bondlength : 3e-10",
+        "lat : flat : lowerbound_x : surface", "lat : flat : upperbound_x : mirror",
+        "lat : flat : lowerbound_y : periodic", "lat : flat : upperbound_y : periodic",
+        "mon : S : freedom : frozen", "mon : S : frozen_range : lowerbound",
+        "mon : X : freedom : pinned", "mon : X : pinned_range : firstlayer",
+        "mon : A : freedom : free", "mon : W : freedom : free",
+        "mon : Na : freedom : free", "mon : Na : valence : 1", "mon : Cl : freedom : free", "mon : Cl : valence : -1",
+        "mon : A : chi_S : -1", "mon : X : chi_W : 0.5",
+        "state : AH : mon : A", "state : AH : valence : 0", "state : AM : mon : A", "state : AM : valence : -1",
+        "state : H3O : mon : W", "state : H3O : valence : 1", "state : H2O : mon : W", "state : H2O : valence : 0",
+        "state : OH : mon : W", "state : OH : valence : -1", f"state : H3O : alphabulk : {h3o}",
+        "state : AH : chi_H2O : 0.8",
+        "reaction : weak : equation : 1(AH) + 1(H2O) = 1(AM) + 1(H3O)", "reaction : weak : pK : 6",
+        "reaction : auto : equation : 2(H2O) = 1(OH) + 1(H3O)", "reaction : auto : pK : 14",
+        f"mol : pol : composition : (X)1(A){N - 1}", "mol : pol : freedom : restricted", f"mol : pol : n : {n!r}",
+        "mol : water : composition : (W)1", "mol : water : freedom : solvent",
+        "mol : Na : composition : (Na)1", "mol : Na : freedom : neutralizer",
+        "mol : Cl : composition : (Cl)1", "mol : Cl : freedom : free", "mol : Cl : phibulk : 0.01",
+        "newton : isaac : method : DIIS", f"newton : isaac : tolerance : {tol}",
+        f"newton : isaac : iterationlimit : {itlim}", "newton : isaac : deltamax : 0.1", "newton : isaac : m : 10",
+    ]) + "\n"
+
+
+def run_weak2d(args) -> dict:
+    """On one GPU: the weak-polyacid brush with internal states (weak2d_text,
+    100×100, A_200, sigma 0.05).  A step is `--iters` DIIS iterations from a
+    seeded field x ~ U(-0.01, 0.01) (ψ and the state blocks included); its
+    time is the context stream's CUDA-event interval; L2 is flushed between
+    steps.  value = DIIS iterations per second, FP64 propagators; the FP32
+    arm (one exponent per lattice row, FP64 composition, residual, Poisson
+    update and DIIS) beside it.  Also the max |Δφ| of one residual at the
+    seeded field against the CPU oracle, and the oracle's time for that
+    residual on one core."""
+    import torch
+    from namics_gb300 import build as b
+    b.build_product()
+    from namics_gb300 import NM_FP32, NM_FP64, Context, Plan
+    nx = ny = args.n2d
+    N, sigma = 200, 0.05
+    plan = Plan(weak2d_text(nx, ny, N, sigma * ny, itlim=args.iters))
+    x0h = np.random.default_rng(SEED + 11).uniform(-0.01, 0.01, size=plan.iv)
+    x0 = torch.from_numpy(x0h).cuda()
+    flush = torch.empty(int(256e6) // 4, dtype=torch.float32, device="cuda")
+    out = {}
+    for prec, name in ((NM_FP64, "fp64"), (NM_FP32, "fp32")):
+        st = torch.cuda.Stream()
+        ctx = Context(plan, prec, stream=st.cuda_stream)
+        xw = torch.empty_like(x0)
+        times, its, res = [], [], None
+        clocks = ClockSampler(0)
+        with clocks:
+            for k in range(args.warmup + args.steps):
+                flush.zero_()
+                xw.copy_(x0)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                res = ctx.solve_dev(xw.data_ptr())
+                e1.record(st)
+                e1.synchronize()
+                if k >= args.warmup:
+                    times.append(e0.elapsed_time(e1))
+                    its.append(res.iterations + 1)
+        ms = statistics.mean(times)
+        n_its = statistics.mean(its)
+        gd = torch.zeros_like(x0)
+        ctx.residual_dev(x0.data_ptr(), gd.data_ptr())
+        out[name] = {"ms_per_step": ms, "residuals_per_step": n_its, "iterations_per_s": 1000.0 * n_its / ms,
+                     "residual_after_step": res.residual, "launches": ctx.launch_count(),
+                     "clocks": clocks.summary(), "phi": ctx.field(0), "phi_states": ctx.field(9)}
+        ctx.close()
+    if not args.no_cpu:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        b.build_oracle()
+        from orc import Oracle
+        orc = Oracle(plan)
+        t0 = time.perf_counter()
+        rc, _ = orc.residual(x0h)
+        t_orc = time.perf_counter() - t0
+        if rc == 0:
+            mask = np.tile(plan.interior_mask(), plan.n_seg)
+            po, ps = orc.field(0)[mask], orc.field(9)
+            smask = np.tile(plan.interior_mask(), plan.c.n_state)
+            for name in out:
+                out[name]["max_abs_dphi_vs_oracle"] = float(np.max(np.abs(out[name]["phi"][mask] - po)))
+                out[name]["max_abs_dphi_states_vs_oracle"] = float(
+                    np.max(np.abs(out[name]["phi_states"][smask] - ps[smask])))
+            out["cpu_residual_seconds"] = t_orc
+    f32, f64 = out["fp32"], out["fp64"]
+    updates = float(plan.segment_updates())
+    strip = lambda d: {k: v for k, v in d.items() if k not in ("phi", "phi_states")}
+    return {
+        "metric": f"SCF DIIS iterations/s, {nx}x{ny} weak-polyacid brush with internal states and reactions "
+                  "(FP64 GPU; FP32 propagators beside it)",
+        "value": f64["iterations_per_s"], "unit": "iterations/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": f64["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded field)",
+        "config": {"workload": f"{nx}x{ny} planar weak-polyacid brush, (X)1(A){N - 1} pinned, sigma {sigma}, "
+                               "states AH/AM and H3O+/H2O/OH-, pK 6 and 14, H3O+ fraction 1e-7, Na neutraliser, "
+                               "Cl phi_b 0.01",
+                   "iteration_blocks": plan.c.n_it, "iterations_per_step": args.iters,
+                   "l2": "flushed between steps (256 MB write)", "segment_site_updates_per_residual": updates},
+        "updates_per_s": updates * f64["iterations_per_s"],
+        "fp32": strip(f32), "fp64_gpu": dict(strip(f64), value=f64["iterations_per_s"], unit="iterations/s"),
+        "cpu_residual_seconds": out.get("cpu_residual_seconds"),
+    }
+
+
 def run_served(args) -> dict:
     """A Poisson request stream served on one GPU by nm_server
     (continuous batching: 1-gradient requests go into the streaming work
@@ -636,11 +755,12 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU comparison")
-    ap.add_argument("--workload", default="brush1d", choices=["brush1d", "melt3d", "cyl2d", "served"],
+    ap.add_argument("--workload", default="brush1d", choices=["brush1d", "melt3d", "cyl2d", "weak2d", "served"],
                     help="brush1d: 512 batched 1-D brushes/stars, the headline; melt3d: 128³ melt (DIIS iterations/s); "
                          "cyl2d: 200×200 charged cylindrical brushes at two chi values (DIIS iterations/s); "
+                         "weak2d: 2-D weak-polyacid brush with internal states (DIIS iterations/s); "
                          "served: Poisson request stream of mixed solves")
-    ap.add_argument("--n2d", type=int, default=200, help="cyl2d: lattice edge (r and z)")
+    ap.add_argument("--n2d", type=int, default=200, help="cyl2d, weak2d: lattice edge")
     ap.add_argument("--no-solve", action="store_true", help="cyl2d: skip the timed full solves")
     ap.add_argument("--rate", type=float, default=20.0, help="served: arrivals per second")
     ap.add_argument("--requests", type=int, default=200, help="served: requests in the stream")
@@ -650,7 +770,7 @@ def main():
     ap.add_argument("--ckpt", type=int, default=10, help="melt3d: checkpoint stride of the FP32 arm (0: store all)")
     ap.add_argument("--instances", type=int, default=N_INSTANCES)
     ap.add_argument("--no-others", action="store_true",
-                    help="brush1d: skip the short runs of the melt, cylinder and served workloads")
+                    help="brush1d: skip the short runs of the melt, cylinder, weak-polyacid and served workloads")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -663,6 +783,9 @@ def main():
         return
     if args.workload == "cyl2d":
         print(json.dumps(run_cyl2d(args)), flush=True)
+        return
+    if args.workload == "weak2d":
+        print(json.dumps(run_weak2d(args)), flush=True)
         return
     run_brush1d(args)
 
@@ -715,9 +838,10 @@ def other_workloads(args) -> dict:
     import copy
     out = {}
     keep = ("metric", "value", "unit", "ms_per_step", "config", "roofline", "updates_per_s", "latency",
-            "fp32", "fp32_full_storage", "fp32_autotuned", "fp64_gpu", "fp64_plain")
+            "fp32", "fp32_full_storage", "fp32_autotuned", "fp64_gpu", "fp64_plain", "cpu_residual_seconds")
     runs = (("melt128", run_melt3d, dict(n3d=128, iters=5, steps=2, warmup=1, ckpt=10)),
             ("cylinder200", run_cyl2d, dict(n2d=200, iters=5, steps=2, warmup=1, no_solve=True)),
+            ("weak_polyacid100", run_weak2d, dict(n2d=100, iters=5, steps=2, warmup=1)),
             ("served_mix", run_served, dict(rate=400.0, requests=200, workers=24)))
     for name, fn, over in runs:
         a = copy.copy(args)
