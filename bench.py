@@ -690,8 +690,11 @@ def run_served(args) -> dict:
             x = np.concatenate([u, -u])
         reqs.append((int(k), p, x))
     out = {}
-    for prec, name in ((NM_FP32, "fp32"), (NM_FP64, "fp64")):
-        srv = Server(precision=prec, workers=args.workers, max_batch=64, memory_budget=64 << 30)
+    sweeps = getattr(args, "context_sweeps", 0)
+    arms = ((NM_FP32, "fp32"),) if args.no_fp64 else ((NM_FP32, "fp32"), (NM_FP64, "fp64"))
+    for prec, name in arms:
+        srv = Server(precision=prec, workers=args.workers, max_batch=64, memory_budget=64 << 30,
+                     context_sweeps=sweeps)
         t0 = time.perf_counter()
         ids = []
         for (k, p, x), ta in zip(reqs, arrivals):
@@ -721,17 +724,18 @@ def run_served(args) -> dict:
     # the plain FP64 GPU path: the same requests one after another, each in a
     # device context with FP64 propagators and the host-driven DIIS loop
     from namics_gb300 import Context
-    t0 = time.perf_counter()
-    ok = 0
-    for k, p, x in reqs:
-        c = Context(p, NM_FP64)
-        r, _ = c.solve_host(x.copy(), want_phi=False)
-        ok += r.status == 0
-        c.close()
-    span = time.perf_counter() - t0
-    out["fp64_plain"] = {"value": ok / span, "unit": "solves/s", "converged": int(ok), "requests": n_req,
-                         "span_s": span, "what": "the same requests one at a time (no server), FP64 propagators, "
-                                                 "DIIS with a host synchronisation per iteration"}
+    if not args.no_fp64:
+        t0 = time.perf_counter()
+        ok = 0
+        for k, p, x in reqs:
+            c = Context(p, NM_FP64)
+            r, _ = c.solve_host(x.copy(), want_phi=False)
+            ok += r.status == 0
+            c.close()
+        span = time.perf_counter() - t0
+        out["fp64_plain"] = {"value": ok / span, "unit": "solves/s", "converged": int(ok), "requests": n_req,
+                             "span_s": span, "what": "the same requests one at a time (no server), FP64 "
+                                                     "propagators, DIIS with a host synchronisation per iteration"}
     f32 = out["fp32"]
     line = {
         "metric": METRIC, "value": f32["value"], "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 0,
@@ -739,9 +743,10 @@ def run_served(args) -> dict:
         "dtype": "f32", "data": "synthetic (seeded request stream)",
         "config": {"workload": f"Poisson request stream, {args.rate:g} requests/s, {n_req} requests; 70% "
                                "1-D brushes/stars as in the batched workload, 25% 2-D 100x100 (A)200 adsorption, 5% 3-D 64^3 (A)20(B)20 melts",
-                   "workers": args.workers, "max_batch": 64, "memory_budget_gb": 64},
+                   "workers": args.workers, "max_batch": 64, "memory_budget_gb": 64,
+                   "context_sweeps": sweeps},
         "latency": {"p50_ms": f32["p50_ms"], "p99_ms": f32["p99_ms"], "what": "submit to completion"},
-        "fp32": f32, "fp64_gpu": out["fp64"], "fp64_plain": out["fp64_plain"],
+        "fp32": f32, "fp64_gpu": out.get("fp64"), "fp64_plain": out.get("fp64_plain"),
     }
     return line
 
@@ -765,6 +770,9 @@ def main():
     ap.add_argument("--rate", type=float, default=20.0, help="served: arrivals per second")
     ap.add_argument("--requests", type=int, default=200, help="served: requests in the stream")
     ap.add_argument("--workers", type=int, default=8, help="served: concurrent solves")
+    ap.add_argument("--context-sweeps", type=int, default=0,
+                    help="served: options of the 2-D/3-D request contexts (bit mask: 1 persistent 2-D sweeps, "
+                         "2 cluster sweeps of small FP32 3-D boxes, 4 device-resident solve loop)")
     ap.add_argument("--iters", type=int, default=20, help="melt3d: DIIS iterations per step")
     ap.add_argument("--n3d", type=int, default=128, help="melt3d: box edge")
     ap.add_argument("--ckpt", type=int, default=10, help="melt3d: checkpoint stride of the FP32 arm (0: store all)")

@@ -545,6 +545,14 @@ typedef struct nm_server_options {
                                 CTAs; 0: two per SM; -1: no loop, batched
                                 launches only.  The loop's memory is fixed
                                 at creation and outside memory_budget. */
+    int    context_sweeps;   /* options of the 2-D and 3-D request contexts,
+                                a bit mask: 1 persistent 2-D sweeps
+                                (NM_OPT_SWEEP2D), 2 cluster sweeps of small
+                                FP32 3-D boxes (NM_OPT_CLUSTER3D), 4 the
+                                device-resident solve loop
+                                (NM_OPT_DEVICE_LOOP); 0: one launch per
+                                step and a host-driven loop.  Each applies
+                                where the context supports it. */
 } nm_server_options;
 int nm_server_create(const nm_server_options* opt, nm_server** out);
 /* Queue one solve from the field x_host (plan->iv values, copied).  The plan

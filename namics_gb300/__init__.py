@@ -474,11 +474,16 @@ class Server:
     """Continuous-batching request server on one GPU (nm_server_*)."""
 
     def __init__(self, precision: int = NM_FP32, workers: int = 4, max_batch: int = 64,
-                 memory_budget: int = 64 << 30, device: int = 0, stream_slots: int = 0):
+                 memory_budget: int = 64 << 30, device: int = 0, stream_slots: int = 0,
+                 context_sweeps: int = 0):
         """stream_slots: resident CTAs of the 1-gradient streaming loop (0: two
-        per SM; -1: no loop, 1-gradient requests in batched launches)."""
+        per SM; -1: no loop, 1-gradient requests in batched launches).
+        context_sweeps: bit mask of the 2-D/3-D request contexts' options (1
+        persistent 2-D sweeps, 2 cluster sweeps of small FP32 3-D boxes, 4 the
+        device-resident solve loop)."""
         lib = _abi.load()
-        opt = _abi.nm_server_options(precision, device, workers, max_batch, memory_budget, stream_slots)
+        opt = _abi.nm_server_options(precision, device, workers, max_batch, memory_budget, stream_slots,
+                                     context_sweeps)
         h = C.c_void_p()
         _check(lib.nm_server_create(C.byref(opt), C.byref(h)))
         self._h = h

@@ -106,7 +106,8 @@ class nm_stream_options(C.Structure):
 
 class nm_server_options(C.Structure):
     _fields_ = [("precision", C.c_int), ("device", C.c_int), ("workers", C.c_int),
-                ("max_batch", C.c_int), ("memory_budget", C.c_size_t), ("stream_slots", C.c_int)]
+                ("max_batch", C.c_int), ("memory_budget", C.c_size_t), ("stream_slots", C.c_int),
+                ("context_sweeps", C.c_int)]
 
 # (name, restype, argtypes) for every entry point declared in the header
 SIGNATURES = [

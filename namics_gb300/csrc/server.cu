@@ -133,6 +133,11 @@ void Server::run_single(Request* r, cudaStream_t st) {
     nm_ctx* c = nullptr;
     int rc = nm_ctx_create(r->plan, &o, &c);
     if (!rc) {
+        // fewer launches per iteration where the caller asked for them; an
+        // option that does not apply to this context leaves it as it was
+        if (opt.context_sweeps & 1) nm_ctx_set_option(c, NM_OPT_SWEEP2D, 1);
+        if (opt.context_sweeps & 2) nm_ctx_set_option(c, NM_OPT_CLUSTER3D, 1);
+        if (opt.context_sweeps & 4) nm_ctx_set_option(c, NM_OPT_DEVICE_LOOP, 1);
         rc = nm_solve_host(c, r->x.data(), nullptr, &r->res);
         if (rc == NM_ERR_NOT_CONVERGED) rc = NM_OK;  // reported in res.status
         launches += nm_ctx_launch_count(c);
