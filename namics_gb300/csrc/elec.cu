@@ -148,6 +148,59 @@ __global__ void k_charge(Lat L, int ns, ChgArgs a, const double* __restrict__ ph
     }
 }
 
+// 2-D planar with MX ≤ 1024: the same wavefront with one thread per row x.
+// Site (x, y) of anti-diagonal d = x + y needs X(x, y-1), which the same
+// thread made on diagonal d-1 (kept in a register), and X(x-1, y), which
+// its neighbour thread made (read from shared memory, double-buffered by
+// diagonal parity, one block barrier per diagonal).  The global loads of the
+// next diagonal's site do not depend on the wavefront and are issued before
+// the barrier.  Same expression as k_psi_sweep2, so the same values.
+__global__ void __launch_bounds__(1024) k_psi_wave2(Lat L, ElecConst c, const double* __restrict__ xpsi,
+                                                     const double* __restrict__ psi, const double* __restrict__ q,
+                                                     const double* __restrict__ eps, double* __restrict__ X,
+                                                     double* __restrict__ g) {
+    __shared__ double wave[2][1026];
+    const int MX = L.MX, MY = L.MY, JX = L.JX, M = L.M;
+    const int x = 1 + (int)threadIdx.x;
+    const bool row = x <= MX;
+    double mine = 0;  // X(x, y-1)
+    // the operands of site (x, d - x), loaded ahead of the wavefront
+    double e0 = 0, exm = 0, exp_ = 0, eym = 0, eyp = 0, cq = 0, pxp = 0, pyp = 0, pxm = 0, pym = 0, xp = 0;
+    auto load = [&](int d) {
+        const int y = d - x;
+        if (!row || y < 1 || y > MY) return;
+        const int i = x * JX + y;
+        e0 = eps[i];
+        exm = e0 + eps[i - JX]; exp_ = e0 + eps[i + JX];
+        eym = e0 + eps[i - 1]; eyp = e0 + eps[i + 1];
+        cq = c.C * q[i];
+        pxp = psi[i + JX]; pyp = psi[i + 1];
+        pxm = psi[i - JX]; pym = psi[i - 1];
+        xp = xpsi[i];
+    };
+    load(2);
+    for (int d = 2; d <= MX + MY; d++) {
+        const int y = d - x;
+        const bool on = row && y >= 1 && y <= MY;
+        double v = 0;
+        if (on) {
+            const int i = x * JX + y;
+            const double ax = x == 1 ? pxm : wave[(d - 1) & 1][x - 1];
+            const double ay = y == 1 ? pym : mine;
+            v = (cq + exm * ax + exp_ * pxp + eym * ay + eyp * pyp) / (exm + exp_ + eym + eyp);
+            X[i] = v;
+            g[i] = xp - v;
+            mine = v;
+            wave[d & 1][x] = v;
+        }
+        load(d + 1);
+        __syncthreads();
+    }
+    // halo sites of the ψ block of g
+    for (int s = threadIdx.x; s < M; s += blockDim.x)
+        if (!nmdev::is_interior(L, s)) g[s] = 0.0;
+}
+
 // 1-D planar and cylindrical: upwind sweep along x in one thread
 __global__ void k_psi_sweep1(Lat L, ElecConst c, const double* __restrict__ xpsi, const double* __restrict__ psi,
                              const double* __restrict__ q, const double* __restrict__ eps, double* __restrict__ g) {
@@ -319,7 +372,10 @@ int Ctx::elec_residual(const double* x, double* g) {
     if (plan->gradients == 1 && plan->geometry != NM_SPHERICAL)
         k_psi_sweep1<<<1, 32, 0, stream>>>(lat, ec, xpsi, d_psi, d_q, d_eps, gp);
     else if (plan->gradients == 2 && plan->geometry == NM_PLANAR)
-        k_psi_sweep2<<<1, 512, 0, stream>>>(lat, ec, xpsi, d_psi, d_q, d_eps, d_X, gp);
+        if (plan->MX <= 1024)
+            k_psi_wave2<<<1, (plan->MX + 31) / 32 * 32, 0, stream>>>(lat, ec, xpsi, d_psi, d_q, d_eps, d_X, gp);
+        else
+            k_psi_sweep2<<<1, 512, 0, stream>>>(lat, ec, xpsi, d_psi, d_q, d_eps, d_X, gp);
     else if (plan->gradients == 3)
         k_psi_gs3<<<1, 1024, 0, stream>>>(lat, ec, xpsi, d_psi, d_q, d_eps, gp);
     else
