@@ -343,7 +343,9 @@ int nm_solve_host(nm_ctx* ctx, double* x_host, double* phi_host,
  * 4 molecule φ_tot [n_mol*M], 5 φ_side [n_seg*M]; charged systems also
  * 6 ψ with mirror bounds [M], 7 charge density q [M], 8 relative
  * permittivity ε [M] (every site, halo layers included); plans with
- * internal states also 9 the states' φ [n_state*M] (Segment::phi_state). */
+ * internal states also 9 the states' φ, 10 their fractions α of the
+ * segment's sites and 11 their potentials u, each [n_state*M]
+ * (Segment::phi_state, alpha, u; segment.cpp:861-873, 1337-1343). */
 int nm_get_field(nm_ctx* ctx, int which, double* out_host);
 
 /* Per-molecule scalars of the last residual: GN, n, θ, φ_bulk.  Restricted

@@ -228,7 +228,7 @@ class Context:
     def field(self, which: int) -> np.ndarray:
         p = self.plan
         n = {0: p.n_seg, 1: p.n_seg, 2: 1, 3: 1, 4: p.n_mol, 5: p.n_seg, 6: 1, 7: 1, 8: 1,
-             9: p.c.n_state}[which] * p.M
+             9: p.c.n_state, 10: p.c.n_state, 11: p.c.n_state}[which] * p.M
         out = np.empty(n)
         _check(_abi.load().nm_get_field(self._h, which, _dptr(out)))
         return out

@@ -1483,9 +1483,11 @@ int nm_get_field(nm_ctx* ctx, int which, double* out_host) {
         case 6: src = c->d_psi; n = M; break;
         case 7: src = c->d_q; n = M; break;
         case 8: src = c->d_eps; n = M; break;
-        case 9:
+        case 9: case 10: case 11:
             if (!c->nst) { nm::set_error("nm_get_field: the plan has no internal states"); return NM_ERR_ARG; }
-            src = c->d_phi + ns * M; n = (size_t)c->nst * M; break;
+            src = which == 9 ? c->d_phi + ns * M : (which == 10 ? c->d_ast : c->d_ust);
+            n = (size_t)c->nst * M;
+            break;
         default: nm::set_error("nm_get_field: unknown field"); return NM_ERR_ARG;
     }
     cudaError_t e = cudaMemcpyAsync(out_host, src, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream);

@@ -43,6 +43,12 @@ int seg_index(const nm_plan* p, const std::string& n) {
         if (n == p->seg_name[i]) return i;
     return -1;
 }
+// state j of segment k named `st`, or -1
+int state_of(const nm_plan* p, int k, const std::string& st) {
+    for (int j = 0; j < p->n_state; j++)
+        if (p->state_seg[j] == k && st == p->state_name[j]) return j;
+    return -1;
+}
 int mol_index(const nm_plan* p, const std::string& n) {
     for (int m = 0; m < p->n_mol; m++)
         if (p->mol_name && n == p->mol_name[m]) return m;
@@ -63,7 +69,7 @@ int nm_write_pro(nm_ctx* ctx, const char* path, const char* const* items, int n_
     const nm_plan* p = c->plan;
     const size_t M = p->M;
     // the fields the items draw from, fetched once each
-    std::vector<std::vector<double>> field(9);
+    std::vector<std::vector<double>> field(12);
     auto get = [&](int which, size_t n) -> int {
         if (field[which].empty()) {
             field[which].resize(n);
@@ -83,6 +89,17 @@ int nm_write_pro(nm_ctx* ctx, const char* path, const char* const* items, int n_
             int k = seg_index(p, name);
             if (k >= 0 && prop == "phi") { rc = get(0, p->n_seg * M); col = field[0].data() + k * M; }
             else if (k >= 0 && prop == "G1") { rc = get(1, p->n_seg * M); col = field[1].data() + k * M; }
+            else if (k >= 0 && p->n_state > 0) {
+                // a state's φ, α or u (Segment::GetPointer, segment.cpp:1896-1910).
+                // The reference's file holds zeros in the φ column of a mon's
+                // first state (its profile index 2 is the 3-D φ[z] average,
+                // reached for 1 and 2 gradients too); this writes the values.
+                const size_t dash = prop.find('-');
+                const std::string what = dash == std::string::npos ? "" : prop.substr(0, dash);
+                const int j = dash == std::string::npos ? -1 : state_of(p, k, prop.substr(dash + 1));
+                const int which = what == "phi" ? 9 : what == "alpha" ? 10 : what == "u" ? 11 : -1;
+                if (j >= 0 && which > 0) { rc = get(which, (size_t)p->n_state * M); col = field[which].data() + j * M; }
+            }
         } else if (key == "mol") {
             int m = mol_index(p, name);
             if (m >= 0 && prop == "phi") { rc = get(4, p->n_mol * M); col = field[4].data() + m * M; }
@@ -164,6 +181,47 @@ int nm_write_kal(nm_ctx* ctx, const char* path, const char* const* items, int n_
             if (prop == "residual") v.d = res->residual;
             else { v.is_int = true; v.i = res->iterations; }
             ok = true;
+        } else if (key == "mon" && p->n_state > 0 && seg_index(p, name) >= 0) {
+            // a state's scalars (Segment::PushOutput, segment.cpp:1820-1830):
+            // alphabulk_, valence_, phibulk_ (φ_bulk of the mon × α_bulk),
+            // theta_ (Σ over the interior of L·φ_state) and theta_exc_
+            // (θ − volume·φ_bulk)
+            const int k = seg_index(p, name);
+            static const char* const kinds[] = {"alphabulk_", "valence_", "phibulk_", "theta_exc_", "theta_"};
+            for (const char* kd : kinds) {
+                const std::string pre(kd);
+                if (prop.compare(0, pre.size(), pre) != 0) continue;
+                const int j = state_of(p, k, prop.substr(pre.size()));
+                if (j < 0) break;
+                if (pre == "alphabulk_") v.d = p->state_alphabulk[j];
+                else if (pre == "valence_") v.d = p->state_valence[j];
+                else {
+                    std::vector<double> spb((size_t)c->nsp);
+                    cudaError_t e = cudaMemcpyAsync(spb.data(), c->d_seg_phibulk, sizeof(double) * spb.size(),
+                                                    cudaMemcpyDeviceToHost, c->stream);
+                    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+                    if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
+                    const double pb = spb[(size_t)p->n_seg + j];
+                    if (pre == "phibulk_") v.d = pb;
+                    else {
+                        const size_t M = p->M;
+                        std::vector<double> ph((size_t)p->n_state * M);
+                        int rc = nm_get_field(ctx, 9, ph.data());
+                        if (rc) return rc;
+                        const bool w = p->gradients < 3 && p->geometry != NM_PLANAR;
+                        double sum = 0;
+                        for (int x = 1; x <= p->MX; x++)
+                            for (int y = (p->gradients > 1 ? 1 : 0); y <= (p->gradients > 1 ? p->MY : 0); y++)
+                                for (int z = (p->gradients > 2 ? 1 : 0); z <= (p->gradients > 2 ? p->MZ : 0); z++) {
+                                    const size_t s = (size_t)x * p->JX + (size_t)y * p->JY + z;
+                                    sum += w ? ph[(size_t)j * M + s] * p->L[s] : ph[(size_t)j * M + s];
+                                }
+                        v.d = pre == "theta_" ? sum : sum - p->volume * pb;
+                    }
+                }
+                ok = true;
+                break;
+            }
         } else if (key == "mol") {
             int m = mol_index(p, name);
             if (m >= 0) {

@@ -92,7 +92,7 @@ class Oracle:
     def field(self, which: int) -> np.ndarray:
         p = self.plan
         rows = {0: p.n_seg, 1: p.n_seg, 2: 1, 3: 1, 4: p.n_mol, 5: p.n_seg, 6: 1, 7: 1, 8: 1}
-        n = (rows[which] if which != 9 else p.c.n_state) * p.M
+        n = (rows[which] if which < 9 else p.c.n_state) * p.M
         out = np.zeros(n)
         rc = load().orc_get_field(self._h, which, _p(out))
         if rc:

@@ -1127,6 +1127,8 @@ int orc_get_field(orc_state* st, int which, double* out) {
         case 7: if (!P->charged) return NM_ERR_ARG; Cp(out, st->q, M); return NM_OK;
         case 8: if (!P->charged) return NM_ERR_ARG; Cp(out, st->eps, M); return NM_OK;
         case 9: if (!P->n_state) return NM_ERR_ARG; Cp(out, st->phi + (size_t)P->n_seg * M, P->n_state * M); return NM_OK;
+        case 10: if (!P->n_state) return NM_ERR_ARG; Cp(out, st->ast, P->n_state * M); return NM_OK;
+        case 11: if (!P->n_state) return NM_ERR_ARG; Cp(out, st->ust, P->n_state * M); return NM_OK;
     }
     return NM_ERR_ARG;
 }

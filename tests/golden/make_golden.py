@@ -290,10 +290,19 @@ def outputs_block(plan: Plan) -> list[str]:
         s.append(f"pro : mon : {name} : phi")
     for name in plan.seg_names:
         s.append(f"pro : mon : {name} : G1")
-    # the states' volume fractions (Segment::GetPointer's phi-<state>,
-    # segment.cpp:1898-1902) and their bulk fractions
+    # the states' profiles (Segment::GetPointer's phi-, alpha- and u-<state>,
+    # segment.cpp:1896-1910).  phi- of a mon's first state is left out: the
+    # reference writes zeros there (its profile index 2 is the 3-D phi[z]
+    # average, reached for 1 and 2 gradients too).
+    first = {}
     for j, st in enumerate(plan.state_names):
-        s.append(f"pro : mon : {plan.seg_names[plan.c.state_seg[j]]} : phi-{st}")
+        seg = plan.seg_names[plan.c.state_seg[j]]
+        if seg in first:
+            s.append(f"pro : mon : {seg} : phi-{st}")
+        first.setdefault(seg, st)
+    for j, st in enumerate(plan.state_names):
+        seg = plan.seg_names[plan.c.state_seg[j]]
+        s += [f"pro : mon : {seg} : alpha-{st}", f"pro : mon : {seg} : u-{st}"]
     s.append("pro : sys : noname : alpha")
     if plan.c.charged:
         s += ["pro : sys : noname : psi", "pro : sys : noname : q", "pro : sys : noname : eps"]
@@ -301,7 +310,8 @@ def outputs_block(plan: Plan) -> list[str]:
     s += ["kal : sys : noname : free_energy", "kal : sys : noname : grand_potential",
           "kal : newton : isaac : residual", "kal : newton : isaac : iterations"]
     for j, st in enumerate(plan.state_names):
-        s.append(f"kal : mon : {plan.seg_names[plan.c.state_seg[j]]} : alphabulk_{st}")
+        seg = plan.seg_names[plan.c.state_seg[j]]
+        s += [f"kal : mon : {seg} : {q}_{st}" for q in ("alphabulk", "valence", "phibulk", "theta", "theta_exc")]
     for m in range(plan.n_mol):
         mn = MOLNAMES[m]
         s += [f"kal : mol : {mn} : GN", f"kal : mol : {mn} : n", f"kal : mol : {mn} : theta",
@@ -396,7 +406,7 @@ def run_case(case: dict, mode: str, workdir: Path) -> dict:
     return out
 
 
-RAW_CASES = ["brush1d_x100", "brush2d_cyl", "melt3d", "charged1d"]
+RAW_CASES = ["brush1d_x100", "brush2d_cyl", "melt3d", "charged1d", "states_weak1d", "states_weak2d"]
 
 
 def main_raw():

@@ -53,10 +53,11 @@ def test_residual_matches_oracle(name):
         for i in range(plan.n_seg):
             assert rel_err(interior(plan, a[i]), interior(plan, b[i])) < 1e-10, (which, i)
     assert rel_err(interior(plan, ctx.field(2)), interior(plan, orc.field(2))) < 1e-10
-    if plan.c.n_state:  # the internal states' volume fractions
-        a, b = ctx.field(9).reshape(plan.c.n_state, -1), orc.field(9).reshape(plan.c.n_state, -1)
-        for j in range(plan.c.n_state):
-            assert rel_err(interior(plan, a[j]), interior(plan, b[j])) < 1e-10, ("state", j)
+    if plan.c.n_state:  # the internal states' volume fractions, fractions α and potentials u
+        for which in (9, 10, 11):
+            a, b = ctx.field(which).reshape(plan.c.n_state, -1), orc.field(which).reshape(plan.c.n_state, -1)
+            for j in range(plan.c.n_state):
+                assert rel_err(interior(plan, a[j]), interior(plan, b[j])) < 1e-10, ("state", which, j)
     for m in range(plan.n_mol):
         assert abs(ctx.molecule(m)["GN"] / orc.molecule(m)["GN"] - 1) < 1e-10
     F, O, mu = ctx.free_energy()

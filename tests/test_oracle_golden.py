@@ -79,6 +79,16 @@ def test_oracle_matches_reference(name):
                     continue
                 err = rel_err(interior(plan, phs[j]), pro_column(run, f"mon_{seg}_phi-{st}"))
                 assert err < max(tol, 2 * dab), (mode, st, err)
+            # each state's fraction α and potential u per site, and its scalars
+            als = orc.field(10).reshape(plan.c.n_state, plan.M)
+            us = orc.field(11).reshape(plan.c.n_state, plan.M)
+            for j, st in enumerate(plan.state_names):
+                seg = plan.seg_names[plan.c.state_seg[j]]
+                ab = k[f"mon_{seg}_alphabulk_{st}"]
+                tol_j = max(tol, 2 * abs(plan.state_alphabulk[j] - ab) / ab)
+                assert rel_err(interior(plan, als[j]), pro_column(run, f"mon_{seg}_alpha-{st}")) < tol_j, (mode, st)
+                assert rel_err(interior(plan, us[j]), pro_column(run, f"mon_{seg}_u-{st}")) < max(tol, 1e-12), (mode, st)
+                assert k[f"mon_{seg}_valence_{st}"] == plan.c.state_valence[j]
         alpha = orc.field(2)
         assert rel_err(interior(plan, alpha), pro_column(run, "sys_noname_alpha")) < max(tol, 1e-12)
         if plan.c.charged:
