@@ -199,6 +199,13 @@ typedef struct nm_plan {
     const int*    it_sp;            /* [n_it] species of each iteration
                                        block's representative (ItMonList,
                                        then ItStateList)                  */
+    /* a scan of a fixed state's bulk fraction (`var : state-<name> : scan :
+     * alphabulk`, State::PutVarScan / UpdateVarInfo, state.cpp:262-318):
+     * the state's index, or -1.  Its steps use scan_n, scan_exponential,
+     * scan_start (the input's alphabulk), scan_end and scan_step, and
+     * nm_plan_scan_value gives their values; nm_ctx_set_values takes each as
+     * `state : <name> : alphabulk`. */
+    int    scan_state;
 } nm_plan;
 
 /* Parse Namics input text (the `lat/mon/mol/sys/newton` key subset of the
@@ -294,10 +301,15 @@ int nm_plan_scan_value(const nm_plan* plan, int k, double* value);
 
 /* Scans (the reference's Variate: variate.cpp, solve_scf.cpp:717-868): change
  * values of a live context and solve again from its current field (a warm
- * start).  items: "mon : <seg> : chi_<seg>" (set both ways), "mol : <mol> :
- * n | theta" (restricted), "mol : <mol> : phibulk" (free).  All are applied,
- * then checked: χ must keep the iteration species (segments with equal χ
- * rows) unchanged.  On error nothing changes (NM_ERR_ARG, NM_ERR_INPUT). */
+ * start).  items: "mon : <seg> : chi_<seg>" (set both ways; not on a plan
+ * with internal states), "mol : <mol> : n | theta" (restricted), "mol :
+ * <mol> : phibulk" (free), "state : <state> : alphabulk" (a state whose
+ * alphabulk the input fixes).  All are applied, then checked: χ must keep
+ * the iteration species (segments with equal χ rows) unchanged.  A state's
+ * new value solves the bulk equilibrium again, its pK_eff from the bulk
+ * volume fractions of the context's last residual, as the reference's next
+ * solve does (Reaction::pKeff, reaction.cpp:253-266); the molecules' bulk
+ * charges follow.  On error nothing changes (NM_ERR_ARG, NM_ERR_INPUT). */
 int nm_ctx_set_values(nm_ctx* ctx, const char* const* items, const double* values, int n);
 
 /* One residual evaluation g(x) on device buffers of length plan->iv.

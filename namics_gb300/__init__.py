@@ -134,7 +134,7 @@ class Plan:
         """The values of the input's scan (`var : … : scan`), step 0 first;
         empty without a scan."""
         c = self.c
-        if c.scan_mol < 0:
+        if c.scan_mol < 0 and c.scan_state < 0:
             return []
         out = []
         for k in range(c.scan_n + 1):
@@ -311,7 +311,8 @@ class Context:
                                         C.byref(r) if r is not None else None, int(append)))
 
     def set_values(self, values: dict[str, float]) -> None:
-        """Change χ or a molecule's amount for the next solve (a scan step)."""
+        """Change χ, a molecule's amount or a fixed state's alphabulk for the
+        next solve (a scan step)."""
         items = list(values)
         arr = (C.c_char_p * len(items))(*[s.encode() for s in items])
         v = np.ascontiguousarray([float(values[k]) for k in items], dtype=np.float64)

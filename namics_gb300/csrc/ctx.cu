@@ -1057,6 +1057,7 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
         TRY(dalloc(&d_ust, (size_t)nst * M, stream));
         TRY(dalloc(&d_ast, (size_t)nst * M, stream));
         chi_sp.assign(p->chi_sp, p->chi_sp + (size_t)nsp * nsp);
+        st_fixed = reinterpret_cast<const PlanHolder*>(p)->state_ab_in;
     }
     // state
     TRY(dalloc(&d_G1, (size_t)ns * M, stream));
@@ -1253,6 +1254,8 @@ int nm_ctx_set_values(nm_ctx* ctx, const char* const* items, const double* value
     const int ns = p->n_seg;
     std::vector<double> chi = c->chi;
     nm::NormArgs na = c->norm_args;
+    std::vector<double> st_fixed = c->st_fixed;
+    bool states_changed = false;
     auto trim = [](std::string s) {
         size_t a = s.find_first_not_of(" \t"), b = s.find_last_not_of(" \t");
         return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
@@ -1276,6 +1279,11 @@ int nm_ctx_set_values(nm_ctx* ctx, const char* const* items, const double* value
                 if (prop.substr(4) == p->seg_name[k]) b = k;
             }
             if (a >= 0 && b >= 0 && a != b) { chi[a * ns + b] = chi[b * ns + a] = v; ok = true; }
+        } else if (key == "state" && prop == "alphabulk" && c->nst > 0) {
+            // a fixed state's bulk fraction (State::PutValue, state.cpp:350-357)
+            const nm::PlanHolder& H = *reinterpret_cast<const nm::PlanHolder*>(p);
+            for (int j = 0; j < c->nst; j++)
+                if (name == p->state_name[j] && H.state_fixed[j]) { st_fixed[j] = v; states_changed = ok = true; }
         } else if (key == "mol") {
             for (int m = 0; m < p->n_mol; m++) {
                 if (!p->mol_name || name != p->mol_name[m]) continue;
@@ -1299,9 +1307,35 @@ int nm_ctx_set_values(nm_ctx* ctx, const char* const* items, const double* value
                 return NM_ERR_INPUT;
             }
         }
+    nm::StArgs stn = c->st;
+    if (states_changed) {
+        // the bulk equilibrium again, its pK_eff from the bulk fractions of
+        // the last residual as the reference's next solve reads them
+        std::vector<double> spb((size_t)c->nsp), ab, charge;
+        if (c->have_state) {
+            cudaError_t e = cudaMemcpyAsync(spb.data(), c->d_seg_phibulk, sizeof(double) * spb.size(),
+                                            cudaMemcpyDeviceToHost, c->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+            if (e != cudaSuccess) { nm::set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
+        }
+        std::string err;
+        if (int rc = nm::plan_state_bulk(p, st_fixed, c->have_state ? spb.data() : nullptr, ab, charge, err)) {
+            nm::set_error("nm_ctx_set_values: " + err);
+            return rc;
+        }
+        for (int j = 0; j < c->nst; j++) stn.ab[j] = ab[j];
+        for (int m = 0; m < p->n_mol; m++) na.mol[m].charge = charge[m];
+        na.st = stn;
+    }
     c->chi = chi;
-    for (int k = 0; k < ns * ns; k++) c->res_args.chi[k] = chi[k];
+    if (!c->nst)  // with states the residual's χ is the species matrix, which no item changes
+        for (int k = 0; k < ns * ns; k++) c->res_args.chi[k] = chi[k];
     c->norm_args = na;
+    if (states_changed) {
+        c->st = stn;
+        c->phi_args.st = stn;
+        c->st_fixed = st_fixed;
+    }
     if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
     nm::ctx_loop_drop(*c);
     return NM_OK;

@@ -193,7 +193,7 @@ int nm_write_kal(nm_ctx* ctx, const char* path, const char* const* items, int n_
                 if (prop.compare(0, pre.size(), pre) != 0) continue;
                 const int j = state_of(p, k, prop.substr(pre.size()));
                 if (j < 0) break;
-                if (pre == "alphabulk_") v.d = p->state_alphabulk[j];
+                if (pre == "alphabulk_") v.d = c->st.ab[j];  // the context's (a scan may have moved them)
                 else if (pre == "valence_") v.d = p->state_valence[j];
                 else {
                     std::vector<double> spb((size_t)c->nsp);

@@ -676,15 +676,6 @@ static bool check_unread(const InputBlock& in, std::string& err) {
 
 // ---- internal states and reactions ----------------------------------------
 
-// One reaction: the states of its equation in written order and their
-// stoichiometric numbers, negative on the left-hand side (Reaction::
-// CheckInput, reaction.cpp:37-145).
-struct ReactionDef {
-    std::string name;
-    double pK = 0;
-    std::vector<int> sto, state;
-};
-
 // The states' bulk fractions as the reference fixes them before its SCF
 // loop (Solve_scf::Solve, solve_scf.cpp:562-603): one unknown x_r per
 // reaction, the residual of the WEAK case of Solve_scf::residuals
@@ -693,6 +684,7 @@ struct ReactionDef {
 // by exp(x_r), then g_r = -1 + Σ -ν·log10(α_bulk)/pK_eff.
 struct Chem {
     const std::vector<ReactionDef>& R;
+    std::vector<double> pke;           // pK_eff of each reaction
     const std::vector<int>& seg;       // segment of each state
     const std::vector<double>& val;    // valence of each state
     const std::vector<char>& fixed;    // alphabulk given in the input
@@ -704,16 +696,17 @@ struct Chem {
 
     Chem(const std::vector<ReactionDef>& r, const std::vector<int>& s, const std::vector<double>& v,
          const std::vector<char>& f, const std::vector<double>& ab0, int n_seg)
-        : R(r), seg(s), val(v), fixed(f), seg_states(n_seg), local(s.size()), ab(ab0), item(n_seg, -1) {
+        : R(r), pke(r.size()), seg(s), val(v), fixed(f), seg_states(n_seg), local(s.size()), ab(ab0), item(n_seg, -1) {
+        for (size_t i = 0; i < r.size(); i++) pke[i] = r[i].pK;
         for (size_t j = 0; j < s.size(); j++) {
             local[j] = (int)seg_states[s[j]].size();
             seg_states[s[j]].push_back((int)j);
         }
     }
-    // pK_eff = pK + Σ ν·ChemIntBulk/ln 10 (reaction.cpp:253-266).  The bulk
-    // χ sums there read the segments' and states' bulk fractions, which are
-    // still zero when the pre-iteration of a first solve runs.
-    static double pK_eff(const ReactionDef& r) { return r.pK; }
+    // pK_eff = pK + Σ ν·ChemIntBulk/ln 10 (reaction.cpp:253-266): pke, set
+    // by the caller (pK itself before any solve, when the bulk fractions the
+    // χ sums read are still zero)
+    double pK_eff(const ReactionDef& r) const { return pke[&r - R.data()]; }
 
     // Reaction::GuessAlpha, reaction.cpp:300-378
     bool guess(const ReactionDef& r) {
@@ -988,6 +981,9 @@ static bool build_states(const InputBlock& in, PlanHolder& H, std::string& err) 
     }
     Chem chem(R, H.state_seg, H.state_valence, fixed, ab0, ns);
     if (!chem.solve()) { err = chem.err; return false; }
+    H.reactions = R;
+    H.state_fixed = fixed;
+    H.state_ab_in = ab0;
     for (int j = 0; j < nst; j++)
         if (!(chem.ab[j] >= 0 && chem.ab[j] <= 1)) {
             err = "state " + H.state_names[j] + ": its bulk fraction is fixed by no reaction"; return false;
@@ -1044,6 +1040,67 @@ static bool build_states(const InputBlock& in, PlanHolder& H, std::string& err) 
     P.n_state = nst;
     P.n_sp = nsp;
     return true;
+}
+
+int plan_state_bulk(const nm_plan* p, const std::vector<double>& fixed_ab, const double* sp_phibulk,
+                    std::vector<double>& alphabulk, std::vector<double>& mol_charge, std::string& err) {
+    const PlanHolder& H = *reinterpret_cast<const PlanHolder*>(p);
+    const int ns = p->n_seg, nst = p->n_state, nsp = p->n_sp;
+    if (nst == 0 || (int)fixed_ab.size() != nst) { err = "no internal states"; return NM_ERR_ARG; }
+    std::vector<double> ab0 = H.state_ab_in;
+    for (int j = 0; j < nst; j++)
+        if (H.state_fixed[j]) {
+            if (!(fixed_ab[j] >= 0 && fixed_ab[j] <= 1)) { err = "alphabulk out of range 0 ... 1"; return NM_ERR_ARG; }
+            ab0[j] = fixed_ab[j];
+        }
+    Chem chem(H.reactions, H.state_seg, H.state_valence, H.state_fixed, ab0, ns);
+    if (sp_phibulk) {
+        // Reaction::pKeff (reaction.cpp:253-266) with ChemIntBulk
+        // (reaction.cpp:243-251) over the bulk volume fractions of the last
+        // solve; the reference indexes the states by the term's position in
+        // the equation (Sta[i]), and so does this
+        auto cib = [&](int j) {
+            double v = 0;
+            for (int k = 0; k < ns; k++)
+                if (H.seg_nstate[k] == 0) v += p->chi_sp[(size_t)(ns + j) * nsp + k] * sp_phibulk[k];
+            for (int l = 0; l < nst; l++) v += p->chi_sp[(size_t)(ns + j) * nsp + ns + l] * sp_phibulk[ns + l];
+            return v;
+        };
+        for (size_t r = 0; r < H.reactions.size(); r++) {
+            const ReactionDef& R = H.reactions[r];
+            double v = 0;
+            for (size_t i = 0; i < R.sto.size() && (int)i < nst; i++) v += R.sto[i] * cib((int)i);
+            chem.pke[r] = R.pK + v / std::log(10.0);
+        }
+    }
+    if (!chem.solve()) { err = chem.err; return NM_ERR_INPUT; }
+    for (int j = 0; j < nst; j++)
+        if (!(chem.ab[j] >= 0 && chem.ab[j] <= 1)) { err = "a state's bulk fraction left [0, 1]"; return NM_ERR_INPUT; }
+    alphabulk = chem.ab;
+    // Molecule::Charge with the new fractions, as the plan computes it
+    mol_charge.assign(p->n_mol, 0.0);
+    size_t off = 0;
+    for (int m = 0; m < p->n_mol; m++) {
+        const nm_molecule& mol = p->mols[m];
+        bool with_states = false;
+        for (int k = 0; k < mol.n_molmon; k++) with_states = with_states || H.seg_nstate[mol.molmon_seg[k]] > 0;
+        if (!with_states) {
+            mol_charge[m] = mol.charge;
+        } else {
+            double q = 0;
+            for (int k = 0; k < mol.n_molmon; k++) {
+                const int sgi = mol.molmon_seg[k];
+                const double nmon = H.mol_nmon[off + k];
+                if (H.seg_nstate[sgi] > 0) {
+                    for (int j = 0; j < nst; j++)
+                        if (H.state_seg[j] == sgi) q += alphabulk[j] * H.state_valence[j] * nmon;
+                } else q += H.seg_valence[sgi] * nmon;
+            }
+            mol_charge[m] = q / mol.chainlength;
+        }
+        off += mol.n_molmon;
+    }
+    return NM_OK;
 }
 
 static nm_plan* build_plan(const InputBlock& in, std::string& err) {
@@ -1242,6 +1299,14 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
             if (H->seg_freedom[B.seg] == NM_SEG_PINNED) mb.mol.pinned = 1;
         }
         for (auto& f : mb.fraction) f /= N;
+        {
+            std::vector<double> nm(mb.molmon.size(), 0.0);
+            for (auto& B : mb.blocks) {
+                const int k = (int)(std::find(mb.molmon.begin(), mb.molmon.end(), B.seg) - mb.molmon.begin());
+                nm[k] += B.length * B.degeneracy;
+            }
+            H->mol_nmon.insert(H->mol_nmon.end(), nm.begin(), nm.end());
+        }
         mb.mol.charge = 0;
         bool with_states = false;
         for (int sgi : mb.molmon) with_states = with_states || H->seg_nstate[sgi] > 0;
@@ -1408,7 +1473,7 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
     // target, `var : sys-<name> : free_energy|grand_potential : <value>` or
     // `var : mol-<name> : theta|n|phibulk|mu : <value>` (Variate::CheckInput,
     // variate.cpp:60-200; Molecule::PutVarInfo, molecule.cpp:679-740) ----
-    P.scan_mol = -1; P.scan_what = -1; P.scan_n = 0; P.scan_exponential = 0;
+    P.scan_mol = -1; P.scan_what = -1; P.scan_n = 0; P.scan_exponential = 0; P.scan_state = -1;
     P.scan_start = P.scan_end = P.scan_step = 0;
     P.search_mol = -1; P.search_what = -1;
     P.target_kind = -1; P.target_mol = -1; P.target_what = -1; P.target_value = 0;
@@ -1503,6 +1568,52 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
                     P.scan_mol = mi; P.scan_what = w; P.scan_n = nsteps;
                     P.scan_start = start; P.scan_end = end; P.scan_step = step;
                 }
+            } else if (item == "state" && in.has("var", vn, "scan")) {
+                // a fixed state's bulk fraction (State::PutVarInfo / PutVarScan,
+                // state.cpp:229-304): the same step rules as a molecule's scan
+                int sj = -1;
+                for (int j = 0; j < P.n_state; j++) if (H->state_names[j] == name) sj = j;
+                if (sj < 0) { err = "var '" + vn + "': no state " + name; delete H; return nullptr; }
+                if (in.get("var", vn, "scan") != "alphabulk" || !H->state_fixed[sj]) {
+                    err = "var '" + vn + "': a state scan takes the alphabulk of a state that fixes it";
+                    delete H; return nullptr;
+                }
+                if (P.scan_mol >= 0 || P.scan_state >= 0) { err = "one scan per input"; delete H; return nullptr; }
+                double end = 0, step = 0;
+                if (!in.has("var", vn, "end_value") || !to_real(in.get("var", vn, "end_value"), end)) {
+                    err = "var '" + vn + "': a scan needs a numeric end_value"; delete H; return nullptr;
+                }
+                const std::string scale = in.get("var", vn, "scale", "linear");
+                const double start = H->state_ab_in[sj];
+                int nsteps = 0;
+                if (scale == "exponential") {
+                    int steps = 1;
+                    if (in.has("var", vn, "steps") && (!to_int(in.get("var", vn, "steps"), steps) || steps < 1)) {
+                        err = "var '" + vn + "': steps (per decade) must be a positive integer"; delete H; return nullptr;
+                    }
+                    if (!(end > 0 && start > 0)) {
+                        err = "var '" + vn + "': an exponential scan needs a positive start and end_value";
+                        delete H; return nullptr;
+                    }
+                    const double ns_real = end > start ? steps * std::log10(end / start) : steps * std::log10(start / end);
+                    if (!(ns_real < 1e6)) { err = "var '" + vn + "': more than 10^6 scan steps"; delete H; return nullptr; }
+                    nsteps = (int)ns_real;
+                    P.scan_exponential = 1;
+                } else if (scale == "linear") {
+                    if (!in.has("var", vn, "step") || !to_real(in.get("var", vn, "step"), step) || step == 0) {
+                        err = "var '" + vn + "': a linear scan needs a nonzero step"; delete H; return nullptr;
+                    }
+                    const double ns_real = (end - start) / step;
+                    if (!(ns_real < 1e6 && ns_real > -1e6)) {
+                        err = "var '" + vn + "': more than 10^6 scan steps"; delete H; return nullptr;
+                    }
+                    nsteps = (int)ns_real;
+                    if (nsteps < 0) { err = "var '" + vn + "': (end_value - start)/step is negative"; delete H; return nullptr; }
+                } else {
+                    err = "var '" + vn + "': scale is linear or exponential"; delete H; return nullptr;
+                }
+                P.scan_state = sj; P.scan_what = 3; P.scan_n = nsteps;
+                P.scan_start = start; P.scan_end = end; P.scan_step = step;
             } else if (item == "sys") {
                 if (in.has("var", vn, "free_energy") && !set_target(0, -1, -1, in.get("var", vn, "free_energy"))) {
                     delete H; return nullptr;
@@ -1589,7 +1700,7 @@ int nm_plan_create(const char* input_text, nm_plan** out) {
 }
 
 int nm_plan_scan_value(const nm_plan* plan, int k, double* value) {
-    if (!plan || !value || plan->scan_mol < 0 || k < 0 || k > plan->scan_n) {
+    if (!plan || !value || (plan->scan_mol < 0 && plan->scan_state < 0) || k < 0 || k > plan->scan_n) {
         nm::set_error("nm_plan_scan_value: no scan, or step out of range");
         return NM_ERR_ARG;
     }

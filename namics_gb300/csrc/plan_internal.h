@@ -20,6 +20,15 @@ struct MolBuild {
     bool is_dendrimer = false;
 };
 
+// One reaction: the states of its equation in written order and their
+// stoichiometric numbers, negative on the left-hand side (Reaction::
+// CheckInput, reaction.cpp:37-145).
+struct ReactionDef {
+    std::string name;
+    double pK = 0;
+    std::vector<int> sto, state;
+};
+
 // `plan` must stay the first member: nm_plan* and PlanHolder* are converted
 // into each other.
 struct PlanHolder {
@@ -37,9 +46,22 @@ struct PlanHolder {
     std::vector<const char*> state_name_ptrs;
     std::vector<int> state_seg, state_it, seg_nstate, it_sp;
     std::vector<double> state_valence, state_alphabulk, chi_sp;
+    std::vector<ReactionDef> reactions;
+    std::vector<char> state_fixed;     // alphabulk given in the input
+    std::vector<double> state_ab_in;   // the input's alphabulk (-1 where none)
+    std::vector<double> mol_nmon;      // per molecule and molmon: segments of that type
     std::vector<std::string> mol_names;
     std::vector<const char*> mol_name_ptrs;
     std::string method_note;
 };
+
+// The states' bulk fractions and the molecules' charges of a plan with
+// internal states, the fixed states' alphabulk taken from `fixed_ab`
+// [n_state] (other entries unused; a `var : state-<name> : scan :
+// alphabulk` step, State::UpdateVarInfo, state.cpp:306-318) and the
+// reactions' pK_eff from the species' bulk volume fractions `sp_phibulk`
+// [n_sp] of the last solve (null before any).
+int plan_state_bulk(const nm_plan* p, const std::vector<double>& fixed_ab, const double* sp_phibulk,
+                    std::vector<double>& alphabulk, std::vector<double>& mol_charge, std::string& err);
 
 }  // namespace nm

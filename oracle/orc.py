@@ -35,6 +35,7 @@ def load() -> C.CDLL:
         lib.orc_compose.argtypes = [C.c_void_p, dp, C.c_int, dp, dp]
         lib.orc_side.argtypes = [C.c_void_p, dp, dp]
         lib.orc_set_amount.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double]
+        lib.orc_set_states.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         lib.orc_search.argtypes = [C.c_void_p, dp, dp, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         _lib = lib
     return _lib
@@ -80,6 +81,14 @@ class Oracle:
         rc = load().orc_set_amount(self._h, mol, what, value)
         if rc:
             raise RuntimeError(f"orc_set_amount rc={rc}")
+
+    def set_states(self, alphabulk) -> None:
+        """The states' bulk fractions for the next solves (a scan of a fixed
+        state's alphabulk; the bulk equilibrium comes from the caller)."""
+        ab = np.ascontiguousarray(alphabulk, dtype=np.float64)
+        rc = load().orc_set_states(self._h, _p(ab))
+        if rc:
+            raise RuntimeError(f"orc_set_states rc={rc}")
 
     def search(self, x: np.ndarray):
         """The plan's search from x: (rc, x, value, error, iterations, solves)."""

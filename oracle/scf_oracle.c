@@ -31,6 +31,9 @@ struct orc_state {
      * a molecule (SysMonList) */
     double *ust, *ast, *sp_phibulk;
     int *in_mol;
+    /* the states' bulk fractions and the molecules' bulk charges in force
+     * (the plan's, until orc_set_states changes them) */
+    double *st_ab, *mol_charge;
     int have_state;
     /* molecule amounts in force (the plan's, until orc_set_amount changes
      * them, as a Variate scan or search step does) and a search's inner
@@ -763,7 +766,7 @@ static void prepare_G1(orc_state* st, const double* x) {
                 }
                 set_bounds(st, uj);
                 for (int s = 0; s < M; s++) aj[s] = exp(-uj[s]);
-                Norm(aj, P->state_alphabulk[j], M);
+                Norm(aj, st->st_ab[j], M);
                 Add(G1, aj, M);
             }
             for (int j = 0; j < P->n_state; j++)
@@ -844,14 +847,14 @@ static int compute_phis(orc_state* st, const double* x) {
             norm = a_phibulk / N;
             st->mol_n[m] = norm * st->GN[m];
             st->mol_theta[m] = st->mol_n[m] * N;  /* θ = n·N (Molecule::theta of a free molecule) */
-            A += a_phibulk * mol->charge; B += a_phibulk;
+            A += a_phibulk * st->mol_charge[m]; B += a_phibulk;
         } else if (mol->freedom == NM_MOL_RESTRICTED) {
             if (st->GN[m] > 0) {
                 norm = a_n / st->GN[m];
                 if (mol->pinned) st->mol_phibulk[m] = 0;
                 else {
                     st->mol_phibulk[m] = N * norm;
-                    A += st->mol_phibulk[m] * mol->charge; B += st->mol_phibulk[m];
+                    A += st->mol_phibulk[m] * st->mol_charge[m]; B += st->mol_phibulk[m];
                 }
             } else return NM_ERR_GN;
         } else st->mol_phibulk[m] = 0;
@@ -867,8 +870,8 @@ static int compute_phis(orc_state* st, const double* x) {
          * neutral (system.cpp:2487-2515, 2560-2570) */
         int nt = P->neutralizer;
         const nm_molecule* mol = &P->mols[nt];
-        double qs = P->solvent >= 0 ? P->mols[P->solvent].charge : 0;
-        if (mol->charge != qs) st->mol_phibulk[nt] = ((B - 1.0) * qs - A) / (mol->charge - qs);
+        double qs = P->solvent >= 0 ? st->mol_charge[P->solvent] : 0;
+        if (st->mol_charge[nt] != qs) st->mol_phibulk[nt] = ((B - 1.0) * qs - A) / (st->mol_charge[nt] - qs);
         B += st->mol_phibulk[nt];
         double norm = st->mol_phibulk[nt] / mol->chainlength;
         st->mol_n[nt] = norm * st->GN[nt];
@@ -913,7 +916,7 @@ static int compute_phis(orc_state* st, const double* x) {
         double* pj = st->phi + (size_t)(ns + j) * M;
         Times(pj, st->ast + (size_t)j * M, st->phi + (size_t)sg * M, M);
         stencil(st, st->phi_side + (size_t)(ns + j) * M, pj, 1);
-        st->sp_phibulk[ns + j] = st->seg_phibulk[sg] * P->state_alphabulk[j];
+        st->sp_phibulk[ns + j] = st->seg_phibulk[sg] * st->st_ab[j];
     }
     return NM_OK;
 }
@@ -1311,14 +1314,14 @@ int orc_free_energy(orc_state* st, double* Fout, double* Omega, double* mu) {
                 }
                 for (int l = 0; l < P->n_state; l++) {  /* system.cpp:3345-3358 */
                     double pbB = st->sp_phibulk[ns + l];
-                    double FB = mol_fraction(mol, P->state_seg[l]) * P->state_alphabulk[l];
+                    double FB = mol_fraction(mol, P->state_seg[l]) * st->st_ab[l];
                     double chi = chi_of(P, j, ns + l) / 2;
                     Mu = Mu - NA * chi * (pbA - FA) * (pbB - FB);
                 }
             }
             for (int j = 0; j < P->n_state; j++) {  /* system.cpp:3361-3400 */
                 double pbA = st->sp_phibulk[ns + j];
-                double FA = mol_fraction(mol, P->state_seg[j]) * P->state_alphabulk[j];
+                double FA = mol_fraction(mol, P->state_seg[j]) * st->st_ab[j];
                 for (int k = 0; k < ns; k++) {
                     if (has_states(P, k)) continue;
                     double pbB = st->seg_phibulk[k], FB = mol_fraction(mol, k);
@@ -1329,7 +1332,7 @@ int orc_free_energy(orc_state* st, double* Fout, double* Omega, double* mu) {
                  * (system.cpp:3388-3391) */
                 for (int k = 0; k < P->n_state; k++) {
                     double pbB = st->sp_phibulk[ns + k];
-                    double FB = mol_fraction(mol, P->state_seg[j]) * P->state_alphabulk[j];
+                    double FB = mol_fraction(mol, P->state_seg[j]) * st->st_ab[j];
                     double chi = chi_of(P, ns + j, ns + k) / 2;
                     Mu = Mu - NA * chi * (pbA - FA) * (pbB - FB);
                 }
@@ -1361,6 +1364,10 @@ orc_state* orc_create(const nm_plan* P) {
     st->ast = calloc((size_t)(P->n_state + 1) * M, sizeof(double));
     st->sp_phibulk = calloc((size_t)nsp, sizeof(double));
     st->in_mol = calloc((size_t)ns, sizeof(int));
+    st->st_ab = calloc((size_t)(P->n_state + 1), sizeof(double));
+    for (int j = 0; j < P->n_state; j++) st->st_ab[j] = P->state_alphabulk[j];
+    st->mol_charge = calloc((size_t)nm, sizeof(double));
+    for (int m = 0; m < nm; m++) st->mol_charge[m] = P->mols[m].charge;
     for (int m = 0; m < nm; m++)
         for (int k = 0; k < P->mols[m].n_molmon; k++) st->in_mol[P->mols[m].molmon_seg[k]] = 1;
     st->phitot = calloc((size_t)M, sizeof(double));
@@ -1410,6 +1417,33 @@ orc_state* orc_create(const nm_plan* P) {
     st->eps = calloc((size_t)M, sizeof(double));
     st->X = calloc((size_t)M, sizeof(double));
     return st;
+}
+
+/* New bulk fractions of the states (a scan step of a fixed state's
+ * alphabulk, with the bulk equilibrium solved by the caller): the molecules'
+ * bulk charges follow as Molecule::Charge (molecule.cpp:1866-1879) counts
+ * them, Σ α_bulk·valence over each state segment's states. */
+int orc_set_states(orc_state* st, const double* alphabulk) {
+    const nm_plan* P = st->P;
+    if (!P->n_state) return NM_ERR_ARG;
+    for (int j = 0; j < P->n_state; j++) st->st_ab[j] = alphabulk[j];
+    for (int m = 0; m < P->n_mol; m++) {
+        const nm_molecule* mol = &P->mols[m];
+        int with_states = 0;
+        for (int k = 0; k < mol->n_molmon; k++) with_states |= has_states(P, mol->molmon_seg[k]);
+        if (!with_states) continue;
+        double q = 0;
+        for (int k = 0; k < mol->n_molmon; k++) {
+            const int sg = mol->molmon_seg[k];
+            const double nmon = mol->molmon_fraction[k] * mol->chainlength;
+            if (has_states(P, sg)) {
+                for (int j = 0; j < P->n_state; j++)
+                    if (P->state_seg[j] == sg) q += st->st_ab[j] * P->state_valence[j] * nmon;
+            } else q += P->seg_valence[sg] * nmon;
+        }
+        st->mol_charge[m] = q / mol->chainlength;
+    }
+    return NM_OK;
 }
 
 /* A scan or search step's value change (Molecule::PutValue,
@@ -1526,6 +1560,6 @@ void orc_destroy(orc_state* st) {
     free(st->seg_phibulk);
     free(st->psi); free(st->EE); free(st->q); free(st->eps); free(st->X);
     free(st->gb3); free(st->m2l1); free(st->m2l11); free(st->m2l_1); free(st->m2l_11);
-    free(st->ust); free(st->ast); free(st->sp_phibulk); free(st->in_mol);
+    free(st->ust); free(st->ast); free(st->sp_phibulk); free(st->in_mol); free(st->st_ab); free(st->mol_charge);
     free(st);
 }

@@ -35,6 +35,9 @@ int orc_free_energy(orc_state* st, double* F, double* Omega, double* mu);
 /* a molecule amount in force for the next solves (what: 0 θ, 1 n, 2 φ_bulk),
  * and the plan's search from x (updated in place) */
 int orc_set_amount(orc_state* st, int mol, int what, double value);
+/* the states' bulk fractions in force for the next solves [n_state] (a scan
+ * of a fixed state's alphabulk; the bulk equilibrium is the caller's) */
+int orc_set_states(orc_state* st, const double* alphabulk);
 int orc_search(orc_state* st, double* x, double* value, double* error, int* iterations, int* solves);
 /* Molecule::ComputePhi of molecule m at the field x: rho [n_molmon*M] =
  * Σ d·Gf·Gb per segment type (before System::ComputePhis divides by G1 and

@@ -69,3 +69,38 @@ def test_scan_refuses_splitting_an_iteration_species():
     assert e.value.code == NM_ERR_INPUT
     r1, xb, Fb = _solve(ctx, np.array(run["x"]))
     assert r1.iterations == r0.iterations and np.array_equal(xa, xb) and Fa == Fb
+
+
+def test_state_scan_matches_reference(tmp_path):
+    """A pH scan of the weak-polyacid brush (`var : state-H3O : scan :
+    alphabulk`, 1e-7 to 1e-5, one step per decade), each step set with
+    nm_ctx_set_values and solved from the previous step's field, against the
+    reference's own rows.  Each step's bulk equilibrium reads the previous
+    solve's bulk volume fractions (Reaction::pKeff), which moves pK_eff by
+    about 0.3 here: the bulk fractions must follow that, not the input pK."""
+    g = load_golden("scan_states_h3o")
+    plan = Plan(g["input"])
+    assert plan.c.scan_state >= 0
+    values = plan.scan_values()
+    assert len(values) == len(g["rows"]) == 3
+    ctx = Context(plan, NM_FP64)
+    x = np.array(g["x"])
+    items = [it for it in g["items"] if not it.startswith("newton")]
+    for k, (v, row) in enumerate(zip(values, g["rows"])):
+        if k > 0:
+            ctx.set_values({"state : H3O : alphabulk": v})
+        r, x, F = _solve(ctx, x)
+        assert r.status == 0
+        path = tmp_path / f"s{k}.kal"
+        ctx.write_kal(path, items)
+        head, vals = path.read_text().strip().splitlines()
+        got = dict(zip(head.split("\t"), (float(t) for t in vals.split("\t"))))
+        for h, want in row.items():
+            if h.startswith("newton"):
+                continue
+            # the two solves' bulk volume fractions agree to their
+            # convergence (‖g‖ < 1e-7), and pK_eff and the bulk fractions
+            # (relative: the OH- fraction is ~5e-9) with them
+            tol = 1e-6 * (abs(want) if "alphabulk" in h else max(1.0, abs(want)))
+            assert abs(got[h] - want) <= tol, (k, h, got[h], want)
+        assert abs(r.iterations - int(row["newton_isaac_iterations"])) <= 3, (k, r.iterations)

@@ -101,12 +101,18 @@ SCANS = sorted(p.stem for p in GOLDEN.glob("scan_*.json"))
 @pytest.mark.parametrize("name", SCANS)
 def test_scan_values_are_the_reference_steps(name):
     """tests/golden/scan_*.json (make_golden.py --scan): the reference's scans
-    of θ, one .kal row per step.  The plan's step values are the reference's
-    (the step count truncated like its integer division)."""
+    of θ and of a fixed state's alphabulk, one .kal row per step.  The plan's
+    step values are the reference's (the step count truncated like its
+    integer division)."""
     g = _load(name)
     plan = Plan(g["input"])
     vals = plan.scan_values()
-    ref = [r["mol_pol_theta"] for r in g["rows"]]
+    c = plan.c
+    if c.scan_state >= 0:
+        col = f"mon_{plan.seg_names[c.state_seg[c.scan_state]]}_alphabulk_{plan.state_names[c.scan_state]}"
+    else:
+        col = "mol_pol_theta"
+    ref = [r[col] for r in g["rows"]]
     assert len(vals) == len(ref)
     assert np.allclose(vals, ref, rtol=1e-12, atol=0)
 
@@ -152,8 +158,10 @@ def test_scan_matches_reference(name):
     plan = Plan(g["input"])
     ctx = Context(plan, NM_FP64)
     x = torch.from_numpy(np.array(g["x"])).cuda()
+    c = plan.c
+    item = f"state : {plan.state_names[c.scan_state]} : alphabulk" if c.scan_state >= 0 else "mol : pol : theta"
     for v, row in zip(plan.scan_values(), g["rows"]):
-        ctx.set_values({"mol : pol : theta": v})
+        ctx.set_values({item: v})
         r = ctx.solve_dev(x.data_ptr())
         assert r.status == 0, (v, r)
         F, O, _ = ctx.free_energy()
@@ -212,8 +220,16 @@ def test_oracle_scan_follows_the_reference(name):
     plan = Plan(g["input"])
     orc = _oracle(plan)
     x = np.array(g["x"])
+    c = plan.c
     for v, row in zip(plan.scan_values(), g["rows"]):
-        orc.set_amount(plan.c.scan_mol, plan.c.scan_what, v)
+        if c.scan_state >= 0:
+            # a pH scan: the states' bulk fractions of each step are the
+            # reference's own (its bulk equilibrium reads the previous solve;
+            # the device context's restatement of that is tested on the GPU)
+            orc.set_states([row[f"mon_{plan.seg_names[c.state_seg[j]]}_alphabulk_{st}"]
+                            for j, st in enumerate(plan.state_names)])
+        else:
+            orc.set_amount(c.scan_mol, c.scan_what, v)
         rc, x, _, res = orc.solve(x)
         assert rc == 0 and res < plan.c.tolerance
         F, O, _ = orc.free_energy()
