@@ -206,6 +206,11 @@ typedef struct nm_plan {
      * nm_plan_scan_value gives their values; nm_ctx_set_values takes each as
      * `state : <name> : alphabulk`. */
     int    scan_state;
+    /* a scan of a reaction's pK (`var : reaction-<name> : scan : pK`,
+     * linear steps, Reaction::PutVarScan, reaction.cpp:390-408): the
+     * reaction's index in input order, or -1; nm_ctx_set_values takes each
+     * step as `reaction : <name> : pK` */
+    int    scan_reaction;
 } nm_plan;
 
 /* Parse Namics input text (the `lat/mon/mol/sys/newton` key subset of the
@@ -304,9 +309,10 @@ int nm_plan_scan_value(const nm_plan* plan, int k, double* value);
  * start).  items: "mon : <seg> : chi_<seg>" (set both ways; not on a plan
  * with internal states), "mol : <mol> : n | theta" (restricted), "mol :
  * <mol> : phibulk" (free), "state : <state> : alphabulk" (a state whose
- * alphabulk the input fixes).  All are applied, then checked: χ must keep
+ * alphabulk the input fixes), "reaction : <reaction> : pK".  All are
+ * applied, then checked: χ must keep
  * the iteration species (segments with equal χ rows) unchanged.  A state's
- * new value solves the bulk equilibrium again, its pK_eff from the bulk
+ * or a reaction's new value solves the bulk equilibrium again, its pK_eff from the bulk
  * volume fractions of the context's last residual, as the reference's next
  * solve does (Reaction::pKeff, reaction.cpp:253-266); the molecules' bulk
  * charges follow.  On error nothing changes (NM_ERR_ARG, NM_ERR_INPUT). */

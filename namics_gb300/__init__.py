@@ -134,7 +134,7 @@ class Plan:
         """The values of the input's scan (`var : … : scan`), step 0 first;
         empty without a scan."""
         c = self.c
-        if c.scan_mol < 0 and c.scan_state < 0:
+        if c.scan_mol < 0 and c.scan_state < 0 and c.scan_reaction < 0:
             return []
         out = []
         for k in range(c.scan_n + 1):

@@ -69,7 +69,8 @@ class nm_plan(C.Structure):
                 ("save_memory", C.c_int),
                 ("n_state", C.c_int), ("state_name", C.POINTER(C.c_char_p)), ("state_seg", ip),
                 ("state_valence", dp), ("state_alphabulk", dp), ("state_it", ip), ("seg_nstate", ip),
-                ("n_sp", C.c_int), ("chi_sp", dp), ("it_sp", ip), ("scan_state", C.c_int)]
+                ("n_sp", C.c_int), ("chi_sp", dp), ("it_sp", ip), ("scan_state", C.c_int),
+                ("scan_reaction", C.c_int)]
 
 
 class nm_ctx_options(C.Structure):

@@ -1058,6 +1058,7 @@ int Ctx::init(const nm_plan* p, const nm_ctx_options* opt) {
         TRY(dalloc(&d_ast, (size_t)nst * M, stream));
         chi_sp.assign(p->chi_sp, p->chi_sp + (size_t)nsp * nsp);
         st_fixed = reinterpret_cast<const PlanHolder*>(p)->state_ab_in;
+        st_pK = plan_reaction_pK(p);
     }
     // state
     TRY(dalloc(&d_G1, (size_t)ns * M, stream));
@@ -1254,7 +1255,7 @@ int nm_ctx_set_values(nm_ctx* ctx, const char* const* items, const double* value
     const int ns = p->n_seg;
     std::vector<double> chi = c->chi;
     nm::NormArgs na = c->norm_args;
-    std::vector<double> st_fixed = c->st_fixed;
+    std::vector<double> st_fixed = c->st_fixed, st_pK = c->st_pK;
     bool states_changed = false;
     auto trim = [](std::string s) {
         size_t a = s.find_first_not_of(" \t"), b = s.find_last_not_of(" \t");
@@ -1284,6 +1285,10 @@ int nm_ctx_set_values(nm_ctx* ctx, const char* const* items, const double* value
             const nm::PlanHolder& H = *reinterpret_cast<const nm::PlanHolder*>(p);
             for (int j = 0; j < c->nst; j++)
                 if (name == p->state_name[j] && H.state_fixed[j]) { st_fixed[j] = v; states_changed = ok = true; }
+        } else if (key == "reaction" && prop == "pK" && c->nst > 0) {
+            // a reaction's pK (Reaction::PutValue, reaction.cpp:443-452)
+            const int r = nm::plan_reaction_index(p, name);
+            if (r >= 0) { st_pK[r] = v; states_changed = ok = true; }
         } else if (key == "mol") {
             for (int m = 0; m < p->n_mol; m++) {
                 if (!p->mol_name || name != p->mol_name[m]) continue;
@@ -1319,7 +1324,7 @@ int nm_ctx_set_values(nm_ctx* ctx, const char* const* items, const double* value
             if (e != cudaSuccess) { nm::set_error(cudaGetErrorString(e)); return NM_ERR_CUDA; }
         }
         std::string err;
-        if (int rc = nm::plan_state_bulk(p, st_fixed, c->have_state ? spb.data() : nullptr, ab, charge, err)) {
+        if (int rc = nm::plan_state_bulk(p, st_fixed, st_pK, c->have_state ? spb.data() : nullptr, ab, charge, err)) {
             nm::set_error("nm_ctx_set_values: " + err);
             return rc;
         }
@@ -1335,6 +1340,7 @@ int nm_ctx_set_values(nm_ctx* ctx, const char* const* items, const double* value
         c->st = stn;
         c->phi_args.st = stn;
         c->st_fixed = st_fixed;
+        c->st_pK = st_pK;
     }
     if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
     nm::ctx_loop_drop(*c);

@@ -269,6 +269,7 @@ struct Ctx {
     double *d_ust = nullptr, *d_ast = nullptr;
     std::vector<double> chi_sp;  // χ between species (plans with states)
     std::vector<double> st_fixed;  // the fixed states' alphabulk in force (nm_ctx_set_values)
+    std::vector<double> st_pK;     // the reactions' pK in force (nm_ctx_set_values)
     // electrostatics (charged systems, 1 and 2 gradients): ψ is the last
     // block of x; halo sites of the composition are evaluated (nh of them)
     bool charged = false;

@@ -222,6 +222,10 @@ int nm_write_kal(nm_ctx* ctx, const char* path, const char* const* items, int n_
                 ok = true;
                 break;
             }
+        } else if (key == "reaction" && prop == "pK" && p->n_state > 0) {
+            // the reaction's pK in force (Reaction::PushOutput, reaction.cpp:188-201)
+            const int r = plan_reaction_index(p, name);
+            if (r >= 0) { v.d = c->st_pK[r]; ok = true; }
         } else if (key == "mol") {
             int m = mol_index(p, name);
             if (m >= 0) {

@@ -1042,18 +1042,38 @@ static bool build_states(const InputBlock& in, PlanHolder& H, std::string& err) 
     return true;
 }
 
-int plan_state_bulk(const nm_plan* p, const std::vector<double>& fixed_ab, const double* sp_phibulk,
-                    std::vector<double>& alphabulk, std::vector<double>& mol_charge, std::string& err) {
+std::vector<double> plan_reaction_pK(const nm_plan* p) {
+    const PlanHolder& H = *reinterpret_cast<const PlanHolder*>(p);
+    std::vector<double> pk;
+    for (auto& r : H.reactions) pk.push_back(r.pK);
+    return pk;
+}
+
+int plan_reaction_index(const nm_plan* p, const std::string& name) {
+    const PlanHolder& H = *reinterpret_cast<const PlanHolder*>(p);
+    for (size_t r = 0; r < H.reactions.size(); r++)
+        if (H.reactions[r].name == name) return (int)r;
+    return -1;
+}
+
+int plan_state_bulk(const nm_plan* p, const std::vector<double>& fixed_ab, const std::vector<double>& pK,
+                    const double* sp_phibulk, std::vector<double>& alphabulk, std::vector<double>& mol_charge,
+                    std::string& err) {
     const PlanHolder& H = *reinterpret_cast<const PlanHolder*>(p);
     const int ns = p->n_seg, nst = p->n_state, nsp = p->n_sp;
-    if (nst == 0 || (int)fixed_ab.size() != nst) { err = "no internal states"; return NM_ERR_ARG; }
+    if (nst == 0 || (int)fixed_ab.size() != nst || pK.size() != H.reactions.size()) {
+        err = "no internal states";
+        return NM_ERR_ARG;
+    }
+    std::vector<ReactionDef> R = H.reactions;
+    for (size_t r = 0; r < R.size(); r++) R[r].pK = pK[r];
     std::vector<double> ab0 = H.state_ab_in;
     for (int j = 0; j < nst; j++)
         if (H.state_fixed[j]) {
             if (!(fixed_ab[j] >= 0 && fixed_ab[j] <= 1)) { err = "alphabulk out of range 0 ... 1"; return NM_ERR_ARG; }
             ab0[j] = fixed_ab[j];
         }
-    Chem chem(H.reactions, H.state_seg, H.state_valence, H.state_fixed, ab0, ns);
+    Chem chem(R, H.state_seg, H.state_valence, H.state_fixed, ab0, ns);
     if (sp_phibulk) {
         // Reaction::pKeff (reaction.cpp:253-266) with ChemIntBulk
         // (reaction.cpp:243-251) over the bulk volume fractions of the last
@@ -1066,11 +1086,10 @@ int plan_state_bulk(const nm_plan* p, const std::vector<double>& fixed_ab, const
             for (int l = 0; l < nst; l++) v += p->chi_sp[(size_t)(ns + j) * nsp + ns + l] * sp_phibulk[ns + l];
             return v;
         };
-        for (size_t r = 0; r < H.reactions.size(); r++) {
-            const ReactionDef& R = H.reactions[r];
+        for (size_t r = 0; r < R.size(); r++) {
             double v = 0;
-            for (size_t i = 0; i < R.sto.size() && (int)i < nst; i++) v += R.sto[i] * cib((int)i);
-            chem.pke[r] = R.pK + v / std::log(10.0);
+            for (size_t i = 0; i < R[r].sto.size() && (int)i < nst; i++) v += R[r].sto[i] * cib((int)i);
+            chem.pke[r] = R[r].pK + v / std::log(10.0);
         }
     }
     if (!chem.solve()) { err = chem.err; return NM_ERR_INPUT; }
@@ -1474,6 +1493,7 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
     // `var : mol-<name> : theta|n|phibulk|mu : <value>` (Variate::CheckInput,
     // variate.cpp:60-200; Molecule::PutVarInfo, molecule.cpp:679-740) ----
     P.scan_mol = -1; P.scan_what = -1; P.scan_n = 0; P.scan_exponential = 0; P.scan_state = -1;
+    P.scan_reaction = -1;
     P.scan_start = P.scan_end = P.scan_step = 0;
     P.search_mol = -1; P.search_what = -1;
     P.target_kind = -1; P.target_mol = -1; P.target_what = -1; P.target_value = 0;
@@ -1578,7 +1598,9 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
                     err = "var '" + vn + "': a state scan takes the alphabulk of a state that fixes it";
                     delete H; return nullptr;
                 }
-                if (P.scan_mol >= 0 || P.scan_state >= 0) { err = "one scan per input"; delete H; return nullptr; }
+                if (P.scan_mol >= 0 || P.scan_state >= 0 || P.scan_reaction >= 0) {
+                    err = "one scan per input"; delete H; return nullptr;
+                }
                 double end = 0, step = 0;
                 if (!in.has("var", vn, "end_value") || !to_real(in.get("var", vn, "end_value"), end)) {
                     err = "var '" + vn + "': a scan needs a numeric end_value"; delete H; return nullptr;
@@ -1613,6 +1635,33 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
                     err = "var '" + vn + "': scale is linear or exponential"; delete H; return nullptr;
                 }
                 P.scan_state = sj; P.scan_what = 3; P.scan_n = nsteps;
+                P.scan_start = start; P.scan_end = end; P.scan_step = step;
+            } else if (item == "reaction" && in.has("var", vn, "scan")) {
+                // a reaction's pK, linear steps only (Reaction::PutVarInfo /
+                // PutVarScan, reaction.cpp:381-408)
+                int ri = -1;
+                for (size_t r = 0; r < H->reactions.size(); r++) if (H->reactions[r].name == name) ri = (int)r;
+                if (ri < 0) { err = "var '" + vn + "': no reaction " + name; delete H; return nullptr; }
+                if (in.get("var", vn, "scan") != "pK") { err = "var '" + vn + "': a reaction scan takes pK"; delete H; return nullptr; }
+                if (P.scan_mol >= 0 || P.scan_state >= 0 || P.scan_reaction >= 0) {
+                    err = "one scan per input"; delete H; return nullptr;
+                }
+                if (in.get("var", vn, "scale", "linear") != "linear") {
+                    err = "var '" + vn + "': a pK scan is linear"; delete H; return nullptr;
+                }
+                double end = 0, step = 0;
+                if (!in.has("var", vn, "end_value") || !to_real(in.get("var", vn, "end_value"), end)) {
+                    err = "var '" + vn + "': a scan needs a numeric end_value"; delete H; return nullptr;
+                }
+                if (!in.has("var", vn, "step") || !to_real(in.get("var", vn, "step"), step) || step == 0) {
+                    err = "var '" + vn + "': a linear scan needs a nonzero step"; delete H; return nullptr;
+                }
+                const double start = H->reactions[ri].pK;
+                const double ns_real = (end - start) / step;
+                if (!(ns_real < 1e6 && ns_real > -1e6)) { err = "var '" + vn + "': more than 10^6 scan steps"; delete H; return nullptr; }
+                const int nsteps = (int)ns_real;
+                if (nsteps < 0) { err = "var '" + vn + "': (end_value - start)/step is negative"; delete H; return nullptr; }
+                P.scan_reaction = ri; P.scan_what = 4; P.scan_n = nsteps;
                 P.scan_start = start; P.scan_end = end; P.scan_step = step;
             } else if (item == "sys") {
                 if (in.has("var", vn, "free_energy") && !set_target(0, -1, -1, in.get("var", vn, "free_energy"))) {
@@ -1700,7 +1749,8 @@ int nm_plan_create(const char* input_text, nm_plan** out) {
 }
 
 int nm_plan_scan_value(const nm_plan* plan, int k, double* value) {
-    if (!plan || !value || (plan->scan_mol < 0 && plan->scan_state < 0) || k < 0 || k > plan->scan_n) {
+    if (!plan || !value || (plan->scan_mol < 0 && plan->scan_state < 0 && plan->scan_reaction < 0) || k < 0 ||
+        k > plan->scan_n) {
         nm::set_error("nm_plan_scan_value: no scan, or step out of range");
         return NM_ERR_ARG;
     }

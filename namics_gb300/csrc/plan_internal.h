@@ -58,10 +58,17 @@ struct PlanHolder {
 // The states' bulk fractions and the molecules' charges of a plan with
 // internal states, the fixed states' alphabulk taken from `fixed_ab`
 // [n_state] (other entries unused; a `var : state-<name> : scan :
-// alphabulk` step, State::UpdateVarInfo, state.cpp:306-318) and the
-// reactions' pK_eff from the species' bulk volume fractions `sp_phibulk`
-// [n_sp] of the last solve (null before any).
-int plan_state_bulk(const nm_plan* p, const std::vector<double>& fixed_ab, const double* sp_phibulk,
-                    std::vector<double>& alphabulk, std::vector<double>& mol_charge, std::string& err);
+// alphabulk` step, State::UpdateVarInfo, state.cpp:306-318), the
+// reactions' pK from `pK` [reactions] (a `var : reaction-<name> : scan :
+// pK` step, Reaction::UpdateVarInfo, reaction.cpp:410-425) and their pK_eff
+// from the species' bulk volume fractions `sp_phibulk` [n_sp] of the last
+// solve (null before any).
+int plan_state_bulk(const nm_plan* p, const std::vector<double>& fixed_ab, const std::vector<double>& pK,
+                    const double* sp_phibulk, std::vector<double>& alphabulk, std::vector<double>& mol_charge,
+                    std::string& err);
+// the reactions' pK of the input, in input order
+std::vector<double> plan_reaction_pK(const nm_plan* p);
+// reaction index by name, or -1
+int plan_reaction_index(const nm_plan* p, const std::string& name);
 
 }  // namespace nm

@@ -75,7 +75,8 @@ class PlanRecord(C.Structure):
                 ("scan_end", C.c_double), ("scan_step", C.c_double), ("save_memory", C.c_int),
                 ("n_state", C.c_int), ("state_name", C.POINTER(C.c_char_p)), ("state_seg", ip),
                 ("state_valence", dp), ("state_alphabulk", dp), ("state_it", ip), ("seg_nstate", ip),
-                ("n_sp", C.c_int), ("chi_sp", dp), ("it_sp", ip), ("scan_state", C.c_int)]
+                ("n_sp", C.c_int), ("chi_sp", dp), ("it_sp", ip), ("scan_state", C.c_int),
+                ("scan_reaction", C.c_int)]
 
 
 def _entries(text: str):
@@ -387,6 +388,7 @@ class OraclePlan:
         P.n_seg = ns
         P.n_sp = ns
         P.scan_state = -1
+        P.scan_reaction = -1
         names = (C.c_char_p * ns)(*[s.encode() for s in segs])
         mnames = (C.c_char_p * len(mols))(*[s.encode() for s in mols])
         keep += [names, mnames]

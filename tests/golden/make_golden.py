@@ -554,29 +554,39 @@ def main_scan():
         # a pH scan of the weak-polyacid brush: the fixed H3O+ fraction from
         # 1e-7 to 1e-5, one step per decade; each step's bulk equilibrium
         # reads the previous solve's bulk fractions (Reaction::pKeff)
+        # and a scan of the acid's pK from 6 to 8
         case = next(c for c in cases() if c["name"] == "states_weak1d")
-        name = "scan_states_h3o"
-        extra = ["var : state-H3O : scan : alphabulk", "var : state-H3O : scale : exponential",
-                 "var : state-H3O : end_value : 1e-5", "var : state-H3O : steps : 1"]
-        text = "\n".join(list(case["lines"]) + extra + newton()) + "\n"
-        plan = Plan(text)
-        x = make_field(plan, *case["field"], case["seed"], False)
-        write_guess(wd / f"{name}.guess", plan, x)
-        full = text + "sys : noname : initial_guess : file\n" + f"sys : noname : guess_inputfile : {name}.guess\n"
-        items = [f"mon : {plan.seg_names[plan.c.state_seg[j]]} : alphabulk_{st}" for j, st in enumerate(plan.state_names)]
-        items += ["mol : pol : theta", "sys : noname : free_energy", "sys : noname : grand_potential",
-                  "newton : isaac : iterations"]
-        full += "output : kal : append : true\n" + "\n".join(f"kal : {k}" for k in items) + "\nstart\n"
-        (wd / f"{name}.in").write_text(full)
-        r = subprocess.run([str(REF_BIN), f"{name}.in"], cwd=wd, capture_output=True, text=True, timeout=600)
-        kal = wd / "output" / f"{name}.kal"
-        if r.returncode != 0 or not kal.exists():
-            raise RuntimeError(f"reference failed on {name}: {r.stdout[-1500:]}")
-        lines = kal.read_text().strip().splitlines()
-        head = lines[0].split("\t")
-        rows = [dict(zip(head, (float(t) for t in ln.split("\t")))) for ln in lines[1:]]
-        (GOLDEN / f"{name}.json").write_text(json.dumps(dict(input=text, x=x.tolist(), items=items, rows=rows)))
-        print(name, [round(rw["mon_A_alphabulk_AM"], 6) for rw in rows], flush=True)
+        for name, extra in (("scan_states_h3o", ["var : state-H3O : scan : alphabulk",
+                                                 "var : state-H3O : scale : exponential",
+                                                 "var : state-H3O : end_value : 1e-5", "var : state-H3O : steps : 1"]),
+                            ("scan_states_pk", ["var : reaction-weak : scan : pK", "var : reaction-weak : step : 1",
+                                                "var : reaction-weak : end_value : 8"])):
+            state_scan(wd, case, name, extra)
+
+
+def state_scan(wd: Path, case: dict, name: str, extra: list[str]) -> None:
+    """A scan of the weak-polyacid brush (states_weak1d) by the reference,
+    one .kal row per step: the states' bulk fractions, θ, F, Ω (the
+    reference's output has no reaction items)."""
+    text = "\n".join(list(case["lines"]) + extra + newton()) + "\n"
+    plan = Plan(text)
+    x = make_field(plan, *case["field"], case["seed"], False)
+    write_guess(wd / f"{name}.guess", plan, x)
+    full = text + "sys : noname : initial_guess : file\n" + f"sys : noname : guess_inputfile : {name}.guess\n"
+    items = [f"mon : {plan.seg_names[plan.c.state_seg[j]]} : alphabulk_{st}" for j, st in enumerate(plan.state_names)]
+    items += ["mol : pol : theta", "sys : noname : free_energy", "sys : noname : grand_potential",
+              "newton : isaac : iterations"]
+    full += "output : kal : append : true\n" + "\n".join(f"kal : {k}" for k in items) + "\nstart\n"
+    (wd / f"{name}.in").write_text(full)
+    r = subprocess.run([str(REF_BIN), f"{name}.in"], cwd=wd, capture_output=True, text=True, timeout=600)
+    kal = wd / "output" / f"{name}.kal"
+    if r.returncode != 0 or not kal.exists():
+        raise RuntimeError(f"reference failed on {name}: {r.stdout[-1500:]}")
+    lines = kal.read_text().strip().splitlines()
+    head = lines[0].split("\t")
+    rows = [dict(zip(head, (float(t) for t in ln.split("\t")))) for ln in lines[1:]]
+    (GOLDEN / f"{name}.json").write_text(json.dumps(dict(input=text, x=x.tolist(), items=items, rows=rows)))
+    print(name, [round(rw["mon_A_alphabulk_AM"], 6) for rw in rows], flush=True)
 
 
 def main():

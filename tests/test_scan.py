@@ -71,16 +71,19 @@ def test_scan_refuses_splitting_an_iteration_species():
     assert r1.iterations == r0.iterations and np.array_equal(xa, xb) and Fa == Fb
 
 
-def test_state_scan_matches_reference(tmp_path):
+@pytest.mark.parametrize("name,item", [("scan_states_h3o", "state : H3O : alphabulk"),
+                                       ("scan_states_pk", "reaction : weak : pK")])
+def test_state_scan_matches_reference(name, item, tmp_path):
     """A pH scan of the weak-polyacid brush (`var : state-H3O : scan :
-    alphabulk`, 1e-7 to 1e-5, one step per decade), each step set with
+    alphabulk`, 1e-7 to 1e-5, one step per decade) and a scan of the acid's
+    pK (`var : reaction-weak : scan : pK`, 6 to 8), each step set with
     nm_ctx_set_values and solved from the previous step's field, against the
     reference's own rows.  Each step's bulk equilibrium reads the previous
     solve's bulk volume fractions (Reaction::pKeff), which moves pK_eff by
     about 0.3 here: the bulk fractions must follow that, not the input pK."""
-    g = load_golden("scan_states_h3o")
+    g = load_golden(name)
     plan = Plan(g["input"])
-    assert plan.c.scan_state >= 0
+    assert plan.c.scan_state >= 0 or plan.c.scan_reaction >= 0
     values = plan.scan_values()
     assert len(values) == len(g["rows"]) == 3
     ctx = Context(plan, NM_FP64)
@@ -88,7 +91,7 @@ def test_state_scan_matches_reference(tmp_path):
     items = [it for it in g["items"] if not it.startswith("newton")]
     for k, (v, row) in enumerate(zip(values, g["rows"])):
         if k > 0:
-            ctx.set_values({"state : H3O : alphabulk": v})
+            ctx.set_values({item: v})
         r, x, F = _solve(ctx, x)
         assert r.status == 0
         path = tmp_path / f"s{k}.kal"

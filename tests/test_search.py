@@ -108,11 +108,15 @@ def test_scan_values_are_the_reference_steps(name):
     plan = Plan(g["input"])
     vals = plan.scan_values()
     c = plan.c
-    if c.scan_state >= 0:
+    if c.scan_reaction >= 0:
+        # the reference writes no reaction items: its pK steps start + k·step
+        assert len(vals) == len(g["rows"]) and vals[0] == c.scan_start
+        ref = [c.scan_start + k * c.scan_step for k in range(len(vals))]
+    elif c.scan_state >= 0:
         col = f"mon_{plan.seg_names[c.state_seg[c.scan_state]]}_alphabulk_{plan.state_names[c.scan_state]}"
+        ref = [r[col] for r in g["rows"]]
     else:
-        col = "mol_pol_theta"
-    ref = [r[col] for r in g["rows"]]
+        ref = [r["mol_pol_theta"] for r in g["rows"]]
     assert len(vals) == len(ref)
     assert np.allclose(vals, ref, rtol=1e-12, atol=0)
 
@@ -144,6 +148,17 @@ def test_scan_ratio_truncating_to_zero_steps_is_accepted():
     assert plan.scan_values() == pytest.approx([5.0], rel=1e-12)
 
 
+def _scan_item(plan, text):
+    """The nm_ctx_set_values item a scan step sets."""
+    c = plan.c
+    if c.scan_state >= 0:
+        return f"state : {plan.state_names[c.scan_state]} : alphabulk"
+    if c.scan_reaction >= 0:
+        vn = next(ln.split(":")[1].strip() for ln in text.splitlines() if ln.startswith("var : reaction-"))
+        return f"reaction : {vn.split('-', 1)[1]} : pK"
+    return "mol : pol : theta"
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", SCANS)
 def test_scan_matches_reference(name):
@@ -158,8 +173,7 @@ def test_scan_matches_reference(name):
     plan = Plan(g["input"])
     ctx = Context(plan, NM_FP64)
     x = torch.from_numpy(np.array(g["x"])).cuda()
-    c = plan.c
-    item = f"state : {plan.state_names[c.scan_state]} : alphabulk" if c.scan_state >= 0 else "mol : pol : theta"
+    item = _scan_item(plan, g["input"])
     for v, row in zip(plan.scan_values(), g["rows"]):
         ctx.set_values({item: v})
         r = ctx.solve_dev(x.data_ptr())
@@ -222,8 +236,8 @@ def test_oracle_scan_follows_the_reference(name):
     x = np.array(g["x"])
     c = plan.c
     for v, row in zip(plan.scan_values(), g["rows"]):
-        if c.scan_state >= 0:
-            # a pH scan: the states' bulk fractions of each step are the
+        if c.scan_state >= 0 or c.scan_reaction >= 0:
+            # a pH or pK scan: the states' bulk fractions of each step are the
             # reference's own (its bulk equilibrium reads the previous solve;
             # the device context's restatement of that is tested on the GPU)
             orc.set_states([row[f"mon_{plan.seg_names[c.state_seg[j]]}_alphabulk_{st}"]
