@@ -1677,6 +1677,13 @@ static nm_plan* build_plan(const InputBlock& in, std::string& err) {
             err = "a search needs one 'search' and one target";
             delete H; return nullptr;
         }
+        // the reference's search solves the bulk equilibrium again before
+        // each inner solve (Solve_scf::residuals -> Solve, solve_scf.cpp:848),
+        // from the previous inner solve's bulk fractions; not restated
+        if (P.search_mol >= 0 && P.n_state > 0) {
+            err = "a search on a system with internal states is not supported";
+            delete H; return nullptr;
+        }
         // a free molecule's θ or n as the target: the reference's run of
         // such a search (φ_bulk of an adsorbing free polymer for a target θ)
         // ends in NaN, so it is refused rather than run

@@ -147,6 +147,12 @@ def test_a_lone_state_and_reactions_without_states_are_refused():
         Plan(none)
 
 
+def test_search_with_states_is_refused():
+    t = BASE.format(h3o="1e-7") + "var : mol-pol : search : theta\nvar : sys-noname : free_energy : -5\n"
+    with pytest.raises(NamicsError):
+        Plan(t)
+
+
 def test_batched_solver_refuses_states():
     from namics_gb300 import NM_FP64, Batch
     p = Plan(BASE.format(h3o="1e-7"))
