@@ -745,13 +745,14 @@ __device__ __forceinline__ void b1_solve(B1Prob& P, const int mode) {
             __syncthreads();
         }
         if (use32) {
-            // Leave the FP32 phase at the switch tolerance; or on a stall near
-            // the FP32 accuracy floor sw_floor (~1e-7 per chain segment: a
-            // residual there is noise and DIIS stops making progress); or on
-            // a long stall close to convergence.  Instances far from
-            // convergence stay in FP32.
+            // Leave the FP32 phase at the switch tolerance; at the FP32
+            // accuracy floor sw_floor (~1e-7 per chain segment: below it a
+            // residual is noise, so FP32 steps gain nothing more); on a stall
+            // near the floor (DIIS stops making progress); or on a long stall
+            // close to convergence.  Instances far from convergence stay in
+            // FP32.
             if (resid < 0.9 * best) { best = resid; since_best = 0; } else since_best++;
-            if (!(resid > P.sw_tol) || (since_best > 10 && resid < 10.0 * P.sw_floor) ||
+            if (!(resid > P.sw_tol) || !(resid > P.sw_floor) || (since_best > 10 && resid < 10.0 * P.sw_floor) ||
                 (since_best > 25 && resid < 1e-2)) {
                 use32 = false;
                 k_diis = 0;  // restart the DIIS history on the FP64 residual
