@@ -864,8 +864,8 @@ def other_workloads(args) -> dict:
 
 
 # DRAM bytes (read + write) per problem of the work loop on this workload,
-# from an ncu capture of a 1024-problem launch: 42.31 + 57.11 GB
-TRAFFIC_PER_PROBLEM = (42.31e9 + 57.11e9) / 1024
+# from an ncu capture of a 1024-problem launch: 36.94 + 50.59 GB
+TRAFFIC_PER_PROBLEM = (36.94e9 + 50.59e9) / 1024
 
 
 def run_brush1d(args) -> None:
