@@ -4,7 +4,7 @@
 // arrays of the context's lattice (length M, the reference's padded layout)
 // on the context's stream, and returns after the stream has finished.
 //
-// Markov-1 chains (the only kind this build runs); the arithmetic over all M
+// Markov-1 chains (the kind these entry points take); the arithmetic over all M
 // entries, halo layers included, as the reference's flat-array loops do:
 //   AddPhiS(phi, Gf, Gb)              phi += Gf·Gb          (AddTimes)
 //   AddPhiS(phi, Gf, Gb, d)           phi += d·Gf·Gb        (YplusisCtimesAtimesB)

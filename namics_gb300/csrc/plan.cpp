@@ -638,7 +638,7 @@ static bool setup_lattice(const InputBlock& in, PlanHolder& H, std::string& err)
 // guess files (the caller passes the field), the parameters of the other
 // Newton methods (sfnewton.cpp; iterate_DIIS reads none of them) and of the
 // outer loop of constraints (refused themselves).  Any other key is refused
-// by name, so an input that relies on a feature this build does not have
+// by name, so an input that relies on a feature this library does not have
 // cannot run with it silently dropped.
 static bool no_effect(const Entry& e) {
     static const char* const newton_keys[] = {

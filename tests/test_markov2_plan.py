@@ -6,7 +6,7 @@ lattice P[k] ∝ exp(-k_stiff/2·(k·π/2)²) for k = 0, 1, normalised by
 P[0] + 4·P[1], and P[2] = 0.  The reference prints them when it allocates a
 Markov 2 molecule; for k_stiff = 1 it printed P[0] = 0.461925 and
 P[1] = 0.134519 (six significant digits, its default cout precision).  What
-this build does not cover is refused by name: other gradient counts, the
+the compiler does not cover is refused by name: other gradient counts, the
 hexagonal lattice, branched or dendrimer chains, charged systems, a missing
 k_stiff (the reference's default is the lattice's k_stiff, which it never
 sets) and a k_stiff outside the reference's [0, 10].  The golden fixtures
