@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/liborc.so) — TEST INFRASTRUCTURE.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
-module, and only as the checker / the timed CPU baseline.
+module, and only as the parity reference of the tests and the timed CPU baseline.
 """
 from __future__ import annotations
 
