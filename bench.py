@@ -864,8 +864,8 @@ def other_workloads(args) -> dict:
 
 
 # DRAM bytes (read + write) per problem of the work loop on this workload,
-# from an ncu capture of a 1024-problem launch: 36.94 + 50.59 GB
-TRAFFIC_PER_PROBLEM = (36.94e9 + 50.59e9) / 1024
+# from an ncu capture of a 1024-problem launch: 32.01 + 47.16 GB
+TRAFFIC_PER_PROBLEM = (32.01e9 + 47.16e9) / 1024
 
 
 def run_brush1d(args) -> None:
