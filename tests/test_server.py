@@ -79,3 +79,20 @@ def test_server_rejects_request_beyond_budget():
     with pytest.raises(NamicsError):
         srv.submit(plan, x)
     srv.close()
+
+
+def test_server_context_sweep_options_keep_results():
+    """nm_server_options.context_sweeps 1 and 2 (persistent 2-D sweeps,
+    cluster sweeps of small FP32 3-D boxes) change how the request contexts
+    launch their steps, not their arithmetic: the results are those of the
+    requests solved alone with one launch per step."""
+    cases = [c for c in _cases() if c[1].c.gradients > 1]
+    assert {c[1].c.gradients for c in cases} == {2, 3}
+    srv = Server(precision=NM_FP32, workers=2, max_batch=8, memory_budget=256 << 20, context_sweeps=3)
+    ids = [(n, plan, x, srv.submit(plan, x)) for n, plan, x in cases]
+    results = [(n, plan, x) + srv.wait(rid) for n, plan, x, rid in ids]
+    srv.close()
+    for n, plan, x, res, xs, sec in results:
+        its, resid, st, xa = _alone(plan, x, NM_FP32)
+        assert res.status == st and res.iterations == its, (n, res, its, st)
+        assert np.array_equal(xs, xa), n
