@@ -754,8 +754,8 @@ struct Chem {
             }
             if (s1 < 0) { s1 = local[s]; continue; }
             if (s2 >= 0 || r.sto[i] <= 0) {
-                err = "reaction " + r.name + ": the second state of " + std::to_string(other) +
-                      " must be a single right-hand-side term";
+                err = "reaction " + r.name + ": needs exactly two states of its other segment, the second "
+                      "on the right-hand side";
                 return false;
             }
             s2 = local[s];
