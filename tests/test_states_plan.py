@@ -158,3 +158,30 @@ def test_batched_solver_refuses_states():
     p = Plan(BASE.format(h3o="1e-7"))
     with pytest.raises(NamicsError):
         Batch([p], NM_FP64)
+
+
+def test_K_is_ten_to_the_minus_pK():
+    """`reaction : <name> : K` instead of pK (reaction.cpp:60-68): pK = -log10(K)."""
+    a = Plan(BASE.format(h3o="1e-5"))
+    b = Plan(BASE.format(h3o="1e-5").replace("reaction : weak : pK : 7", "reaction : weak : K : 1e-7"))
+    for x, y in zip(a.state_alphabulk, b.state_alphabulk):
+        assert abs(x - y) <= 1e-12 * x
+
+
+def test_state_scan_keys():
+    """`var : state-<name> : scan : alphabulk` on a fixed state, and a reaction's
+    pK scan; a scan of a state the reactions set is refused."""
+    t = BASE.format(h3o="1e-7")
+    p = Plan(t + "var : state-H3O : scan : alphabulk\nvar : state-H3O : scale : exponential\n"
+                 "var : state-H3O : end_value : 1e-4\nvar : state-H3O : steps : 2\n")
+    assert p.c.scan_state == p.state_names.index("H3O") and p.c.scan_n == 6
+    v = p.scan_values()
+    assert v[0] == pytest.approx(1e-7) and v[-1] == pytest.approx(1e-4) and v[2] == pytest.approx(1e-6)
+    q = Plan(t + "var : reaction-weak : scan : pK\nvar : reaction-weak : step : 0.5\n"
+                 "var : reaction-weak : end_value : 8\n")
+    assert q.c.scan_reaction == 0 and q.scan_values() == [7.0, 7.5, 8.0]
+    with pytest.raises(NamicsError):  # AM's fraction follows from the reactions
+        Plan(t + "var : state-AM : scan : alphabulk\nvar : state-AM : step : 0.1\nvar : state-AM : end_value : 0.9\n")
+    with pytest.raises(NamicsError):  # a pK scan is linear
+        Plan(t + "var : reaction-weak : scan : pK\nvar : reaction-weak : scale : exponential\n"
+                 "var : reaction-weak : end_value : 8\n")
