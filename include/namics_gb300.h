@@ -304,6 +304,18 @@ int nm_ctx_autotune(nm_ctx* ctx, const double* x_dev, nm_ctx_tuning* out);
  * NM_ERR_ARG without a scan or with k out of range. */
 int nm_plan_scan_value(const nm_plan* plan, int k, double* value);
 
+/* The bulk equilibrium of a plan with internal states, as Solve_scf::Solve
+ * runs it before each solve (solve_scf.cpp:562-603): the fixed states'
+ * alphabulk from fixed_ab [n_state] (entries of states the reactions set
+ * are ignored; NULL: the input's), the reactions' pK from pK [reactions, in
+ * input order] (NULL: the input's), and pK_eff from the species' bulk
+ * volume fractions sp_phibulk [n_sp] of the previous solve (NULL before
+ * any: pK_eff = pK).  Writes the states' bulk fractions [n_state] and the
+ * molecules' bulk charges [n_mol] (either may be NULL).  NM_ERR_ARG without
+ * states, NM_ERR_INPUT where the equilibrium cannot be solved. */
+int nm_plan_state_bulk(const nm_plan* plan, const double* fixed_ab, const double* pK,
+                       const double* sp_phibulk, double* alphabulk, double* mol_charge);
+
 /* Scans (the reference's Variate: variate.cpp, solve_scf.cpp:717-868): change
  * values of a live context and solve again from its current field (a warm
  * start).  items: "mon : <seg> : chi_<seg>" (set both ways; not on a plan

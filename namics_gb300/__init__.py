@@ -105,6 +105,23 @@ class Plan:
     def state_alphabulk(self) -> list[float]:
         return [self.c.state_alphabulk[j] for j in range(self.c.n_state)]
 
+    def state_bulk(self, fixed_ab=None, pK=None, sp_phibulk=None):
+        """The bulk equilibrium of the states (nm_plan_state_bulk): the
+        states' bulk fractions and the molecules' bulk charges for the given
+        fixed fractions, pK values and previous bulk volume fractions of the
+        species (each None: the input's, or before any solve)."""
+        c = self.c
+        arr = lambda v: None if v is None else np.ascontiguousarray(v, dtype=np.float64)  # noqa: E731
+        fx, pk, spb = arr(fixed_ab), arr(pK), arr(sp_phibulk)
+        if fx is not None:
+            _check_len(fx, c.n_state, "Plan.state_bulk fixed_ab")
+        if spb is not None:
+            _check_len(spb, c.n_sp, "Plan.state_bulk sp_phibulk")
+        ab, q = np.empty(c.n_state), np.empty(c.n_mol)
+        ptr = lambda a: _dptr(a) if a is not None else None  # noqa: E731
+        _check(_abi.load().nm_plan_state_bulk(self._p, ptr(fx), ptr(pk), ptr(spb), _dptr(ab), _dptr(q)))
+        return ab, q
+
     @property
     def it_names(self) -> list[str]:
         """Name of each iteration block's representative: the mon of an

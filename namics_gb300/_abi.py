@@ -124,6 +124,7 @@ SIGNATURES = [
     ("nm_solve_dev", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(nm_solve_result)]),
     ("nm_ctx_search", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(nm_search_result)]),
     ("nm_plan_scan_value", C.c_int, [P_plan, C.c_int, dp]),
+    ("nm_plan_state_bulk", C.c_int, [P_plan, dp, dp, dp, dp, dp]),
     ("nm_solve_host", C.c_int, [C.c_void_p, dp, dp, C.POINTER(nm_solve_result)]),
     ("nm_get_field", C.c_int, [C.c_void_p, C.c_int, dp]),
     ("nm_get_molecule", C.c_int, [C.c_void_p, C.c_int, dp, dp, dp, dp]),

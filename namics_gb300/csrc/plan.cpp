@@ -1755,6 +1755,21 @@ int nm_plan_create(const char* input_text, nm_plan** out) {
     return NM_OK;
 }
 
+int nm_plan_state_bulk(const nm_plan* plan, const double* fixed_ab, const double* pK, const double* sp_phibulk,
+                       double* alphabulk, double* mol_charge) {
+    if (!plan || plan->n_state == 0) { nm::set_error("nm_plan_state_bulk: the plan has no internal states"); return NM_ERR_ARG; }
+    const nm::PlanHolder& H = *reinterpret_cast<const nm::PlanHolder*>(plan);
+    std::vector<double> fx = fixed_ab ? std::vector<double>(fixed_ab, fixed_ab + plan->n_state) : H.state_ab_in;
+    std::vector<double> pk = nm::plan_reaction_pK(plan);
+    if (pK) pk.assign(pK, pK + pk.size());
+    std::vector<double> ab, q;
+    std::string err;
+    if (int rc = nm::plan_state_bulk(plan, fx, pk, sp_phibulk, ab, q, err)) { nm::set_error("nm_plan_state_bulk: " + err); return rc; }
+    if (alphabulk) std::copy(ab.begin(), ab.end(), alphabulk);
+    if (mol_charge) std::copy(q.begin(), q.end(), mol_charge);
+    return NM_OK;
+}
+
 int nm_plan_scan_value(const nm_plan* plan, int k, double* value) {
     if (!plan || !value || (plan->scan_mol < 0 && plan->scan_state < 0 && plan->scan_reaction < 0) || k < 0 ||
         k > plan->scan_n) {

@@ -36,6 +36,7 @@ def load() -> C.CDLL:
         lib.orc_side.argtypes = [C.c_void_p, dp, dp]
         lib.orc_set_amount.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double]
         lib.orc_set_states.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        lib.orc_get_species_phibulk.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         lib.orc_search.argtypes = [C.c_void_p, dp, dp, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         _lib = lib
     return _lib
@@ -81,6 +82,14 @@ class Oracle:
         rc = load().orc_set_amount(self._h, mol, what, value)
         if rc:
             raise RuntimeError(f"orc_set_amount rc={rc}")
+
+    def species_phibulk(self) -> np.ndarray:
+        """Bulk volume fractions of the species of the last residual."""
+        out = np.zeros(self.plan.n_seg + self.plan.c.n_state)
+        rc = load().orc_get_species_phibulk(self._h, _p(out))
+        if rc:
+            raise RuntimeError(f"orc_get_species_phibulk rc={rc}")
+        return out
 
     def set_states(self, alphabulk) -> None:
         """The states' bulk fractions for the next solves (a scan of a fixed

@@ -1136,6 +1136,16 @@ int orc_get_field(orc_state* st, int which, double* out) {
     return NM_ERR_ARG;
 }
 
+/* the bulk volume fractions of the interaction species of the last
+ * residual (segments, then states) [n_sp] */
+int orc_get_species_phibulk(orc_state* st, double* out) {
+    const nm_plan* P = st->P;
+    if (!st->have_state) return NM_ERR_ARG;
+    const int nsp = P->n_seg + P->n_state;
+    for (int k = 0; k < nsp; k++) out[k] = st->sp_phibulk[k];
+    return NM_OK;
+}
+
 int orc_get_molecule(orc_state* st, int m, double* GN, double* n, double* theta, double* phibulk) {
     if (!st->have_state || m < 0 || m >= st->P->n_mol) return NM_ERR_ARG;
     if (GN) *GN = st->GN[m];

@@ -31,6 +31,8 @@ int orc_solve_n(orc_state* st, double* x, int max_iter, int* iterations, double*
 int orc_get_field(orc_state* st, int which, double* out);
 int orc_get_molecule(orc_state* st, int mol, double* GN, double* n, double* theta,
                      double* phibulk);
+/* bulk volume fractions of the interaction species [n_seg + n_state] */
+int orc_get_species_phibulk(orc_state* st, double* out);
 int orc_free_energy(orc_state* st, double* F, double* Omega, double* mu);
 /* a molecule amount in force for the next solves (what: 0 θ, 1 n, 2 φ_bulk),
  * and the plan's search from x (updated in place) */

@@ -185,3 +185,43 @@ def test_state_scan_keys():
     with pytest.raises(NamicsError):  # a pK scan is linear
         Plan(t + "var : reaction-weak : scan : pK\nvar : reaction-weak : scale : exponential\n"
                  "var : reaction-weak : end_value : 8\n")
+
+
+@pytest.mark.parametrize("name", ["scan_states_h3o", "scan_states_pk"])
+def test_bulk_equilibrium_follows_the_reference_scan(name):
+    """nm_plan_state_bulk with the previous step's bulk volume fractions
+    gives the reference's bulk fractions of the next scan step: the oracle
+    solves each step with the reference's own fractions, its species' bulk
+    fractions then feed the next step's equilibrium (Reaction::pKeff reads
+    them, with the reference's term-position indexing of the states)."""
+    import sys
+    from pathlib import Path
+    import numpy as np
+    from conftest import load_golden
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1] / "oracle"))
+    from orc import Oracle
+    g = load_golden(name)
+    plan = Plan(g["input"])
+    c = plan.c
+    orc = Oracle(plan)
+    names = [f"mon_{plan.seg_names[c.state_seg[j]]}_alphabulk_{st}" for j, st in enumerate(plan.state_names)]
+    values = plan.scan_values()
+    x = np.array(g["x"])
+    # step 0: no previous solve, pK_eff = pK, the plan's fractions
+    ab0, _ = plan.state_bulk()
+    assert np.allclose(ab0, plan.state_alphabulk, rtol=1e-15, atol=0)
+    fixed = np.array(plan.state_alphabulk)
+    pk = None
+    for k, row in enumerate(g["rows"]):
+        if k > 0:
+            if c.scan_state >= 0:
+                fixed[c.scan_state] = values[k]
+            else:  # the input's reactions: weak (scanned), then auto at pK 14
+                assert c.scan_reaction == 0
+                pk = [values[k], 14.0]
+            ab, _ = plan.state_bulk(fixed_ab=fixed, pK=pk, sp_phibulk=orc.species_phibulk())
+            ref = np.array([row[n] for n in names])
+            assert np.max(np.abs(ab - ref) / ref) < 1e-6, (k, ab, ref)
+        orc.set_states([row[n] for n in names])
+        rc, x, _, res = orc.solve(x)
+        assert rc == 0
