@@ -458,7 +458,12 @@ long long nm_ctx_launch_count(nm_ctx* ctx);
  * next problem from a queue in device memory (longest first) as soon as its
  * previous one converged, with DIIS on the device.  Stored propagators and
  * DIIS histories live in the slot's scratch; fields x and residuals g are
- * per problem. */
+ * per problem.  With NM_FP32 a problem starts with FP32 propagators and a
+ * 5-deep DIIS history (at most the input's m) and switches to FP64 residuals
+ * with the input's m, history restarted, at the FP32 accuracy floor
+ * (1e-7·N + 1e-6), on a stall near it, or on any FP32 failure; its stopping
+ * test is always made on an FP64 residual.  NM_FP64 runs the reference's
+ * DIIS throughout. */
 typedef struct nm_batch nm_batch;
 
 int nm_batch_create(const nm_plan* const* plans, int n_plans,
